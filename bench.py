@@ -1,0 +1,390 @@
+#!/usr/bin/env python3
+"""Benchmark of the Trinity k-mer hot path on one GB300.
+
+Workload (the plain path at scale): 20,000 multi-isoform genes, 20M read
+pairs of 2x100 nt (fragment normal(300, 50), 1% substitutions, 0.01% N),
+constant-quality FASTQ, generated from a fixed seed.  One step is the plain
+pipeline the reference runs for in-silico normalization
+(util/insilico_read_normalization.pl:588-654, 816-898): parse both mates,
+canonical k=25 count of all 40M reads (jellyfish count), histogram
+(jellyfish histo), the -L 2 catalogue as text (jellyfish dump), and per-read
+median/mean/stdev coverage of each mate file (fastaToKmerCoverageStats).
+
+value  = k-mer occurrences counted / step time, inputs resident in HBM
+e2e    = the same through the C ABI from pinned host FASTQ, with the dump text
+         and the statistics copied back to the host inside the timed region
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--pairs P]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "exact k=25 k-mers/s and reads/s on 1 GB300, batched/served vs plain; p50/p99 job latency"
+UNIT = "k-mers/s"
+FULL_PAIRS = 20_000_000
+N_GENES = 20_000
+SEED = 20240
+K = 25
+MIN_COUNT = 2           # the catalogue fastaToKmerCoverageStats reads (util/insilico_read_normalization.pl:45)
+L2_BYTES = 129 * 2**20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for independent replicas (the path shards by
+    reads with no data exchange, so ranks never talk on the data path)."""
+
+    def __init__(self, world: int):
+        self.world = world
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks.dev{device}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(pairs: int, seed: int):
+    from trinityrnaseq_gb300 import synth
+    t = time.time()
+    left, right = synth.gene_pairs(seed=seed, n_genes=N_GENES, n_pairs=pairs, read_len=100, frag_mean=300.0,
+                                   frag_sd=50.0, err=0.01, n_rate=0.0001, fastq=True)
+    log(f"generated {pairs} pairs ({(left.nbytes + right.nbytes) / 1e9:.2f} GB FASTQ) in {time.time() - t:.1f}s")
+    return left, right
+
+
+# ---------------------------------------------------------------- GPU arm
+
+class GpuPipeline:
+    def __init__(self, ctx, left, right):
+        import torch
+        from trinityrnaseq_gb300 import kmer
+        self.torch, self.kmer, self.ctx = torch, kmer, ctx
+        dev = torch.device(f"cuda:{ctx.device}")
+        # device-resident inputs (value) and pinned host inputs (e2e)
+        self.h_left = torch.from_numpy(left).pin_memory()
+        self.h_right = torch.from_numpy(right).pin_memory()
+        self.d_left = self.h_left.to(dev)
+        self.d_right = self.h_right.to(dev)
+        torch.cuda.synchronize(dev)
+        self.dev = dev
+        self.n_reads = None
+        self.out = None
+
+    def _alloc_out(self, n_left, n_right):
+        t = self.torch
+        if self.out is None:
+            self.out = {}
+            for side, n in (("l", n_left), ("r", n_right)):
+                self.out[side + "_dev"] = [t.empty(n, dtype=t.int32, device=self.dev) for _ in range(3)]
+                self.out[side + "_host"] = [t.empty(n, dtype=t.int32).pin_memory() for _ in range(3)]
+            self.out["dump_host"] = None
+
+    def step(self, e2e: bool):
+        """One plain pipeline pass; returns (windows, reads, h2d_bytes, d2h_bytes)."""
+        kmer, t = self.kmer, self.torch
+        ctx = self.ctx
+        if e2e:
+            rl = kmer.ReadSet(ctx, self.h_left.numpy())
+            rr = kmer.ReadSet(ctx, self.h_right.numpy())
+            h2d = self.h_left.numel() + self.h_right.numel()
+        else:
+            rl = kmer.ReadSet(ctx, self.d_left.data_ptr(), self.d_left.numel(), device=True)
+            rr = kmer.ReadSet(ctx, self.d_right.data_ptr(), self.d_right.numel(), device=True)
+            h2d = 0
+        table = kmer.KmerTable(ctx, K, True)
+        table.add(rl)
+        table.add(rr)
+        hist = table.histo(1, 10000)
+        dump_len = table.dump_fasta_len(MIN_COUNT)
+        self._alloc_out(rl.n_reads, rr.n_reads)
+        d2h = hist.nbytes
+        if e2e:
+            if self.out["dump_host"] is None or self.out["dump_host"].numel() < dump_len:
+                self.out["dump_host"] = t.empty(int(dump_len * 1.1) + 16, dtype=t.uint8).pin_memory()
+            table.dump_fasta_into(MIN_COUNT, self.out["dump_host"].data_ptr(), self.out["dump_host"].numel())
+            d2h += dump_len
+        for side, rs in (("l", rl), ("r", rr)):
+            bufs = self.out[side + ("_host" if e2e else "_dev")]
+            kmer.coverage_stats_into(table, rs, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(),
+                                     device=not e2e)
+            if e2e:
+                d2h += 12 * rs.n_reads
+        windows = table.info()[1]
+        reads = rl.n_reads + rr.n_reads
+        packed = rl.n_bases + rl.n_reads + rr.n_bases + rr.n_reads
+        table.free()
+        rl.free()
+        rr.free()
+        return windows, reads, h2d, d2h, packed
+
+
+def timed(pipe, stream, steps, e2e, dist):
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    res = []
+    dist.barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            ev[i][0].record(stream)
+            res.append(pipe.step(e2e))
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    return ms, res
+
+
+def run_gpu(args, dist, world, rank, local):
+    import torch
+    from trinityrnaseq_gb300 import Context, native
+    native.load()
+    torch.cuda.set_device(local)
+    ctx = Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device(f"cuda:{local}"))
+    left, right = workload(args.pairs, SEED + rank)
+    pipe = GpuPipeline(ctx, left, right)
+    input_bytes = left.nbytes + right.nbytes
+    for _ in range(args.warmup):
+        pipe.step(False)
+    for _ in range(max(1, args.warmup // 2)):
+        pipe.step(True)
+    # device-resident timed region, with per-kernel CUDA-event profiling
+    ctx.set_profiling(True)
+    ctx.reset_profile()
+    launches0 = ctx.kernel_launches
+    clocks = Clocks(local)
+    clocks.start()
+    ms, res = timed(pipe, stream, args.steps, False, dist)
+    clk = clocks.stop()
+    launches = ctx.kernel_launches - launches0
+    prof = {k: ctx.profile(k) for k in ("parse", "hll", "count", "compact", "sort", "dump", "coverage")}
+    ctx.set_profiling(False)
+    # end-to-end timed region (host FASTQ in, dump text + stats out)
+    ms_e2e, res_e2e = timed(pipe, stream, args.steps, True, dist)
+    windows, reads = res[0][0], res[0][1]
+    t_step = dist.max(statistics.mean(ms)) / 1e3
+    t_e2e = dist.max(statistics.mean(ms_e2e)) / 1e3
+    tot_windows = dist.sum(windows)
+    tot_reads = dist.sum(reads)
+    out = None
+    if rank == 0:
+        # K2 algorithmic bytes: one 32-byte sector per k-mer occurrence plus one
+        # byte per packed base it streams; each launch counts one mate file
+        count_ms, count_launches, count_units = prof["count"]
+        per_launch_units = count_units / max(count_launches, 1)
+        per_launch_ms = count_ms / max(count_launches, 1)
+        packed_per_launch = res[0][4] / 2.0
+        alg_bytes = 32.0 * per_launch_units + packed_per_launch
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+        out = {
+            "metric": METRIC, "value": tot_windows / t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded; no public dataset for this path)",
+            "config": {"workload": f"plain path at scale: {N_GENES} genes, {args.pairs} pairs 2x100 FASTQ, "
+                                   "1% substitutions, 0.01% N; count + histo + dump -L 2 + coverage stats",
+                       "pairs_per_gpu": args.pairs, "reads_per_gpu": reads, "k": K, "canonical": True,
+                       "dump_min_count": MIN_COUNT, "input_bytes_per_gpu": input_bytes,
+                       "l2": "inputs larger than L2 (%.1f GB FASTQ vs 129 MB)" % (input_bytes / 1e9),
+                       "parallelism": f"replicas x{world}"},
+            "reads_per_s": tot_reads / t_step,
+            "kmer_occurrences_per_step": tot_windows,
+            "e2e": {"value": tot_windows / t_e2e, "unit": UNIT, "reads_per_s": tot_reads / t_e2e,
+                    "ms_per_step": t_e2e * 1e3, "h2d_bytes_per_step": res_e2e[0][2],
+                    "d2h_bytes_per_step": res_e2e[0][3]},
+            "roofline": {"bound": "hbm", "kernel": "k_count (canonical k-mer count insert)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                         "alg_bytes_per_launch": alg_bytes, "kmers_per_launch": per_launch_units,
+                         "ms_per_launch": per_launch_ms, "traffic": None},
+            "kernels_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(args)
+    ctx.close()
+    return out
+
+
+# ---------------------------------------------------------------- CPU arms
+
+def cpu_pipeline(left: bytes, right: bytes, threads: int):
+    """The plain pipeline with the oracle on the host cores: count (hash order,
+    as jellyfish dumps), histo, dump -L 2, catalogue parse, stats per mate."""
+    from oracle import oracle as O
+    keys, counts = O.count(left + right, K, True, threads, sorted_=False)
+    O.histo(counts, 1, 10000)
+    dump = O.dump(keys, counts, K, MIN_COUNT)
+    k2, c2 = O.load_dump(dump, K, True)
+    O.cov_stats(left, k2, c2, K, True, False, threads)
+    O.cov_stats(right, k2, c2, K, True, False, threads)
+    return int(counts.sum(dtype="uint64"))
+
+
+def cpu_sample(pairs: int):
+    from trinityrnaseq_gb300 import synth
+    left, right = synth.gene_pairs(seed=SEED, n_genes=N_GENES, n_pairs=pairs, read_len=100, err=0.01,
+                                   n_rate=0.0001, fastq=True)
+    return left.tobytes(), right.tobytes()
+
+
+def cpu_baseline(args):
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    left, right = cpu_sample(args.cpu_pairs)
+    t = time.time()
+    windows = cpu_pipeline(left, right, threads)
+    dt = time.time() - t
+    return {"value": windows / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "reads_per_s": 2 * args.cpu_pairs / dt, "seconds": dt,
+            "sample": f"first {args.cpu_pairs} pairs of the same seeded workload; the CPU oracle (C, OpenMP) "
+                      "count + histo + dump -L 2 + catalogue load + coverage stats of both mates"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    left, right = cpu_sample(args.cpu_pairs)
+    for _ in range(args.warmup):
+        cpu_pipeline(left, right, threads)
+    ts, windows = [], 0
+    for _ in range(args.steps):
+        t = time.time()
+        windows = cpu_pipeline(left, right, threads)
+        ts.append(time.time() - t)
+    dt = statistics.mean(ts)
+    v = windows / dt
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": f"plain path at scale (bounded sample: {args.cpu_pairs} pairs of the 20M-pair "
+                                   "workload)", "k": K, "canonical": True, "dump_min_count": MIN_COUNT},
+            "reads_per_s": 2 * args.cpu_pairs / dt,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.cpu_pairs} pairs per step; the reference's jellyfish, Inchworm and "
+                                       "Chrysalis sources are not in its checkout, so the CPU oracle stands in"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pairs", type=int, default=FULL_PAIRS)
+    ap.add_argument("--cpu-pairs", type=int, default=1_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    dist = Dist(world)
+    out = run_gpu(args, dist, world, rank, local)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+/*
+ * trinkmer.h -- C ABI of the GB300 k-mer library (libtrinkmer_cuda.so).
+ *
+ * The reference reaches this hot path only through three executables that
+ * Perl starts with system() (PerlLib/Pipeliner.pm:143-209,
+ * util/insilico_read_normalization.pl:797-813, Trinity:2910): jellyfish
+ * (Trinity:2612-2638), Inchworm's fastaToKmerCoverageStats
+ * (util/insilico_read_normalization.pl:837-846) and Chrysalis'
+ * ReadsToTranscripts (Trinity:2237-2251).  There is no library interface in
+ * the reference, so this ABI is the one the drop-in executables of this
+ * package (tools/) and any foreign-language caller bind; each group below
+ * names the command it replaces.
+ *
+ * Conventions: every function returns TK_OK (0) or a negative TK_E_* status;
+ * no C++ exception crosses the ABI; handles are opaque and owned by the
+ * library, which also owns all device memory.  Buffers passed in are owned by
+ * the caller and described by (pointer, length); `where` says whether a
+ * buffer is host memory (TK_HOST) or device memory of the context's GPU
+ * (TK_DEVICE).  A handle is used by one thread at a time.  All work of one
+ * context is ordered on that context's CUDA stream; functions that return
+ * host data synchronise it.
+ */
+#ifndef TRINKMER_H
+#define TRINKMER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TK_OK 0
+#define TK_E_INVAL (-1)       /* bad argument */
+#define TK_E_CUDA (-2)        /* CUDA runtime error */
+#define TK_E_OOM (-3)         /* device or host allocation failed */
+#define TK_E_PARSE (-4)       /* malformed FASTA/FASTQ/dump input */
+#define TK_E_TABLE_FULL (-5)  /* hash table overflow could not be resolved */
+#define TK_E_BUDGET (-6)      /* job does not fit the HBM admission budget */
+#define TK_E_NODEV (-7)       /* no usable CUDA device */
+#define TK_E_RANGE (-8)       /* caller buffer too small */
+
+#define TK_HOST 0
+#define TK_DEVICE 1
+
+#define TK_FMT_NONE 0
+#define TK_FMT_FASTA 1
+#define TK_FMT_FASTQ 2
+
+/* kernel classes for tk_ctx_profile */
+#define TK_KID_PARSE 0        /* FASTA/FASTQ split + pack */
+#define TK_KID_HLL 1          /* distinct-k-mer estimate (table sizing) */
+#define TK_KID_COUNT 2        /* k-mer count insert */
+#define TK_KID_COMPACT 3      /* table scan: -L filter + histogram */
+#define TK_KID_SORT 4         /* radix sort of keys */
+#define TK_KID_DUMP 5         /* dump text formatter */
+#define TK_KID_LOAD 6         /* k-mer catalogue load */
+#define TK_KID_COVERAGE 7     /* per-read coverage statistics */
+#define TK_KID_R2T_BUILD 8    /* bundle k-mer -> record table */
+#define TK_KID_R2T_ASSIGN 9   /* read -> component vote */
+#define TK_KID_BINS 10        /* batched per-bin counting */
+#define TK_KID_NUM 11        /* number of kernel classes */
+
+typedef struct tk_ctx tk_ctx;
+typedef struct tk_reads tk_reads;
+typedef struct tk_table tk_table;
+typedef struct tk_r2t tk_r2t;
+
+/* ------------------------------------------------------------- context */
+
+const char *tk_version(void);
+const char *tk_status_string(int status);
+
+/* Creates a context on CUDA device `device` with its own stream. */
+int tk_ctx_create(int device, tk_ctx **out);
+void tk_ctx_destroy(tk_ctx *ctx);
+/* Human-readable detail of the context's most recent error. */
+const char *tk_ctx_last_error(const tk_ctx *ctx);
+/* The context's cudaStream_t, as an opaque pointer. */
+void *tk_ctx_stream(tk_ctx *ctx);
+int tk_ctx_synchronize(tk_ctx *ctx);
+/* CUDA-event timing of the hot kernels on the context's stream. */
+int tk_ctx_set_profiling(tk_ctx *ctx, int on);
+int tk_ctx_profile(tk_ctx *ctx, int kid, double *ms, uint64_t *launches, uint64_t *units);
+int tk_ctx_reset_profile(tk_ctx *ctx);
+/* Number of kernels this library has launched on the context. */
+uint64_t tk_ctx_kernel_launches(const tk_ctx *ctx);
+/* Bytes of device memory currently free / total on the context's GPU. */
+int tk_ctx_mem_info(tk_ctx *ctx, uint64_t *free_bytes, uint64_t *total_bytes);
+/* Probe limit of the hash tables before a key is sent to the overflow list
+ * and the table grows (jellyfish count -p/--reprobes; default 4096). */
+int tk_ctx_set_reprobes(tk_ctx *ctx, int max_probes);
+
+/* ------------------------------------------------------------- read sets
+ * Parse FASTA (PerlLib/Fasta_reader.pm:45-118 semantics: a record starts at a
+ * '>' line, its sequence is the following lines with whitespace removed, its
+ * accession is the first header token) or 4-line FASTQ
+ * (util/support_scripts/fastQ_to_fastA.pl:80-106) into a device-resident read
+ * set.  The text is copied to the device when where == TK_HOST; a TK_DEVICE
+ * text must stay valid while the read set lives. */
+int tk_reads_parse(tk_ctx *ctx, const char *text, uint64_t len, int where, tk_reads **out);
+int tk_reads_info(const tk_reads *reads, uint64_t *n_reads, uint64_t *n_bases,
+                  uint32_t *max_len, int *format);
+/* Host copies: accession offset/length into the parsed text (n_reads each). */
+int tk_reads_names(const tk_reads *reads, uint64_t *name_off, uint32_t *name_len);
+/* Host copies of read starts in the packed sequence (n_reads + 1 entries) and
+ * of the packed sequence itself (upper-cased bases, '\n' after each read). */
+int tk_reads_offsets(const tk_reads *reads, uint64_t *rd_off);
+int tk_reads_copy_seq(const tk_reads *reads, char *dst, uint64_t cap);
+void tk_reads_free(tk_reads *reads);
+
+/* ------------------------------------------------------------- counting
+ * Replaces `jellyfish count -m K [--canonical] -s H -t N -o db reads.fa`
+ * (Trinity:2612-2621, util/insilico_read_normalization.pl:617-626),
+ * `jellyfish histo` (Trinity:2630, util/insilico_read_normalization.pl:636)
+ * and `jellyfish dump -L m` (Trinity:2625, util/insilico_read_normalization.pl:641).
+ * A k-mer is k consecutive A/C/G/T (either case); canonical keys are the
+ * smaller of a k-mer and its reverse complement in 2-bit A<C<G<T order.
+ * capacity_hint = 0 sizes the table from a distinct-k-mer estimate of each
+ * batch; the table grows (rehash) whenever it would exceed half load. */
+int tk_table_create(tk_ctx *ctx, int k, int canonical, uint64_t capacity_hint, tk_table **out);
+int tk_table_add_reads(tk_table *table, const tk_reads *reads);
+int tk_table_count_text(tk_table *table, const char *text, uint64_t len, int where);
+int tk_table_info(tk_table *table, uint64_t *distinct, uint64_t *total, uint64_t *capacity);
+/* hist[0] = keys with count < low, hist[1 + c - low] for low <= c <= high,
+ * hist[high - low + 2] = keys with count > high (high - low + 3 entries). */
+int tk_table_histo(tk_table *table, uint64_t low, uint64_t high, uint64_t *hist);
+/* (key, count) pairs with count >= min_count sorted by key.  keys == NULL
+ * only reports *n_out.  TK_E_RANGE when cap < the number of pairs. */
+int tk_table_dump(tk_table *table, uint32_t min_count, int where, uint64_t *keys,
+                  uint32_t *counts, uint64_t cap, uint64_t *n_out);
+/* The dump as text, ">COUNT\nKMER\n" per pair, sorted by key, into `out`
+ * (host or device memory per `where`).  out == NULL formats the dump on the
+ * device and only reports *len_out; the formatted text is kept with the
+ * table, so the following call with a buffer copies it without recomputing
+ * (until the table changes). */
+int tk_table_dump_fasta(tk_table *table, uint32_t min_count, int where, char *out, uint64_t cap,
+                        uint64_t *len_out);
+/* Adds (key, count) pairs (a stored database, or another table's dump). */
+int tk_table_load_pairs(tk_table *table, const uint64_t *keys, const uint32_t *counts,
+                        uint64_t n, int where);
+/* Adds the pairs of a ">COUNT\nKMER\n" dump (fastaToKmerCoverageStats --kmers;
+ * canonicalised when the table is canonical, i.e. --DS). */
+int tk_table_load_dump_fasta(tk_table *table, const char *text, uint64_t len, int where);
+void tk_table_free(tk_table *table);
+
+/* ------------------------------------------------------------- coverage
+ * Replaces Inchworm's `fastaToKmerCoverageStats --reads R --kmers K
+ * --kmer_size 25 [--DS]` (util/insilico_read_normalization.pl:837-846).  Per
+ * read, over its windows of k A/C/G/T bases, each k-mer's count in `table`
+ * (canonical lookup when the table is canonical; a k-mer absent from the
+ * table counts 1, Changelog.txt:536-538): median = element n/2 of the sorted
+ * counts, mean = (float)(sum / n), stdev = population standard deviation
+ * from exact integer sums; 0, 0, 0 for a read with no window.  Outputs hold
+ * n_reads entries each, in read order. */
+int tk_coverage_stats(tk_table *table, const tk_reads *reads, int where, uint32_t *median,
+                      float *mean, float *stdev);
+
+/* ------------------------------------------------------------- read -> component
+ * Replaces Chrysalis' `ReadsToTranscripts -i reads.fa -f bundle.fasta -o out
+ * -t N -max_mem_reads M [-strand] [-p P]` (Trinity:2237-2251).  The bundle is
+ * FASTA with one '>s_<component>' record per component whose contigs are
+ * joined by 'X' (util/support_scripts/add_LR_reads_to_iworm_bundle.pl:19-47).
+ * Each bundle k-mer belongs to the first record holding it; a read votes once
+ * per window for the owner of the window's k-mer; rec = the record with most
+ * votes (ties to the earlier record) or -1 without any vote; hits = its votes;
+ * nwin = L - k + 1 (0 when L < k). */
+int tk_r2t_create(tk_ctx *ctx, const char *bundle, uint64_t len, int where, int k,
+                  int strand, tk_r2t **out);
+int tk_r2t_info(const tk_r2t *r2t, uint64_t *n_records, uint64_t *n_kmers);
+/* Component id (the integer after "s_", else the record ordinal) per record. */
+int tk_r2t_component_ids(const tk_r2t *r2t, uint64_t *ids);
+int tk_r2t_assign(tk_r2t *r2t, const tk_reads *reads, int where, int32_t *rec,
+                  uint32_t *hits, uint32_t *nwin);
+void tk_r2t_free(tk_r2t *r2t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,744 @@
+/*
+ * oracle.c -- CPU restatement of Trinity's k-mer hot path (TEST INFRASTRUCTURE).
+ *
+ * Only the test suite, __graft_entry__.smoke() and bench.py's CPU-baseline /
+ * reference arm load this file's library, and only as the checker or the
+ * timed CPU reference.  The shipped GPU library never touches it.
+ *
+ * What it restates (reference file:line of each behaviour):
+ *  - record parsing: PerlLib/Fasta_reader.pm:45-73 (records split at '>' lines,
+ *    sequence = lines joined with all whitespace removed) and Sequence->new,
+ *    PerlLib/Fasta_reader.pm:107-118 (accession = first whitespace token);
+ *    FASTQ 4-line records as util/support_scripts/fastQ_to_fastA.pl:80-106.
+ *  - k-mer windows: every length-k substring, util/misc/print_kmers.pl:19-27;
+ *    a window holding a base other than A/C/G/T (any case) is not a k-mer
+ *    (jellyfish 2.3.0, called at Trinity:2612-2619).
+ *  - canonical counting: util/misc/kmer_counter.pl:26-37 counts a window and
+ *    its reverse complement in DS mode; jellyfish --canonical keeps one key, the
+ *    lexicographically smaller strand (A<C<G<T), which is the same count for
+ *    odd k.
+ *  - dump ">COUNT\nKMER\n" with -L: Trinity:2625, util/insilico_read_normalization.pl:641.
+ *  - histo "<count> <n>" lines, overflow bin high+1:
+ *    util/misc/insilico_norm_kmer_hists/kmer_histo.all.txt:1-10001.
+ *  - coverage stats: util/insilico_read_normalization.pl:837-846 (tool call),
+ *    Changelog.txt:536-538 (a k-mer missing from the -L 2 catalogue counts 1,
+ *    unsigned counters), Changelog.txt:423-424 (an empty read is a row, not EOF);
+ *    columns acc/median_cov/mean_cov/stdev consumed by name at
+ *    util/support_scripts/nbkc_normalize.pl:85-97 and
+ *    nbkc_merge_left_right_stats.pl:95-103, acc first for `sort -k1,1`
+ *    (util/insilico_read_normalization.pl:874).
+ *  - ReadsToTranscripts: Trinity:2237-2251 (tool call), Changelog.txt:467
+ *    (reads upper-cased), Changelog.txt:870-873 (-p min percent of a read's
+ *    k-mers), bundle format util/support_scripts/add_LR_reads_to_iworm_bundle.pl:19-47,
+ *    output columns Trinity:2474 and partition_chrysalis_graphs_n_reads.pl:103.
+ *
+ * Documented decisions (not pinned by any file of the reference tree):
+ *  D1 median of n values = the element at index n/2 of the ascending sort.
+ *  D2 mean = (float)((double)sum / n); stdev = population standard deviation,
+ *     (float)sqrt(((double)hi * 2^64 + (double)lo) / ((double)n * n)) where
+ *     hi:lo = n*sum(v^2) - sum(v)^2 computed exactly in 128-bit integers.
+ *     Both printed with C's %g (the default precision of a C++ ostream).
+ *  D3 windows holding a non-ACGT base are skipped by the statistics; a read with
+ *     no valid window prints median 0, mean 0, stdev 0.
+ *  D4 ReadsToTranscripts: a k-mer found in several bundle records belongs to the
+ *     first record holding it; a read votes once per valid window for the record
+ *     owning that window's k-mer; the winner is the record with most votes,
+ *     ties to the earlier record; pct = floor(100 * votes / (L - k + 1)); a read
+ *     with no vote, shorter than k, or pct < -p is not written.
+ *  D5 the component id is the integer after "s_" in the bundle header; a header
+ *     without it takes its record ordinal.
+ */
+#include "oracle.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_E_INVAL (-1)
+#define ORC_E_OOM (-3)
+#define ORC_E_PARSE (-4)
+
+static const uint64_t EMPTY = ~0ULL;
+
+/* ---------------------------------------------------------------- parsing */
+
+typedef struct {
+    size_t n, cap;
+    size_t *acc_off;   /* accession start in the input text */
+    uint32_t *acc_len;
+    size_t *seq_off;   /* sequence start in seqbuf */
+    uint32_t *seq_len;
+    char *seqbuf;
+    size_t seqlen, seqcap;
+} recs_t;
+
+static int is_ws(unsigned char c) {
+    return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\f' || c == '\v';
+}
+
+static void recs_free(recs_t *r) {
+    free(r->acc_off); free(r->acc_len); free(r->seq_off); free(r->seq_len);
+    free(r->seqbuf);
+    memset(r, 0, sizeof(*r));
+}
+
+static int recs_push(recs_t *r, size_t acc_off, uint32_t acc_len) {
+    if (r->n == r->cap) {
+        size_t nc = r->cap ? r->cap * 2 : 1024;
+        size_t *a = realloc(r->acc_off, nc * sizeof(size_t));
+        uint32_t *b = realloc(r->acc_len, nc * sizeof(uint32_t));
+        size_t *c = realloc(r->seq_off, nc * sizeof(size_t));
+        uint32_t *d = realloc(r->seq_len, nc * sizeof(uint32_t));
+        if (!a || !b || !c || !d) return ORC_E_OOM;
+        r->acc_off = a; r->acc_len = b; r->seq_off = c; r->seq_len = d;
+        r->cap = nc;
+    }
+    r->acc_off[r->n] = acc_off;
+    r->acc_len[r->n] = acc_len;
+    r->seq_off[r->n] = r->seqlen;
+    r->seq_len[r->n] = 0;
+    r->n++;
+    return 0;
+}
+
+static int recs_append(recs_t *r, const char *p, size_t len) {
+    if (r->seqlen + len + 1 > r->seqcap) {
+        size_t nc = r->seqcap ? r->seqcap : 1 << 20;
+        while (nc < r->seqlen + len + 1) nc *= 2;
+        char *b = realloc(r->seqbuf, nc);
+        if (!b) return ORC_E_OOM;
+        r->seqbuf = b; r->seqcap = nc;
+    }
+    for (size_t i = 0; i < len; i++) {
+        unsigned char c = (unsigned char)p[i];
+        if (!is_ws(c)) r->seqbuf[r->seqlen++] = (char)c;
+    }
+    r->seq_len[r->n - 1] = (uint32_t)(r->seqlen - r->seq_off[r->n - 1]);
+    return 0;
+}
+
+/* first whitespace-delimited token of the header line starting at h */
+static uint32_t token_len(const char *h, const char *end) {
+    const char *q = h;
+    while (q < end && !is_ws((unsigned char)*q)) q++;
+    return (uint32_t)(q - h);
+}
+
+static int parse_records(const char *text, size_t len, recs_t *r) {
+    memset(r, 0, sizeof(*r));
+    size_t i = 0;
+    while (i < len && is_ws((unsigned char)text[i])) i++;
+    if (i == len) return 0;
+    const char *end = text + len;
+    if (text[i] == '@') {
+        /* FASTQ: header, sequence, '+' line, quality */
+        size_t line = 0;
+        size_t pos = i;
+        while (pos < len) {
+            const char *ls = text + pos;
+            const char *nl = memchr(ls, '\n', (size_t)(end - ls));
+            const char *le = nl ? nl : end;
+            size_t ll = (size_t)(le - ls);
+            int kind = (int)(line & 3);
+            if (kind == 0) {
+                if (ll == 0) {  /* trailing blank lines end the file */
+                    size_t q = pos;
+                    while (q < len && is_ws((unsigned char)text[q])) q++;
+                    if (q == len) break;
+                    recs_free(r); return ORC_E_PARSE;
+                }
+                if (ls[0] != '@') { recs_free(r); return ORC_E_PARSE; }
+                int e = recs_push(r, (size_t)(ls + 1 - text), token_len(ls + 1, le));
+                if (e) { recs_free(r); return e; }
+            } else if (kind == 1) {
+                int e = recs_append(r, ls, ll);
+                if (e) { recs_free(r); return e; }
+            } else if (kind == 2) {
+                if (ll == 0 || ls[0] != '+') { recs_free(r); return ORC_E_PARSE; }
+            }
+            line++;
+            pos = (size_t)(le - text) + 1;
+        }
+        if ((line & 3) != 0) { recs_free(r); return ORC_E_PARSE; }
+        return 0;
+    }
+    /* FASTA */
+    size_t pos = i;
+    int in_rec = 0;
+    while (pos < len) {
+        const char *ls = text + pos;
+        const char *nl = memchr(ls, '\n', (size_t)(end - ls));
+        const char *le = nl ? nl : end;
+        if (le > ls && ls[0] == '>') {
+            int e = recs_push(r, (size_t)(ls + 1 - text), token_len(ls + 1, le));
+            if (e) { recs_free(r); return e; }
+            in_rec = 1;
+        } else if (in_rec) {
+            int e = recs_append(r, ls, (size_t)(le - ls));
+            if (e) { recs_free(r); return e; }
+        }
+        pos = (size_t)(le - text) + 1;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------- k-mers */
+
+static inline int base_code(unsigned char c) {
+    switch (c) {
+    case 'A': case 'a': return 0;
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+    default: return -1;
+    }
+}
+
+static inline uint64_t mix64(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33; return x;
+}
+
+/* Calls fn(key, window_index) for each valid window of seq. */
+#define FOR_EACH_KMER(seq, L, k, canonical, KEY, WIN, ...)                    \
+    do {                                                                       \
+        uint64_t _mask = (k) == 32 ? ~0ULL : ((1ULL << (2 * (k))) - 1);       \
+        int _shift = 2 * ((k) - 1);                                            \
+        uint64_t _fw = 0, _rc = 0;                                             \
+        int _run = 0;                                                          \
+        for (size_t _p = 0; _p < (size_t)(L); _p++) {                          \
+            int _c = base_code((unsigned char)(seq)[_p]);                      \
+            if (_c < 0) { _run = 0; continue; }                                \
+            _fw = ((_fw << 2) | (uint64_t)_c) & _mask;                         \
+            _rc = (_rc >> 2) | ((uint64_t)(3 - _c) << _shift);                 \
+            if (++_run >= (k)) {                                               \
+                uint64_t KEY = (canonical) && _rc < _fw ? _rc : _fw;           \
+                size_t WIN = _p + 1 - (size_t)(k);                             \
+                (void)WIN;                                                     \
+                __VA_ARGS__                                                    \
+            }                                                                  \
+        }                                                                      \
+    } while (0)
+
+/* Lock-free open-addressing table (keys + u32 values), CPU side. */
+typedef struct {
+    uint64_t *keys;
+    uint32_t *vals;
+    uint64_t mask;
+} ctab_t;
+
+static int ctab_init(ctab_t *t, uint64_t want, uint32_t init_val) {
+    uint64_t cap = 1024;
+    while (cap < want) cap <<= 1;
+    t->keys = malloc(cap * sizeof(uint64_t));
+    t->vals = malloc(cap * sizeof(uint32_t));
+    if (!t->keys || !t->vals) { free(t->keys); free(t->vals); return ORC_E_OOM; }
+    t->mask = cap - 1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)cap; i++) { t->keys[i] = EMPTY; t->vals[i] = init_val; }
+    return 0;
+}
+
+static void ctab_free(ctab_t *t) { free(t->keys); free(t->vals); t->keys = NULL; t->vals = NULL; }
+
+static uint64_t ctab_slot(ctab_t *t, uint64_t key) {
+    uint64_t s = mix64(key) & t->mask;
+    for (;;) {
+        uint64_t cur = __atomic_load_n(&t->keys[s], __ATOMIC_ACQUIRE);
+        if (cur == key) return s;
+        if (cur == EMPTY) {
+            uint64_t exp = EMPTY;
+            if (__atomic_compare_exchange_n(&t->keys[s], &exp, key, 0,
+                                            __ATOMIC_ACQ_REL, __ATOMIC_ACQUIRE))
+                return s;
+            if (exp == key) return s;
+        }
+        s = (s + 1) & t->mask;
+    }
+}
+
+static int ctab_find(const ctab_t *t, uint64_t key, uint32_t *val) {
+    uint64_t s = mix64(key) & t->mask;
+    for (;;) {
+        uint64_t cur = t->keys[s];
+        if (cur == key) { *val = t->vals[s]; return 1; }
+        if (cur == EMPTY) return 0;
+        s = (s + 1) & t->mask;
+    }
+}
+
+static int set_threads(int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+    return omp_get_max_threads();
+#else
+    (void)threads;
+    return 1;
+#endif
+}
+
+typedef struct { uint64_t k; uint32_t c; } kc_t;
+
+static int cmp_kc(const void *a, const void *b) {
+    uint64_t x = ((const kc_t *)a)->k, y = ((const kc_t *)b)->k;
+    return x < y ? -1 : x > y;
+}
+
+static int extract_table(ctab_t *t, int sorted, uint64_t **keys, uint32_t **counts, uint64_t *n) {
+    uint64_t cap = t->mask + 1, m = 0;
+    for (uint64_t i = 0; i < cap; i++) m += t->keys[i] != EMPTY;
+    kc_t *kc = malloc((m ? m : 1) * sizeof(kc_t));
+    uint64_t *ko = malloc((m ? m : 1) * sizeof(uint64_t));
+    uint32_t *co = malloc((m ? m : 1) * sizeof(uint32_t));
+    if (!kc || !ko || !co) { free(kc); free(ko); free(co); return ORC_E_OOM; }
+    uint64_t j = 0;
+    for (uint64_t i = 0; i < cap; i++)
+        if (t->keys[i] != EMPTY) { kc[j].k = t->keys[i]; kc[j].c = t->vals[i]; j++; }
+    if (sorted) qsort(kc, m, sizeof(kc_t), cmp_kc);
+    for (uint64_t i = 0; i < m; i++) { ko[i] = kc[i].k; co[i] = kc[i].c; }
+    free(kc);
+    *keys = ko; *counts = co; *n = m;
+    return 0;
+}
+
+int orc_count(const char *text, size_t len, int k, int canonical, int threads,
+              int sorted, uint64_t **keys, uint32_t **counts, uint64_t *n) {
+    if (k < 1 || k > 31 || !keys || !counts || !n) return ORC_E_INVAL;
+    set_threads(threads);
+    recs_t r;
+    int e = parse_records(text, len, &r);
+    if (e) return e;
+    uint64_t windows = 0;
+    for (size_t i = 0; i < r.n; i++)
+        if (r.seq_len[i] >= (uint32_t)k) windows += r.seq_len[i] - k + 1;
+    ctab_t t;
+    e = ctab_init(&t, windows + windows / 2 + 16, 0);
+    if (e) { recs_free(&r); return e; }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)r.n; i++) {
+        const char *s = r.seqbuf + r.seq_off[i];
+        FOR_EACH_KMER(s, r.seq_len[i], k, canonical, key, w, {
+            uint64_t slot = ctab_slot(&t, key);
+            __atomic_fetch_add(&t.vals[slot], 1u, __ATOMIC_RELAXED);
+        });
+    }
+    recs_free(&r);
+    e = extract_table(&t, sorted, keys, counts, n);
+    ctab_free(&t);
+    return e;
+}
+
+void orc_histo(const uint32_t *counts, uint64_t n, uint64_t low, uint64_t high, uint64_t *hist) {
+    uint64_t nb = high - low + 3;
+    memset(hist, 0, nb * sizeof(uint64_t));
+    for (uint64_t i = 0; i < n; i++) {
+        uint64_t c = counts[i];
+        if (c < low) hist[0]++;
+        else if (c > high) hist[nb - 1]++;
+        else hist[1 + c - low]++;
+    }
+}
+
+static const char BASES[4] = {'A', 'C', 'G', 'T'};
+
+int orc_dump(const uint64_t *keys, const uint32_t *counts, uint64_t n, int k,
+             uint32_t min_count, char **out, size_t *out_len) {
+    size_t cap = 1024, m = 0;
+    for (uint64_t i = 0; i < n; i++) if (counts[i] >= min_count) cap += (size_t)k + 14;
+    char *b = malloc(cap);
+    if (!b) return ORC_E_OOM;
+    for (uint64_t i = 0; i < n; i++) {
+        if (counts[i] < min_count) continue;
+        m += (size_t)sprintf(b + m, ">%u\n", counts[i]);
+        for (int j = 0; j < k; j++) b[m++] = BASES[(keys[i] >> (2 * (k - 1 - j))) & 3];
+        b[m++] = '\n';
+    }
+    *out = b; *out_len = m;
+    return 0;
+}
+
+static uint64_t revcomp(uint64_t fw, int k) {
+    uint64_t rc = 0;
+    for (int i = 0; i < k; i++) { rc = (rc << 2) | (3 - (fw & 3)); fw >>= 2; }
+    return rc;
+}
+
+int orc_load_dump(const char *text, size_t len, int k, int canonical,
+                  uint64_t **keys, uint32_t **counts, uint64_t *n) {
+    if (k < 1 || k > 31) return ORC_E_INVAL;
+    recs_t r;
+    int e = parse_records(text, len, &r);
+    if (e) return e;
+    kc_t *kc = malloc((r.n ? r.n : 1) * sizeof(kc_t));
+    if (!kc) { recs_free(&r); return ORC_E_OOM; }
+    for (size_t i = 0; i < r.n; i++) {
+        const char *h = text + r.acc_off[i];
+        uint64_t c = 0;
+        if (r.acc_len[i] == 0) { free(kc); recs_free(&r); return ORC_E_PARSE; }
+        for (uint32_t j = 0; j < r.acc_len[i]; j++) {
+            if (h[j] < '0' || h[j] > '9') { free(kc); recs_free(&r); return ORC_E_PARSE; }
+            c = c * 10 + (uint64_t)(h[j] - '0');
+        }
+        if (r.seq_len[i] != (uint32_t)k) { free(kc); recs_free(&r); return ORC_E_PARSE; }
+        uint64_t fw = 0;
+        for (int j = 0; j < k; j++) {
+            int b = base_code((unsigned char)r.seqbuf[r.seq_off[i] + j]);
+            if (b < 0) { free(kc); recs_free(&r); return ORC_E_PARSE; }
+            fw = (fw << 2) | (uint64_t)b;
+        }
+        if (canonical) { uint64_t rc = revcomp(fw, k); if (rc < fw) fw = rc; }
+        kc[i].k = fw;
+        kc[i].c = c > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)c;
+    }
+    size_t m = r.n;
+    recs_free(&r);
+    qsort(kc, m, sizeof(kc_t), cmp_kc);
+    /* duplicates (possible when a non-canonical dump is loaded canonically) add */
+    size_t j = 0;
+    for (size_t i = 0; i < m; i++) {
+        if (j && kc[j - 1].k == kc[i].k) {
+            uint64_t s = (uint64_t)kc[j - 1].c + kc[i].c;
+            kc[j - 1].c = s > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)s;
+        } else kc[j++] = kc[i];
+    }
+    uint64_t *ko = malloc((j ? j : 1) * sizeof(uint64_t));
+    uint32_t *co = malloc((j ? j : 1) * sizeof(uint32_t));
+    if (!ko || !co) { free(ko); free(co); free(kc); return ORC_E_OOM; }
+    for (size_t i = 0; i < j; i++) { ko[i] = kc[i].k; co[i] = kc[i].c; }
+    free(kc);
+    *keys = ko; *counts = co; *n = j;
+    return 0;
+}
+
+/* ---------------------------------------------------------------- stats */
+
+static int cmp_u32(const void *a, const void *b) {
+    uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+    return x < y ? -1 : x > y;
+}
+
+static int build_lookup(ctab_t *t, const uint64_t *keys, const uint32_t *counts, uint64_t n) {
+    int e = ctab_init(t, 2 * n + 16, 0);
+    if (e) return e;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        uint64_t s = ctab_slot(t, keys[i]);
+        t->vals[s] = counts[i];
+    }
+    return 0;
+}
+
+/* Per-read statistics of one read (decisions D1-D3). */
+static void read_stats(const ctab_t *t, const char *s, uint32_t L, int k, int ds,
+                       uint32_t *vals, uint32_t *nv, uint32_t *median, float *mean, float *stdev) {
+    uint32_t m = 0;
+    FOR_EACH_KMER(s, L, k, ds, key, w, {
+        uint32_t c = 1;
+        uint32_t got;
+        if (ctab_find(t, key, &got)) c = got;
+        vals[m++] = c;
+    });
+    *nv = m;
+    if (m == 0) { *median = 0; *mean = 0.0f; *stdev = 0.0f; return; }
+    uint64_t sum = 0;
+    unsigned __int128 sumsq = 0;
+    for (uint32_t i = 0; i < m; i++) {
+        sum += vals[i];
+        sumsq += (unsigned __int128)vals[i] * vals[i];
+    }
+    uint32_t *tmp = vals + m;
+    memcpy(tmp, vals, m * sizeof(uint32_t));
+    qsort(tmp, m, sizeof(uint32_t), cmp_u32);
+    *median = tmp[m / 2];
+    *mean = (float)((double)sum / (double)m);
+    unsigned __int128 num = (unsigned __int128)m * sumsq - (unsigned __int128)sum * sum;
+    double hi = (double)(uint64_t)(num >> 64), lo = (double)(uint64_t)num;
+    double var = (hi * 18446744073709551616.0 + lo) / ((double)m * (double)m);
+    *stdev = (float)sqrt(var);
+}
+
+typedef struct { char *b; size_t n, cap; } sbuf_t;
+
+static int sb_reserve(sbuf_t *s, size_t extra) {
+    if (s->n + extra <= s->cap) return 0;
+    size_t nc = s->cap ? s->cap : 4096;
+    while (nc < s->n + extra) nc *= 2;
+    char *b = realloc(s->b, nc);
+    if (!b) return ORC_E_OOM;
+    s->b = b; s->cap = nc;
+    return 0;
+}
+
+static int concat_chunks(sbuf_t *chunks, int nchunks, const char *head, char **out, size_t *out_len) {
+    size_t total = strlen(head);
+    for (int c = 0; c < nchunks; c++) total += chunks[c].n;
+    char *o = malloc(total + 1);
+    if (!o) return ORC_E_OOM;
+    size_t m = strlen(head);
+    memcpy(o, head, m);
+    for (int c = 0; c < nchunks; c++) { memcpy(o + m, chunks[c].b, chunks[c].n); m += chunks[c].n; }
+    o[m] = 0;
+    *out = o; *out_len = m;
+    return 0;
+}
+
+#define CHUNK_READS 4096
+
+int orc_cov_stats(const char *reads, size_t len, const uint64_t *keys,
+                  const uint32_t *counts, uint64_t n, int k, int ds,
+                  int capture, int threads, char **out, size_t *out_len) {
+    if (k < 1 || k > 31) return ORC_E_INVAL;
+    set_threads(threads);
+    recs_t r;
+    int e = parse_records(reads, len, &r);
+    if (e) return e;
+    ctab_t t;
+    e = build_lookup(&t, keys, counts, n);
+    if (e) { recs_free(&r); return e; }
+    uint32_t maxlen = 0;
+    for (size_t i = 0; i < r.n; i++) if (r.seq_len[i] > maxlen) maxlen = r.seq_len[i];
+    int nchunks = (int)((r.n + CHUNK_READS - 1) / CHUNK_READS);
+    sbuf_t *chunks = calloc((size_t)(nchunks ? nchunks : 1), sizeof(sbuf_t));
+    int err = 0;
+#pragma omp parallel
+    {
+        uint32_t *vals = malloc(2 * ((size_t)maxlen + 1) * sizeof(uint32_t));
+#pragma omp for schedule(dynamic, 1)
+        for (int c = 0; c < nchunks; c++) {
+            sbuf_t *sb = &chunks[c];
+            size_t lo = (size_t)c * CHUNK_READS, hi = lo + CHUNK_READS;
+            if (hi > r.n) hi = r.n;
+            for (size_t i = lo; i < hi; i++) {
+                uint32_t med, nv; float mean, sd;
+                read_stats(&t, r.seqbuf + r.seq_off[i], r.seq_len[i], k, ds, vals, &nv, &med, &mean, &sd);
+                if (sb_reserve(sb, r.acc_len[i] + 64 + (capture ? (size_t)nv * 11 : 0))) { err = ORC_E_OOM; continue; }
+                sb->n += (size_t)sprintf(sb->b + sb->n, "%.*s\t%u\t%g\t%g", (int)r.acc_len[i],
+                                         reads + r.acc_off[i], med, (double)mean, (double)sd);
+                if (capture) {
+                    sb->b[sb->n++] = '\t';
+                    for (uint32_t j = 0; j < nv; j++)
+                        sb->n += (size_t)sprintf(sb->b + sb->n, j ? ",%u" : "%u", vals[j]);
+                }
+                sb->b[sb->n++] = '\n';
+            }
+        }
+        free(vals);
+    }
+    ctab_free(&t);
+    recs_free(&r);
+    if (!err)
+        err = concat_chunks(chunks, nchunks,
+                            capture ? "acc\tmedian_cov\tmean_cov\tstdev\tkmer_coverage\n"
+                                    : "acc\tmedian_cov\tmean_cov\tstdev\n",
+                            out, out_len);
+    for (int c = 0; c < nchunks; c++) free(chunks[c].b);
+    free(chunks);
+    return err;
+}
+
+int orc_cov_values(const char *reads, size_t len, const uint64_t *keys,
+                   const uint32_t *counts, uint64_t n, int k, int ds,
+                   int threads, uint64_t *n_reads, uint32_t **median,
+                   float **mean, float **stdev) {
+    if (k < 1 || k > 31) return ORC_E_INVAL;
+    set_threads(threads);
+    recs_t r;
+    int e = parse_records(reads, len, &r);
+    if (e) return e;
+    ctab_t t;
+    e = build_lookup(&t, keys, counts, n);
+    if (e) { recs_free(&r); return e; }
+    uint32_t maxlen = 0;
+    for (size_t i = 0; i < r.n; i++) if (r.seq_len[i] > maxlen) maxlen = r.seq_len[i];
+    uint32_t *md = malloc((r.n ? r.n : 1) * sizeof(uint32_t));
+    float *mn = malloc((r.n ? r.n : 1) * sizeof(float));
+    float *sd = malloc((r.n ? r.n : 1) * sizeof(float));
+#pragma omp parallel
+    {
+        uint32_t *vals = malloc(2 * ((size_t)maxlen + 1) * sizeof(uint32_t));
+#pragma omp for schedule(dynamic, 1024)
+        for (int64_t i = 0; i < (int64_t)r.n; i++) {
+            uint32_t nv;
+            read_stats(&t, r.seqbuf + r.seq_off[i], r.seq_len[i], k, ds, vals, &nv, &md[i], &mn[i], &sd[i]);
+        }
+        free(vals);
+    }
+    *n_reads = r.n;
+    *median = md; *mean = mn; *stdev = sd;
+    ctab_free(&t);
+    recs_free(&r);
+    return 0;
+}
+
+/* ---------------------------------------------------------------- R2T */
+
+typedef struct {
+    ctab_t t;
+    uint64_t nrec;
+    uint64_t *comp_id;
+} r2t_t;
+
+static int r2t_build(r2t_t *z, const char *bundle, size_t blen, int k, int strand) {
+    recs_t b;
+    int e = parse_records(bundle, blen, &b);
+    if (e) return e;
+    uint64_t windows = 0;
+    for (size_t i = 0; i < b.n; i++)
+        if (b.seq_len[i] >= (uint32_t)k) windows += b.seq_len[i] - k + 1;
+    e = ctab_init(&z->t, 2 * windows + 16, 0xFFFFFFFFu);
+    if (e) { recs_free(&b); return e; }
+    z->nrec = b.n;
+    z->comp_id = malloc((b.n ? b.n : 1) * sizeof(uint64_t));
+    for (size_t i = 0; i < b.n; i++) {
+        const char *h = bundle + b.acc_off[i];
+        uint32_t hl = b.acc_len[i];
+        uint64_t id = i;
+        if (hl > 2 && h[0] == 's' && h[1] == '_' && h[2] >= '0' && h[2] <= '9') {
+            id = 0;
+            for (uint32_t j = 2; j < hl && h[j] >= '0' && h[j] <= '9'; j++) id = id * 10 + (uint64_t)(h[j] - '0');
+        }
+        z->comp_id[i] = id;
+    }
+    /* serial in record order: the first record holding a k-mer owns it (D4) */
+    for (size_t i = 0; i < b.n; i++) {
+        const char *s = b.seqbuf + b.seq_off[i];
+        FOR_EACH_KMER(s, b.seq_len[i], k, !strand, key, w, {
+            uint64_t slot = ctab_slot(&z->t, key);
+            if (z->t.vals[slot] > (uint32_t)i) z->t.vals[slot] = (uint32_t)i;
+        });
+    }
+    recs_free(&b);
+    return 0;
+}
+
+static void r2t_read(const r2t_t *z, const char *s, uint32_t L, int k, int strand,
+                     uint32_t *buf, int32_t *rec, uint32_t *hits, uint32_t *nwin) {
+    *rec = -1; *hits = 0; *nwin = L >= (uint32_t)k ? L - k + 1 : 0;
+    uint32_t m = 0;
+    FOR_EACH_KMER(s, L, k, !strand, key, w, {
+        uint32_t v;
+        if (ctab_find(&z->t, key, &v)) buf[m++] = v;
+    });
+    if (!m) return;
+    qsort(buf, m, sizeof(uint32_t), cmp_u32);
+    uint32_t best = 0, bestv = 0;
+    for (uint32_t i = 0; i < m;) {
+        uint32_t j = i;
+        while (j < m && buf[j] == buf[i]) j++;
+        if (j - i > best) { best = j - i; bestv = buf[i]; }
+        i = j;
+    }
+    *rec = (int32_t)bestv; *hits = best;
+}
+
+int orc_r2t_values(const char *reads, size_t rlen, const char *bundle,
+                   size_t blen, int k, int strand, int threads,
+                   uint64_t *n_reads, int32_t **rec, uint32_t **hits,
+                   uint32_t **nwin) {
+    if (k < 1 || k > 31) return ORC_E_INVAL;
+    set_threads(threads);
+    r2t_t z;
+    int e = r2t_build(&z, bundle, blen, k, strand);
+    if (e) return e;
+    recs_t r;
+    e = parse_records(reads, rlen, &r);
+    if (e) { ctab_free(&z.t); free(z.comp_id); return e; }
+    uint32_t maxlen = 0;
+    for (size_t i = 0; i < r.n; i++) if (r.seq_len[i] > maxlen) maxlen = r.seq_len[i];
+    int32_t *rc = malloc((r.n ? r.n : 1) * sizeof(int32_t));
+    uint32_t *h = malloc((r.n ? r.n : 1) * sizeof(uint32_t));
+    uint32_t *nw = malloc((r.n ? r.n : 1) * sizeof(uint32_t));
+#pragma omp parallel
+    {
+        uint32_t *buf = malloc(((size_t)maxlen + 1) * sizeof(uint32_t));
+#pragma omp for schedule(dynamic, 1024)
+        for (int64_t i = 0; i < (int64_t)r.n; i++)
+            r2t_read(&z, r.seqbuf + r.seq_off[i], r.seq_len[i], k, strand, buf, &rc[i], &h[i], &nw[i]);
+        free(buf);
+    }
+    *n_reads = r.n; *rec = rc; *hits = h; *nwin = nw;
+    recs_free(&r);
+    ctab_free(&z.t);
+    free(z.comp_id);
+    return 0;
+}
+
+int orc_r2t(const char *reads, size_t rlen, const char *bundle, size_t blen,
+            int k, int strand, int min_pct, int threads, char **out,
+            size_t *out_len) {
+    if (k < 1 || k > 31) return ORC_E_INVAL;
+    set_threads(threads);
+    r2t_t z;
+    int e = r2t_build(&z, bundle, blen, k, strand);
+    if (e) return e;
+    recs_t r;
+    e = parse_records(reads, rlen, &r);
+    if (e) { ctab_free(&z.t); free(z.comp_id); return e; }
+    uint32_t maxlen = 0;
+    for (size_t i = 0; i < r.n; i++) if (r.seq_len[i] > maxlen) maxlen = r.seq_len[i];
+    int nchunks = (int)((r.n + CHUNK_READS - 1) / CHUNK_READS);
+    sbuf_t *chunks = calloc((size_t)(nchunks ? nchunks : 1), sizeof(sbuf_t));
+    int err = 0;
+#pragma omp parallel
+    {
+        uint32_t *buf = malloc(((size_t)maxlen + 1) * sizeof(uint32_t));
+#pragma omp for schedule(dynamic, 1)
+        for (int c = 0; c < nchunks; c++) {
+            sbuf_t *sb = &chunks[c];
+            size_t lo = (size_t)c * CHUNK_READS, hi = lo + CHUNK_READS;
+            if (hi > r.n) hi = r.n;
+            for (size_t i = lo; i < hi; i++) {
+                int32_t rec; uint32_t hits, nw;
+                const char *s = r.seqbuf + r.seq_off[i];
+                r2t_read(&z, s, r.seq_len[i], k, strand, buf, &rec, &hits, &nw);
+                if (rec < 0) continue;
+                uint32_t pct = (uint32_t)((100ull * hits) / nw);
+                if (min_pct > 0 && pct < (uint32_t)min_pct) continue;
+                if (sb_reserve(sb, r.acc_len[i] + r.seq_len[i] + 64)) { err = ORC_E_OOM; continue; }
+                sb->n += (size_t)sprintf(sb->b + sb->n, "%llu\t>%.*s\t%u\t",
+                                         (unsigned long long)z.comp_id[rec], (int)r.acc_len[i],
+                                         reads + r.acc_off[i], pct);
+                for (uint32_t j = 0; j < r.seq_len[i]; j++) {
+                    char ch = s[j];
+                    sb->b[sb->n++] = (ch >= 'a' && ch <= 'z') ? (char)(ch - 32) : ch;
+                }
+                sb->b[sb->n++] = '\n';
+            }
+        }
+        free(buf);
+    }
+    recs_free(&r);
+    ctab_free(&z.t);
+    free(z.comp_id);
+    if (!err) err = concat_chunks(chunks, nchunks, "", out, out_len);
+    for (int c = 0; c < nchunks; c++) free(chunks[c].b);
+    free(chunks);
+    return err;
+}
+
+int orc_records(const char *text, size_t len, char **out, size_t *out_len) {
+    recs_t r;
+    int e = parse_records(text, len, &r);
+    if (e) return e;
+    size_t cap = 16;
+    for (size_t i = 0; i < r.n; i++) cap += r.acc_len[i] + r.seq_len[i] + 2;
+    char *o = malloc(cap);
+    if (!o) { recs_free(&r); return ORC_E_OOM; }
+    size_t m = 0;
+    for (size_t i = 0; i < r.n; i++) {
+        memcpy(o + m, text + r.acc_off[i], r.acc_len[i]); m += r.acc_len[i];
+        o[m++] = '\t';
+        memcpy(o + m, r.seqbuf + r.seq_off[i], r.seq_len[i]); m += r.seq_len[i];
+        o[m++] = '\n';
+    }
+    recs_free(&r);
+    *out = o; *out_len = m;
+    return 0;
+}
+
+void orc_free(void *p) { free(p); }

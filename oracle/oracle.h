@@ -1,0 +1,86 @@
+/*
+ * oracle.h -- CPU restatement of Trinity's k-mer hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library, the command-line
+ * tools or the serving daemon links, loads or calls this code.  Only the test
+ * suite, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, and
+ * there only as the checker / the timed CPU reference.
+ *
+ * Parity status: the reference's own implementations of these three tools are
+ * NOT part of the reference checkout (Inchworm and Chrysalis are empty git
+ * submodules, .gitmodules:8-13; jellyfish is an external binary pinned to
+ * 2.3.0, Docker/Dockerfile:179-183).  The counting semantics are pinned against
+ * the reference's own Perl k-mer counter (util/misc/kmer_counter.pl with
+ * PerlLib/Ktree.pm) and window enumerator (util/misc/print_kmers.pl) through
+ * committed golden fixtures; the histogram format against
+ * util/misc/insilico_norm_kmer_hists/kmer_histo.all.txt; the coverage-stats
+ * and readsToComponents column layouts against their live Perl consumers
+ * (util/support_scripts/nbkc_merge_left_right_stats.pl, nbkc_normalize.pl,
+ * Trinity:2471-2497, partition_chrysalis_graphs_n_reads.pl:98-118).
+ * The arithmetic of the statistics (median of an even count, mean/stdev
+ * formula and print precision) and the ReadsToTranscripts vote rules are not
+ * pinned by anything in the reference tree: "parity unpinned" for those, and
+ * the decisions below are documented ones.
+ */
+#ifndef TRINKMER_ORACLE_H
+#define TRINKMER_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Count every k-mer of every record (FASTA or FASTQ).  canonical != 0 merges a
+ * k-mer with its reverse complement under the smaller 2-bit code (jellyfish
+ * count --canonical, called at Trinity:2612-2619).  Output sorted by key when
+ * sorted != 0, else in hash-table order.  Returns 0 or a negative error. */
+int orc_count(const char *text, size_t len, int k, int canonical, int threads,
+              int sorted, uint64_t **keys, uint32_t **counts, uint64_t *n);
+
+/* jellyfish histo --low low --high high: hist[0] = counts < low,
+ * hist[1 + c - low] for low <= c <= high, hist[high - low + 2] = counts > high. */
+void orc_histo(const uint32_t *counts, uint64_t n, uint64_t low, uint64_t high,
+               uint64_t *hist);
+
+/* jellyfish dump -L min_count: ">COUNT\nKMER\n" records in array order. */
+int orc_dump(const uint64_t *keys, const uint32_t *counts, uint64_t n, int k,
+             uint32_t min_count, char **out, size_t *out_len);
+
+/* Parse a dump back into (key, count) pairs sorted by key; canonical != 0
+ * canonicalises each k-mer (fastaToKmerCoverageStats --DS lookups). */
+int orc_load_dump(const char *text, size_t len, int k, int canonical,
+                  uint64_t **keys, uint32_t **counts, uint64_t *n);
+
+/* fastaToKmerCoverageStats: one row per read (input order) after a header row.
+ * keys/counts: sorted table from orc_count or orc_load_dump. */
+int orc_cov_stats(const char *reads, size_t len, const uint64_t *keys,
+                  const uint32_t *counts, uint64_t n, int k, int ds,
+                  int capture, int threads, char **out, size_t *out_len);
+
+/* Raw per-read statistics (no text), for bit-level comparisons. */
+int orc_cov_values(const char *reads, size_t len, const uint64_t *keys,
+                   const uint32_t *counts, uint64_t n, int k, int ds,
+                   int threads, uint64_t *n_reads, uint32_t **median,
+                   float **mean, float **stdev);
+
+/* ReadsToTranscripts: rows "comp\t>acc\tpct\tSEQ\n" in read order. */
+int orc_r2t(const char *reads, size_t rlen, const char *bundle, size_t blen,
+            int k, int strand, int min_pct, int threads, char **out,
+            size_t *out_len);
+
+/* Raw per-read assignment: comp record index (-1 = unassigned), hits, windows. */
+int orc_r2t_values(const char *reads, size_t rlen, const char *bundle,
+                   size_t blen, int k, int strand, int threads,
+                   uint64_t *n_reads, int32_t **rec, uint32_t **hits,
+                   uint32_t **nwin);
+
+/* "acc\tsequence\n" per parsed record (the parse the other calls use). */
+int orc_records(const char *text, size_t len, char **out, size_t *out_len);
+
+void orc_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,142 @@
+"""GPU parity of parsing (K1), counting (K2), histo/dump (K3/K4) and
+catalogue loading against the CPU oracle, through the C ABI.  Integer work:
+bit-exact."""
+import numpy as np
+import pytest
+
+from trinityrnaseq_gb300 import KmerTable, ReadSet, native, synth
+from tests.helpers import dict_to_arrays, kmer_counter_to_canonical, read_gz
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_count(ctx, text, k=25, canonical=True, capacity=0):
+    t = KmerTable(ctx, k, canonical, capacity)
+    t.count_text(text)
+    return t
+
+
+def assert_pairs(got, want):
+    np.testing.assert_array_equal(got[0], want[0])
+    np.testing.assert_array_equal(got[1], want[1])
+
+
+@pytest.mark.parametrize("name", ["edge", "bulk"])
+def test_parse_matches_fasta_reader(ctx, golden, name):
+    text = (golden / f"{name}.fa").read_bytes()
+    rs = ReadSet(ctx, text)
+    want = [l.split(b"\t") for l in (golden / f"{name}.fasta_reader.tsv").read_bytes().split(b"\n") if l]
+    assert rs.n_reads == len(want)
+    assert rs.accessions() == [w[0] for w in want]
+    assert rs.sequences() == [w[1].upper() for w in want]
+
+
+def test_parse_fastq(ctx, golden):
+    rs = ReadSet(ctx, (golden / "edge.fq").read_bytes())
+    assert rs.format == native.TK_FMT_FASTQ
+    want = (golden / "edge.fastQ_to_fastA.fa").read_bytes().split(b"\n")
+    assert rs.sequences() == [l for l in want[1::2] if l or True][:rs.n_reads]
+
+
+@pytest.mark.parametrize("name", ["edge", "bulk"])
+def test_count_matches_reference_perl_counter(ctx, golden, name):
+    text = (golden / f"{name}.fa").read_bytes()
+    want = dict_to_arrays(kmer_counter_to_canonical(read_gz(golden / f"{name}.kmer_counter.txt.gz")))
+    assert_pairs(gpu_count(ctx, text).dump(1), want)
+
+
+@pytest.mark.parametrize("k", [1, 5, 17, 24, 25, 31])
+@pytest.mark.parametrize("canonical", [True, False])
+def test_count_parity_k(ctx, oracle, golden, k, canonical):
+    text = (golden / "edge.fa").read_bytes() + (golden / "bulk.fa").read_bytes()
+    assert_pairs(gpu_count(ctx, text, k, canonical).dump(1), oracle.count(text, k, canonical))
+
+
+def test_count_parity_transcriptome_1M(ctx, oracle):
+    """Single-end 76-nt transcriptome workload at full size (1M reads)."""
+    text = synth.transcriptome_reads(seed=1, n_reads=1_000_000).tobytes()
+    t = gpu_count(ctx, text)
+    want = oracle.count(text, 25, True)
+    got = t.dump(1)
+    assert_pairs(got, want)
+    d, total, cap = t.info()
+    assert d == len(want[0]) and total == int(want[1].sum()) == 52_000_000
+    np.testing.assert_array_equal(t.histo(1, 10000), oracle.histo(want[1], 1, 10000))
+    for L in (1, 2):
+        assert t.dump_fasta(L) == oracle.dump(want[0], want[1], 25, L)
+
+
+def test_count_fastq_pairs_with_n(ctx, oracle):
+    left, right = synth.gene_pairs(seed=9, n_genes=300, n_pairs=20000, n_rate=0.01)
+    text = left.tobytes() + right.tobytes()
+    assert_pairs(gpu_count(ctx, text).dump(1), oracle.count(text, 25, True))
+
+
+def test_batches_add_up(ctx, oracle):
+    a = synth.transcriptome_reads(seed=3, n_reads=30000).tobytes()
+    b = synth.transcriptome_reads(seed=4, n_reads=50000).tobytes()
+    t = KmerTable(ctx, 25, True)
+    t.count_text(a)
+    t.count_text(b)
+    assert_pairs(t.dump(1), oracle.count(a + b, 25, True))
+
+
+def test_overflow_and_growth_are_exact(ctx, oracle):
+    """One reprobe and a 1,024-slot table: almost every insert overflows and
+    the table doubles repeatedly; the counts stay exact."""
+    text = synth.transcriptome_reads(seed=5, n_reads=3000).tobytes()
+    ctx.set_reprobes(1)
+    try:
+        t = gpu_count(ctx, text, capacity=1024)
+        got = t.dump(1)
+    finally:
+        ctx.set_reprobes(4096)
+    assert_pairs(got, oracle.count(text, 25, True))
+
+
+def test_empty_and_degenerate_inputs(ctx):
+    for text in (b"", b"\n\n  \n", b">a\n\n>b\nNNNNNNNNNNNNNNNNNNNNNNNNNNNNNN\n", b">only_header"):
+        t = gpu_count(ctx, text)
+        k, c = t.dump(1)
+        assert len(k) == 0
+        assert t.dump_fasta(1) == b""
+        assert int(t.histo().sum()) == 0
+
+
+def test_malformed_fastq_is_an_error(ctx):
+    with pytest.raises(native.TrinkmerError) as ei:
+        ReadSet(ctx, b"@r1\nACGT\n+\nIIII\n@r2\nACGT\nIIII\n")
+    assert ei.value.status == native.TK_E_PARSE
+    with pytest.raises(native.TrinkmerError):
+        ReadSet(ctx, b"@r1\nACGT\nXX\nIIII\n")
+
+
+def test_load_dump_roundtrip(ctx, oracle, golden):
+    text = (golden / "bulk.fa").read_bytes() + synth.transcriptome_reads(seed=8, n_reads=20000).tobytes()
+    keys, counts = oracle.count(text, 25, True)
+    d2 = oracle.dump(keys, counts, 25, 2)
+    t = KmerTable(ctx, 25, True)
+    t.load_dump_fasta(d2)
+    assert_pairs(t.dump(1), oracle.load_dump(d2, 25, True))
+    # a non-canonical dump loaded canonically merges strands
+    kf, cf = oracle.count(text, 25, False)
+    df = oracle.dump(kf, cf, 25, 1)
+    t2 = KmerTable(ctx, 25, True)
+    t2.load_dump_fasta(df)
+    assert_pairs(t2.dump(1), oracle.load_dump(df, 25, True))
+
+
+def test_load_pairs(ctx, oracle, golden):
+    text = (golden / "bulk.fa").read_bytes()
+    keys, counts = oracle.count(text, 25, True)
+    t = KmerTable(ctx, 25, True)
+    t.load_pairs(keys, counts)
+    t.load_pairs(keys, counts)
+    assert_pairs(t.dump(1), (keys, counts * 2))
+
+
+def test_bad_dump_is_an_error(ctx):
+    t = KmerTable(ctx, 25, True)
+    with pytest.raises(native.TrinkmerError) as ei:
+        t.load_dump_fasta(b">3\nACGTACGTACGTACGTACGTACGTA\n>x\nACGTACGTACGTACGTACGTACGTA\n")
+    assert ei.value.status == native.TK_E_PARSE

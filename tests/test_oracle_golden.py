@@ -1,0 +1,96 @@
+"""Pins the CPU oracle against fixtures made by the reference's own code
+(tests/golden/make_golden.py): PerlLib/Fasta_reader.pm, util/misc/print_kmers.pl,
+util/misc/kmer_counter.pl, util/support_scripts/fastQ_to_fastA.pl and the
+live consumers of the coverage-stats table.  CPU only."""
+import numpy as np
+import pytest
+
+from tests.helpers import (canonical_counts_from_windows, dict_to_arrays, kmer_counter_to_canonical, read_gz,
+                           sort_stats, trinity_r2t_sort)
+
+
+@pytest.mark.parametrize("name", ["edge", "bulk"])
+def test_records_match_fasta_reader(oracle, golden, name):
+    text = (golden / f"{name}.fa").read_bytes()
+    assert oracle.records(text) == (golden / f"{name}.fasta_reader.tsv").read_bytes()
+
+
+@pytest.mark.parametrize("name", ["edge", "bulk"])
+def test_count_matches_kmer_counter_pl(oracle, golden, name):
+    text = (golden / f"{name}.fa").read_bytes()
+    want = dict_to_arrays(kmer_counter_to_canonical(read_gz(golden / f"{name}.kmer_counter.txt.gz")))
+    keys, counts = oracle.count(text, 25, True)
+    np.testing.assert_array_equal(keys, want[0])
+    np.testing.assert_array_equal(counts, want[1])
+
+
+@pytest.mark.parametrize("name", ["edge", "bulk"])
+@pytest.mark.parametrize("canonical", [True, False])
+def test_count_matches_print_kmers_pl(oracle, golden, name, canonical):
+    text = (golden / f"{name}.fa").read_bytes()
+    windows = read_gz(golden / f"{name}.print_kmers.txt.gz").decode().split()
+    want = dict_to_arrays(canonical_counts_from_windows(windows, canonical))
+    keys, counts = oracle.count(text, 25, canonical)
+    np.testing.assert_array_equal(keys, want[0])
+    np.testing.assert_array_equal(counts, want[1])
+
+
+def test_fastq_counts_like_its_fasta(oracle, golden):
+    fq = (golden / "edge.fq").read_bytes()
+    fa = (golden / "edge.fastQ_to_fastA.fa").read_bytes()
+    a = oracle.count(fq, 25, True)
+    b = oracle.count(fa, 25, True)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_coverage_stats_accepted_by_perl_consumers(oracle, golden):
+    left = (golden / "left.fa").read_bytes()
+    right = (golden / "right.fa").read_bytes()
+    keys, counts = oracle.count(left + right, 25, True)
+    for side, txt in (("left", left), ("right", right)):
+        got = sort_stats(oracle.cov_stats(txt, keys, counts, 25, True))
+        assert got == (golden / f"{side}.stats").read_bytes()
+    # the merged table the reference's nbkc_merge_left_right_stats.pl wrote from them
+    pairs = (golden / "pairs.stats").read_text().splitlines()
+    assert pairs[0].split("\t")[0] == "acc" and len(pairs) == 201
+
+
+def test_stats_from_dump_at_L2_equal_stats_from_full_table(oracle, golden):
+    """A k-mer absent from the -L 2 catalogue counts 1 (Changelog.txt:536-538)."""
+    left = (golden / "left.fa").read_bytes()
+    right = (golden / "right.fa").read_bytes()
+    keys, counts = oracle.count(left + right, 25, True)
+    d2 = oracle.dump(keys, counts, 25, 2)
+    k2, c2 = oracle.load_dump(d2, 25, True)
+    assert (c2 >= 2).all()
+    assert oracle.cov_stats(left, keys, counts) == oracle.cov_stats(left, k2, c2)
+
+
+def test_r2t_sorted_like_trinity(oracle, golden):
+    b = (golden / "r2t.bundle.fa").read_bytes()
+    r = (golden / "r2t.reads.fa").read_bytes()
+    rows = oracle.r2t(r, b, 25, False, 0)
+    assert trinity_r2t_sort(rows) == (golden / "r2t.out.sort").read_bytes()
+
+
+def test_histo_and_dump_roundtrip(oracle, golden):
+    text = (golden / "bulk.fa").read_bytes()
+    keys, counts = oracle.count(text, 25, True)
+    h = oracle.histo(counts, 1, 10000)
+    assert h.sum() == len(keys) and h[0] == 0
+    assert h[1] == (counts == 1).sum()
+    for L in (1, 2, 3):
+        d = oracle.dump(keys, counts, 25, L)
+        k2, c2 = oracle.load_dump(d, 25, True)
+        sel = counts >= L
+        np.testing.assert_array_equal(k2, keys[sel])
+        np.testing.assert_array_equal(c2, counts[sel])
+
+
+def test_r2t_first_record_owns_shared_kmer(oracle):
+    shared = "ACGTTGCAAGCTTAGCATCGATCGGATCCAGT"
+    b = (">s_7\n" + shared + "X" + "T" * 30 + "\n>s_3\n" + "G" * 10 + shared + "\n").encode()
+    r = (">q1\n" + shared + "\n").encode()
+    rows = oracle.r2t(r, b, 25, False, 0).decode().split("\t")
+    assert rows[0] == "7" and rows[1] == ">q1" and rows[2] == "100"

@@ -1,0 +1,621 @@
+// tk_api.cu -- the extern "C" boundary of libtrinkmer_cuda.so (include/trinkmer.h).
+//
+// Host plumbing only: argument checks, stream-ordered device allocation,
+// host<->device staging for TK_HOST buffers, CUDA-event profiling and error
+// text.  All compute is in the tk_*.cu kernels; there is no CPU fallback --
+// without a usable GPU every entry point returns TK_E_NODEV or TK_E_CUDA.
+#include "tk_internal.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+namespace tk {
+int parse_reads(tk_ctx *c, tk_reads *r);
+int table_info(tk_table *t, uint64_t *distinct, uint64_t *total, uint64_t *capacity);
+int table_histo(tk_table *t, uint64_t low, uint64_t high, uint64_t *hist);
+int table_sorted_pairs(tk_table *t, uint32_t min_count, uint64_t **keys, uint32_t **cnt, uint64_t *n);
+int format_dump(tk_ctx *c, const uint64_t *keys, const uint32_t *cnt, uint64_t n, int k, char **text, uint64_t *len);
+int table_insert_pairs(tk_table *t, const uint64_t *d_keys, const uint32_t *d_cnt, uint64_t n);
+int table_load_dump_reads(tk_table *t, const tk_reads *r);
+int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d_mean, float *d_stdev);
+int r2t_build(tk_r2t *z, const tk_reads *b);
+int r2t_assign(tk_r2t *z, const tk_reads *rd, int32_t *d_rec, uint32_t *d_hits, uint32_t *d_nwin);
+
+int set_err(tk_ctx *c, int code, const std::string &msg) {
+    if (c) c->last_error = msg;
+    return code;
+}
+
+int cuda_check(tk_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return TK_OK;
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return set_err(c, TK_E_OOM, m);
+    return set_err(c, TK_E_CUDA, m);
+}
+
+int check_launch(tk_ctx *c, const char *what) { return cuda_check(c, cudaGetLastError(), what); }
+
+int dmalloc(tk_ctx *c, void **p, size_t bytes, const char *what) {
+    *p = nullptr;
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, c->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_err(c, e == cudaErrorMemoryAllocation ? TK_E_OOM : TK_E_CUDA,
+                       std::string("device allocation of ") + std::to_string(bytes) + " bytes for " + what + ": " +
+                           cudaGetErrorString(e));
+    }
+    return TK_OK;
+}
+
+void dfree(tk_ctx *c, void *p) {
+    if (p) cudaFreeAsync(p, c->stream);
+}
+
+static cudaEvent_t take_event(tk_ctx *c) {
+    if (!c->free_events.empty()) {
+        cudaEvent_t e = c->free_events.back();
+        c->free_events.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void prof_begin(tk_ctx *c, int kid, cudaEvent_t *ev) {
+    (void)kid;
+    *ev = nullptr;
+    if (!c->prof) return;
+    *ev = take_event(c);
+    cudaEventRecord(*ev, c->stream);
+}
+
+void prof_end(tk_ctx *c, int kid, cudaEvent_t ev, uint64_t units) {
+    if (!c->prof || !ev) return;
+    cudaEvent_t b = take_event(c);
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({ev, b, kid, units});
+}
+
+void prof_add_units(tk_ctx *c, int kid, uint64_t units) {
+    if (c->prof && kid >= 0 && kid < TK_KID_NUM) c->prof_units[kid] += units;
+}
+
+static int prof_fold(tk_ctx *c) {
+    if (c->pending.empty()) return TK_OK;
+    TK_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (auto &p : c->pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        c->prof_ms[p.kid] += ms;
+        c->prof_launches[p.kid] += 1;
+        c->prof_units[p.kid] += p.units;
+        c->free_events.push_back(p.a);
+        c->free_events.push_back(p.b);
+    }
+    c->pending.clear();
+    return TK_OK;
+}
+
+// copies a caller buffer to a fresh device allocation (or aliases a device one)
+static int stage_in(tk_ctx *c, const void *src, uint64_t bytes, int where, void **dst, bool *owned) {
+    if (where == TK_DEVICE) {
+        *dst = const_cast<void *>(src);
+        *owned = false;
+        return TK_OK;
+    }
+    TK_TRY(dmalloc(c, dst, bytes + 64, "staged input"));
+    *owned = true;
+    if (bytes) TK_CUDA(c, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    return TK_OK;
+}
+
+// drops the cached dump text once the table's contents change
+static void dump_invalidate(tk_table *t) {
+    if (t->d_dump) dfree(t->ctx, t->d_dump);
+    t->d_dump = nullptr;
+    t->dump_len = 0;
+    t->dump_valid = false;
+}
+
+}  // namespace tk
+
+using namespace tk;
+
+#define CHECK_CTX(c) do { if (!(c)) return TK_E_INVAL; if (cudaSetDevice((c)->device) != cudaSuccess) return set_err((c), TK_E_CUDA, "cudaSetDevice"); } while (0)
+
+extern "C" {
+
+const char *tk_version(void) { return "trinkmer-gb300 0.1 (sm_103a)"; }
+
+const char *tk_status_string(int s) {
+    switch (s) {
+    case TK_OK: return "ok";
+    case TK_E_INVAL: return "invalid argument";
+    case TK_E_CUDA: return "CUDA error";
+    case TK_E_OOM: return "out of memory";
+    case TK_E_PARSE: return "malformed input";
+    case TK_E_TABLE_FULL: return "hash table full";
+    case TK_E_BUDGET: return "over the HBM admission budget";
+    case TK_E_NODEV: return "no CUDA device";
+    case TK_E_RANGE: return "buffer too small";
+    default: return "unknown status";
+    }
+}
+
+int tk_ctx_create(int device, tk_ctx **out) {
+    if (!out) return TK_E_INVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return TK_E_NODEV;
+    }
+    if (device < 0 || device >= n) return TK_E_INVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return TK_E_CUDA;
+    tk_ctx *c = new (std::nothrow) tk_ctx();
+    if (!c) return TK_E_OOM;
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return TK_E_CUDA;
+    }
+    c->own_stream = true;
+    // keep freed blocks in the stream-ordered pool: the hot path allocates per call
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    if (cudaMalloc(&c->d_err, DE_COUNT * sizeof(uint32_t)) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return TK_E_OOM;
+    }
+    cudaMemset(c->d_err, 0, DE_COUNT * sizeof(uint32_t));
+    *out = c;
+    return TK_OK;
+}
+
+void tk_ctx_destroy(tk_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (auto e : c->free_events) cudaEventDestroy(e);
+    cudaFree(c->d_err);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    delete c;
+}
+
+const char *tk_ctx_last_error(const tk_ctx *c) { return c ? c->last_error.c_str() : "no context"; }
+
+void *tk_ctx_stream(tk_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int tk_ctx_synchronize(tk_ctx *c) {
+    CHECK_CTX(c);
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "synchronize");
+}
+
+int tk_ctx_set_profiling(tk_ctx *c, int on) {
+    CHECK_CTX(c);
+    TK_TRY(prof_fold(c));
+    c->prof = on != 0;
+    return TK_OK;
+}
+
+int tk_ctx_profile(tk_ctx *c, int kid, double *ms, uint64_t *launches, uint64_t *units) {
+    CHECK_CTX(c);
+    if (kid < 0 || kid >= TK_KID_NUM) return TK_E_INVAL;
+    TK_TRY(prof_fold(c));
+    if (ms) *ms = c->prof_ms[kid];
+    if (launches) *launches = c->prof_launches[kid];
+    if (units) *units = c->prof_units[kid];
+    return TK_OK;
+}
+
+int tk_ctx_reset_profile(tk_ctx *c) {
+    CHECK_CTX(c);
+    TK_TRY(prof_fold(c));
+    for (int i = 0; i < TK_KID_NUM; i++) { c->prof_ms[i] = 0; c->prof_launches[i] = 0; c->prof_units[i] = 0; }
+    return TK_OK;
+}
+
+uint64_t tk_ctx_kernel_launches(const tk_ctx *c) { return c ? c->launches : 0; }
+
+int tk_ctx_set_reprobes(tk_ctx *c, int max_probes) {
+    CHECK_CTX(c);
+    if (max_probes < 1) return TK_E_INVAL;
+    c->max_probes = max_probes;
+    return TK_OK;
+}
+
+int tk_ctx_mem_info(tk_ctx *c, uint64_t *free_bytes, uint64_t *total_bytes) {
+    CHECK_CTX(c);
+    size_t f = 0, t = 0;
+    TK_CUDA(c, cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return TK_OK;
+}
+
+// ------------------------------------------------------------------ reads
+
+int tk_reads_parse(tk_ctx *c, const char *text, uint64_t len, int where, tk_reads **out) {
+    CHECK_CTX(c);
+    if (!out || (!text && len)) return set_err(c, TK_E_INVAL, "tk_reads_parse: null text");
+    *out = nullptr;
+    tk_reads *r = new (std::nothrow) tk_reads();
+    if (!r) return TK_E_OOM;
+    r->ctx = c;
+    r->text_len = len;
+    void *d = nullptr;
+    bool owned = false;
+    int e = stage_in(c, text, len, where, &d, &owned);
+    r->d_text = (char *)d;
+    r->own_text = owned;
+    if (!e) e = parse_reads(c, r);
+    if (e) {
+        tk_reads_free(r);
+        return e;
+    }
+    *out = r;
+    return TK_OK;
+}
+
+int tk_reads_info(const tk_reads *r, uint64_t *n_reads, uint64_t *n_bases, uint32_t *max_len, int *format) {
+    if (!r) return TK_E_INVAL;
+    if (n_reads) *n_reads = r->n_reads;
+    if (n_bases) *n_bases = r->n_bases;
+    if (max_len) *max_len = r->max_len;
+    if (format) *format = r->format;
+    return TK_OK;
+}
+
+int tk_reads_names(const tk_reads *r, uint64_t *name_off, uint32_t *name_len) {
+    if (!r) return TK_E_INVAL;
+    tk_ctx *c = r->ctx;
+    CHECK_CTX(c);
+    if (r->n_reads == 0) return TK_OK;
+    if (name_off) TK_CUDA(c, cudaMemcpyAsync(name_off, r->d_name_off, r->n_reads * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (name_len) TK_CUDA(c, cudaMemcpyAsync(name_len, r->d_name_len, r->n_reads * 4, cudaMemcpyDeviceToHost, c->stream));
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "names sync");
+}
+
+int tk_reads_offsets(const tk_reads *r, uint64_t *rd_off) {
+    if (!r || !rd_off) return TK_E_INVAL;
+    tk_ctx *c = r->ctx;
+    CHECK_CTX(c);
+    TK_CUDA(c, cudaMemcpyAsync(rd_off, r->d_rd_off, (r->n_reads + 1) * 8, cudaMemcpyDeviceToHost, c->stream));
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "offsets sync");
+}
+
+int tk_reads_copy_seq(const tk_reads *r, char *dst, uint64_t cap) {
+    if (!r || (!dst && r->seq_len)) return TK_E_INVAL;
+    tk_ctx *c = r->ctx;
+    CHECK_CTX(c);
+    if (cap < r->seq_len) return set_err(c, TK_E_RANGE, "tk_reads_copy_seq: buffer smaller than the packed reads");
+    if (r->seq_len) TK_CUDA(c, cudaMemcpyAsync(dst, r->d_seq, r->seq_len, cudaMemcpyDeviceToHost, c->stream));
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "seq sync");
+}
+
+void tk_reads_free(tk_reads *r) {
+    if (!r) return;
+    tk_ctx *c = r->ctx;
+    cudaSetDevice(c->device);
+    if (r->own_text) dfree(c, r->d_text);
+    dfree(c, r->d_seq_alloc);
+    dfree(c, r->d_rd_off);
+    dfree(c, r->d_name_off);
+    dfree(c, r->d_name_len);
+    delete r;
+}
+
+// ------------------------------------------------------------------ table
+
+static int table_new(tk_ctx *c, int k, int canonical, tk_table **out) {
+    tk_table *t = new (std::nothrow) tk_table();
+    if (!t) return TK_E_OOM;
+    t->ctx = c;
+    t->k = k;
+    t->canonical = canonical ? 1 : 0;
+    t->ovf_cap = 1 << 20;
+    int e = dmalloc(c, (void **)&t->d_ovf, t->ovf_cap * 12, "overflow list");
+    if (!e) e = dmalloc(c, (void **)&t->d_counters, 2 * sizeof(unsigned long long), "table counters");
+    if (!e) e = dmalloc(c, (void **)&t->d_hll, 4096 * 4, "HLL registers");
+    if (!e) {
+        cudaMemsetAsync(t->d_counters, 0, 2 * sizeof(unsigned long long), c->stream);
+        cudaMemsetAsync(t->d_hll, 0, 4096 * 4, c->stream);
+    }
+    if (e) {
+        tk_table_free(t);
+        return e;
+    }
+    *out = t;
+    return TK_OK;
+}
+
+int tk_table_create(tk_ctx *c, int k, int canonical, uint64_t capacity_hint, tk_table **out) {
+    CHECK_CTX(c);
+    if (!out) return TK_E_INVAL;
+    *out = nullptr;
+    if (k < 1 || k > MAX_K) return set_err(c, TK_E_INVAL, "k must be in 1..31");
+    tk_table *t = nullptr;
+    TK_TRY(table_new(c, k, canonical, &t));
+    if (capacity_hint) {
+        uint64_t cap = 1024;
+        while (cap < capacity_hint) cap <<= 1;
+        int e = table_alloc(t, cap);
+        if (e) {
+            tk_table_free(t);
+            return e;
+        }
+    }
+    *out = t;
+    return TK_OK;
+}
+
+int tk_table_add_reads(tk_table *t, const tk_reads *r) {
+    if (!t || !r) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    if (r->ctx != c) return set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
+    dump_invalidate(t);
+    return table_count_seq(t, r->d_seq, r->seq_len);
+}
+
+int tk_table_count_text(tk_table *t, const char *text, uint64_t len, int where) {
+    if (!t) return TK_E_INVAL;
+    tk_reads *r = nullptr;
+    TK_TRY(tk_reads_parse(t->ctx, text, len, where, &r));
+    int e = tk_table_add_reads(t, r);
+    tk_reads_free(r);
+    return e;
+}
+
+int tk_table_info(tk_table *t, uint64_t *distinct, uint64_t *total, uint64_t *capacity) {
+    if (!t) return TK_E_INVAL;
+    CHECK_CTX(t->ctx);
+    return table_info(t, distinct, total, capacity);
+}
+
+int tk_table_histo(tk_table *t, uint64_t low, uint64_t high, uint64_t *hist) {
+    if (!t || !hist) return TK_E_INVAL;
+    CHECK_CTX(t->ctx);
+    return table_histo(t, low, high, hist);
+}
+
+int tk_table_dump(tk_table *t, uint32_t min_count, int where, uint64_t *keys, uint32_t *counts, uint64_t cap,
+                  uint64_t *n_out) {
+    if (!t || !n_out) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    uint64_t *dk = nullptr;
+    uint32_t *dc = nullptr;
+    uint64_t n = 0;
+    TK_TRY(table_sorted_pairs(t, min_count, &dk, &dc, &n));
+    *n_out = n;
+    int e = TK_OK;
+    if (keys || counts) {
+        if (cap < n) e = set_err(c, TK_E_RANGE, "tk_table_dump: capacity below the number of pairs");
+        cudaMemcpyKind kind = where == TK_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (!e && keys && n) e = cuda_check(c, cudaMemcpyAsync(keys, dk, n * 8, kind, c->stream), "dump keys");
+        if (!e && counts && n) e = cuda_check(c, cudaMemcpyAsync(counts, dc, n * 4, kind, c->stream), "dump counts");
+    }
+    dfree(c, dk);
+    dfree(c, dc);
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "dump sync");
+    return e;
+}
+
+int tk_table_dump_fasta(tk_table *t, uint32_t min_count, int where, char *out, uint64_t cap, uint64_t *len_out) {
+    if (!t || !len_out) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    if (!t->dump_valid || t->dump_min != min_count) {
+        dump_invalidate(t);
+        uint64_t *dk = nullptr;
+        uint32_t *dc = nullptr;
+        uint64_t n = 0;
+        TK_TRY(table_sorted_pairs(t, min_count, &dk, &dc, &n));
+        char *text = nullptr;
+        uint64_t len = 0;
+        int e = format_dump(c, dk, dc, n, t->k, &text, &len);
+        dfree(c, dk);
+        dfree(c, dc);
+        if (e) return e;
+        t->d_dump = text;
+        t->dump_len = len;
+        t->dump_min = min_count;
+        t->dump_valid = true;
+    }
+    *len_out = t->dump_len;
+    int e = TK_OK;
+    if (out) {
+        cudaMemcpyKind kind = where == TK_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (cap < t->dump_len) e = set_err(c, TK_E_RANGE, "tk_table_dump_fasta: buffer smaller than the dump");
+        else if (t->dump_len)
+            e = cuda_check(c, cudaMemcpyAsync(out, t->d_dump, t->dump_len, kind, c->stream), "dump text copy");
+    }
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "dump text sync");
+    return e;
+}
+
+int tk_table_load_pairs(tk_table *t, const uint64_t *keys, const uint32_t *counts, uint64_t n, int where) {
+    if (!t || (!keys && n)) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    if (n == 0) return TK_OK;
+    dump_invalidate(t);
+    void *dk = nullptr, *dc = nullptr;
+    bool ok_k = false, ok_c = false;
+    int e = stage_in(c, keys, n * 8, where, &dk, &ok_k);
+    if (!e && counts) e = stage_in(c, counts, n * 4, where, &dc, &ok_c);
+    if (!e) e = table_insert_pairs(t, (const uint64_t *)dk, (const uint32_t *)dc, n);
+    if (ok_k) dfree(c, dk);
+    if (ok_c) dfree(c, dc);
+    return e;
+}
+
+int tk_table_load_dump_fasta(tk_table *t, const char *text, uint64_t len, int where) {
+    if (!t) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    tk_reads *r = nullptr;
+    TK_TRY(tk_reads_parse(c, text, len, where, &r));
+    int e = TK_OK;
+    if (r->format == TK_FMT_FASTQ) e = set_err(c, TK_E_PARSE, "k-mer catalogue must be FASTA ('>COUNT' headers)");
+    dump_invalidate(t);
+    if (!e) e = table_load_dump_reads(t, r);
+    tk_reads_free(r);
+    return e;
+}
+
+void tk_table_free(tk_table *t) {
+    if (!t) return;
+    tk_ctx *c = t->ctx;
+    cudaSetDevice(c->device);
+    dfree(c, t->t.slots);
+    dfree(c, t->d_ovf);
+    dfree(c, t->d_counters);
+    dfree(c, t->d_hll);
+    dfree(c, t->d_dump);
+    delete t;
+}
+
+// ------------------------------------------------------------------ coverage
+
+int tk_coverage_stats(tk_table *t, const tk_reads *r, int where, uint32_t *median, float *mean, float *stdev) {
+    if (!t || !r || !median || !mean || !stdev) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    if (r->ctx != c) return set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
+    const uint64_t n = r->n_reads;
+    if (n == 0) return TK_OK;
+    if (where == TK_DEVICE) {
+        TK_TRY(coverage_stats(t, r, median, mean, stdev));
+        return cuda_check(c, cudaStreamSynchronize(c->stream), "coverage sync");
+    }
+    uint32_t *dm = nullptr;
+    float *da = nullptr, *ds = nullptr;
+    int e = dmalloc(c, (void **)&dm, n * 4, "median");
+    if (!e) e = dmalloc(c, (void **)&da, n * 4, "mean");
+    if (!e) e = dmalloc(c, (void **)&ds, n * 4, "stdev");
+    if (!e) e = coverage_stats(t, r, dm, da, ds);
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(median, dm, n * 4, cudaMemcpyDeviceToHost, c->stream), "median d2h");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(mean, da, n * 4, cudaMemcpyDeviceToHost, c->stream), "mean d2h");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(stdev, ds, n * 4, cudaMemcpyDeviceToHost, c->stream), "stdev d2h");
+    dfree(c, dm);
+    dfree(c, da);
+    dfree(c, ds);
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "coverage sync");
+    return e;
+}
+
+// ------------------------------------------------------------------ R2T
+
+int tk_r2t_create(tk_ctx *c, const char *bundle, uint64_t len, int where, int k, int strand, tk_r2t **out) {
+    CHECK_CTX(c);
+    if (!out) return TK_E_INVAL;
+    *out = nullptr;
+    if (k < 1 || k > MAX_K) return set_err(c, TK_E_INVAL, "k must be in 1..31");
+    tk_r2t *z = new (std::nothrow) tk_r2t();
+    if (!z) return TK_E_OOM;
+    z->ctx = c;
+    z->k = k;
+    z->strand = strand ? 1 : 0;
+    tk_reads *b = nullptr;
+    int e = table_new(c, k, !strand, &z->table);
+    if (!e) e = tk_reads_parse(c, bundle, len, where, &b);
+    if (!e && b->format == TK_FMT_FASTQ) e = set_err(c, TK_E_PARSE, "bundle must be FASTA");
+    if (!e) e = r2t_build(z, b);
+    if (!e) {
+        // component ids from the headers: integer after "s_", else the record ordinal
+        z->n_records = b->n_reads;
+        z->comp_id.resize(b->n_reads);
+        std::vector<uint64_t> off(b->n_reads);
+        std::vector<uint32_t> nl(b->n_reads);
+        e = tk_reads_names(b, off.data(), nl.data());
+        std::vector<char> host_text;
+        const char *ht = bundle;
+        if (!e && where == TK_DEVICE) {
+            host_text.resize(len);
+            e = cuda_check(c, cudaMemcpy(host_text.data(), bundle, len, cudaMemcpyDeviceToHost), "bundle d2h");
+            ht = host_text.data();
+        }
+        for (uint64_t i = 0; !e && i < b->n_reads; i++) {
+            const char *h = ht + off[i];
+            uint32_t L = nl[i];
+            uint64_t id = i;
+            if (L > 2 && h[0] == 's' && h[1] == '_' && h[2] >= '0' && h[2] <= '9') {
+                id = 0;
+                for (uint32_t j = 2; j < L && h[j] >= '0' && h[j] <= '9'; j++) id = id * 10 + (uint64_t)(h[j] - '0');
+            }
+            z->comp_id[i] = id;
+        }
+    }
+    if (b) tk_reads_free(b);
+    if (e) {
+        tk_r2t_free(z);
+        return e;
+    }
+    *out = z;
+    return TK_OK;
+}
+
+int tk_r2t_info(const tk_r2t *z, uint64_t *n_records, uint64_t *n_kmers) {
+    if (!z) return TK_E_INVAL;
+    if (n_records) *n_records = z->n_records;
+    if (n_kmers) {
+        uint64_t d = 0;
+        TK_TRY(table_info(z->table, &d, nullptr, nullptr));
+        *n_kmers = d;
+    }
+    return TK_OK;
+}
+
+int tk_r2t_component_ids(const tk_r2t *z, uint64_t *ids) {
+    if (!z || !ids) return TK_E_INVAL;
+    std::copy(z->comp_id.begin(), z->comp_id.end(), ids);
+    return TK_OK;
+}
+
+int tk_r2t_assign(tk_r2t *z, const tk_reads *r, int where, int32_t *rec, uint32_t *hits, uint32_t *nwin) {
+    if (!z || !r || !rec || !hits || !nwin) return TK_E_INVAL;
+    tk_ctx *c = z->ctx;
+    CHECK_CTX(c);
+    if (r->ctx != c) return set_err(c, TK_E_INVAL, "read set and bundle belong to different contexts");
+    const uint64_t n = r->n_reads;
+    if (n == 0) return TK_OK;
+    if (where == TK_DEVICE) {
+        TK_TRY(r2t_assign(z, r, rec, hits, nwin));
+        return cuda_check(c, cudaStreamSynchronize(c->stream), "assign sync");
+    }
+    int32_t *dr = nullptr;
+    uint32_t *dh = nullptr, *dn = nullptr;
+    int e = dmalloc(c, (void **)&dr, n * 4, "rec");
+    if (!e) e = dmalloc(c, (void **)&dh, n * 4, "hits");
+    if (!e) e = dmalloc(c, (void **)&dn, n * 4, "nwin");
+    if (!e) e = r2t_assign(z, r, dr, dh, dn);
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(rec, dr, n * 4, cudaMemcpyDeviceToHost, c->stream), "rec d2h");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(hits, dh, n * 4, cudaMemcpyDeviceToHost, c->stream), "hits d2h");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(nwin, dn, n * 4, cudaMemcpyDeviceToHost, c->stream), "nwin d2h");
+    dfree(c, dr);
+    dfree(c, dh);
+    dfree(c, dn);
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "assign sync");
+    return e;
+}
+
+void tk_r2t_free(tk_r2t *z) {
+    if (!z) return;
+    if (z->table) tk_table_free(z->table);
+    delete z;
+}
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+// tk_cov.cu -- K5: per-read k-mer coverage statistics
+// (Inchworm fastaToKmerCoverageStats, called at
+// util/insilico_read_normalization.pl:837-846).
+//
+// For each read, every window of k A/C/G/T bases is looked up in the count
+// table (canonical key with --DS); a k-mer absent from the table counts 1
+// (the catalogue is dumped at -L 2, Changelog.txt:536-538).  Windows holding
+// another character are skipped.  median = element n/2 of the sorted values;
+// mean and stdev come from exact integer sums (see finish_stats).
+//
+// Reads with at most 256 windows: one warp per read, values in registers,
+// warp bitonic sort (tk_warp.cuh).  Longer reads: one block per read, values
+// in a global scratch slab, block bitonic sort.
+#include "tk_warp.cuh"
+
+#include <algorithm>
+
+namespace tk {
+
+constexpr int CV_THREADS = 256;
+constexpr uint32_t CV_WARP_MAX = 256;   // windows handled by the warp path
+
+template <int S, bool CANON>
+__device__ __forceinline__ void cov_warp_read(DevTable t, const uint8_t *__restrict__ seq, uint64_t start, uint32_t nwin,
+                                              int k, uint64_t r, uint32_t *__restrict__ median, float *__restrict__ mean,
+                                              float *__restrict__ stdev) {
+    const uint32_t span = (nwin + 31) / 32;
+    uint32_t v[S];
+    uint32_t cnt = 0;
+    uint64_t sum = 0, hi = 0, lo = 0;
+    lane_windows<S, CANON>(seq, start, nwin, span, k, [&](int j, bool valid, uint64_t key) {
+        uint32_t c = PAD_VAL;
+        if (valid) {
+            c = tbl_get(t, key, 1u);
+            cnt++;
+            sum += c;
+            uint64_t sq = (uint64_t)c * c;   // < 2^64
+            uint64_t nlo = lo + sq;
+            hi += nlo < lo;
+            lo = nlo;
+        }
+        v[j] = c;
+    });
+    cnt = warp_sum(cnt);
+    sum = warp_sum(sum);
+    warp_sum_u128(hi, lo);
+    warp_bitonic_sort<S>(v);
+    uint32_t med = cnt ? warp_elem<S>(v, cnt / 2) : 0u;
+    if (lane_id() == 0) {
+        float m, s;
+        finish_stats(cnt, sum, hi, lo, &m, &s);
+        median[r] = med;
+        mean[r] = m;
+        stdev[r] = s;
+    }
+}
+
+template <bool CANON>
+__global__ void __launch_bounds__(CV_THREADS) k_coverage(DevTable t, const uint8_t *__restrict__ seq,
+                                                        const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
+                                                        uint32_t *__restrict__ median, float *__restrict__ mean,
+                                                        float *__restrict__ stdev, uint32_t *__restrict__ long_list,
+                                                        unsigned long long *__restrict__ long_n) {
+    const uint64_t warps = (uint64_t)gridDim.x * (CV_THREADS / 32);
+    for (uint64_t r = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); r < n_reads; r += warps) {
+        const uint64_t start = rd_off[r];
+        const uint64_t L = rd_off[r + 1] - start - 1;
+        const uint32_t nwin = L >= (uint64_t)k ? (uint32_t)(L - k + 1) : 0u;
+        if (nwin <= 32) cov_warp_read<1, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+        else if (nwin <= 64) cov_warp_read<2, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+        else if (nwin <= 128) cov_warp_read<4, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+        else if (nwin <= CV_WARP_MAX) cov_warp_read<8, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+        else if (lane_id() == 0) long_list[atomicAdd(long_n, 1ULL)] = (uint32_t)r;
+    }
+}
+
+// long reads: one block per read, `slab` = this block's scratch (n2max values)
+template <bool CANON>
+__global__ void __launch_bounds__(CV_THREADS) k_coverage_long(DevTable t, const uint8_t *__restrict__ seq,
+                                                             const uint64_t *__restrict__ rd_off,
+                                                             const uint32_t *__restrict__ list, uint64_t n_long, int k,
+                                                             uint32_t *__restrict__ scratch, uint64_t n2max,
+                                                             uint32_t *__restrict__ median, float *__restrict__ mean,
+                                                             float *__restrict__ stdev) {
+    __shared__ uint32_t s_cnt[CV_THREADS / 32];
+    __shared__ uint64_t s_sum[CV_THREADS / 32], s_hi[CV_THREADS / 32], s_lo[CV_THREADS / 32];
+    uint32_t *slab = scratch + (uint64_t)blockIdx.x * n2max;
+    for (uint64_t i = blockIdx.x; i < n_long; i += gridDim.x) {
+        const uint32_t r = list[i];
+        const uint64_t start = rd_off[r];
+        const uint32_t nwin = (uint32_t)(rd_off[r + 1] - start - 1 - (k - 1));
+        uint32_t n2 = 1;
+        while (n2 < nwin) n2 <<= 1;
+        block_window_values<CANON>(seq, start, nwin, n2, k, slab, [&](uint64_t key) { return tbl_get(t, key, 1u); });
+        uint32_t cnt = 0;
+        uint64_t sum = 0, hi = 0, lo = 0;
+        for (uint32_t w = threadIdx.x; w < nwin; w += blockDim.x) {
+            uint32_t c = slab[w];
+            if (c == PAD_VAL) continue;
+            cnt++;
+            sum += c;
+            uint64_t sq = (uint64_t)c * c, nlo = lo + sq;
+            hi += nlo < lo;
+            lo = nlo;
+        }
+        cnt = warp_sum(cnt);
+        sum = warp_sum(sum);
+        warp_sum_u128(hi, lo);
+        if (lane_id() == 0) {
+            s_cnt[threadIdx.x >> 5] = cnt;
+            s_sum[threadIdx.x >> 5] = sum;
+            s_hi[threadIdx.x >> 5] = hi;
+            s_lo[threadIdx.x >> 5] = lo;
+        }
+        block_bitonic_sort(slab, n2);
+        if (threadIdx.x == 0) {
+            uint32_t tc = 0;
+            uint64_t ts = 0, th = 0, tl = 0;
+            for (int w = 0; w < CV_THREADS / 32; w++) {
+                tc += s_cnt[w];
+                ts += s_sum[w];
+                uint64_t nl = tl + s_lo[w];
+                th += s_hi[w] + (nl < tl);
+                tl = nl;
+            }
+            float m, s;
+            finish_stats(tc, ts, th, tl, &m, &s);
+            median[r] = tc ? slab[tc / 2] : 0u;
+            mean[r] = m;
+            stdev[r] = s;
+        }
+        __syncthreads();
+    }
+}
+
+int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d_mean, float *d_stdev) {
+    tk_ctx *c = t->ctx;
+    const uint64_t n = rd->n_reads;
+    if (n == 0) return TK_OK;
+    const int k = t->k;
+    const bool may_long = rd->max_len >= (uint32_t)k && rd->max_len - k + 1 > CV_WARP_MAX;
+    uint32_t *long_list = nullptr;
+    unsigned long long *long_n = nullptr;
+    TK_TRY(dmalloc(c, (void **)&long_n, 8, "long-read count"));
+    int e = TK_OK;
+    if (may_long) e = dmalloc(c, (void **)&long_list, n * 4, "long-read list");
+    if (!e) e = cuda_check(c, cudaMemsetAsync(long_n, 0, 8, c->stream), "long reset");
+    DevTable dt = t->t;
+    Slot *empty = nullptr;
+    if (!e && t->capacity == 0) {
+        // an empty catalogue: every k-mer counts 1; give the kernel a one-slot table
+        e = dmalloc(c, (void **)&empty, sizeof(Slot) * 2, "empty table");
+        if (!e) {
+            cudaMemsetAsync(empty, 0xFF, sizeof(Slot) * 2, c->stream);
+            dt.slots = empty;
+            dt.mask = 1;
+        }
+    }
+    if (!e) {
+        const unsigned grid = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>((n + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
+        cudaEvent_t ev;
+        prof_begin(c, TK_KID_COVERAGE, &ev);
+        if (t->canonical)
+            k_coverage<true><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
+                                                                 d_stdev, long_list, long_n);
+        else
+            k_coverage<false><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
+                                                                  d_stdev, long_list, long_n);
+        c->launches++;
+        prof_end(c, TK_KID_COVERAGE, ev, rd->n_bases);
+        e = check_launch(c, "coverage");
+    }
+    unsigned long long hl = 0;
+    if (!e && may_long) {
+        e = cuda_check(c, cudaMemcpyAsync(&hl, long_n, 8, cudaMemcpyDeviceToHost, c->stream), "long n");
+        if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "long sync");
+    }
+    if (!e && hl) {
+        uint64_t n2max = 1;
+        while (n2max < (uint64_t)(rd->max_len - k + 1)) n2max <<= 1;
+        uint64_t grid = std::min<uint64_t>(hl, (uint64_t)c->sm_count * 2);
+        uint32_t *scratch = nullptr;
+        e = dmalloc(c, (void **)&scratch, grid * n2max * 4, "long-read scratch");
+        if (!e) {
+            if (t->canonical)
+                k_coverage_long<true><<<(unsigned)grid, CV_THREADS, 0, c->stream>>>(
+                    dt, rd->d_seq, rd->d_rd_off, long_list, hl, k, scratch, n2max, d_median, d_mean, d_stdev);
+            else
+                k_coverage_long<false><<<(unsigned)grid, CV_THREADS, 0, c->stream>>>(
+                    dt, rd->d_seq, rd->d_rd_off, long_list, hl, k, scratch, n2max, d_median, d_mean, d_stdev);
+            c->launches++;
+            e = check_launch(c, "coverage long");
+            dfree(c, scratch);
+        }
+    }
+    if (long_list) dfree(c, long_list);
+    dfree(c, long_n);
+    if (empty) dfree(c, empty);
+    return e;
+}
+
+}  // namespace tk

@@ -1,0 +1,251 @@
+// tk_internal.cuh -- shared definitions of the GB300 k-mer library.
+//
+// Device data layout (all in HBM, owned by the library):
+//  * read batch   : `seq`  = every read's bases upper-cased, each read followed
+//                   by one '\n' separator, 64 bytes of '\n' padding on both
+//                   sides; `rd_off[r]` = first base of read r (n+1 entries);
+//                   `name_off/name_len` = accession (first header token) in
+//                   the device copy of the input text.
+//  * k-mer table  : open addressing, linear probing, 16-byte slots
+//                   {u64 key; u32 value; u32 pad} so a probe touches one
+//                   32-byte DRAM sector; capacity a power of two; empty key
+//                   = ~0 (k <= 31 keeps every real key below it).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include <mutex>
+
+#include "../../include/trinkmer.h"
+
+namespace tk {
+
+constexpr uint64_t EMPTY_KEY = ~0ULL;
+constexpr uint32_t PAD_VAL = 0xFFFFFFFFu;
+constexpr int SEQ_PAD = 64;          // '\n' bytes before and after `seq`
+constexpr int MAX_K = 31;
+
+struct __align__(16) Slot {
+    unsigned long long key;
+    unsigned int val;
+    unsigned int pad;
+};
+
+struct DevTable {
+    Slot *slots;
+    uint64_t mask;      // capacity - 1
+};
+
+// device-side error words (set by kernels, read by the host after a launch)
+enum DevErr : uint32_t {
+    DE_PARSE = 0,       // [0] parse error flag, [1] first bad line (low 32 bits)
+    DE_OVERFLOW = 2,    // [2] overflow list overrun
+    DE_COUNT = 8
+};
+
+__host__ __device__ inline uint64_t mix64(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33; return x;
+}
+
+// A/C/G/T -> 0..3 for upper-case input (`seq` is upper-cased by the parser);
+// anything else -> 4.  ((c>>1)&3) maps A,C,G,T to 0,1,3,2; the xor swaps G,T.
+__device__ __forceinline__ uint32_t base_code(uint32_t c) {
+    uint32_t d = c - 0x41u;
+    bool ok = d < 20u && ((0x80045u >> d) & 1u);
+    uint32_t b = (c >> 1) & 3u;
+    b ^= b >> 1;
+    return ok ? b : 4u;
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// ------------------------------------------------------------------ table ops
+
+// Adds `inc` to key's value, inserting the key if absent.  Returns false after
+// max_probes slots without finding the key or a free slot.
+__device__ __forceinline__ bool tbl_add(DevTable t, uint64_t key, uint32_t inc, int max_probes) {
+    uint64_t s = mix64(key) & t.mask;
+    for (int i = 0; i < max_probes; i++) {
+        unsigned long long cur = __ldcg(&t.slots[s].key);
+        if (cur == EMPTY_KEY) {
+            cur = atomicCAS(&t.slots[s].key, EMPTY_KEY, (unsigned long long)key);
+            if (cur == EMPTY_KEY) cur = key;
+        }
+        if (cur == key) {
+            atomicAdd(&t.slots[s].val, inc);
+            return true;
+        }
+        s = (s + 1) & t.mask;
+    }
+    return false;
+}
+
+// Keeps the minimum value per key (ReadsToTranscripts ownership).
+__device__ __forceinline__ bool tbl_min(DevTable t, uint64_t key, uint32_t v, int max_probes) {
+    uint64_t s = mix64(key) & t.mask;
+    for (int i = 0; i < max_probes; i++) {
+        unsigned long long cur = __ldcg(&t.slots[s].key);
+        if (cur == EMPTY_KEY) {
+            cur = atomicCAS(&t.slots[s].key, EMPTY_KEY, (unsigned long long)key);
+            if (cur == EMPTY_KEY) cur = key;
+        }
+        if (cur == key) {
+            atomicMin(&t.slots[s].val, v);
+            return true;
+        }
+        s = (s + 1) & t.mask;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t tbl_get(DevTable t, uint64_t key, uint32_t miss) {
+    uint64_t s = mix64(key) & t.mask;
+    for (uint64_t i = 0; i <= t.mask; i++) {
+        ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(&t.slots[s]));
+        if (v.x == key) return (uint32_t)v.y;
+        if (v.x == EMPTY_KEY) return miss;
+        s = (s + 1) & t.mask;
+    }
+    return miss;
+}
+
+// ------------------------------------------------------------------ warp scans
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T n = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)lane_id() >= o) v += n;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide exclusive scan; `sm` needs blockDim.x/32 + 1 entries.  Returns the
+// thread's exclusive prefix; *total receives the block total.
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T *sm, T *total) {
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T inc = warp_incl_scan(v);
+    if (lane == 31) sm[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        T w = lane < nw ? sm[lane] : T(0);
+        T wi = warp_incl_scan(w);
+        if (lane < nw) sm[lane] = wi - w;
+        if (lane == nw - 1) sm[nw] = wi;
+    }
+    __syncthreads();
+    T r = sm[warp] + inc - v;
+    *total = sm[nw];
+    __syncthreads();
+    return r;
+}
+
+}  // namespace tk
+
+// ------------------------------------------------------------------ host side
+
+struct tk_prof_rec {
+    cudaEvent_t a, b;
+    int kid;
+    uint64_t units;
+};
+
+struct tk_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint32_t *d_err = nullptr;             // tk::DE_COUNT words
+    std::string last_error;
+    // profiling (CUDA events on `stream` around the hot kernels)
+    bool prof = false;
+    std::vector<tk_prof_rec> pending;
+    std::vector<cudaEvent_t> free_events;
+    double prof_ms[TK_KID_NUM] = {0};
+    uint64_t prof_launches[TK_KID_NUM] = {0};
+    uint64_t prof_units[TK_KID_NUM] = {0};
+    uint64_t launches = 0;                  // every kernel launched by the library
+    int max_probes = 4096;
+    int sm_count = 152;
+};
+
+struct tk_reads {
+    tk_ctx *ctx = nullptr;
+    int format = 0;                         // TK_FMT_FASTA / TK_FMT_FASTQ
+    uint64_t n_reads = 0;
+    uint64_t n_bases = 0;                   // bases over all reads
+    uint64_t seq_len = 0;                   // bytes of seq incl. separators
+    uint32_t max_len = 0;
+    char *d_text = nullptr;                 // device copy of the input text
+    uint64_t text_len = 0;
+    bool own_text = false;
+    uint8_t *d_seq_alloc = nullptr;
+    uint8_t *d_seq = nullptr;               // = d_seq_alloc + SEQ_PAD
+    uint64_t *d_rd_off = nullptr;           // n_reads + 1
+    uint64_t *d_name_off = nullptr;         // n_reads
+    uint32_t *d_name_len = nullptr;         // n_reads
+};
+
+struct tk_table {
+    tk_ctx *ctx = nullptr;
+    int k = 25;
+    int canonical = 1;
+    tk::DevTable t{nullptr, 0};
+    uint64_t capacity = 0;
+    uint64_t distinct = 0;                  // valid after tk_table_finalize-type queries
+    uint64_t total = 0;                     // k-mer occurrences added
+    bool distinct_valid = true;
+    uint64_t *d_ovf = nullptr;              // overflow key list
+    uint64_t ovf_cap = 0;
+    unsigned long long *d_counters = nullptr;  // [0] overflow n, [1] windows added
+    uint32_t *d_hll = nullptr;              // HLL registers
+    double max_load = 0.6;
+    // last formatted dump (valid until the table changes)
+    char *d_dump = nullptr;
+    uint64_t dump_len = 0;
+    uint32_t dump_min = 0;
+    bool dump_valid = false;
+};
+
+struct tk_r2t {
+    tk_ctx *ctx = nullptr;
+    int k = 25;
+    int strand = 0;
+    tk_table *table = nullptr;              // key -> bundle record index
+    uint64_t n_records = 0;
+    std::vector<uint64_t> comp_id;          // per bundle record
+};
+
+// host helpers shared by the translation units
+namespace tk {
+int set_err(tk_ctx *c, int code, const std::string &msg);
+int cuda_check(tk_ctx *c, cudaError_t e, const char *what);
+int dmalloc(tk_ctx *c, void **p, size_t bytes, const char *what);
+void dfree(tk_ctx *c, void *p);
+void prof_begin(tk_ctx *c, int kid, cudaEvent_t *ev);
+void prof_end(tk_ctx *c, int kid, cudaEvent_t ev, uint64_t units);
+void prof_add_units(tk_ctx *c, int kid, uint64_t units);
+int check_launch(tk_ctx *c, const char *what);
+int scan_excl_u64(tk_ctx *c, const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *total_host);
+int scan_excl_u32_to_u64(tk_ctx *c, const uint32_t *in, uint64_t *out, uint64_t n, uint64_t *total_host);
+int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int bits,
+                     uint64_t *tmp_keys, uint32_t *tmp_vals, bool *result_in_tmp);
+int table_alloc(tk_table *t, uint64_t capacity);
+int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val);
+int table_rehash(tk_table *t, uint64_t new_capacity);
+int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len);
+}  // namespace tk
+
+#define TK_TRY(x) do { int _e = (x); if (_e) return _e; } while (0)
+#define TK_CUDA(c, x) do { cudaError_t _e = (x); if (_e != cudaSuccess) return tk::cuda_check((c), _e, #x); } while (0)

@@ -1,0 +1,410 @@
+// tk_parse.cu -- K1: FASTA/FASTQ text -> device read set.
+//
+// The text is split into lines and records entirely on the GPU with tiled,
+// coalesced passes (each thread owns 32 consecutive bytes, read as two 16-byte
+// vectors; a block owns an 8 KB tile):
+//   A1  newlines per tile                 -> scan -> first line of every tile
+//   A2  newline positions (line ends)
+//   L   line kinds: FASTA '>' header / sequence; FASTQ line index mod 4,
+//       with the '@' and '+' checks of a 4-line record; header lines are
+//       scanned into a record index per line
+//   B1  emitted bases per tile (sequence-line bytes that are not whitespace)
+//   B2  emit: base -> seq[emit_prefix + record] upper-cased; a header's first
+//       byte records its read's start
+//   N   accession (first header token) and read length per record
+// Semantics follow PerlLib/Fasta_reader.pm:45-73 (records start at '>' lines,
+// sequence = following lines with whitespace removed), Sequence->new at
+// PerlLib/Fasta_reader.pm:107-118 (accession = first whitespace token), and the
+// 4-line record checks of util/support_scripts/fastQ_to_fastA.pl:80-92.
+#include "tk_internal.cuh"
+
+namespace tk {
+
+constexpr int PT_THREADS = 256;
+constexpr int PT_BYTES = 32;
+constexpr uint64_t PT_TILE = (uint64_t)PT_THREADS * PT_BYTES;
+
+enum LineKind : uint8_t { LK_SKIP = 0, LK_HDR = 1, LK_SEQ = 2 };
+
+__device__ __forceinline__ bool is_ws(uint32_t c) {
+    return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\f' || c == '\v';
+}
+
+struct Bytes32 {
+    uint32_t w[8];
+    __device__ __forceinline__ uint32_t get(int i) const { return (w[i >> 2] >> ((i & 3) * 8)) & 0xFFu; }
+};
+
+// 32 bytes at p (p is 16-byte aligned relative to an aligned base when `vec`)
+__device__ __forceinline__ Bytes32 load32(const char *__restrict__ text, uint64_t len, uint64_t p, bool vec) {
+    Bytes32 b;
+    if (vec && p + 32 <= len) {
+        uint4 a = __ldg(reinterpret_cast<const uint4 *>(text + p));
+        uint4 c = __ldg(reinterpret_cast<const uint4 *>(text + p + 16));
+        b.w[0] = a.x; b.w[1] = a.y; b.w[2] = a.z; b.w[3] = a.w;
+        b.w[4] = c.x; b.w[5] = c.y; b.w[6] = c.z; b.w[7] = c.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            uint32_t v = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                uint64_t q = p + (uint64_t)(i * 4 + j);
+                uint32_t by = q < len ? (uint32_t)(uint8_t)text[q] : 0u;
+                v |= by << (8 * j);
+            }
+            b.w[i] = v;
+        }
+    }
+    return b;
+}
+
+struct ParseGeom {
+    const char *text;
+    uint64_t len;
+    uint64_t S, E;        // parsed byte range (leading/trailing whitespace trimmed)
+    uint64_t A;           // first tile start (S rounded down to 16)
+    bool vec;
+};
+
+// ---- bounds: first non-whitespace byte and one past the last one
+__global__ void k_bounds(const char *__restrict__ text, uint64_t len, unsigned long long *out) {
+    __shared__ unsigned long long found;
+    if (threadIdx.x == 0) found = ~0ULL;
+    __syncthreads();
+    for (uint64_t base = 0; base < len; base += blockDim.x) {
+        uint64_t p = base + threadIdx.x;
+        if (p < len && !is_ws((uint8_t)text[p])) atomicMin(&found, (unsigned long long)p);
+        __syncthreads();
+        if (found != ~0ULL) break;
+        __syncthreads();
+    }
+    unsigned long long S = found;
+    __syncthreads();
+    if (threadIdx.x == 0) found = 0;
+    __syncthreads();
+    if (S != ~0ULL) {
+        for (uint64_t base = 0; base < len; base += blockDim.x) {
+            uint64_t q = base + threadIdx.x;
+            if (q < len) {
+                uint64_t p = len - 1 - q;
+                if (!is_ws((uint8_t)text[p])) atomicMax(&found, (unsigned long long)(p + 1));
+            }
+            __syncthreads();
+            if (found != 0) break;
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        out[0] = S == ~0ULL ? len : S;
+        out[1] = S == ~0ULL ? len : found;
+        out[2] = S == ~0ULL ? 0 : (uint8_t)text[S];
+    }
+}
+
+// ---- A1: newlines per tile
+__global__ void k_tile_newlines(ParseGeom g, uint32_t *__restrict__ tile_nl) {
+    __shared__ uint32_t sm[PT_THREADS / 32 + 1];
+    uint64_t p = g.A + (uint64_t)blockIdx.x * PT_TILE + (uint64_t)threadIdx.x * PT_BYTES;
+    Bytes32 b = load32(g.text, g.len, p, g.vec);
+    uint32_t n = 0;
+#pragma unroll
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        n += (q >= g.S && q < g.E && b.get(i) == '\n');
+    }
+    uint32_t tot;
+    block_excl_scan<uint32_t>(n, sm, &tot);
+    if (threadIdx.x == 0) tile_nl[blockIdx.x] = tot;
+}
+
+// ---- A2: line ends
+__global__ void k_line_ends(ParseGeom g, const uint64_t *__restrict__ tile_line0, uint64_t *__restrict__ line_end) {
+    __shared__ uint32_t sm[PT_THREADS / 32 + 1];
+    uint64_t p = g.A + (uint64_t)blockIdx.x * PT_TILE + (uint64_t)threadIdx.x * PT_BYTES;
+    Bytes32 b = load32(g.text, g.len, p, g.vec);
+    uint32_t n = 0;
+#pragma unroll
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        n += (q >= g.S && q < g.E && b.get(i) == '\n');
+    }
+    uint32_t tot;
+    uint64_t line = tile_line0[blockIdx.x] + block_excl_scan<uint32_t>(n, sm, &tot);
+    if (n == 0) return;
+#pragma unroll
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        if (q >= g.S && q < g.E && b.get(i) == '\n') line_end[line++] = q;
+    }
+}
+
+// ---- L: line kinds.  FASTQ errors record the first offending line.
+__global__ void k_line_kinds(ParseGeom g, const uint64_t *__restrict__ line_end, uint64_t n_lines, int fastq,
+                             uint8_t *__restrict__ kind, uint32_t *__restrict__ is_hdr, uint32_t *__restrict__ err) {
+    uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_lines) return;
+    uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
+    uint64_t le = line_end[j];
+    uint32_t first = le > ls ? (uint8_t)g.text[ls] : 0u;
+    uint8_t kd;
+    uint32_t h = 0;
+    if (!fastq) {
+        h = first == '>';
+        kd = h ? LK_HDR : LK_SEQ;
+    } else {
+        uint32_t m = (uint32_t)(j & 3);
+        if (m == 0) {
+            h = 1;
+            kd = LK_HDR;
+            if (first != '@') { atomicExch(&err[DE_PARSE], 1u); atomicMin(&err[DE_PARSE + 1], (uint32_t)(j + 1)); }
+        } else if (m == 1) {
+            kd = LK_SEQ;
+        } else {
+            kd = LK_SKIP;
+            if (m == 2 && first != '+') { atomicExch(&err[DE_PARSE], 1u); atomicMin(&err[DE_PARSE + 1], (uint32_t)(j + 1)); }
+        }
+    }
+    kind[j] = kd;
+    is_hdr[j] = h;
+}
+
+// record index per line (~0 before the first header) and header line per record
+__global__ void k_line_records(const uint32_t *__restrict__ is_hdr, uint64_t *__restrict__ line_rec_io, uint64_t n_lines,
+                               uint64_t *__restrict__ hdr_line) {
+    uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_lines) return;
+    uint64_t incl = line_rec_io[j] + is_hdr[j];   // exclusive scan + own flag
+    if (is_hdr[j]) hdr_line[incl - 1] = j;
+    line_rec_io[j] = incl == 0 ? ~0ULL : incl - 1;
+}
+
+// per-thread walk over its 32 bytes with the line each byte belongs to
+struct LineWalk {
+    uint64_t line;
+    uint8_t kind;
+    uint64_t rec;
+};
+
+__device__ __forceinline__ void line_info(const uint8_t *__restrict__ kind, const uint64_t *__restrict__ line_rec,
+                                          uint64_t line, uint64_t n_lines, LineWalk &w) {
+    w.line = line;
+    if (line < n_lines) {
+        w.kind = kind[line];
+        w.rec = line_rec[line];
+    } else {
+        w.kind = LK_SKIP;
+        w.rec = ~0ULL;
+    }
+}
+
+// ---- B1: emitted bytes per tile
+__global__ void k_tile_emits(ParseGeom g, const uint64_t *__restrict__ tile_line0, const uint8_t *__restrict__ kind,
+                             const uint64_t *__restrict__ line_rec, uint64_t n_lines, uint32_t *__restrict__ tile_emit) {
+    __shared__ uint32_t sm[PT_THREADS / 32 + 1];
+    uint64_t p = g.A + (uint64_t)blockIdx.x * PT_TILE + (uint64_t)threadIdx.x * PT_BYTES;
+    Bytes32 b = load32(g.text, g.len, p, g.vec);
+    uint32_t nl = 0;
+#pragma unroll
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        nl += (q >= g.S && q < g.E && b.get(i) == '\n');
+    }
+    uint32_t tot;
+    uint64_t line = tile_line0[blockIdx.x] + block_excl_scan<uint32_t>(nl, sm, &tot);
+    LineWalk w;
+    line_info(kind, line_rec, line, n_lines, w);
+    uint32_t em = 0;
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        if (q < g.S || q >= g.E) continue;
+        uint32_t c = b.get(i);
+        if (c == '\n') {
+            line_info(kind, line_rec, w.line + 1, n_lines, w);
+            continue;
+        }
+        em += (w.kind == LK_SEQ && w.rec != ~0ULL && !is_ws(c));
+    }
+    block_excl_scan<uint32_t>(em, sm, &tot);
+    if (threadIdx.x == 0) tile_emit[blockIdx.x] = tot;
+}
+
+// ---- B2: write upper-cased bases and read starts
+__global__ void k_emit(ParseGeom g, const uint64_t *__restrict__ tile_line0, const uint64_t *__restrict__ tile_emit0,
+                       const uint8_t *__restrict__ kind, const uint64_t *__restrict__ line_rec, uint64_t n_lines,
+                       uint8_t *__restrict__ seq, uint64_t *__restrict__ rd_off) {
+    __shared__ uint32_t sm[PT_THREADS / 32 + 1];
+    uint64_t p = g.A + (uint64_t)blockIdx.x * PT_TILE + (uint64_t)threadIdx.x * PT_BYTES;
+    Bytes32 b = load32(g.text, g.len, p, g.vec);
+    uint32_t nl = 0;
+#pragma unroll
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        nl += (q >= g.S && q < g.E && b.get(i) == '\n');
+    }
+    uint32_t tot;
+    uint64_t line = tile_line0[blockIdx.x] + block_excl_scan<uint32_t>(nl, sm, &tot);
+    LineWalk w;
+    line_info(kind, line_rec, line, n_lines, w);
+    uint32_t em = 0;
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        if (q < g.S || q >= g.E) continue;
+        uint32_t c = b.get(i);
+        if (c == '\n') { line_info(kind, line_rec, w.line + 1, n_lines, w); continue; }
+        em += (w.kind == LK_SEQ && w.rec != ~0ULL && !is_ws(c));
+    }
+    uint64_t pos = tile_emit0[blockIdx.x] + block_excl_scan<uint32_t>(em, sm, &tot);
+    line_info(kind, line_rec, line, n_lines, w);
+    bool nl_before = p > g.S && p - 1 < g.E && g.text[p - 1] == '\n';
+    for (int i = 0; i < PT_BYTES; i++) {
+        uint64_t q = p + i;
+        if (q < g.S || q >= g.E) continue;
+        uint32_t c = b.get(i);
+        bool line_start = q == g.S || nl_before;
+        nl_before = c == '\n';
+        if (c == '\n') {
+            line_info(kind, line_rec, w.line + 1, n_lines, w);
+            continue;
+        }
+        if (line_start && w.kind == LK_HDR) rd_off[w.rec] = pos + w.rec;
+        if (w.kind == LK_SEQ && w.rec != ~0ULL && !is_ws(c)) {
+            uint32_t u = (c >= 'a' && c <= 'z') ? c - 32u : c;
+            seq[pos + w.rec] = (uint8_t)u;
+            pos++;
+        }
+    }
+}
+
+// ---- N: accession and read length per record
+__global__ void k_names(ParseGeom g, const uint64_t *__restrict__ hdr_line, const uint64_t *__restrict__ line_end,
+                        uint64_t n_reads, const uint64_t *__restrict__ rd_off, uint64_t *__restrict__ name_off,
+                        uint32_t *__restrict__ name_len, uint32_t *__restrict__ max_len) {
+    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_reads) return;
+    uint64_t j = hdr_line[r];
+    uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
+    uint64_t le = line_end[j];
+    uint64_t s = ls + 1, q = s;
+    while (q < le && !is_ws((uint8_t)g.text[q])) q++;
+    name_off[r] = s;
+    name_len[r] = (uint32_t)(q - s);
+    uint64_t L = rd_off[r + 1] - rd_off[r] - 1;
+    atomicMax(max_len, (uint32_t)(L > 0xFFFFFFFFull ? 0xFFFFFFFFull : L));
+}
+
+static inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+int parse_reads(tk_ctx *c, tk_reads *r) {
+    const char *text = r->d_text;
+    uint64_t len = r->text_len;
+    unsigned long long *d_bounds = nullptr;
+    unsigned long long hb[3] = {0, 0, 0};
+    cudaEvent_t ev;
+    prof_begin(c, TK_KID_PARSE, &ev);
+    TK_TRY(dmalloc(c, (void **)&d_bounds, 3 * sizeof(unsigned long long), "parse bounds"));
+    k_bounds<<<1, 256, 0, c->stream>>>(text, len, d_bounds);
+    c->launches++;
+    int e = cuda_check(c, cudaMemcpyAsync(hb, d_bounds, sizeof(hb), cudaMemcpyDeviceToHost, c->stream), "bounds d2h");
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "bounds sync");
+    dfree(c, d_bounds);
+    if (e) return e;
+    ParseGeom g;
+    g.text = text;
+    g.len = len;
+    g.S = hb[0];
+    g.E = hb[1];
+    g.vec = ((uintptr_t)text & 15u) == 0;
+    g.A = g.vec ? (g.S & ~15ULL) : g.S;
+    r->format = g.S >= g.E ? TK_FMT_NONE : (hb[2] == '@' ? TK_FMT_FASTQ : TK_FMT_FASTA);
+    const int fastq = r->format == TK_FMT_FASTQ;
+
+    uint64_t n_tiles = g.S >= g.E ? 0 : (g.E - g.A + PT_TILE - 1) / PT_TILE;
+    uint32_t *tile_nl = nullptr, *tile_em = nullptr, *is_hdr = nullptr;
+    uint64_t *tile_line0 = nullptr, *tile_emit0 = nullptr, *line_end = nullptr, *line_rec = nullptr, *hdr_line = nullptr;
+    uint8_t *kind = nullptr;
+    uint32_t *d_maxlen = nullptr;
+    uint64_t n_nl = 0, n_lines = 0, n_reads = 0, n_emit = 0;
+    std::vector<void *> tmp;
+    auto alloc = [&](void **p, size_t bytes, const char *what) {
+        int ee = dmalloc(c, p, bytes ? bytes : 16, what);
+        if (!ee) tmp.push_back(*p);
+        return ee;
+    };
+    do {
+        if (n_tiles == 0) break;
+        if ((e = alloc((void **)&tile_nl, n_tiles * 4, "tile newlines"))) break;
+        if ((e = alloc((void **)&tile_line0, (n_tiles + 1) * 8, "tile lines"))) break;
+        k_tile_newlines<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_nl);
+        c->launches++;
+        if ((e = scan_excl_u32_to_u64(c, tile_nl, tile_line0, n_tiles, &n_nl))) break;
+        n_lines = n_nl + 1;
+        if ((e = alloc((void **)&line_end, n_lines * 8, "line ends"))) break;
+        k_line_ends<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, line_end);
+        c->launches++;
+        if ((e = cuda_check(c, cudaMemcpyAsync(line_end + n_nl, &g.E, 8, cudaMemcpyHostToDevice, c->stream), "line end"))) break;
+        if (fastq && (n_lines & 3) != 0) {
+            e = set_err(c, TK_E_PARSE, "FASTQ input: " + std::to_string(n_lines) + " lines is not a multiple of 4");
+            break;
+        }
+        if ((e = alloc((void **)&kind, n_lines, "line kinds"))) break;
+        if ((e = alloc((void **)&is_hdr, n_lines * 4, "header flags"))) break;
+        if ((e = alloc((void **)&line_rec, n_lines * 8, "line records"))) break;
+        if ((e = cuda_check(c, cudaMemsetAsync(c->d_err, 0, DE_COUNT * 4, c->stream), "err reset"))) break;
+        uint32_t big = 0xFFFFFFFFu;
+        cudaMemcpyAsync(c->d_err + DE_PARSE + 1, &big, 4, cudaMemcpyHostToDevice, c->stream);
+        k_line_kinds<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(g, line_end, n_lines, fastq, kind, is_hdr, c->d_err);
+        c->launches++;
+        uint32_t herr[2] = {0, 0};
+        if ((e = cuda_check(c, cudaMemcpyAsync(herr, c->d_err + DE_PARSE, 8, cudaMemcpyDeviceToHost, c->stream), "err d2h"))) break;
+        if ((e = scan_excl_u32_to_u64(c, is_hdr, line_rec, n_lines, &n_reads))) break;  // syncs
+        if (herr[0]) {
+            e = set_err(c, TK_E_PARSE, "FASTQ input: malformed record at line " + std::to_string(herr[1]));
+            break;
+        }
+        if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
+        k_line_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(is_hdr, line_rec, n_lines, hdr_line);
+        c->launches++;
+        if ((e = alloc((void **)&tile_em, n_tiles * 4, "tile emits"))) break;
+        if ((e = alloc((void **)&tile_emit0, (n_tiles + 1) * 8, "tile emit offsets"))) break;
+        k_tile_emits<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, kind, line_rec, n_lines, tile_em);
+        c->launches++;
+        if ((e = scan_excl_u32_to_u64(c, tile_em, tile_emit0, n_tiles, &n_emit))) break;
+    } while (0);
+    if (e) {
+        for (void *p : tmp) dfree(c, p);
+        return e;
+    }
+    r->n_reads = n_reads;
+    r->n_bases = n_emit;
+    r->seq_len = n_emit + n_reads;
+    uint64_t seq_alloc = ((r->seq_len + 2 * SEQ_PAD + 15) / 16) * 16 + 16;
+    e = dmalloc(c, (void **)&r->d_seq_alloc, seq_alloc, "packed reads");
+    if (!e) e = dmalloc(c, (void **)&r->d_rd_off, (n_reads + 1) * 8, "read offsets");
+    if (!e) e = dmalloc(c, (void **)&r->d_name_off, (n_reads ? n_reads : 1) * 8, "name offsets");
+    if (!e) e = dmalloc(c, (void **)&r->d_name_len, (n_reads ? n_reads : 1) * 4, "name lengths");
+    if (!e) e = dmalloc(c, (void **)&d_maxlen, 4, "max length");
+    if (!e) {
+        r->d_seq = r->d_seq_alloc + SEQ_PAD;
+        cudaMemsetAsync(r->d_seq_alloc, '\n', seq_alloc, c->stream);
+        cudaMemsetAsync(d_maxlen, 0, 4, c->stream);
+        uint64_t tail = r->seq_len;
+        cudaMemcpyAsync(r->d_rd_off + n_reads, &tail, 8, cudaMemcpyHostToDevice, c->stream);
+        if (n_tiles && n_reads) {
+            k_emit<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, tile_emit0, kind, line_rec, n_lines,
+                                                                   r->d_seq, r->d_rd_off);
+            c->launches++;
+            k_names<<<grid_for(n_reads, 256), 256, 0, c->stream>>>(g, hdr_line, line_end, n_reads, r->d_rd_off,
+                                                                   r->d_name_off, r->d_name_len, d_maxlen);
+            c->launches++;
+        }
+        e = cuda_check(c, cudaMemcpyAsync(&r->max_len, d_maxlen, 4, cudaMemcpyDeviceToHost, c->stream), "maxlen d2h");
+        if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "parse sync");
+    }
+    for (void *p : tmp) dfree(c, p);
+    if (d_maxlen) dfree(c, d_maxlen);
+    prof_end(c, TK_KID_PARSE, ev, r->text_len);
+    return e;
+}
+
+}  // namespace tk

@@ -1,0 +1,665 @@
+// tk_table.cu -- the k-mer count table: K2 count-insert, HLL sizing, rehash,
+// K3 filter/histogram, sorted dump and the K4 ">COUNT\nKMER\n" formatter,
+// and catalogue loading (a stored database or a jellyfish-style dump).
+//
+// Replaces `jellyfish count/histo/dump` as Trinity drives them
+// (Trinity:2612-2638, util/insilico_read_normalization.pl:617-643).
+//
+// K2 walks the packed read array as one flat stream: each thread owns 32
+// window end positions, reads the 64 bytes [p0-32, p0+32) as four 16-byte
+// vectors, and rolls the forward and reverse-complement 2-bit words in
+// registers; a window is valid after k consecutive A/C/G/T, so read
+// separators and N bases break k-mers with no per-read bookkeeping.  Lanes of
+// a warp that hold the same key in the same step are merged (match.any) and
+// the leader adds the multiplicity with one atomic.  A key that finds no slot
+// within max_probes goes to an overflow list; the host then doubles the table
+// and re-inserts it, so no k-mer is ever dropped silently.
+#include "tk_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace tk {
+
+constexpr int CT_THREADS = 256;
+constexpr int CT_SPAN = 32;              // window end positions per thread
+constexpr int HLL_P = 12;
+constexpr int HLL_M = 1 << HLL_P;
+
+struct Window64 {
+    uint32_t w[16];
+    __device__ __forceinline__ uint32_t get(int i) const { return (w[i >> 2] >> ((i & 3) * 8)) & 0xFFu; }
+};
+
+// bytes [p0 - 32, p0 + 32) of the padded seq array (p0 is a multiple of 32)
+__device__ __forceinline__ Window64 load_window(const uint8_t *__restrict__ seq, uint64_t p0, bool active) {
+    Window64 b;
+    if (active) {
+        const uint4 *v = reinterpret_cast<const uint4 *>(seq + p0 - 32);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            uint4 x = __ldg(v + i);
+            b.w[4 * i] = x.x; b.w[4 * i + 1] = x.y; b.w[4 * i + 2] = x.z; b.w[4 * i + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 16; i++) b.w[i] = 0x0A0A0A0Au;
+    }
+    return b;
+}
+
+template <bool CANON, bool AGG>
+__global__ void __launch_bounds__(CT_THREADS) k_count(const uint8_t *__restrict__ seq, uint64_t n, int k, DevTable t,
+                                                     int max_probes, uint64_t *__restrict__ ovf_keys,
+                                                     uint32_t *__restrict__ ovf_cnt, uint64_t ovf_cap,
+                                                     unsigned long long *__restrict__ counters) {
+    const uint64_t kmask = (1ULL << (2 * k)) - 1;
+    const int shift = 2 * (k - 1);
+    const unsigned lane = lane_id();
+    const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
+    uint32_t windows = 0;
+    for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
+        const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
+        const bool active = p0 < n;
+        Window64 b = load_window(seq, p0, active);
+        uint64_t fw = 0, rc = 0;
+        int run = 0;
+#pragma unroll
+        for (int j = 0; j < 64; j++) {
+            uint32_t c = base_code(b.get(j));
+            if (c > 3) {
+                run = 0;
+            } else {
+                fw = ((fw << 2) | c) & kmask;
+                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
+                run++;
+            }
+            if (j >= 32) {
+                bool want = run >= k;
+                uint64_t key = (CANON && rc < fw) ? rc : fw;
+                uint32_t inc = 1;
+                bool lead = want;
+                if (AGG) {
+                    unsigned act = __ballot_sync(0xffffffffu, want);
+                    if (want) {
+                        unsigned peers = __match_any_sync(act, key);
+                        lead = lane == (unsigned)(__ffs(peers) - 1);
+                        inc = __popc(peers);
+                    }
+                }
+                windows += want;
+                if (lead && !tbl_add(t, key, inc, max_probes)) {
+                    unsigned long long i = atomicAdd(&counters[0], 1ULL);
+                    if (i < ovf_cap) { ovf_keys[i] = key; ovf_cnt[i] = inc; }
+                }
+            }
+        }
+    }
+    windows = warp_sum(windows);
+    if (lane == 0 && windows) atomicAdd(&counters[1], (unsigned long long)windows);
+}
+
+template <bool CANON>
+__global__ void __launch_bounds__(CT_THREADS) k_hll(const uint8_t *__restrict__ seq, uint64_t n, int k,
+                                                   uint32_t *__restrict__ regs) {
+    __shared__ uint32_t sreg[HLL_M];
+    for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS) sreg[i] = 0;
+    __syncthreads();
+    const uint64_t kmask = (1ULL << (2 * k)) - 1;
+    const int shift = 2 * (k - 1);
+    const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
+    for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
+        const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
+        if (p0 >= n) continue;
+        Window64 b = load_window(seq, p0, true);
+        uint64_t fw = 0, rc = 0;
+        int run = 0;
+#pragma unroll
+        for (int j = 0; j < 64; j++) {
+            uint32_t c = base_code(b.get(j));
+            if (c > 3) {
+                run = 0;
+            } else {
+                fw = ((fw << 2) | c) & kmask;
+                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
+                run++;
+            }
+            if (j >= 32 && run >= k) {
+                uint64_t key = (CANON && rc < fw) ? rc : fw;
+                uint64_t h = mix64(key ^ 0x5851F42D4C957F2DULL);
+                uint32_t idx = (uint32_t)(h >> (64 - HLL_P));
+                uint32_t rank = (uint32_t)__clzll((long long)((h << HLL_P) | (1ULL << (HLL_P - 1)))) + 1u;
+                if (rank > sreg[idx]) atomicMax(&sreg[idx], rank);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS)
+        if (sreg[i]) atomicMax(&regs[i], sreg[i]);
+}
+
+__global__ void k_rehash(const Slot *__restrict__ old, uint64_t old_cap, DevTable t, int max_probes,
+                         uint64_t *__restrict__ ovf_keys, uint32_t *__restrict__ ovf_cnt, uint64_t ovf_cap,
+                         unsigned long long *__restrict__ counters) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < old_cap; i += (uint64_t)gridDim.x * blockDim.x) {
+        ulonglong2 v = __ldcs(reinterpret_cast<const ulonglong2 *>(&old[i]));
+        if (v.x == EMPTY_KEY) continue;
+        if (!tbl_add(t, v.x, (uint32_t)v.y, max_probes)) {
+            unsigned long long j = atomicAdd(&counters[0], 1ULL);
+            if (j < ovf_cap) { ovf_keys[j] = v.x; ovf_cnt[j] = (uint32_t)v.y; }
+        }
+    }
+}
+
+__global__ void k_insert_pairs(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ cnt, uint64_t n, DevTable t,
+                               int max_probes, uint64_t *__restrict__ ovf_keys, uint32_t *__restrict__ ovf_cnt,
+                               uint64_t ovf_cap, unsigned long long *__restrict__ counters) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t key = keys[i];
+        uint32_t c = cnt ? cnt[i] : 1u;
+        if (!tbl_add(t, key, c, max_probes)) {
+            unsigned long long j = atomicAdd(&counters[0], 1ULL);
+            if (j < ovf_cap) { ovf_keys[j] = key; ovf_cnt[j] = c; }
+        }
+    }
+}
+
+__global__ void k_fill_empty(Slot *slots, uint64_t cap, uint32_t init_val) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+        ulonglong2 v;
+        v.x = EMPTY_KEY;
+        v.y = init_val;
+        reinterpret_cast<ulonglong2 *>(slots)[i] = v;
+    }
+}
+
+__global__ void k_occupied(const Slot *__restrict__ slots, uint64_t cap, unsigned long long *out) {
+    uint32_t n = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x)
+        n += __ldcs(&slots[i].key) != EMPTY_KEY;
+    n = warp_sum(n);
+    if (lane_id() == 0 && n) atomicAdd(out, (unsigned long long)n);
+}
+
+// K3: keys with count >= min_count, warp-aggregated append (order is fixed by the sort that follows)
+__global__ void k_compact(const Slot *__restrict__ slots, uint64_t cap, uint32_t min_count, uint64_t *__restrict__ okeys,
+                          uint32_t *__restrict__ ovals, unsigned long long *__restrict__ n_out) {
+    const unsigned lane = lane_id();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < cap; base += stride) {
+        uint64_t i = base + threadIdx.x;
+        ulonglong2 v;
+        v.x = EMPTY_KEY;
+        v.y = 0;
+        if (i < cap) v = __ldcs(reinterpret_cast<const ulonglong2 *>(&slots[i]));
+        bool sel = v.x != EMPTY_KEY && (uint32_t)v.y >= min_count;
+        unsigned m = __ballot_sync(0xffffffffu, sel);
+        if (!m) continue;
+        unsigned long long wbase = 0;
+        if (lane == 0) wbase = atomicAdd(n_out, (unsigned long long)__popc(m));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        if (sel) {
+            uint64_t o = wbase + __popc(m & ((1u << lane) - 1u));
+            okeys[o] = v.x;
+            ovals[o] = (uint32_t)v.y;
+        }
+    }
+}
+
+// jellyfish histo bins: [0] below low, [1 + c - low], [nb - 1] above high
+__global__ void k_histo(const Slot *__restrict__ slots, uint64_t cap, uint64_t low, uint64_t high,
+                        unsigned long long *__restrict__ hist, int use_smem) {
+    extern __shared__ uint32_t sh[];
+    const uint64_t nb = high - low + 3;
+    if (use_smem) {
+        for (uint64_t i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+        __syncthreads();
+    }
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+        ulonglong2 v = __ldcs(reinterpret_cast<const ulonglong2 *>(&slots[i]));
+        if (v.x == EMPTY_KEY) continue;
+        uint64_t c = (uint32_t)v.y;
+        uint64_t bin = c < low ? 0 : (c > high ? nb - 1 : 1 + c - low);
+        if (use_smem) atomicAdd(&sh[bin], 1u);
+        else atomicAdd(&hist[bin], 1ULL);
+    }
+    if (use_smem) {
+        __syncthreads();
+        for (uint64_t i = threadIdx.x; i < nb; i += blockDim.x)
+            if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
+    }
+}
+
+__device__ __forceinline__ uint32_t dec_digits(uint32_t v) {
+    uint32_t d = 1;
+    while (v >= 10) { v /= 10; d++; }
+    return d;
+}
+
+// K4 pass 1: record lengths ">" digits "\n" k "\n"
+__global__ void k_dump_len(const uint32_t *__restrict__ cnt, uint64_t n, int k, uint32_t *__restrict__ len) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) len[i] = 3u + dec_digits(cnt[i]) + (uint32_t)k;
+}
+
+// K4 pass 2: write one record per thread
+__global__ void k_dump_write(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ cnt,
+                             const uint64_t *__restrict__ off, uint64_t n, int k, char *__restrict__ out) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    char *p = out + off[i];
+    uint32_t c = cnt[i];
+    uint32_t nd = dec_digits(c);
+    p[0] = '>';
+    for (int d = (int)nd; d >= 1; d--) { p[d] = (char)('0' + c % 10); c /= 10; }
+    p[nd + 1] = '\n';
+    uint64_t key = keys[i];
+    char *q = p + nd + 2;
+    for (int j = 0; j < k; j++) q[j] = "ACGT"[(key >> (2 * (k - 1 - j))) & 3];
+    q[k] = '\n';
+}
+
+// dump records parsed as reads: name = decimal count, sequence = k-mer
+__global__ void k_load_dump(const char *__restrict__ text, const uint64_t *__restrict__ name_off,
+                            const uint32_t *__restrict__ name_len, const uint8_t *__restrict__ seq,
+                            const uint64_t *__restrict__ rd_off, uint64_t n, int k, int canonical,
+                            uint64_t *__restrict__ keys, uint32_t *__restrict__ cnt, uint32_t *__restrict__ err) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const char *h = text + name_off[i];
+    uint32_t hl = name_len[i];
+    uint64_t c = 0;
+    bool bad = hl == 0;
+    for (uint32_t j = 0; j < hl; j++) {
+        uint32_t d = (uint8_t)h[j] - (uint32_t)'0';
+        if (d > 9) { bad = true; break; }
+        c = c * 10 + d;
+        if (c > 0xFFFFFFFFull) c = 0xFFFFFFFFull;
+    }
+    uint64_t s = rd_off[i], L = rd_off[i + 1] - s - 1;
+    if (L != (uint64_t)k) bad = true;
+    uint64_t fw = 0, rc = 0;
+    if (!bad) {
+        for (int j = 0; j < k; j++) {
+            uint32_t b = base_code(seq[s + j]);
+            if (b > 3) { bad = true; break; }
+            fw = (fw << 2) | b;
+            rc |= (uint64_t)(3u - b) << (2 * j);
+        }
+    }
+    if (bad) {
+        atomicExch(&err[DE_PARSE], 1u);
+        atomicMin(&err[DE_PARSE + 1], (uint32_t)min((uint64_t)0xFFFFFFFEull, i + 1));
+        keys[i] = EMPTY_KEY;
+        cnt[i] = 0;
+        return;
+    }
+    keys[i] = (canonical && rc < fw) ? rc : fw;
+    cnt[i] = (uint32_t)c;
+}
+
+// drop EMPTY keys written for bad records (there are none when err is clear)
+static inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+static unsigned stream_grid(tk_ctx *c, uint64_t n, int threads) {
+    uint64_t g = (n + threads - 1) / threads;
+    uint64_t cap = (uint64_t)c->sm_count * 8;
+    return (unsigned)std::max<uint64_t>(1, std::min(g, cap));
+}
+
+// ------------------------------------------------------------------ host side
+
+int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val) {
+    tk_ctx *c = t->ctx;
+    Slot *s = nullptr;
+    TK_TRY(dmalloc(c, (void **)&s, capacity * sizeof(Slot), "k-mer table"));
+    k_fill_empty<<<stream_grid(c, capacity, 256), 256, 0, c->stream>>>(s, capacity, init_val);
+    c->launches++;
+    t->t.slots = s;
+    t->t.mask = capacity - 1;
+    t->capacity = capacity;
+    return check_launch(c, "table fill");
+}
+
+int table_alloc(tk_table *t, uint64_t capacity) { return table_alloc_init(t, capacity, 0); }
+
+static int overflow_reset(tk_table *t) {
+    return cuda_check(t->ctx, cudaMemsetAsync(t->d_counters, 0, sizeof(unsigned long long), t->ctx->stream), "ovf reset");
+}
+
+static int overflow_read(tk_table *t, unsigned long long *n) {
+    tk_ctx *c = t->ctx;
+    TK_CUDA(c, cudaMemcpyAsync(n, t->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+    TK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TK_OK;
+}
+
+// Moves every entry to a table of new_capacity slots.
+int table_rehash(tk_table *t, uint64_t new_capacity) {
+    tk_ctx *c = t->ctx;
+    for (int attempt = 0; attempt < 8; attempt++) {
+        Slot *old = t->t.slots;
+        uint64_t old_cap = t->capacity;
+        TK_TRY(table_alloc(t, new_capacity));
+        TK_TRY(overflow_reset(t));
+        if (old) {
+            k_rehash<<<stream_grid(c, old_cap, 256), 256, 0, c->stream>>>(old, old_cap, t->t, c->max_probes, t->d_ovf,
+                                                                           (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
+                                                                           t->d_counters);
+            c->launches++;
+        }
+        unsigned long long ovf = 0;
+        TK_TRY(overflow_read(t, &ovf));
+        if (ovf == 0) {
+            dfree(c, old);
+            return TK_OK;
+        }
+        // a probe run too long even in the larger table: go bigger from the old copy
+        dfree(c, t->t.slots);
+        t->t.slots = old;
+        t->t.mask = old_cap - 1;
+        t->capacity = old_cap;
+        new_capacity *= 2;
+    }
+    return set_err(c, TK_E_TABLE_FULL, "rehash could not place every key");
+}
+
+// Re-inserts the overflow list after doubling the table, until it drains.
+static int drain_overflow(tk_table *t) {
+    tk_ctx *c = t->ctx;
+    for (int round = 0; round < 8; round++) {
+        unsigned long long ovf = 0;
+        TK_TRY(overflow_read(t, &ovf));
+        if (ovf == 0) return TK_OK;
+        if (ovf > t->ovf_cap)
+            return set_err(c, TK_E_TABLE_FULL,
+                           "table overflow list overran (" + std::to_string(ovf) + " keys); create the table with a larger capacity");
+        // copy the pending pairs aside, grow, and insert them
+        uint64_t *pk = nullptr;
+        uint32_t *pc = nullptr;
+        TK_TRY(dmalloc(c, (void **)&pk, ovf * 8, "overflow keys"));
+        int e = dmalloc(c, (void **)&pc, ovf * 4, "overflow counts");
+        if (!e) {
+            cudaMemcpyAsync(pk, t->d_ovf, ovf * 8, cudaMemcpyDeviceToDevice, c->stream);
+            cudaMemcpyAsync(pc, t->d_ovf + t->ovf_cap, ovf * 4, cudaMemcpyDeviceToDevice, c->stream);
+            e = table_rehash(t, t->capacity * 2);
+        }
+        if (!e) e = overflow_reset(t);
+        if (!e) {
+            k_insert_pairs<<<stream_grid(c, ovf, 256), 256, 0, c->stream>>>(pk, pc, ovf, t->t, c->max_probes, t->d_ovf,
+                                                                             (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
+                                                                             t->d_counters);
+            c->launches++;
+            e = check_launch(c, "overflow insert");
+        }
+        dfree(c, pk);
+        dfree(c, pc);
+        if (e) return e;
+    }
+    return set_err(c, TK_E_TABLE_FULL, "overflow did not drain");
+}
+
+static double hll_estimate(const uint32_t *regs) {
+    double sum = 0;
+    int zeros = 0;
+    for (int i = 0; i < HLL_M; i++) {
+        sum += std::ldexp(1.0, -(int)regs[i]);
+        zeros += regs[i] == 0;
+    }
+    double m = HLL_M, alpha = 0.7213 / (1.0 + 1.079 / m);
+    double est = alpha * m * m / sum;
+    if (est <= 2.5 * m && zeros) est = m * std::log(m / zeros);
+    return est;
+}
+
+static uint64_t pow2_at_least(uint64_t x) {
+    uint64_t p = 1024;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// Counts every window of a packed read array into the table.
+int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
+    tk_ctx *c = t->ctx;
+    if (seq_len == 0) return TK_OK;
+    const uint64_t n = seq_len;
+    const unsigned grid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((n + CT_THREADS * CT_SPAN - 1) / (CT_THREADS * CT_SPAN), (uint64_t)c->sm_count * 16));
+    if (t->d_hll) {
+        // size the table from the union estimate of everything counted so far
+        cudaEvent_t ev;
+        prof_begin(c, TK_KID_HLL, &ev);
+        if (t->canonical) k_hll<true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->d_hll);
+        else k_hll<false><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->d_hll);
+        c->launches++;
+        prof_end(c, TK_KID_HLL, ev, n);
+        std::vector<uint32_t> regs(HLL_M);
+        TK_CUDA(c, cudaMemcpyAsync(regs.data(), t->d_hll, HLL_M * 4, cudaMemcpyDeviceToHost, c->stream));
+        TK_CUDA(c, cudaStreamSynchronize(c->stream));
+        double est = hll_estimate(regs.data());
+        uint64_t want = pow2_at_least((uint64_t)(est * 1.08 / t->max_load) + 1);
+        if (t->capacity == 0) TK_TRY(table_alloc(t, want));
+        else if (want > t->capacity) TK_TRY(table_rehash(t, want));
+    } else if (t->capacity == 0) {
+        TK_TRY(table_alloc(t, 1024));
+    }
+    TK_TRY(overflow_reset(t));
+    cudaEvent_t ev;
+    prof_begin(c, TK_KID_COUNT, &ev);
+    uint32_t *ovc = (uint32_t *)(t->d_ovf + t->ovf_cap);
+    if (t->canonical)
+        k_count<true, true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->t, c->max_probes, t->d_ovf, ovc,
+                                                                 t->ovf_cap, t->d_counters);
+    else
+        k_count<false, true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->t, c->max_probes, t->d_ovf, ovc,
+                                                                  t->ovf_cap, t->d_counters);
+    c->launches++;
+    prof_end(c, TK_KID_COUNT, ev, 0);
+    TK_TRY(check_launch(c, "count"));
+    // windows counted by this launch
+    unsigned long long hc[2] = {0, 0};
+    TK_CUDA(c, cudaMemcpyAsync(hc, t->d_counters, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+    TK_CUDA(c, cudaStreamSynchronize(c->stream));
+    prof_add_units(c, TK_KID_COUNT, hc[1]);
+    t->total += hc[1];
+    cudaMemsetAsync(t->d_counters + 1, 0, sizeof(unsigned long long), c->stream);
+    t->distinct_valid = false;
+    return drain_overflow(t);
+}
+
+static int table_distinct(tk_table *t) {
+    tk_ctx *c = t->ctx;
+    if (t->distinct_valid) return TK_OK;
+    if (!t->capacity) {
+        t->distinct = 0;
+        t->distinct_valid = true;
+        return TK_OK;
+    }
+    unsigned long long *d = nullptr, h = 0;
+    TK_TRY(dmalloc(c, (void **)&d, 8, "occupied"));
+    cudaMemsetAsync(d, 0, 8, c->stream);
+    k_occupied<<<stream_grid(c, t->capacity, 256), 256, 0, c->stream>>>(t->t.slots, t->capacity, d);
+    c->launches++;
+    int e = cuda_check(c, cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, c->stream), "occupied d2h");
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "occupied sync");
+    dfree(c, d);
+    if (!e) {
+        t->distinct = h;
+        t->distinct_valid = true;
+    }
+    return e;
+}
+
+int table_info(tk_table *t, uint64_t *distinct, uint64_t *total, uint64_t *capacity) {
+    TK_TRY(table_distinct(t));
+    if (distinct) *distinct = t->distinct;
+    if (total) *total = t->total;
+    if (capacity) *capacity = t->capacity;
+    return TK_OK;
+}
+
+int table_histo(tk_table *t, uint64_t low, uint64_t high, uint64_t *hist) {
+    tk_ctx *c = t->ctx;
+    if (high < low) return set_err(c, TK_E_INVAL, "histo: high < low");
+    uint64_t nb = high - low + 3;
+    unsigned long long *d = nullptr;
+    TK_TRY(dmalloc(c, (void **)&d, nb * 8, "histo"));
+    cudaMemsetAsync(d, 0, nb * 8, c->stream);
+    int e = TK_OK;
+    if (t->capacity) {
+        cudaEvent_t ev;
+        prof_begin(c, TK_KID_COMPACT, &ev);
+        size_t smem = nb * 4;
+        int use_smem = smem <= 96 * 1024;
+        if (use_smem && smem > 48 * 1024)
+            cudaFuncSetAttribute(k_histo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_histo<<<(unsigned)c->sm_count * 2, 512, use_smem ? smem : 0, c->stream>>>(t->t.slots, t->capacity, low, high, d,
+                                                                                    use_smem);
+        c->launches++;
+        prof_end(c, TK_KID_COMPACT, ev, t->capacity);
+        e = check_launch(c, "histo");
+    }
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(hist, d, nb * 8, cudaMemcpyDeviceToHost, c->stream), "histo d2h");
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "histo sync");
+    dfree(c, d);
+    return e;
+}
+
+// Sorted (key, count) pairs with count >= min_count into freshly allocated
+// device arrays (caller frees with dfree).
+int table_sorted_pairs(tk_table *t, uint32_t min_count, uint64_t **keys_out, uint32_t **cnt_out, uint64_t *n_out) {
+    tk_ctx *c = t->ctx;
+    *keys_out = nullptr;
+    *cnt_out = nullptr;
+    *n_out = 0;
+    TK_TRY(table_distinct(t));
+    uint64_t upper = std::max<uint64_t>(t->distinct, 1);
+    uint64_t *k0 = nullptr, *k1 = nullptr;
+    uint32_t *v0 = nullptr, *v1 = nullptr;
+    unsigned long long *d_n = nullptr;
+    int e = dmalloc(c, (void **)&k0, upper * 8, "dump keys");
+    if (!e) e = dmalloc(c, (void **)&v0, upper * 4, "dump counts");
+    if (!e) e = dmalloc(c, (void **)&k1, upper * 8, "dump keys tmp");
+    if (!e) e = dmalloc(c, (void **)&v1, upper * 4, "dump counts tmp");
+    if (!e) e = dmalloc(c, (void **)&d_n, 8, "dump n");
+    unsigned long long hn = 0;
+    if (!e && t->capacity) {
+        cudaMemsetAsync(d_n, 0, 8, c->stream);
+        cudaEvent_t ev;
+        prof_begin(c, TK_KID_COMPACT, &ev);
+        k_compact<<<stream_grid(c, t->capacity, 256), 256, 0, c->stream>>>(t->t.slots, t->capacity, min_count, k0, v0, d_n);
+        c->launches++;
+        prof_end(c, TK_KID_COMPACT, ev, t->capacity);
+        e = cuda_check(c, cudaMemcpyAsync(&hn, d_n, 8, cudaMemcpyDeviceToHost, c->stream), "compact n");
+        if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "compact sync");
+    }
+    bool in_tmp = false;
+    if (!e && hn > 1) {
+        cudaEvent_t ev;
+        prof_begin(c, TK_KID_SORT, &ev);
+        e = radix_sort_pairs(c, k0, v0, hn, 2 * t->k, k1, v1, &in_tmp);
+        prof_end(c, TK_KID_SORT, ev, hn);
+    }
+    if (d_n) dfree(c, d_n);
+    if (e) {
+        dfree(c, k0); dfree(c, k1); dfree(c, v0); dfree(c, v1);
+        return e;
+    }
+    if (in_tmp) {
+        std::swap(k0, k1);
+        std::swap(v0, v1);
+    }
+    dfree(c, k1);
+    dfree(c, v1);
+    *keys_out = k0;
+    *cnt_out = v0;
+    *n_out = hn;
+    return TK_OK;
+}
+
+// K4: format sorted pairs as ">COUNT\nKMER\n" into a device buffer.
+int format_dump(tk_ctx *c, const uint64_t *keys, const uint32_t *cnt, uint64_t n, int k, char **text_out,
+                uint64_t *len_out) {
+    *text_out = nullptr;
+    *len_out = 0;
+    if (n == 0) return TK_OK;
+    uint32_t *lens = nullptr;
+    uint64_t *offs = nullptr;
+    TK_TRY(dmalloc(c, (void **)&lens, n * 4, "dump lengths"));
+    int e = dmalloc(c, (void **)&offs, n * 8, "dump offsets");
+    uint64_t total = 0;
+    cudaEvent_t ev;
+    prof_begin(c, TK_KID_DUMP, &ev);
+    if (!e) {
+        k_dump_len<<<grid_for(n, 256), 256, 0, c->stream>>>(cnt, n, k, lens);
+        c->launches++;
+        e = scan_excl_u32_to_u64(c, lens, offs, n, &total);
+    }
+    char *text = nullptr;
+    if (!e) e = dmalloc(c, (void **)&text, total, "dump text");
+    if (!e) {
+        k_dump_write<<<grid_for(n, 256), 256, 0, c->stream>>>(keys, cnt, offs, n, k, text);
+        c->launches++;
+        e = check_launch(c, "dump write");
+    }
+    prof_end(c, TK_KID_DUMP, ev, n);
+    dfree(c, lens);
+    if (offs) dfree(c, offs);
+    if (e) {
+        if (text) dfree(c, text);
+        return e;
+    }
+    *text_out = text;
+    *len_out = total;
+    return TK_OK;
+}
+
+int table_insert_pairs(tk_table *t, const uint64_t *d_keys, const uint32_t *d_cnt, uint64_t n) {
+    tk_ctx *c = t->ctx;
+    if (n == 0) return TK_OK;
+    TK_TRY(table_distinct(t));
+    uint64_t need = pow2_at_least((uint64_t)((double)(t->distinct + n) / t->max_load) + 1);
+    if (t->capacity == 0) TK_TRY(table_alloc(t, need));
+    else if (need > t->capacity) TK_TRY(table_rehash(t, need));
+    TK_TRY(overflow_reset(t));
+    cudaEvent_t ev;
+    prof_begin(c, TK_KID_LOAD, &ev);
+    k_insert_pairs<<<stream_grid(c, n, 256), 256, 0, c->stream>>>(d_keys, d_cnt, n, t->t, c->max_probes, t->d_ovf,
+                                                                   (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
+                                                                   t->d_counters);
+    c->launches++;
+    prof_end(c, TK_KID_LOAD, ev, n);
+    TK_TRY(check_launch(c, "insert pairs"));
+    t->distinct_valid = false;
+    return drain_overflow(t);
+}
+
+int table_load_dump_reads(tk_table *t, const tk_reads *r) {
+    tk_ctx *c = t->ctx;
+    uint64_t n = r->n_reads;
+    if (n == 0) return TK_OK;
+    uint64_t *keys = nullptr;
+    uint32_t *cnt = nullptr;
+    TK_TRY(dmalloc(c, (void **)&keys, n * 8, "catalogue keys"));
+    int e = dmalloc(c, (void **)&cnt, n * 4, "catalogue counts");
+    if (!e) e = cuda_check(c, cudaMemsetAsync(c->d_err, 0, DE_COUNT * 4, c->stream), "err reset");
+    if (!e) {
+        uint32_t big = 0xFFFFFFFFu;
+        cudaMemcpyAsync(c->d_err + DE_PARSE + 1, &big, 4, cudaMemcpyHostToDevice, c->stream);
+        k_load_dump<<<grid_for(n, 256), 256, 0, c->stream>>>(r->d_text, r->d_name_off, r->d_name_len, r->d_seq, r->d_rd_off,
+                                                             n, t->k, t->canonical, keys, cnt, c->d_err);
+        c->launches++;
+        uint32_t herr[2] = {0, 0};
+        e = cuda_check(c, cudaMemcpyAsync(herr, c->d_err + DE_PARSE, 8, cudaMemcpyDeviceToHost, c->stream), "load err");
+        if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "load sync");
+        if (!e && herr[0])
+            e = set_err(c, TK_E_PARSE, "k-mer catalogue: record " + std::to_string(herr[1]) +
+                                           " is not '>COUNT' followed by a " + std::to_string(t->k) + "-mer of A/C/G/T");
+    }
+    if (!e) e = table_insert_pairs(t, keys, cnt, n);
+    dfree(c, keys);
+    if (cnt) dfree(c, cnt);
+    return e;
+}
+
+}  // namespace tk

@@ -1,0 +1,195 @@
+// tk_warp.cuh -- per-read warp machinery shared by the coverage-statistics
+// (K5) and read-to-component (K6) kernels.
+//
+// One warp owns one read.  Lane l owns `span` consecutive windows starting at
+// window l*span: it primes the rolling forward/reverse-complement words with
+// k-1 bases and then rolls one base per window, so each lane reads span+k-1
+// bytes of the read (L1-resident) and its values stay in registers.  The
+// warp then sorts its 32*S register values with a bitonic network (compare
+// exchanges inside a lane for strides < S, xor-shuffles across lanes for the
+// rest).  Element i of the sorted sequence lives in lane i / S, register i % S.
+#pragma once
+#include "tk_internal.cuh"
+
+namespace tk {
+
+// S = registers per lane (power of two) able to hold `span` windows
+// f(j, valid, key) is called for j = 0..S-1 (window lane*span + j)
+template <int S, bool CANON, typename F>
+__device__ __forceinline__ void lane_windows(const uint8_t *__restrict__ seq, uint64_t start, uint32_t nwin,
+                                             uint32_t span, int k, F &&f) {
+    const unsigned lane = lane_id();
+    const uint64_t kmask = (1ULL << (2 * k)) - 1;
+    const int shift = 2 * (k - 1);
+    const uint32_t w0 = lane * span;
+    uint64_t fw = 0, rc = 0;
+    int run = 0;
+    const uint8_t *p = seq + start + w0;
+    if (w0 < nwin) {
+        for (int i = 0; i < k - 1; i++) {
+            uint32_t c = base_code(__ldg(p + i));
+            if (c > 3) {
+                run = 0;
+            } else {
+                fw = ((fw << 2) | c) & kmask;
+                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
+                run++;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+        bool in = (uint32_t)j < span && w0 + j < nwin;
+        bool valid = false;
+        uint64_t key = 0;
+        if (in) {
+            uint32_t c = base_code(__ldg(p + k - 1 + j));
+            if (c > 3) {
+                run = 0;
+            } else {
+                fw = ((fw << 2) | c) & kmask;
+                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
+                run++;
+            }
+            valid = run >= k;
+            key = (CANON && rc < fw) ? rc : fw;
+        }
+        f(j, valid, key);
+    }
+}
+
+template <int S>
+__device__ __forceinline__ void warp_bitonic_sort(uint32_t (&v)[S]) {
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (int size = 2; size <= 32 * S; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride < S) {
+#pragma unroll
+                for (int j = 0; j < S; j++) {
+                    const int pj = j ^ stride;
+                    if (pj > j) {
+                        const unsigned i = lane * S + j;
+                        const bool asc = (i & size) == 0;
+                        uint32_t a = v[j], b = v[pj];
+                        bool sw = asc ? (a > b) : (a < b);
+                        v[j] = sw ? b : a;
+                        v[pj] = sw ? a : b;
+                    }
+                }
+            } else {
+                const int ls = stride / S;
+#pragma unroll
+                for (int j = 0; j < S; j++) {
+                    uint32_t o = __shfl_xor_sync(0xffffffffu, v[j], ls);
+                    const unsigned i = lane * S + j;
+                    const bool asc = (i & size) == 0;
+                    const bool lower = (lane & ls) == 0;
+                    uint32_t mn = min(v[j], o), mx = max(v[j], o);
+                    v[j] = (lower == asc) ? mn : mx;
+                }
+            }
+        }
+    }
+}
+
+// element m of the sorted blocked sequence, broadcast to the warp
+template <int S>
+__device__ __forceinline__ uint32_t warp_elem(const uint32_t (&v)[S], uint32_t m) {
+    uint32_t jj = m % S, x = v[0];
+#pragma unroll
+    for (int j = 1; j < S; j++)
+        if ((uint32_t)j == jj) x = v[j];
+    return __shfl_sync(0xffffffffu, x, (int)(m / S));
+}
+
+__device__ __forceinline__ void warp_sum_u128(uint64_t &hi, uint64_t &lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        uint64_t ohi = __shfl_xor_sync(0xffffffffu, hi, o);
+        uint64_t olo = __shfl_xor_sync(0xffffffffu, lo, o);
+        uint64_t nlo = lo + olo;
+        hi = hi + ohi + (nlo < lo ? 1u : 0u);
+        lo = nlo;
+    }
+}
+
+// Statistics in the documented arithmetic: mean = (float)(sum / n);
+// stdev = (float)sqrt((hi * 2^64 + lo) / (n * n)) with hi:lo = n*sumsq - sum^2.
+__device__ __forceinline__ void finish_stats(uint32_t n, uint64_t sum, uint64_t sq_hi, uint64_t sq_lo,
+                                             float *mean, float *stdev) {
+    if (n == 0) {
+        *mean = 0.0f;
+        *stdev = 0.0f;
+        return;
+    }
+    unsigned __int128 sq = ((unsigned __int128)sq_hi << 64) | sq_lo;
+    unsigned __int128 num = (unsigned __int128)n * sq - (unsigned __int128)sum * sum;
+    double dhi = (double)(uint64_t)(num >> 64), dlo = (double)(uint64_t)num;
+    double dn = (double)n;
+    double var = __ddiv_rn(__dadd_rn(__dmul_rn(dhi, 18446744073709551616.0), dlo), __dmul_rn(dn, dn));
+    *mean = __double2float_rn(__ddiv_rn((double)sum, dn));
+    *stdev = __double2float_rn(__dsqrt_rn(var));
+}
+
+// Block-wide bitonic sort of n2 (power of two) values in global scratch.
+__device__ __forceinline__ void block_bitonic_sort(uint32_t *v, uint32_t n2) {
+    for (uint32_t size = 2; size <= n2; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncthreads();
+            for (uint32_t t = threadIdx.x; t < n2 / 2; t += blockDim.x) {
+                uint32_t i = 2 * t - (t & (stride - 1));   // i has bit `stride` clear
+                uint32_t p = i + stride;
+                bool asc = (i & size) == 0;
+                uint32_t a = v[i], b = v[p];
+                if (asc ? (a > b) : (a < b)) {
+                    v[i] = b;
+                    v[p] = a;
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Fills scratch[0, n2) with the read's per-window values (PAD for windows with
+// a non-ACGT base and for the padding); g(valid, key) maps a window to its value.
+template <bool CANON, typename G>
+__device__ __forceinline__ void block_window_values(const uint8_t *__restrict__ seq, uint64_t start, uint32_t nwin,
+                                                    uint32_t n2, int k, uint32_t *scratch, G &&g) {
+    const uint64_t kmask = (1ULL << (2 * k)) - 1;
+    const int shift = 2 * (k - 1);
+    const uint32_t span = (nwin + blockDim.x - 1) / blockDim.x;
+    const uint32_t w0 = threadIdx.x * span;
+    uint64_t fw = 0, rc = 0;
+    int run = 0;
+    if (w0 < nwin) {
+        const uint8_t *p = seq + start + w0;
+        for (int i = 0; i < k - 1; i++) {
+            uint32_t c = base_code(p[i]);
+            if (c > 3) run = 0;
+            else {
+                fw = ((fw << 2) | c) & kmask;
+                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
+                run++;
+            }
+        }
+        for (uint32_t j = 0; j < span && w0 + j < nwin; j++) {
+            uint32_t c = base_code(p[k - 1 + j]);
+            if (c > 3) run = 0;
+            else {
+                fw = ((fw << 2) | c) & kmask;
+                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
+                run++;
+            }
+            bool valid = run >= k;
+            uint64_t key = (CANON && rc < fw) ? rc : fw;
+            scratch[w0 + j] = valid ? g(key) : PAD_VAL;
+        }
+    }
+    for (uint32_t i = nwin + threadIdx.x; i < n2; i += blockDim.x) scratch[i] = PAD_VAL;
+    __syncthreads();
+}
+
+}  // namespace tk

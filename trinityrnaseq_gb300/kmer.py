@@ -1,0 +1,334 @@
+"""Host-side mirror of the three reference tools over the C ABI.
+
+``KmerTable`` is ``jellyfish count/histo/dump`` (Trinity:2612-2638),
+``coverage_stats`` is Inchworm's ``fastaToKmerCoverageStats``
+(util/insilico_read_normalization.pl:837-846) and ``ReadsToTranscripts`` is
+Chrysalis' ``ReadsToTranscripts`` (Trinity:2237-2251).  The ``format_*``
+helpers write the reference's text formats; the C++ drop-in executables under
+``tools/`` write the same bytes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import native as N
+
+Buffer = Union[bytes, bytearray, memoryview, np.ndarray]
+
+
+def _host_ptr(buf: Buffer) -> Tuple[int, int, object]:
+    """(address, length, keep-alive) of a host buffer."""
+    if isinstance(buf, np.ndarray):
+        a = np.ascontiguousarray(buf)
+        return a.ctypes.data, a.nbytes, a
+    if isinstance(buf, (bytes, bytearray)):
+        a = np.frombuffer(buf, dtype=np.uint8)
+        return (a.ctypes.data if a.size else 0), a.size, (buf, a)
+    if isinstance(buf, memoryview):
+        a = np.frombuffer(buf, dtype=np.uint8)
+        return (a.ctypes.data if a.size else 0), a.size, (buf, a)
+    raise TypeError(f"unsupported buffer type {type(buf)}")
+
+
+class Context:
+    """A CUDA device context with its own stream (tk_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = N.load()
+        h = C.c_void_p()
+        st = self.lib.tk_ctx_create(device, C.byref(h))
+        N.check(st, "tk_ctx_create")
+        self.h = h
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.tk_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st: int, where: str) -> None:
+        N.check(st, where, self.h)
+
+    @property
+    def stream(self) -> int:
+        return self.lib.tk_ctx_stream(self.h) or 0
+
+    def synchronize(self) -> None:
+        self.check(self.lib.tk_ctx_synchronize(self.h), "tk_ctx_synchronize")
+
+    def set_profiling(self, on: bool) -> None:
+        self.check(self.lib.tk_ctx_set_profiling(self.h, int(on)), "tk_ctx_set_profiling")
+
+    def reset_profile(self) -> None:
+        self.check(self.lib.tk_ctx_reset_profile(self.h), "tk_ctx_reset_profile")
+
+    def profile(self, kernel: str) -> Tuple[float, int, int]:
+        ms, ln, un = C.c_double(), C.c_uint64(), C.c_uint64()
+        self.check(self.lib.tk_ctx_profile(self.h, N.KID[kernel], C.byref(ms), C.byref(ln), C.byref(un)),
+                   "tk_ctx_profile")
+        return ms.value, ln.value, un.value
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.tk_ctx_kernel_launches(self.h))
+
+    def set_reprobes(self, n: int) -> None:
+        self.check(self.lib.tk_ctx_set_reprobes(self.h, int(n)), "tk_ctx_set_reprobes")
+
+    def mem_info(self) -> Tuple[int, int]:
+        f, t = C.c_uint64(), C.c_uint64()
+        self.check(self.lib.tk_ctx_mem_info(self.h, C.byref(f), C.byref(t)), "tk_ctx_mem_info")
+        return f.value, t.value
+
+
+class ReadSet:
+    """FASTA/FASTQ text parsed into a device-resident read set (tk_reads).
+
+    ``text`` is a host buffer, or a device address (int) with ``length`` and
+    ``device=True``; a device text must outlive the read set."""
+
+    def __init__(self, ctx: Context, text, length: Optional[int] = None, device: bool = False):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = C.c_void_p()
+        if device:
+            ptr, n, keep = int(text), int(length), None
+            where = N.TK_DEVICE
+        else:
+            ptr, n, keep = _host_ptr(text)
+            where = N.TK_HOST
+        self._keep = keep if device else None   # a host text is copied; a device text is aliased
+        self._host_text = None if device else text
+        ctx.check(self.lib.tk_reads_parse(ctx.h, C.c_void_p(ptr), n, where, C.byref(h)), "tk_reads_parse")
+        self.h = h
+        nr, nb, ml, fm = C.c_uint64(), C.c_uint64(), C.c_uint32(), C.c_int()
+        ctx.check(self.lib.tk_reads_info(h, C.byref(nr), C.byref(nb), C.byref(ml), C.byref(fm)), "tk_reads_info")
+        self.n_reads, self.n_bases, self.max_len, self.format = nr.value, nb.value, ml.value, fm.value
+
+    def free(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.tk_reads_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def names(self) -> Tuple[np.ndarray, np.ndarray]:
+        off = np.zeros(self.n_reads, dtype=np.uint64)
+        ln = np.zeros(self.n_reads, dtype=np.uint32)
+        if self.n_reads:
+            self.ctx.check(self.lib.tk_reads_names(self.h, off.ctypes.data, ln.ctypes.data), "tk_reads_names")
+        return off, ln
+
+    def accessions(self) -> list:
+        assert self._host_text is not None, "accessions need the host text"
+        off, ln = self.names()
+        t = bytes(self._host_text) if not isinstance(self._host_text, bytes) else self._host_text
+        return [t[o:o + l] for o, l in zip(off.tolist(), ln.tolist())]
+
+    def offsets(self) -> np.ndarray:
+        off = np.zeros(self.n_reads + 1, dtype=np.uint64)
+        self.ctx.check(self.lib.tk_reads_offsets(self.h, off.ctypes.data), "tk_reads_offsets")
+        return off
+
+    def packed(self) -> bytes:
+        n = self.n_bases + self.n_reads
+        buf = np.zeros(max(n, 1), dtype=np.uint8)
+        self.ctx.check(self.lib.tk_reads_copy_seq(self.h, buf.ctypes.data, n), "tk_reads_copy_seq")
+        return buf[:n].tobytes()
+
+    def sequences(self) -> list:
+        off = self.offsets().tolist()
+        s = self.packed()
+        return [s[off[i]:off[i + 1] - 1] for i in range(self.n_reads)]
+
+
+class KmerTable:
+    """Device-resident k-mer -> count table (tk_table): jellyfish count/histo/dump."""
+
+    def __init__(self, ctx: Context, k: int = 25, canonical: bool = True, capacity: int = 0):
+        self.ctx, self.lib, self.k, self.canonical = ctx, ctx.lib, k, canonical
+        h = C.c_void_p()
+        ctx.check(self.lib.tk_table_create(ctx.h, k, int(canonical), capacity, C.byref(h)), "tk_table_create")
+        self.h = h
+
+    def free(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.tk_table_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def add(self, reads: ReadSet) -> None:
+        self.ctx.check(self.lib.tk_table_add_reads(self.h, reads.h), "tk_table_add_reads")
+
+    def count_text(self, text: Buffer) -> None:
+        ptr, n, keep = _host_ptr(text)
+        self.ctx.check(self.lib.tk_table_count_text(self.h, C.c_void_p(ptr), n, N.TK_HOST), "tk_table_count_text")
+
+    def info(self) -> Tuple[int, int, int]:
+        d, t, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.ctx.check(self.lib.tk_table_info(self.h, C.byref(d), C.byref(t), C.byref(c)), "tk_table_info")
+        return d.value, t.value, c.value
+
+    def histo(self, low: int = 1, high: int = 10000) -> np.ndarray:
+        h = np.zeros(high - low + 3, dtype=np.uint64)
+        self.ctx.check(self.lib.tk_table_histo(self.h, low, high, h.ctypes.data), "tk_table_histo")
+        return h
+
+    def dump(self, min_count: int = 1) -> Tuple[np.ndarray, np.ndarray]:
+        n = C.c_uint64()
+        self.ctx.check(self.lib.tk_table_dump(self.h, min_count, N.TK_HOST, None, None, 0, C.byref(n)), "tk_table_dump")
+        keys = np.zeros(max(n.value, 1), dtype=np.uint64)
+        cnt = np.zeros(max(n.value, 1), dtype=np.uint32)
+        m = C.c_uint64()
+        self.ctx.check(self.lib.tk_table_dump(self.h, min_count, N.TK_HOST, keys.ctypes.data, cnt.ctypes.data,
+                                              keys.size, C.byref(m)), "tk_table_dump")
+        return keys[:m.value], cnt[:m.value]
+
+    def dump_fasta_len(self, min_count: int = 1) -> int:
+        """Formats the dump on the device (kept with the table); returns its size."""
+        n = C.c_uint64()
+        self.ctx.check(self.lib.tk_table_dump_fasta(self.h, min_count, N.TK_HOST, None, 0, C.byref(n)),
+                       "tk_table_dump_fasta")
+        return n.value
+
+    def dump_fasta_into(self, min_count: int, ptr: int, cap: int, device: bool = False) -> int:
+        """Copies the dump text to a caller buffer (host or device address)."""
+        m = C.c_uint64()
+        self.ctx.check(self.lib.tk_table_dump_fasta(self.h, min_count, N.TK_DEVICE if device else N.TK_HOST,
+                                                    C.c_void_p(ptr), cap, C.byref(m)), "tk_table_dump_fasta")
+        return m.value
+
+    def dump_fasta(self, min_count: int = 1) -> bytes:
+        n = self.dump_fasta_len(min_count)
+        buf = np.zeros(max(n, 1), dtype=np.uint8)
+        m = self.dump_fasta_into(min_count, buf.ctypes.data, buf.size)
+        return buf[:m].tobytes()
+
+    def load_pairs(self, keys: np.ndarray, counts: np.ndarray) -> None:
+        k = np.ascontiguousarray(keys, dtype=np.uint64)
+        c = np.ascontiguousarray(counts, dtype=np.uint32)
+        self.ctx.check(self.lib.tk_table_load_pairs(self.h, k.ctypes.data, c.ctypes.data, k.size, N.TK_HOST),
+                       "tk_table_load_pairs")
+
+    def load_dump_fasta(self, text: Buffer) -> None:
+        ptr, n, keep = _host_ptr(text)
+        self.ctx.check(self.lib.tk_table_load_dump_fasta(self.h, C.c_void_p(ptr), n, N.TK_HOST),
+                       "tk_table_load_dump_fasta")
+
+
+def coverage_stats(table: KmerTable, reads: ReadSet) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Per-read (median, mean, stdev) of k-mer coverage, in read order."""
+    n = reads.n_reads
+    med = np.zeros(max(n, 1), dtype=np.uint32)
+    mean = np.zeros(max(n, 1), dtype=np.float32)
+    sd = np.zeros(max(n, 1), dtype=np.float32)
+    table.ctx.check(table.lib.tk_coverage_stats(table.h, reads.h, N.TK_HOST, med.ctypes.data, mean.ctypes.data,
+                                                sd.ctypes.data), "tk_coverage_stats")
+    return med[:n], mean[:n], sd[:n]
+
+
+def coverage_stats_into(table: KmerTable, reads: ReadSet, median_ptr: int, mean_ptr: int, stdev_ptr: int,
+                        device: bool = True) -> None:
+    """coverage_stats writing n_reads entries to caller arrays (device addresses by default)."""
+    table.ctx.check(table.lib.tk_coverage_stats(table.h, reads.h, N.TK_DEVICE if device else N.TK_HOST,
+                                                C.c_void_p(median_ptr), C.c_void_p(mean_ptr),
+                                                C.c_void_p(stdev_ptr)), "tk_coverage_stats")
+
+
+class ReadsToTranscripts:
+    """Bundle k-mer table and read-to-component vote (tk_r2t)."""
+
+    def __init__(self, ctx: Context, bundle: Buffer, k: int = 25, strand: bool = False):
+        self.ctx, self.lib, self.k, self.strand = ctx, ctx.lib, k, strand
+        ptr, n, keep = _host_ptr(bundle)
+        h = C.c_void_p()
+        ctx.check(self.lib.tk_r2t_create(ctx.h, C.c_void_p(ptr), n, N.TK_HOST, k, int(strand), C.byref(h)),
+                  "tk_r2t_create")
+        self.h = h
+        nr, nk = C.c_uint64(), C.c_uint64()
+        ctx.check(self.lib.tk_r2t_info(h, C.byref(nr), C.byref(nk)), "tk_r2t_info")
+        self.n_records, self.n_kmers = nr.value, nk.value
+        ids = np.zeros(max(self.n_records, 1), dtype=np.uint64)
+        ctx.check(self.lib.tk_r2t_component_ids(h, ids.ctypes.data), "tk_r2t_component_ids")
+        self.component_ids = ids[:self.n_records]
+
+    def free(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.tk_r2t_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def assign(self, reads: ReadSet) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = reads.n_reads
+        rec = np.zeros(max(n, 1), dtype=np.int32)
+        hits = np.zeros(max(n, 1), dtype=np.uint32)
+        nwin = np.zeros(max(n, 1), dtype=np.uint32)
+        self.ctx.check(self.lib.tk_r2t_assign(self.h, reads.h, N.TK_HOST, rec.ctypes.data, hits.ctypes.data,
+                                              nwin.ctypes.data), "tk_r2t_assign")
+        return rec[:n], hits[:n], nwin[:n]
+
+
+# ---------------------------------------------------------------- text formats
+
+def format_histo(hist: np.ndarray, low: int = 1, high: int = 10000, full: bool = False) -> bytes:
+    """``jellyfish histo`` lines "<count> <n>": bin 0 is labelled low-1, the
+    overflow bin high+1 (util/misc/insilico_norm_kmer_hists/kmer_histo.all.txt);
+    empty bins are skipped unless ``full``."""
+    out = []
+    labels = [low - 1] + list(range(low, high + 1)) + [high + 1]
+    for lab, v in zip(labels, hist.tolist()):
+        if v or full:
+            if lab == low - 1 and not v:
+                continue
+            out.append(f"{lab} {v}\n")
+    return "".join(out).encode()
+
+
+def format_stats(accs: Sequence[bytes], med, mean, sd, header: bool = True) -> bytes:
+    """fastaToKmerCoverageStats rows: acc, median_cov, mean_cov, stdev."""
+    rows = [b"acc\tmedian_cov\tmean_cov\tstdev\n"] if header else []
+    for a, m, u, s in zip(accs, med.tolist(), mean.tolist(), sd.tolist()):
+        rows.append(a + (f"\t{m}\t{u:g}\t{s:g}\n").encode())
+    return b"".join(rows)
+
+
+def format_r2t(accs: Sequence[bytes], seqs: Sequence[bytes], comp_ids, rec, hits, nwin, min_pct: int = 0) -> bytes:
+    """readsToComponents rows: comp_id, '>'acc, pct, SEQ (Trinity:2474)."""
+    rows = []
+    for a, s, r, h, w in zip(accs, seqs, rec.tolist(), hits.tolist(), nwin.tolist()):
+        if r < 0 or w == 0:
+            continue
+        pct = (100 * h) // w
+        if min_pct > 0 and pct < min_pct:
+            continue
+        rows.append(b"%d\t>%s\t%d\t%s\n" % (int(comp_ids[r]), a, pct, s))
+    return b"".join(rows)
