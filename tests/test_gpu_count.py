@@ -82,10 +82,10 @@ def test_batches_add_up(ctx, oracle):
 
 
 def test_overflow_and_growth_are_exact(ctx, oracle):
-    """One reprobe and a 1,024-slot table: almost every insert overflows and
-    the table doubles repeatedly; the counts stay exact."""
+    """Eight reprobes at up to 0.6 load: many inserts overflow, the table
+    doubles and the overflow list is re-inserted; the counts stay exact."""
     text = synth.transcriptome_reads(seed=5, n_reads=3000).tobytes()
-    ctx.set_reprobes(1)
+    ctx.set_reprobes(8)
     try:
         t = gpu_count(ctx, text, capacity=1024)
         got = t.dump(1)

@@ -180,8 +180,21 @@ int tk_ctx_create(int device, tk_ctx **out) {
     return TK_OK;
 }
 
+static void ctx_release_now(tk_ctx *c);
+
+// a child handle (read set, table, bundle) starts / stops using the context
+static void ctx_acquire(tk_ctx *c) { c->live.fetch_add(1); }
+static void ctx_release(tk_ctx *c) {
+    if (c->live.fetch_sub(1) == 1 && c->closing.load()) ctx_release_now(c);
+}
+
 void tk_ctx_destroy(tk_ctx *c) {
     if (!c) return;
+    c->closing.store(true);
+    if (c->live.load() == 0) ctx_release_now(c);
+}
+
+static void ctx_release_now(tk_ctx *c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
@@ -253,6 +266,7 @@ int tk_reads_parse(tk_ctx *c, const char *text, uint64_t len, int where, tk_read
     tk_reads *r = new (std::nothrow) tk_reads();
     if (!r) return TK_E_OOM;
     r->ctx = c;
+    ctx_acquire(c);
     r->text_len = len;
     void *d = nullptr;
     bool owned = false;
@@ -314,6 +328,7 @@ void tk_reads_free(tk_reads *r) {
     dfree(c, r->d_name_off);
     dfree(c, r->d_name_len);
     delete r;
+    ctx_release(c);
 }
 
 // ------------------------------------------------------------------ table
@@ -322,6 +337,7 @@ static int table_new(tk_ctx *c, int k, int canonical, tk_table **out) {
     tk_table *t = new (std::nothrow) tk_table();
     if (!t) return TK_E_OOM;
     t->ctx = c;
+    ctx_acquire(c);
     t->k = k;
     t->canonical = canonical ? 1 : 0;
     t->ovf_cap = 1 << 20;
@@ -486,6 +502,7 @@ void tk_table_free(tk_table *t) {
     dfree(c, t->d_hll);
     dfree(c, t->d_dump);
     delete t;
+    ctx_release(c);
 }
 
 // ------------------------------------------------------------------ coverage
@@ -527,6 +544,7 @@ int tk_r2t_create(tk_ctx *c, const char *bundle, uint64_t len, int where, int k,
     tk_r2t *z = new (std::nothrow) tk_r2t();
     if (!z) return TK_E_OOM;
     z->ctx = c;
+    ctx_acquire(c);
     z->k = k;
     z->strand = strand ? 1 : 0;
     tk_reads *b = nullptr;
@@ -614,8 +632,10 @@ int tk_r2t_assign(tk_r2t *z, const tk_reads *r, int where, int32_t *rec, uint32_
 
 void tk_r2t_free(tk_r2t *z) {
     if (!z) return;
+    tk_ctx *c = z->ctx;
     if (z->table) tk_table_free(z->table);
     delete z;
+    ctx_release(c);
 }
 
 }  // extern "C"

@@ -13,9 +13,9 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <string>
 #include <vector>
-#include <mutex>
 
 #include "../../include/trinkmer.h"
 
@@ -178,6 +178,10 @@ struct tk_ctx {
     uint64_t launches = 0;                  // every kernel launched by the library
     int max_probes = 4096;
     int sm_count = 152;
+    // read sets, tables and bundles alive on this context; tk_ctx_destroy
+    // defers the release until the last of them is freed
+    std::atomic<int> live{0};
+    std::atomic<bool> closing{false};
 };
 
 struct tk_reads {
