@@ -156,6 +156,22 @@ void tk_table_free(tk_table *table);
 int tk_coverage_stats(tk_table *table, const tk_reads *reads, int where, uint32_t *median,
                       float *mean, float *stdev);
 
+/* tk_coverage_stats without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory while
+ * they compute -- a resident service whose HBM is already divided into job
+ * slots under an admission budget, or a pipeline that must not meet an
+ * allocation failure or the implicit synchronisation of cudaMalloc/cudaFree
+ * mid-run.  The table and read set are created beforehand (that is where
+ * their memory is allocated); median/mean/stdev are DEVICE arrays of n_reads
+ * entries owned by the caller.  Reads longer than 256 windows use a fixed
+ * 16 MiB slab of static device memory (held by every GPU that loads the
+ * library until exit), which limits a read to 131,072 windows (TK_E_RANGE
+ * beyond that).  The first call on a device looks up that slab's address.
+ * All calls share the slab: calls that overlap on the GPU race.  Returns after
+ * synchronising the context's stream. */
+int tk_coverage_stats_noalloc(tk_table *table, const tk_reads *reads, uint32_t *median,
+                              float *mean, float *stdev);
+
 /* ------------------------------------------------------------- read -> component
  * Replaces Chrysalis' `ReadsToTranscripts -i reads.fa -f bundle.fasta -o out
  * -t N -max_mem_reads M [-strand] [-p P]` (Trinity:2237-2251).  The bundle is

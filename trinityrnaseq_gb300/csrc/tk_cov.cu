@@ -14,6 +14,8 @@
 #include "tk_warp.cuh"
 
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 namespace tk {
 
@@ -200,4 +202,178 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
     return e;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant (tk_coverage_stats_noalloc).
+//
+// Some callers cannot allocate device memory while they compute: a resident
+// service that has already carved all of its HBM into job slots under an
+// admission budget, or a pipeline that must not risk an allocation failure or
+// the implicit device synchronisation cudaMalloc/cudaFree can bring in the
+// middle of its work.  For them the long-read statistics use a fixed slab in
+// this file-scope device array instead of cudaMalloc'd scratch.  Every GPU
+// that loads the library holds the array (16 MiB) until the process exits.
+// Host code must not pass `g_noalloc_scratch` itself to a kernel: in host code
+// that name is a host-side stand-in, so its device address is fetched once per
+// device with cudaGetSymbolAddress (see noalloc_scratch_ptr).
+
+constexpr uint64_t NOALLOC_SCRATCH_BYTES = 16ULL << 20;
+constexpr int NOALLOC_BLOCKS = 32;
+constexpr uint64_t NOALLOC_SLAB = NOALLOC_SCRATCH_BYTES / 4 / NOALLOC_BLOCKS;   // 131,072 windows per block
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[NOALLOC_SCRATCH_BYTES / 4];
+static __device__ __align__(16) Slot g_noalloc_empty[2] = {{EMPTY_KEY, 0u, 0u}, {EMPTY_KEY, 0u, 0u}};
+
+// short reads only (<= 256 windows); longer reads are left to k_coverage_long_slab
+template <bool CANON>
+__global__ void __launch_bounds__(CV_THREADS) k_coverage_short(DevTable t, const uint8_t *__restrict__ seq,
+                                                              const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
+                                                              uint32_t *__restrict__ median, float *__restrict__ mean,
+                                                              float *__restrict__ stdev) {
+    const uint64_t warps = (uint64_t)gridDim.x * (CV_THREADS / 32);
+    for (uint64_t r = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); r < n_reads; r += warps) {
+        const uint64_t start = rd_off[r];
+        const uint64_t L = rd_off[r + 1] - start - 1;
+        const uint32_t nwin = L >= (uint64_t)k ? (uint32_t)(L - k + 1) : 0u;
+        if (nwin <= 32) cov_warp_read<1, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+        else if (nwin <= 64) cov_warp_read<2, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+        else if (nwin <= 128) cov_warp_read<4, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+        else if (nwin <= CV_WARP_MAX) cov_warp_read<8, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
+    }
+}
+
+// reads with more than 256 windows, one block per read, found by a strided scan
+// of all reads; block b works in slab b of the static array
+template <bool CANON>
+__global__ void __launch_bounds__(CV_THREADS) k_coverage_long_slab(DevTable t, const uint8_t *__restrict__ seq,
+                                                                  const uint64_t *__restrict__ rd_off, uint64_t n_reads,
+                                                                  int k, uint32_t *__restrict__ scratch,
+                                                                  uint32_t *__restrict__ median, float *__restrict__ mean,
+                                                                  float *__restrict__ stdev) {
+    __shared__ uint32_t s_cnt[CV_THREADS / 32];
+    __shared__ uint64_t s_sum[CV_THREADS / 32], s_hi[CV_THREADS / 32], s_lo[CV_THREADS / 32];
+    uint32_t *slab = scratch + (uint64_t)blockIdx.x * NOALLOC_SLAB;
+    for (uint64_t r = blockIdx.x; r < n_reads; r += gridDim.x) {
+        const uint64_t start = rd_off[r];
+        const uint64_t L = rd_off[r + 1] - start - 1;
+        if (L < (uint64_t)k || L - k + 1 <= CV_WARP_MAX) continue;   // uniform over the block
+        const uint32_t nwin = (uint32_t)(L - k + 1);
+        uint32_t n2 = 1;
+        while (n2 < nwin) n2 <<= 1;
+        // every slab entry read below is written first: nothing carries over between reads or calls
+        block_window_values<CANON>(seq, start, nwin, n2, k, slab, [&](uint64_t key) { return tbl_get(t, key, 1u); });
+        uint32_t cnt = 0;
+        uint64_t sum = 0, hi = 0, lo = 0;
+        for (uint32_t w = threadIdx.x; w < nwin; w += blockDim.x) {
+            uint32_t c = slab[w];
+            if (c == PAD_VAL) continue;
+            cnt++;
+            sum += c;
+            uint64_t sq = (uint64_t)c * c, nlo = lo + sq;
+            hi += nlo < lo;
+            lo = nlo;
+        }
+        cnt = warp_sum(cnt);
+        sum = warp_sum(sum);
+        warp_sum_u128(hi, lo);
+        if (lane_id() == 0) {
+            s_cnt[threadIdx.x >> 5] = cnt;
+            s_sum[threadIdx.x >> 5] = sum;
+            s_hi[threadIdx.x >> 5] = hi;
+            s_lo[threadIdx.x >> 5] = lo;
+        }
+        block_bitonic_sort(slab, n2);
+        if (threadIdx.x == 0) {
+            uint32_t tc = 0;
+            uint64_t ts = 0, th = 0, tl = 0;
+            for (int w = 0; w < CV_THREADS / 32; w++) {
+                tc += s_cnt[w];
+                ts += s_sum[w];
+                uint64_t nl = tl + s_lo[w];
+                th += s_hi[w] + (nl < tl);
+                tl = nl;
+            }
+            float m, s;
+            finish_stats(tc, ts, th, tl, &m, &s);
+            median[r] = tc ? slab[tc / 2] : 0u;
+            mean[r] = m;
+            stdev[r] = s;
+        }
+        __syncthreads();
+    }
+}
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_scratch_dev[NOALLOC_MAX_DEVICES];
+static void *g_noalloc_empty_dev[NOALLOC_MAX_DEVICES];
+
+// Set-up, once per device, with that device current: the device addresses of
+// the static scratch array and of the empty two-slot table.
+static int noalloc_scratch_ptr(tk_ctx *c, uint32_t **scratch, Slot **empty) {
+    if (c->device < 0 || c->device >= NOALLOC_MAX_DEVICES) return set_err(c, TK_E_INVAL, "device ordinal too large");
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_scratch_dev[c->device]) {
+        void *p = nullptr, *q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_check(c, e, "cudaGetSymbolAddress(no-allocation scratch)");
+        e = cudaGetSymbolAddress(&q, g_noalloc_empty);
+        if (e != cudaSuccess) return cuda_check(c, e, "cudaGetSymbolAddress(empty table)");
+        g_noalloc_scratch_dev[c->device] = p;
+        g_noalloc_empty_dev[c->device] = q;
+    }
+    *scratch = (uint32_t *)g_noalloc_scratch_dev[c->device];
+    *empty = (Slot *)g_noalloc_empty_dev[c->device];
+    return TK_OK;
+}
+
+int coverage_stats_noalloc(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d_mean, float *d_stdev) {
+    tk_ctx *c = t->ctx;
+    const uint64_t n = rd->n_reads;
+    const int k = t->k;
+    if (rd->max_len >= (uint32_t)k && (uint64_t)(rd->max_len - k + 1) > NOALLOC_SLAB)
+        return set_err(c, TK_E_RANGE, "tk_coverage_stats_noalloc: a read has " + std::to_string(rd->max_len - k + 1) +
+                                          " windows; the allocation-free path handles at most " +
+                                          std::to_string(NOALLOC_SLAB) + " per read");
+    uint32_t *scratch = nullptr;
+    Slot *empty = nullptr;
+    TK_TRY(noalloc_scratch_ptr(c, &scratch, &empty));
+    if (n == 0) return TK_OK;
+    DevTable dt = t->t;
+    if (t->capacity == 0) {
+        dt.slots = empty;
+        dt.mask = 1;
+    }
+    const unsigned grid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((n + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
+    if (t->canonical)
+        k_coverage_short<true><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
+                                                                   d_stdev);
+    else
+        k_coverage_short<false><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
+                                                                    d_stdev);
+    c->launches++;
+    TK_TRY(check_launch(c, "coverage (no allocation)"));
+    if (rd->max_len >= (uint32_t)k && rd->max_len - k + 1 > CV_WARP_MAX) {
+        if (t->canonical)
+            k_coverage_long_slab<true><<<NOALLOC_BLOCKS, CV_THREADS, 0, c->stream>>>(
+                dt, rd->d_seq, rd->d_rd_off, n, k, scratch, d_median, d_mean, d_stdev);
+        else
+            k_coverage_long_slab<false><<<NOALLOC_BLOCKS, CV_THREADS, 0, c->stream>>>(
+                dt, rd->d_seq, rd->d_rd_off, n, k, scratch, d_median, d_mean, d_stdev);
+        c->launches++;
+        TK_TRY(check_launch(c, "coverage long reads (no allocation)"));
+    }
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "coverage (no allocation) sync");
+}
+
 }  // namespace tk
+
+// Allocation-free coverage statistics; declared in include/trinkmer.h.
+extern "C" int tk_coverage_stats_noalloc(tk_table *table, const tk_reads *reads, uint32_t *median, float *mean,
+                                         float *stdev) {
+    if (!table || !reads || !median || !mean || !stdev) return TK_E_INVAL;
+    tk_ctx *c = table->ctx;
+    if (cudaSetDevice(c->device) != cudaSuccess) return tk::set_err(c, TK_E_CUDA, "cudaSetDevice");
+    if (reads->ctx != c) return tk::set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
+    return tk::coverage_stats_noalloc(table, reads, median, mean, stdev);
+}

@@ -67,6 +67,7 @@ SIGNATURES = {
     "tk_table_load_dump_fasta": (C.c_int, [vp, vp, u64, C.c_int]),
     "tk_table_free": (None, [vp]),
     "tk_coverage_stats": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
+    "tk_coverage_stats_noalloc": (C.c_int, [vp, vp, vp, vp, vp]),
     "tk_r2t_create": (C.c_int, [vp, vp, u64, C.c_int, C.c_int, C.c_int, P(vp)]),
     "tk_r2t_info": (C.c_int, [vp, P(u64), P(u64)]),
     "tk_r2t_component_ids": (C.c_int, [vp, vp]),
