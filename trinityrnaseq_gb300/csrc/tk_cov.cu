@@ -154,8 +154,7 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
         e = dmalloc(c, (void **)&empty, sizeof(Slot) * 2, "empty table");
         if (!e) {
             cudaMemsetAsync(empty, 0xFF, sizeof(Slot) * 2, c->stream);
-            dt.slots = empty;
-            dt.mask = 1;
+            dt = tbl_empty(empty);
         }
     }
     if (!e) {
@@ -339,10 +338,7 @@ int coverage_stats_noalloc(tk_table *t, const tk_reads *rd, uint32_t *d_median, 
     TK_TRY(noalloc_scratch_ptr(c, &scratch, &empty));
     if (n == 0) return TK_OK;
     DevTable dt = t->t;
-    if (t->capacity == 0) {
-        dt.slots = empty;
-        dt.mask = 1;
-    }
+    if (t->capacity == 0) dt = tbl_empty(empty);
     const unsigned grid = (unsigned)std::max<uint64_t>(
         1, std::min<uint64_t>((n + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
     if (t->canonical)

@@ -32,10 +32,20 @@ struct __align__(16) Slot {
     unsigned int pad;
 };
 
+// Capacity = 2^(pbits + lbits) slots in 2^pbits partitions of 2^lbits slots.
+// A key's partition is the top pbits of its hash and its home slot inside the
+// partition the low lbits; probing wraps inside the partition.  With
+// partitions of at most 32 MB, the counting pass that inserts keys in
+// partition order works on an L2-resident slice at a time.
 struct DevTable {
     Slot *slots;
-    uint64_t mask;      // capacity - 1
+    uint64_t lmask;     // 2^lbits - 1
+    int lbits;
+    int pbits;
 };
+
+constexpr int MAX_LBITS = 21;        // 2M slots = 32 MB per partition
+constexpr int BUCKET_BITS = 12;      // hash buckets of the partitioned count (>= pbits)
 
 // device-side error words (set by kernels, read by the host after a launch)
 enum DevErr : uint32_t {
@@ -64,10 +74,19 @@ __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // ------------------------------------------------------------------ table ops
 
+__host__ __device__ __forceinline__ uint64_t tbl_home(const DevTable &t, uint64_t h) {
+    uint64_t part = t.pbits ? (h >> (64 - t.pbits)) : 0;
+    return (part << t.lbits) | (h & t.lmask);
+}
+
+__host__ __device__ __forceinline__ uint64_t tbl_next(const DevTable &t, uint64_t s) {
+    return (s & ~t.lmask) | ((s + 1) & t.lmask);
+}
+
 // Adds `inc` to key's value, inserting the key if absent.  Returns false after
 // max_probes slots without finding the key or a free slot.
 __device__ __forceinline__ bool tbl_add(DevTable t, uint64_t key, uint32_t inc, int max_probes) {
-    uint64_t s = mix64(key) & t.mask;
+    uint64_t s = tbl_home(t, mix64(key));
     for (int i = 0; i < max_probes; i++) {
         unsigned long long cur = __ldcg(&t.slots[s].key);
         if (cur == EMPTY_KEY) {
@@ -78,14 +97,14 @@ __device__ __forceinline__ bool tbl_add(DevTable t, uint64_t key, uint32_t inc, 
             atomicAdd(&t.slots[s].val, inc);
             return true;
         }
-        s = (s + 1) & t.mask;
+        s = tbl_next(t, s);
     }
     return false;
 }
 
 // Keeps the minimum value per key (ReadsToTranscripts ownership).
 __device__ __forceinline__ bool tbl_min(DevTable t, uint64_t key, uint32_t v, int max_probes) {
-    uint64_t s = mix64(key) & t.mask;
+    uint64_t s = tbl_home(t, mix64(key));
     for (int i = 0; i < max_probes; i++) {
         unsigned long long cur = __ldcg(&t.slots[s].key);
         if (cur == EMPTY_KEY) {
@@ -96,20 +115,30 @@ __device__ __forceinline__ bool tbl_min(DevTable t, uint64_t key, uint32_t v, in
             atomicMin(&t.slots[s].val, v);
             return true;
         }
-        s = (s + 1) & t.mask;
+        s = tbl_next(t, s);
     }
     return false;
 }
 
 __device__ __forceinline__ uint32_t tbl_get(DevTable t, uint64_t key, uint32_t miss) {
-    uint64_t s = mix64(key) & t.mask;
-    for (uint64_t i = 0; i <= t.mask; i++) {
+    uint64_t s = tbl_home(t, mix64(key));
+    for (uint64_t i = 0; i <= t.lmask; i++) {
         ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(&t.slots[s]));
         if (v.x == key) return (uint32_t)v.y;
         if (v.x == EMPTY_KEY) return miss;
-        s = (s + 1) & t.mask;
+        s = tbl_next(t, s);
     }
     return miss;
+}
+
+// one-slot-pair table every lookup misses in (an empty catalogue)
+__host__ __device__ __forceinline__ DevTable tbl_empty(Slot *two_slots) {
+    DevTable t;
+    t.slots = two_slots;
+    t.lmask = 1;
+    t.lbits = 1;
+    t.pbits = 0;
+    return t;
 }
 
 // ------------------------------------------------------------------ warp scans

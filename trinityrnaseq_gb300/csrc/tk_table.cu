@@ -25,6 +25,9 @@ constexpr int CT_THREADS = 256;
 constexpr int CT_SPAN = 32;              // window end positions per thread
 constexpr int HLL_P = 12;
 constexpr int HLL_M = 1 << HLL_P;
+constexpr int NBUCKETS = 1 << BUCKET_BITS;
+constexpr int INS_PER_THREAD = 8;
+constexpr uint64_t INS_CHUNK = (uint64_t)CT_THREADS * INS_PER_THREAD;
 
 struct Window64 {
     uint32_t w[16];
@@ -48,94 +51,159 @@ __device__ __forceinline__ Window64 load_window(const uint8_t *__restrict__ seq,
     return b;
 }
 
-template <bool CANON, bool AGG>
-__global__ void __launch_bounds__(CT_THREADS) k_count(const uint8_t *__restrict__ seq, uint64_t n, int k, DevTable t,
-                                                     int max_probes, uint64_t *__restrict__ ovf_keys,
-                                                     uint32_t *__restrict__ ovf_cnt, uint64_t ovf_cap,
-                                                     unsigned long long *__restrict__ counters) {
+// Calls f(key) for every valid window ending in [p0, p0 + 32) of the padded
+// packed-read array (the 64 bytes [p0-32, p0+32) cover the k-1 bases before).
+template <bool CANON, typename F>
+__device__ __forceinline__ void thread_windows(const uint8_t *__restrict__ seq, uint64_t p0, bool active, int k, F &&f) {
     const uint64_t kmask = (1ULL << (2 * k)) - 1;
     const int shift = 2 * (k - 1);
-    const unsigned lane = lane_id();
-    const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
-    uint32_t windows = 0;
-    for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
-        const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
-        const bool active = p0 < n;
-        Window64 b = load_window(seq, p0, active);
-        uint64_t fw = 0, rc = 0;
-        int run = 0;
+    Window64 b = load_window(seq, p0, active);
+    uint64_t fw = 0, rc = 0;
+    int run = 0;
 #pragma unroll
-        for (int j = 0; j < 64; j++) {
-            uint32_t c = base_code(b.get(j));
-            if (c > 3) {
-                run = 0;
-            } else {
-                fw = ((fw << 2) | c) & kmask;
-                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
-                run++;
-            }
-            if (j >= 32) {
-                bool want = run >= k;
-                uint64_t key = (CANON && rc < fw) ? rc : fw;
-                uint32_t inc = 1;
-                bool lead = want;
-                if (AGG) {
-                    unsigned act = __ballot_sync(0xffffffffu, want);
-                    if (want) {
-                        unsigned peers = __match_any_sync(act, key);
-                        lead = lane == (unsigned)(__ffs(peers) - 1);
-                        inc = __popc(peers);
-                    }
-                }
-                windows += want;
-                if (lead && !tbl_add(t, key, inc, max_probes)) {
-                    unsigned long long i = atomicAdd(&counters[0], 1ULL);
-                    if (i < ovf_cap) { ovf_keys[i] = key; ovf_cnt[i] = inc; }
-                }
-            }
+    for (int j = 0; j < 64; j++) {
+        uint32_t c = base_code(b.get(j));
+        if (c > 3) {
+            run = 0;
+        } else {
+            fw = ((fw << 2) | c) & kmask;
+            rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
+            run++;
         }
+        if (j >= 32 && run >= k) f((CANON && rc < fw) ? rc : fw);
     }
-    windows = warp_sum(windows);
-    if (lane == 0 && windows) atomicAdd(&counters[1], (unsigned long long)windows);
 }
 
+// Pass 1a: k-mers per (hash bucket, block) and the HLL sketch of the batch.
+// hist is bucket-major: hist[bucket * gridDim.x + block].
 template <bool CANON>
-__global__ void __launch_bounds__(CT_THREADS) k_hll(const uint8_t *__restrict__ seq, uint64_t n, int k,
-                                                   uint32_t *__restrict__ regs) {
+__global__ void __launch_bounds__(CT_THREADS) k_part_hist(const uint8_t *__restrict__ seq, uint64_t n, int k,
+                                                         uint32_t *__restrict__ hist, uint32_t *__restrict__ regs,
+                                                         unsigned long long *__restrict__ windows_out) {
+    __shared__ uint32_t sh[NBUCKETS];
     __shared__ uint32_t sreg[HLL_M];
+    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) sh[i] = 0;
     for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS) sreg[i] = 0;
     __syncthreads();
-    const uint64_t kmask = (1ULL << (2 * k)) - 1;
-    const int shift = 2 * (k - 1);
+    uint32_t windows = 0;
     const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
     for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
         const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
-        if (p0 >= n) continue;
-        Window64 b = load_window(seq, p0, true);
-        uint64_t fw = 0, rc = 0;
-        int run = 0;
-#pragma unroll
-        for (int j = 0; j < 64; j++) {
-            uint32_t c = base_code(b.get(j));
-            if (c > 3) {
-                run = 0;
-            } else {
-                fw = ((fw << 2) | c) & kmask;
-                rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
-                run++;
+        thread_windows<CANON>(seq, p0, p0 < n, k, [&](uint64_t key) {
+            uint64_t h = mix64(key);
+            atomicAdd(&sh[h >> (64 - BUCKET_BITS)], 1u);
+            uint32_t idx = (uint32_t)(h & (HLL_M - 1));
+            uint32_t rank = (uint32_t)__clzll((long long)(h >> HLL_P)) - HLL_P + 1u;
+            if (rank > sreg[idx]) atomicMax(&sreg[idx], rank);
+            windows++;
+        });
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) hist[(uint64_t)i * gridDim.x + blockIdx.x] = sh[i];
+    for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS)
+        if (sreg[i]) atomicMax(&regs[i], sreg[i]);
+    windows = warp_sum(windows);
+    if (lane_id() == 0 && windows) atomicAdd(windows_out, (unsigned long long)windows);
+}
+
+// Pass 1b: the same windows, written bucket-major into the key buffer at the
+// offsets of the scanned histogram (same grid, same tiles as pass 1a).
+template <bool CANON>
+__global__ void __launch_bounds__(CT_THREADS) k_part_scatter(const uint8_t *__restrict__ seq, uint64_t n, int k,
+                                                            const uint64_t *__restrict__ offs,
+                                                            uint64_t *__restrict__ keys) {
+    __shared__ unsigned long long soff[NBUCKETS];
+    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) soff[i] = offs[(uint64_t)i * gridDim.x + blockIdx.x];
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
+    for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
+        const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
+        thread_windows<CANON>(seq, p0, p0 < n, k, [&](uint64_t key) {
+            uint64_t h = mix64(key);
+            unsigned long long pos = atomicAdd(&soff[h >> (64 - BUCKET_BITS)], 1ULL);
+            keys[pos] = key;
+        });
+    }
+}
+
+__device__ __forceinline__ void l2_prefetch_bulk(const void *p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Pass 2: insert the bucket-ordered keys.  Blocks walk the buffer in memory
+// order, so the live keys span about one partition: its table slice stays in
+// L2.  Thread 0 of each block prefetches (TMA bulk prefetch to L2) its share of
+// the next partition's slice while the current one is being filled.
+__global__ void __launch_bounds__(CT_THREADS) k_part_insert(const uint64_t *__restrict__ keys, uint64_t n, DevTable t,
+                                                           const uint64_t *__restrict__ offs, uint32_t hist_cols,
+                                                           int max_probes, uint64_t *__restrict__ ovf_keys,
+                                                           uint32_t *__restrict__ ovf_cnt, uint64_t ovf_cap,
+                                                           unsigned long long *__restrict__ counters) {
+    const uint64_t nchunks = (n + INS_CHUNK - 1) / INS_CHUNK;
+    const uint32_t nparts = 1u << t.pbits;
+    const uint32_t bpp = NBUCKETS >> t.pbits;            // buckets per partition
+    const uint64_t slice_bytes = (t.lmask + 1) * sizeof(Slot);
+    for (uint64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const uint64_t base = ch * INS_CHUNK;
+        if (threadIdx.x == 0 && t.pbits > 0) {
+            uint32_t p = (uint32_t)(mix64(__ldcs(keys + base)) >> (64 - t.pbits));
+            if (p + 1 < nparts) {
+                uint64_t ps = offs[(uint64_t)p * bpp * hist_cols];
+                uint64_t pe = offs[(uint64_t)(p + 1) * bpp * hist_cols];
+                uint64_t nch = (pe - ps + INS_CHUNK - 1) / INS_CHUNK;
+                uint64_t idx = base >= ps ? (base - ps) / INS_CHUNK : 0;
+                if (nch && idx < nch) {
+                    uint64_t share = ((slice_bytes + nch - 1) / nch + 15) & ~15ULL;
+                    uint64_t lo = idx * share;
+                    if (lo < slice_bytes) {
+                        // at most 4 x 64 KB per chunk; 16-byte aligned start, multiple-of-16 size
+                        uint64_t hi = lo + min(share, slice_bytes - lo);
+                        const char *slice = reinterpret_cast<const char *>(t.slots + ((uint64_t)(p + 1) << t.lbits));
+                        for (int q = 0; q < 4 && lo < hi; q++) {
+                            uint64_t bytes = min(hi - lo, (uint64_t)65536);
+                            l2_prefetch_bulk(slice + lo, (uint32_t)bytes);
+                            lo += bytes;
+                        }
+                    }
+                }
             }
-            if (j >= 32 && run >= k) {
-                uint64_t key = (CANON && rc < fw) ? rc : fw;
-                uint64_t h = mix64(key ^ 0x5851F42D4C957F2DULL);
-                uint32_t idx = (uint32_t)(h >> (64 - HLL_P));
-                uint32_t rank = (uint32_t)__clzll((long long)((h << HLL_P) | (1ULL << (HLL_P - 1)))) + 1u;
-                if (rank > sreg[idx]) atomicMax(&sreg[idx], rank);
+        }
+        uint64_t kk[INS_PER_THREAD], s[INS_PER_THREAD];
+        unsigned long long cur[INS_PER_THREAD];
+#pragma unroll
+        for (int j = 0; j < INS_PER_THREAD; j++) {
+            uint64_t i = base + (uint64_t)j * CT_THREADS + threadIdx.x;
+            kk[j] = i < n ? __ldcs(keys + i) : EMPTY_KEY;
+            s[j] = tbl_home(t, mix64(kk[j]));
+        }
+#pragma unroll
+        for (int j = 0; j < INS_PER_THREAD; j++) cur[j] = kk[j] != EMPTY_KEY ? __ldcg(&t.slots[s[j]].key) : 0ULL;
+#pragma unroll
+        for (int j = 0; j < INS_PER_THREAD; j++) {
+            if (kk[j] == EMPTY_KEY) continue;
+            const uint64_t key = kk[j];
+            uint64_t slot = s[j];
+            unsigned long long c = cur[j];
+            bool done = false;
+            for (int probe = 0; probe < max_probes; probe++) {
+                if (probe) c = __ldcg(&t.slots[slot].key);
+                if (c == EMPTY_KEY) {
+                    c = atomicCAS(&t.slots[slot].key, EMPTY_KEY, (unsigned long long)key);
+                    if (c == EMPTY_KEY) c = key;
+                }
+                if (c == key) {
+                    atomicAdd(&t.slots[slot].val, 1u);
+                    done = true;
+                    break;
+                }
+                slot = tbl_next(t, slot);
+            }
+            if (!done) {
+                unsigned long long o = atomicAdd(&counters[0], 1ULL);
+                if (o < ovf_cap) { ovf_keys[o] = key; ovf_cnt[o] = 1u; }
             }
         }
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS)
-        if (sreg[i]) atomicMax(&regs[i], sreg[i]);
 }
 
 __global__ void k_rehash(const Slot *__restrict__ old, uint64_t old_cap, DevTable t, int max_probes,
@@ -315,8 +383,14 @@ int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val) {
     TK_TRY(dmalloc(c, (void **)&s, capacity * sizeof(Slot), "k-mer table"));
     k_fill_empty<<<stream_grid(c, capacity, 256), 256, 0, c->stream>>>(s, capacity, init_val);
     c->launches++;
+    int bits = 0;
+    while ((1ULL << bits) < capacity) bits++;
+    int lbits = std::min(bits, MAX_LBITS);
+    if (bits - lbits > BUCKET_BITS) lbits = bits - BUCKET_BITS;   // > 2^33 slots: larger partitions
     t->t.slots = s;
-    t->t.mask = capacity - 1;
+    t->t.lbits = lbits;
+    t->t.pbits = bits - lbits;
+    t->t.lmask = (1ULL << lbits) - 1;
     t->capacity = capacity;
     return check_launch(c, "table fill");
 }
@@ -339,6 +413,7 @@ int table_rehash(tk_table *t, uint64_t new_capacity) {
     tk_ctx *c = t->ctx;
     for (int attempt = 0; attempt < 8; attempt++) {
         Slot *old = t->t.slots;
+        const DevTable old_t = t->t;
         uint64_t old_cap = t->capacity;
         TK_TRY(table_alloc(t, new_capacity));
         TK_TRY(overflow_reset(t));
@@ -356,8 +431,7 @@ int table_rehash(tk_table *t, uint64_t new_capacity) {
         }
         // a probe run too long even in the larger table: go bigger from the old copy
         dfree(c, t->t.slots);
-        t->t.slots = old;
-        t->t.mask = old_cap - 1;
+        t->t = old_t;
         t->capacity = old_cap;
         new_capacity *= 2;
     }
@@ -423,46 +497,65 @@ int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
     tk_ctx *c = t->ctx;
     if (seq_len == 0) return TK_OK;
     const uint64_t n = seq_len;
+    // the two passes over the reads use one fixed grid so that every tile goes
+    // to the same block in both (the histogram columns are per block)
     const unsigned grid = (unsigned)std::max<uint64_t>(
-        1, std::min<uint64_t>((n + CT_THREADS * CT_SPAN - 1) / (CT_THREADS * CT_SPAN), (uint64_t)c->sm_count * 16));
-    if (t->d_hll) {
-        // size the table from the union estimate of everything counted so far
-        cudaEvent_t ev;
+        1, std::min<uint64_t>((n + CT_THREADS * CT_SPAN - 1) / (CT_THREADS * CT_SPAN), (uint64_t)c->sm_count * 2));
+    uint32_t *hist = nullptr;
+    uint64_t *offs = nullptr, *keys = nullptr;
+    const uint64_t cells = (uint64_t)NBUCKETS * grid;
+    TK_TRY(dmalloc(c, (void **)&hist, cells * 4, "bucket histogram"));
+    int e = dmalloc(c, (void **)&offs, (cells + 1) * 8, "bucket offsets");
+    if (!e) e = cuda_check(c, cudaMemsetAsync(t->d_counters + 1, 0, 8, c->stream), "window counter");
+    cudaEvent_t ev;
+    uint64_t windows = 0;
+    if (!e) {
+        // pass 1a: bucket histogram + HLL sketch (union with everything counted before)
         prof_begin(c, TK_KID_HLL, &ev);
-        if (t->canonical) k_hll<true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->d_hll);
-        else k_hll<false><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->d_hll);
+        if (t->canonical) k_part_hist<true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, hist, t->d_hll, t->d_counters + 1);
+        else k_part_hist<false><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, hist, t->d_hll, t->d_counters + 1);
         c->launches++;
         prof_end(c, TK_KID_HLL, ev, n);
-        std::vector<uint32_t> regs(HLL_M);
-        TK_CUDA(c, cudaMemcpyAsync(regs.data(), t->d_hll, HLL_M * 4, cudaMemcpyDeviceToHost, c->stream));
-        TK_CUDA(c, cudaStreamSynchronize(c->stream));
-        double est = hll_estimate(regs.data());
-        uint64_t want = pow2_at_least((uint64_t)(est * 1.08 / t->max_load) + 1);
-        if (t->capacity == 0) TK_TRY(table_alloc(t, want));
-        else if (want > t->capacity) TK_TRY(table_rehash(t, want));
-    } else if (t->capacity == 0) {
-        TK_TRY(table_alloc(t, 1024));
+        e = check_launch(c, "bucket histogram");
     }
-    TK_TRY(overflow_reset(t));
-    cudaEvent_t ev;
-    prof_begin(c, TK_KID_COUNT, &ev);
-    uint32_t *ovc = (uint32_t *)(t->d_ovf + t->ovf_cap);
-    if (t->canonical)
-        k_count<true, true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->t, c->max_probes, t->d_ovf, ovc,
-                                                                 t->ovf_cap, t->d_counters);
-    else
-        k_count<false, true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, t->t, c->max_probes, t->d_ovf, ovc,
-                                                                  t->ovf_cap, t->d_counters);
-    c->launches++;
-    prof_end(c, TK_KID_COUNT, ev, 0);
-    TK_TRY(check_launch(c, "count"));
-    // windows counted by this launch
-    unsigned long long hc[2] = {0, 0};
-    TK_CUDA(c, cudaMemcpyAsync(hc, t->d_counters, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
-    TK_CUDA(c, cudaStreamSynchronize(c->stream));
-    prof_add_units(c, TK_KID_COUNT, hc[1]);
-    t->total += hc[1];
-    cudaMemsetAsync(t->d_counters + 1, 0, sizeof(unsigned long long), c->stream);
+    if (!e) e = scan_excl_u32_to_u64(c, hist, offs, cells, &windows);   // synchronises
+    if (!e) {
+        cudaMemcpyAsync(offs + cells, &windows, 8, cudaMemcpyHostToDevice, c->stream);
+        std::vector<uint32_t> regs(HLL_M);
+        e = cuda_check(c, cudaMemcpyAsync(regs.data(), t->d_hll, HLL_M * 4, cudaMemcpyDeviceToHost, c->stream), "hll d2h");
+        if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "hll sync");
+        if (!e) {
+            double est = hll_estimate(regs.data());
+            uint64_t want = pow2_at_least((uint64_t)(est * 1.08 / t->max_load) + 1);
+            if (t->capacity == 0) e = table_alloc(t, want);
+            else if (want > t->capacity) e = table_rehash(t, want);
+        }
+    }
+    if (!e && windows) e = dmalloc(c, (void **)&keys, windows * 8, "bucketed k-mers");
+    if (!e && windows) {
+        prof_begin(c, TK_KID_COUNT, &ev);
+        // pass 1b: k-mers into their buckets
+        if (t->canonical) k_part_scatter<true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, offs, keys);
+        else k_part_scatter<false><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, offs, keys);
+        c->launches++;
+        e = overflow_reset(t);
+        // pass 2: partition-ordered insert
+        const unsigned igrid = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>((windows + INS_CHUNK - 1) / INS_CHUNK, (uint64_t)c->sm_count * 8));
+        if (!e) {
+            k_part_insert<<<igrid, CT_THREADS, 0, c->stream>>>(keys, windows, t->t, offs, grid, c->max_probes, t->d_ovf,
+                                                               (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
+                                                               t->d_counters);
+            c->launches++;
+            prof_end(c, TK_KID_COUNT, ev, windows);
+            e = check_launch(c, "count insert");
+        }
+    }
+    if (keys) dfree(c, keys);
+    if (offs) dfree(c, offs);
+    dfree(c, hist);
+    if (e) return e;
+    t->total += windows;
     t->distinct_valid = false;
     return drain_overflow(t);
 }
