@@ -182,8 +182,7 @@ class GpuPipeline:
             rr = kmer.ReadSet(ctx, self.d_right.data_ptr(), self.d_right.numel(), device=True)
             h2d = 0
         table = kmer.KmerTable(ctx, K, True)
-        table.add(rl)
-        table.add(rr)
+        table.add_many([rl, rr])
         hist = table.histo(1, 10000)
         dump_len = table.dump_fasta_len(MIN_COUNT)
         self._alloc_out(rl.n_reads, rr.n_reads)
@@ -260,11 +259,11 @@ def run_gpu(args, dist, world, rank, local):
     out = None
     if rank == 0:
         # K2 algorithmic bytes: one 32-byte sector per k-mer occurrence plus one
-        # byte per packed base it streams; each launch counts one mate file
+        # byte per packed base it streams; one count pass covers both mate files
         count_ms, count_launches, count_units = prof["count"]
         per_launch_units = count_units / max(count_launches, 1)
         per_launch_ms = count_ms / max(count_launches, 1)
-        packed_per_launch = res[0][4] / 2.0
+        packed_per_launch = res[0][4] * args.steps / max(count_launches, 1)
         alg_bytes = 32.0 * per_launch_units + packed_per_launch
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         peak = peaks.get("hbm_gbs", 6800.0)

@@ -120,6 +120,9 @@ void tk_reads_free(tk_reads *reads);
  * batch; the table grows (rehash) whenever it would exceed half load. */
 int tk_table_create(tk_ctx *ctx, int k, int canonical, uint64_t capacity_hint, tk_table **out);
 int tk_table_add_reads(tk_table *table, const tk_reads *reads);
+/* Adds several read sets in one pass over the table (e.g. both mate files:
+ * jellyfish counts `cat left.fa right.fa`, Trinity:1641). */
+int tk_table_add_reads_multi(tk_table *table, const tk_reads *const *sets, uint32_t n_sets);
 int tk_table_count_text(tk_table *table, const char *text, uint64_t len, int where);
 int tk_table_info(tk_table *table, uint64_t *distinct, uint64_t *total, uint64_t *capacity);
 /* hist[0] = keys with count < low, hist[1 + c - low] for low <= c <= high,

@@ -81,6 +81,27 @@ def test_batches_add_up(ctx, oracle):
     assert_pairs(t.dump(1), oracle.count(a + b, 25, True))
 
 
+def test_add_many_equals_concatenation(ctx, oracle):
+    a = synth.transcriptome_reads(seed=13, n_reads=40000).tobytes()
+    b, c = synth.gene_pairs(seed=14, n_genes=400, n_pairs=30000)
+    sets = [ReadSet(ctx, x) for x in (a, b.tobytes(), b"", c.tobytes())]
+    t = KmerTable(ctx, 25, True)
+    t.add_many(sets)
+    assert_pairs(t.dump(1), oracle.count(a + b.tobytes() + c.tobytes(), 25, True))
+    # a second multi-set pass into the now non-empty table
+    t.add_many(sets[:2])
+    assert_pairs(t.dump(1), oracle.count(a + b.tobytes() + c.tobytes() + a + b.tobytes(), 25, True))
+
+
+def test_large_partitioned_table(ctx, oracle):
+    """Enough distinct k-mers for a multi-partition table (> 2M slots)."""
+    text = synth.transcriptome_reads(seed=15, n_transcripts=4000, n_reads=600_000, err=0.02).tobytes()
+    t = gpu_count(ctx, text)
+    d, total, cap = t.info()
+    assert cap > (1 << 21)
+    assert_pairs(t.dump(1), oracle.count(text, 25, True))
+
+
 def test_overflow_and_growth_are_exact(ctx, oracle):
     """Eight reprobes at up to 0.6 load: many inserts overflow, the table
     doubles and the overflow list is re-inserted; the counts stay exact."""

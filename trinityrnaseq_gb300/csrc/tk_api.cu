@@ -385,6 +385,22 @@ int tk_table_add_reads(tk_table *t, const tk_reads *r) {
     return table_count_seq(t, r->d_seq, r->seq_len);
 }
 
+int tk_table_add_reads_multi(tk_table *t, const tk_reads *const *sets, uint32_t n_sets) {
+    if (!t || (!sets && n_sets)) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    std::vector<const uint8_t *> seqs(n_sets);
+    std::vector<uint64_t> lens(n_sets);
+    for (uint32_t i = 0; i < n_sets; i++) {
+        if (!sets[i]) return set_err(c, TK_E_INVAL, "tk_table_add_reads_multi: null read set");
+        if (sets[i]->ctx != c) return set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
+        seqs[i] = sets[i]->d_seq;
+        lens[i] = sets[i]->seq_len;
+    }
+    dump_invalidate(t);
+    return table_count_many(t, seqs.data(), lens.data(), (int)n_sets);
+}
+
 int tk_table_count_text(tk_table *t, const char *text, uint64_t len, int where) {
     if (!t) return TK_E_INVAL;
     tk_reads *r = nullptr;

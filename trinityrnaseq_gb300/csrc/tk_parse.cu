@@ -179,6 +179,70 @@ __global__ void k_line_records(const uint32_t *__restrict__ is_hdr, uint64_t *__
     line_rec_io[j] = incl == 0 ? ~0ULL : incl - 1;
 }
 
+// ---- fast path, L2: bytes each line would emit if sequence lines hold no
+// whitespace besides their newline (checked while copying)
+__global__ void k_line_lengths(ParseGeom g, const uint64_t *__restrict__ line_end, const uint8_t *__restrict__ kind,
+                               const uint64_t *__restrict__ line_rec, uint64_t n_lines, uint32_t *__restrict__ len) {
+    uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_lines) return;
+    uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
+    uint64_t le = line_end[j];
+    len[j] = (kind[j] == LK_SEQ && line_rec[j] != ~0ULL) ? (uint32_t)(le - ls) : 0u;
+}
+
+// ---- fast path, copy.  A warp takes 32 consecutive lines: lane l loads line
+// l's metadata (coalesced), header lines record their read's start, and then
+// the warp copies the group's sequence lines one after another, 32 bytes per
+// step with four steps in flight, upper-casing into seq.  A sequence line
+// holding whitespace sets *ws_seen and the byte-wise path redoes the emit.
+__global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end, const uint8_t *__restrict__ kind,
+                             const uint64_t *__restrict__ line_rec, const uint64_t *__restrict__ line_out,
+                             uint64_t n_lines, uint8_t *__restrict__ seq, uint64_t *__restrict__ rd_off,
+                             uint32_t *__restrict__ ws_seen) {
+    const unsigned lane = lane_id();
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    bool ws = false;
+    for (uint64_t j0 = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; j0 < n_lines; j0 += warps * 32) {
+        const uint64_t j = j0 + lane;
+        uint64_t src = 0, dst = 0;
+        uint32_t len = 0;
+        if (j < n_lines) {
+            const uint8_t kd = kind[j];
+            const uint64_t rec = line_rec[j];
+            if (rec != ~0ULL) {
+                const uint64_t out = line_out[j] + rec;
+                if (kd == LK_HDR) rd_off[rec] = out;
+                else if (kd == LK_SEQ) {
+                    src = j == 0 ? g.S : line_end[j - 1] + 1;
+                    len = (uint32_t)(line_end[j] - src);
+                    dst = out;
+                }
+            }
+        }
+        unsigned todo = __ballot_sync(0xffffffffu, len > 0);
+        while (todo) {
+            const int l = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint64_t s0 = __shfl_sync(0xffffffffu, src, l);
+            const uint64_t d0 = __shfl_sync(0xffffffffu, dst, l);
+            const uint32_t n = __shfl_sync(0xffffffffu, len, l);
+            for (uint32_t q = lane; q < n; q += 128) {
+                uint32_t c[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) c[u] = q + 32 * u < n ? (uint8_t)g.text[s0 + q + 32 * u] : (uint32_t)'A';
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (q + 32 * u < n) {
+                        ws |= is_ws(c[u]);
+                        seq[d0 + q + 32 * u] = (uint8_t)((c[u] >= 'a' && c[u] <= 'z') ? c[u] - 32u : c[u]);
+                    }
+                }
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, ws) && lane == 0) atomicExch(ws_seen, 1u);
+}
+
 // per-thread walk over its 32 bytes with the line each byte belongs to
 struct LineWalk {
     uint64_t line;
@@ -322,6 +386,8 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
     uint64_t n_tiles = g.S >= g.E ? 0 : (g.E - g.A + PT_TILE - 1) / PT_TILE;
     uint32_t *tile_nl = nullptr, *tile_em = nullptr, *is_hdr = nullptr;
     uint64_t *tile_line0 = nullptr, *tile_emit0 = nullptr, *line_end = nullptr, *line_rec = nullptr, *hdr_line = nullptr;
+    uint32_t *line_len = nullptr;
+    uint64_t *line_out = nullptr;
     uint8_t *kind = nullptr;
     uint32_t *d_maxlen = nullptr;
     uint64_t n_nl = 0, n_lines = 0, n_reads = 0, n_emit = 0;
@@ -365,11 +431,12 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
         if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
         k_line_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(is_hdr, line_rec, n_lines, hdr_line);
         c->launches++;
-        if ((e = alloc((void **)&tile_em, n_tiles * 4, "tile emits"))) break;
-        if ((e = alloc((void **)&tile_emit0, (n_tiles + 1) * 8, "tile emit offsets"))) break;
-        k_tile_emits<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, kind, line_rec, n_lines, tile_em);
+        // fast path: emitted bytes per line assuming no whitespace inside sequence lines
+        if ((e = alloc((void **)&line_len, n_lines * 4, "line lengths"))) break;
+        if ((e = alloc((void **)&line_out, (n_lines + 1) * 8, "line outputs"))) break;
+        k_line_lengths<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(g, line_end, kind, line_rec, n_lines, line_len);
         c->launches++;
-        if ((e = scan_excl_u32_to_u64(c, tile_em, tile_emit0, n_tiles, &n_emit))) break;
+        if ((e = scan_excl_u32_to_u64(c, line_len, line_out, n_lines, &n_emit))) break;
     } while (0);
     if (e) {
         for (void *p : tmp) dfree(c, p);
@@ -390,15 +457,40 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
         cudaMemsetAsync(d_maxlen, 0, 4, c->stream);
         uint64_t tail = r->seq_len;
         cudaMemcpyAsync(r->d_rd_off + n_reads, &tail, 8, cudaMemcpyHostToDevice, c->stream);
+        uint32_t ws_seen = 0;
         if (n_tiles && n_reads) {
-            k_emit<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, tile_emit0, kind, line_rec, n_lines,
-                                                                   r->d_seq, r->d_rd_off);
+            cudaMemsetAsync(c->d_err + DE_WS, 0, 4, c->stream);
+            const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n_lines + 7) / 8, (uint64_t)c->sm_count * 32));
+            k_copy_lines<<<grid, 256, 0, c->stream>>>(g, line_end, kind, line_rec, line_out, n_lines, r->d_seq, r->d_rd_off,
+                                                      c->d_err + DE_WS);
             c->launches++;
+            e = cuda_check(c, cudaMemcpyAsync(&ws_seen, c->d_err + DE_WS, 4, cudaMemcpyDeviceToHost, c->stream), "ws flag");
+            if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "copy sync");
+        }
+        if (!e && ws_seen) {
+            // some sequence line holds spaces, tabs or CRs: redo the emit byte by byte
+            do {
+                if ((e = alloc((void **)&tile_em, n_tiles * 4, "tile emits"))) break;
+                if ((e = alloc((void **)&tile_emit0, (n_tiles + 1) * 8, "tile emit offsets"))) break;
+                k_tile_emits<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, kind, line_rec, n_lines, tile_em);
+                c->launches++;
+                if ((e = scan_excl_u32_to_u64(c, tile_em, tile_emit0, n_tiles, &n_emit))) break;
+                r->n_bases = n_emit;
+                r->seq_len = n_emit + n_reads;
+                tail = r->seq_len;
+                cudaMemsetAsync(r->d_seq_alloc, '\n', seq_alloc, c->stream);
+                cudaMemcpyAsync(r->d_rd_off + n_reads, &tail, 8, cudaMemcpyHostToDevice, c->stream);
+                k_emit<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, tile_emit0, kind, line_rec, n_lines,
+                                                                       r->d_seq, r->d_rd_off);
+                c->launches++;
+            } while (0);
+        }
+        if (!e && n_tiles && n_reads) {
             k_names<<<grid_for(n_reads, 256), 256, 0, c->stream>>>(g, hdr_line, line_end, n_reads, r->d_rd_off,
                                                                    r->d_name_off, r->d_name_len, d_maxlen);
             c->launches++;
         }
-        e = cuda_check(c, cudaMemcpyAsync(&r->max_len, d_maxlen, 4, cudaMemcpyDeviceToHost, c->stream), "maxlen d2h");
+        if (!e) e = cuda_check(c, cudaMemcpyAsync(&r->max_len, d_maxlen, 4, cudaMemcpyDeviceToHost, c->stream), "maxlen d2h");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "parse sync");
     }
     for (void *p : tmp) dfree(c, p);

@@ -26,8 +26,9 @@ constexpr int CT_SPAN = 32;              // window end positions per thread
 constexpr int HLL_P = 12;
 constexpr int HLL_M = 1 << HLL_P;
 constexpr int NBUCKETS = 1 << BUCKET_BITS;
-constexpr int INS_PER_THREAD = 8;
+constexpr int INS_PER_THREAD = 2;
 constexpr uint64_t INS_CHUNK = (uint64_t)CT_THREADS * INS_PER_THREAD;
+enum NextMode { NEXT_NONE = 0, NEXT_FILL = 1, NEXT_PREFETCH = 2 };
 
 struct Window64 {
     uint32_t w[16];
@@ -74,11 +75,13 @@ __device__ __forceinline__ void thread_windows(const uint8_t *__restrict__ seq, 
     }
 }
 
-// Pass 1a: k-mers per (hash bucket, block) and the HLL sketch of the batch.
-// hist is bucket-major: hist[bucket * gridDim.x + block].
+// Pass 1a: k-mers per (hash bucket, column) and the HLL sketch of the batch.
+// hist is bucket-major with `cols` columns per bucket; read set s uses the
+// columns [col0, col0 + gridDim.x), one per block: hist[bucket * cols + col0 + block].
 template <bool CANON>
 __global__ void __launch_bounds__(CT_THREADS) k_part_hist(const uint8_t *__restrict__ seq, uint64_t n, int k,
-                                                         uint32_t *__restrict__ hist, uint32_t *__restrict__ regs,
+                                                         uint32_t *__restrict__ hist, uint64_t cols, uint64_t col0,
+                                                         uint32_t *__restrict__ regs,
                                                          unsigned long long *__restrict__ windows_out) {
     __shared__ uint32_t sh[NBUCKETS];
     __shared__ uint32_t sreg[HLL_M];
@@ -99,7 +102,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_hist(const uint8_t *__restr
         });
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) hist[(uint64_t)i * gridDim.x + blockIdx.x] = sh[i];
+    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) hist[(uint64_t)i * cols + col0 + blockIdx.x] = sh[i];
     for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS)
         if (sreg[i]) atomicMax(&regs[i], sreg[i]);
     windows = warp_sum(windows);
@@ -110,18 +113,21 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_hist(const uint8_t *__restr
 // offsets of the scanned histogram (same grid, same tiles as pass 1a).
 template <bool CANON>
 __global__ void __launch_bounds__(CT_THREADS) k_part_scatter(const uint8_t *__restrict__ seq, uint64_t n, int k,
-                                                            const uint64_t *__restrict__ offs,
-                                                            uint64_t *__restrict__ keys) {
-    __shared__ unsigned long long soff[NBUCKETS];
-    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) soff[i] = offs[(uint64_t)i * gridDim.x + blockIdx.x];
+                                                            const uint64_t *__restrict__ offs, uint64_t cols,
+                                                            uint64_t col0, uint64_t *__restrict__ keys) {
+    __shared__ unsigned long long sbase[NBUCKETS];   // region start of (bucket, this block)
+    __shared__ uint32_t scur[NBUCKETS];              // keys written to it so far
+    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) {
+        sbase[i] = offs[(uint64_t)i * cols + col0 + blockIdx.x];
+        scur[i] = 0;
+    }
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
     for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
         const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
         thread_windows<CANON>(seq, p0, p0 < n, k, [&](uint64_t key) {
-            uint64_t h = mix64(key);
-            unsigned long long pos = atomicAdd(&soff[h >> (64 - BUCKET_BITS)], 1ULL);
-            keys[pos] = key;
+            const uint32_t b = (uint32_t)(mix64(key) >> (64 - BUCKET_BITS));
+            keys[sbase[b] + atomicAdd(&scur[b], 1u)] = key;
         });
     }
 }
@@ -130,54 +136,57 @@ __device__ __forceinline__ void l2_prefetch_bulk(const void *p, uint32_t bytes) 
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Pass 2: insert the bucket-ordered keys.  Blocks walk the buffer in memory
-// order, so the live keys span about one partition: its table slice stays in
-// L2.  Thread 0 of each block prefetches (TMA bulk prefetch to L2) its share of
-// the next partition's slice while the current one is being filled.
-__global__ void __launch_bounds__(CT_THREADS) k_part_insert(const uint64_t *__restrict__ keys, uint64_t n, DevTable t,
-                                                           const uint64_t *__restrict__ offs, uint32_t hist_cols,
-                                                           int max_probes, uint64_t *__restrict__ ovf_keys,
-                                                           uint32_t *__restrict__ ovf_cnt, uint64_t ovf_cap,
-                                                           unsigned long long *__restrict__ counters) {
-    const uint64_t nchunks = (n + INS_CHUNK - 1) / INS_CHUNK;
-    const uint32_t nparts = 1u << t.pbits;
-    const uint32_t bpp = NBUCKETS >> t.pbits;            // buckets per partition
-    const uint64_t slice_bytes = (t.lmask + 1) * sizeof(Slot);
-    for (uint64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-        const uint64_t base = ch * INS_CHUNK;
-        if (threadIdx.x == 0 && t.pbits > 0) {
-            uint32_t p = (uint32_t)(mix64(__ldcs(keys + base)) >> (64 - t.pbits));
-            if (p + 1 < nparts) {
-                uint64_t ps = offs[(uint64_t)p * bpp * hist_cols];
-                uint64_t pe = offs[(uint64_t)(p + 1) * bpp * hist_cols];
-                uint64_t nch = (pe - ps + INS_CHUNK - 1) / INS_CHUNK;
-                uint64_t idx = base >= ps ? (base - ps) / INS_CHUNK : 0;
-                if (nch && idx < nch) {
-                    uint64_t share = ((slice_bytes + nch - 1) / nch + 15) & ~15ULL;
-                    uint64_t lo = idx * share;
-                    if (lo < slice_bytes) {
-                        // at most 4 x 64 KB per chunk; 16-byte aligned start, multiple-of-16 size
-                        uint64_t hi = lo + min(share, slice_bytes - lo);
-                        const char *slice = reinterpret_cast<const char *>(t.slots + ((uint64_t)(p + 1) << t.lbits));
-                        for (int q = 0; q < 4 && lo < hi; q++) {
-                            uint64_t bytes = min(hi - lo, (uint64_t)65536);
-                            l2_prefetch_bulk(slice + lo, (uint32_t)bytes);
-                            lo += bytes;
-                        }
-                    }
-                }
+// Pass 2, one launch per partition p (p = -1 only prepares slice 0).  The
+// launch first prepares slice p+1 -- on a fresh table it writes the empty
+// slots (those writes allocate in L2, so the slice is never read from DRAM);
+// on a table that already holds keys it bulk-prefetches the slice to L2 --
+// and then inserts partition p's keys, whose slice launch p-1 prepared.  Stream
+// order between the launches is the only synchronisation.
+__global__ void __launch_bounds__(CT_THREADS) k_part_step(const uint64_t *__restrict__ keys,
+                                                         const uint64_t *__restrict__ offs, uint64_t cols, int p,
+                                                         DevTable t, int next_mode, int max_probes,
+                                                         uint64_t *__restrict__ ovf_keys, uint32_t *__restrict__ ovf_cnt,
+                                                         uint64_t ovf_cap, unsigned long long *__restrict__ counters) {
+    const int nparts = 1 << t.pbits;
+    const uint64_t nslot = t.lmask + 1;
+    if (p + 1 < nparts) {
+        Slot *nxt = t.slots + ((uint64_t)(p + 1) << t.lbits);
+        if (next_mode == NEXT_FILL) {
+            ulonglong2 e;
+            e.x = EMPTY_KEY;
+            e.y = 0;
+            ulonglong2 *v = reinterpret_cast<ulonglong2 *>(nxt);
+            for (uint64_t i = (uint64_t)blockIdx.x * CT_THREADS + threadIdx.x; i < nslot; i += (uint64_t)gridDim.x * CT_THREADS)
+                v[i] = e;
+        } else if (next_mode == NEXT_PREFETCH && threadIdx.x == 0) {
+            const uint64_t bytes = nslot * sizeof(Slot);
+            const uint64_t share = ((bytes + gridDim.x - 1) / gridDim.x + 15) & ~15ULL;
+            uint64_t lo = (uint64_t)blockIdx.x * share;
+            const uint64_t hi = min(bytes, lo + share);
+            const char *base = reinterpret_cast<const char *>(nxt);
+            for (int q = 0; q < 8 && lo < hi; q++) {   // 16-byte aligned start, multiple-of-16 size, <= 64 KB each
+                uint64_t b = min(hi - lo, (uint64_t)65536);
+                l2_prefetch_bulk(base + lo, (uint32_t)b);
+                lo += b;
             }
         }
+    }
+    if (p < 0) return;
+    const uint64_t bpp = (uint64_t)(NBUCKETS >> t.pbits);
+    const uint64_t ps = offs[(uint64_t)p * bpp * cols];
+    const uint64_t pe = offs[(uint64_t)(p + 1) * bpp * cols];
+    for (uint64_t base = ps + (uint64_t)blockIdx.x * INS_CHUNK; base < pe; base += (uint64_t)gridDim.x * INS_CHUNK) {
         uint64_t kk[INS_PER_THREAD], s[INS_PER_THREAD];
         unsigned long long cur[INS_PER_THREAD];
 #pragma unroll
         for (int j = 0; j < INS_PER_THREAD; j++) {
             uint64_t i = base + (uint64_t)j * CT_THREADS + threadIdx.x;
-            kk[j] = i < n ? __ldcs(keys + i) : EMPTY_KEY;
+            kk[j] = i < pe ? __ldcs(keys + i) : EMPTY_KEY;
             s[j] = tbl_home(t, mix64(kk[j]));
         }
+        // first probes of all keys issued back to back
 #pragma unroll
-        for (int j = 0; j < INS_PER_THREAD; j++) cur[j] = kk[j] != EMPTY_KEY ? __ldcg(&t.slots[s[j]].key) : 0ULL;
+        for (int j = 0; j < INS_PER_THREAD; j++) cur[j] = kk[j] != EMPTY_KEY ? tbl_claim(&t.slots[s[j]], kk[j]) : 0ULL;
 #pragma unroll
         for (int j = 0; j < INS_PER_THREAD; j++) {
             if (kk[j] == EMPTY_KEY) continue;
@@ -186,11 +195,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_insert(const uint64_t *__re
             unsigned long long c = cur[j];
             bool done = false;
             for (int probe = 0; probe < max_probes; probe++) {
-                if (probe) c = __ldcg(&t.slots[slot].key);
-                if (c == EMPTY_KEY) {
-                    c = atomicCAS(&t.slots[slot].key, EMPTY_KEY, (unsigned long long)key);
-                    if (c == EMPTY_KEY) c = key;
-                }
+                if (probe) c = tbl_claim(&t.slots[slot], key);
                 if (c == key) {
                     atomicAdd(&t.slots[slot].val, 1u);
                     done = true;
@@ -377,12 +382,17 @@ static unsigned stream_grid(tk_ctx *c, uint64_t n, int threads) {
 
 // ------------------------------------------------------------------ host side
 
-int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val) {
+// fill = false leaves the slots unwritten: the partitioned count pass fills
+// each slice right before its inserts (a "fresh" table)
+static int table_alloc_geom(tk_table *t, uint64_t capacity, uint32_t init_val, bool fill) {
     tk_ctx *c = t->ctx;
     Slot *s = nullptr;
     TK_TRY(dmalloc(c, (void **)&s, capacity * sizeof(Slot), "k-mer table"));
-    k_fill_empty<<<stream_grid(c, capacity, 256), 256, 0, c->stream>>>(s, capacity, init_val);
-    c->launches++;
+    if (fill) {
+        k_fill_empty<<<stream_grid(c, capacity, 256), 256, 0, c->stream>>>(s, capacity, init_val);
+        c->launches++;
+    }
+    t->fresh = !fill;
     int bits = 0;
     while ((1ULL << bits) < capacity) bits++;
     int lbits = std::min(bits, MAX_LBITS);
@@ -395,7 +405,11 @@ int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val) {
     return check_launch(c, "table fill");
 }
 
-int table_alloc(tk_table *t, uint64_t capacity) { return table_alloc_init(t, capacity, 0); }
+int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val) {
+    return table_alloc_geom(t, capacity, init_val, true);
+}
+
+int table_alloc(tk_table *t, uint64_t capacity) { return table_alloc_geom(t, capacity, 0, true); }
 
 static int overflow_reset(tk_table *t) {
     return cuda_check(t->ctx, cudaMemsetAsync(t->d_counters, 0, sizeof(unsigned long long), t->ctx->stream), "ovf reset");
@@ -492,18 +506,27 @@ static uint64_t pow2_at_least(uint64_t x) {
     return p;
 }
 
-// Counts every window of a packed read array into the table.
-int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
+// Counts every window of one or more packed read arrays into the table in a
+// single partitioned pass (the table is touched once for all of them).
+int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *lens, int nsets) {
     tk_ctx *c = t->ctx;
-    if (seq_len == 0) return TK_OK;
-    const uint64_t n = seq_len;
-    // the two passes over the reads use one fixed grid so that every tile goes
-    // to the same block in both (the histogram columns are per block)
-    const unsigned grid = (unsigned)std::max<uint64_t>(
-        1, std::min<uint64_t>((n + CT_THREADS * CT_SPAN - 1) / (CT_THREADS * CT_SPAN), (uint64_t)c->sm_count * 2));
+    uint64_t total_len = 0;
+    for (int s = 0; s < nsets; s++) total_len += lens[s];
+    if (total_len == 0) return TK_OK;
+    // the two passes over each read array use one fixed grid, so every tile
+    // goes to the same block (histogram column) in both
+    std::vector<unsigned> grids(nsets);
+    std::vector<uint64_t> col0(nsets);
+    uint64_t cols = 0;
+    for (int s = 0; s < nsets; s++) {
+        grids[s] = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>((lens[s] + CT_THREADS * CT_SPAN - 1) / (CT_THREADS * CT_SPAN), (uint64_t)c->sm_count * 6));
+        col0[s] = cols;
+        cols += grids[s];
+    }
     uint32_t *hist = nullptr;
     uint64_t *offs = nullptr, *keys = nullptr;
-    const uint64_t cells = (uint64_t)NBUCKETS * grid;
+    const uint64_t cells = (uint64_t)NBUCKETS * cols;
     TK_TRY(dmalloc(c, (void **)&hist, cells * 4, "bucket histogram"));
     int e = dmalloc(c, (void **)&offs, (cells + 1) * 8, "bucket offsets");
     if (!e) e = cuda_check(c, cudaMemsetAsync(t->d_counters + 1, 0, 8, c->stream), "window counter");
@@ -512,10 +535,16 @@ int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
     if (!e) {
         // pass 1a: bucket histogram + HLL sketch (union with everything counted before)
         prof_begin(c, TK_KID_HLL, &ev);
-        if (t->canonical) k_part_hist<true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, hist, t->d_hll, t->d_counters + 1);
-        else k_part_hist<false><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, hist, t->d_hll, t->d_counters + 1);
-        c->launches++;
-        prof_end(c, TK_KID_HLL, ev, n);
+        for (int s = 0; s < nsets; s++) {
+            if (t->canonical)
+                k_part_hist<true><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
+                                                                          t->d_hll, t->d_counters + 1);
+            else
+                k_part_hist<false><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
+                                                                           t->d_hll, t->d_counters + 1);
+            c->launches++;
+        }
+        prof_end(c, TK_KID_HLL, ev, total_len);
         e = check_launch(c, "bucket histogram");
     }
     if (!e) e = scan_excl_u32_to_u64(c, hist, offs, cells, &windows);   // synchronises
@@ -527,7 +556,7 @@ int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
         if (!e) {
             double est = hll_estimate(regs.data());
             uint64_t want = pow2_at_least((uint64_t)(est * 1.08 / t->max_load) + 1);
-            if (t->capacity == 0) e = table_alloc(t, want);
+            if (t->capacity == 0) e = table_alloc_geom(t, want, 0, false);   // fresh: filled slice by slice below
             else if (want > t->capacity) e = table_rehash(t, want);
         }
     }
@@ -535,29 +564,50 @@ int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
     if (!e && windows) {
         prof_begin(c, TK_KID_COUNT, &ev);
         // pass 1b: k-mers into their buckets
-        if (t->canonical) k_part_scatter<true><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, offs, keys);
-        else k_part_scatter<false><<<grid, CT_THREADS, 0, c->stream>>>(d_seq, n, t->k, offs, keys);
-        c->launches++;
-        e = overflow_reset(t);
-        // pass 2: partition-ordered insert
-        const unsigned igrid = (unsigned)std::max<uint64_t>(
-            1, std::min<uint64_t>((windows + INS_CHUNK - 1) / INS_CHUNK, (uint64_t)c->sm_count * 8));
-        if (!e) {
-            k_part_insert<<<igrid, CT_THREADS, 0, c->stream>>>(keys, windows, t->t, offs, grid, c->max_probes, t->d_ovf,
-                                                               (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
-                                                               t->d_counters);
+        for (int s = 0; s < nsets; s++) {
+            if (t->canonical)
+                k_part_scatter<true><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
+            else
+                k_part_scatter<false><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
             c->launches++;
-            prof_end(c, TK_KID_COUNT, ev, windows);
-            e = check_launch(c, "count insert");
         }
+        e = overflow_reset(t);
+        // pass 2: one launch per partition, slice p+1 prepared while p is filled
+        const int nparts = 1 << t->t.pbits;
+        const int mode = t->fresh ? NEXT_FILL : (t->t.pbits > 0 ? NEXT_PREFETCH : NEXT_NONE);
+        const unsigned igrid = (unsigned)c->sm_count * 8;
+        for (int p = -1; !e && p < nparts; p++) {
+            k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(keys, offs, cols, p, t->t, mode, c->max_probes, t->d_ovf,
+                                                             (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap, t->d_counters);
+            c->launches++;
+        }
+        prof_end(c, TK_KID_COUNT, ev, windows);
+        if (!e) e = check_launch(c, "count insert");
+        if (!e) t->fresh = false;
+    } else if (!e && t->fresh) {
+        // nothing to insert: still leave every slot empty
+        k_fill_empty<<<stream_grid(c, t->capacity, 256), 256, 0, c->stream>>>(t->t.slots, t->capacity, 0);
+        c->launches++;
+        t->fresh = false;
+        e = check_launch(c, "table fill");
     }
     if (keys) dfree(c, keys);
     if (offs) dfree(c, offs);
     dfree(c, hist);
+    if (e && t->fresh && t->t.slots) {
+        // a failed first pass must not leave unwritten slots behind
+        k_fill_empty<<<stream_grid(c, t->capacity, 256), 256, 0, c->stream>>>(t->t.slots, t->capacity, 0);
+        c->launches++;
+        t->fresh = false;
+    }
     if (e) return e;
     t->total += windows;
     t->distinct_valid = false;
     return drain_overflow(t);
+}
+
+int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
+    return table_count_many(t, &d_seq, &seq_len, 1);
 }
 
 static int table_distinct(tk_table *t) {

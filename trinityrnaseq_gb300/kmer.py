@@ -184,6 +184,11 @@ class KmerTable:
     def add(self, reads: ReadSet) -> None:
         self.ctx.check(self.lib.tk_table_add_reads(self.h, reads.h), "tk_table_add_reads")
 
+    def add_many(self, sets: Sequence["ReadSet"]) -> None:
+        """Counts several read sets in one pass over the table."""
+        arr = (C.c_void_p * len(sets))(*[s.h.value for s in sets])
+        self.ctx.check(self.lib.tk_table_add_reads_multi(self.h, arr, len(sets)), "tk_table_add_reads_multi")
+
     def count_text(self, text: Buffer) -> None:
         ptr, n, keep = _host_ptr(text)
         self.ctx.check(self.lib.tk_table_count_text(self.h, C.c_void_p(ptr), n, N.TK_HOST), "tk_table_count_text")

@@ -58,6 +58,7 @@ SIGNATURES = {
     "tk_reads_free": (None, [vp]),
     "tk_table_create": (C.c_int, [vp, C.c_int, C.c_int, u64, P(vp)]),
     "tk_table_add_reads": (C.c_int, [vp, vp]),
+    "tk_table_add_reads_multi": (C.c_int, [vp, P(vp), u32]),
     "tk_table_count_text": (C.c_int, [vp, vp, u64, C.c_int]),
     "tk_table_info": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
     "tk_table_histo": (C.c_int, [vp, u64, u64, vp]),
