@@ -193,6 +193,27 @@ int tk_r2t_assign(tk_r2t *r2t, const tk_reads *reads, int where, int32_t *rec,
                   uint32_t *hits, uint32_t *nwin);
 void tk_r2t_free(tk_r2t *r2t);
 
+/* ------------------------------------------------------------- batched bins
+ * Replaces the per-bin k-mer counting of Trinity's phase 2 (one
+ * `Trinity --single c<comp>.trinity.reads.fa --trinity_complete` per read bin,
+ * fanned out by ParaFly, Trinity:3628-3735; each counts its own k-mers,
+ * Trinity:2669-2672) with one batched GPU pass.  `text` holds every bin's
+ * FASTA back to back; bin b is the records whose header starts in
+ * [bin_off[b], bin_off[b+1]) (n_bins + 1 offsets).  Each bin is counted in its
+ * own table slice (sized per bin from a sketch, block shape autotuned) by one
+ * persistent, CUDA-graph-captured launch, and its ">COUNT\nKMER\n" dump
+ * (count >= min_count, sorted by key) is bytes [off[b], off[b+1]) of the
+ * result text -- the same bytes as a separate tk_table_dump_fasta of that bin. */
+typedef struct tk_bins tk_bins;
+int tk_count_bins(tk_ctx *ctx, const char *text, uint64_t len, int where, const uint64_t *bin_off,
+                  uint32_t n_bins, int k, int canonical, uint32_t min_count, tk_bins **out);
+/* total dump bytes and k-mer windows counted */
+int tk_bins_info(const tk_bins *bins, uint64_t *text_len, uint64_t *kmers);
+/* n_bins + 1 byte offsets of each bin's dump in the text */
+int tk_bins_dump_offsets(const tk_bins *bins, uint64_t *offsets);
+int tk_bins_dump_text(const tk_bins *bins, char *dst, uint64_t cap);
+void tk_bins_free(tk_bins *bins);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,39 @@
+"""Batched per-bin counting (tk_count_bins): every bin's dump equals a
+separate plain count + dump of that bin, on the GPU and in the oracle."""
+import numpy as np
+import pytest
+
+from trinityrnaseq_gb300 import KmerTable, synth
+from trinityrnaseq_gb300.kmer import count_bins
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("min_count", [1, 2])
+def test_bins_equal_separate_plain_runs(ctx, oracle, min_count):
+    text, off, reads = synth.power_law_bins(seed=3, n_bins=60, alpha=1.8, min_reads=5, max_reads=3000)
+    t = text.tobytes()
+    dump, toff, kmers = count_bins(ctx, t, off, 25, True, min_count)
+    assert toff[0] == 0 and toff[-1] == len(dump)
+    total = 0
+    for b in range(len(off) - 1):
+        bt = t[int(off[b]):int(off[b + 1])]
+        got = dump[int(toff[b]):int(toff[b + 1])]
+        keys, counts = oracle.count(bt, 25, True)
+        total += int(counts.sum())
+        assert got == oracle.dump(keys, counts, 25, min_count), f"bin {b}"
+        if b % 15 == 0:
+            plain = KmerTable(ctx, 25, True)
+            plain.count_text(bt)
+            assert got == plain.dump_fasta(min_count)
+    assert kmers == total
+
+
+def test_bins_with_empty_and_tiny_bins(ctx, oracle):
+    parts = [b"", b">a\nACGTACGTACGTACGTACGTACGTACGT\n", b"", b">b\nNNNN\n>c\nACG\n",
+             synth.transcriptome_reads(seed=9, n_reads=500).tobytes()]
+    off = np.cumsum([0] + [len(p) for p in parts]).astype(np.uint64)
+    dump, toff, _ = count_bins(ctx, b"".join(parts), off, 25, False, 1)
+    for b, p in enumerate(parts):
+        k, c = oracle.count(p, 25, False)
+        assert dump[int(toff[b]):int(toff[b + 1])] == oracle.dump(k, c, 25, 1)

@@ -302,6 +302,28 @@ class ReadsToTranscripts:
         return rec[:n], hits[:n], nwin[:n]
 
 
+def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool = True,
+               min_count: int = 1) -> Tuple[bytes, np.ndarray, int]:
+    """Per-bin k-mer dumps of back-to-back FASTA bins in one batched GPU pass
+    (tk_count_bins).  Returns (dump text, n_bins + 1 byte offsets, k-mers counted)."""
+    ptr, n, keep = _host_ptr(text)
+    off = np.ascontiguousarray(bin_off, dtype=np.uint64)
+    nb = off.size - 1
+    h = C.c_void_p()
+    ctx.check(ctx.lib.tk_count_bins(ctx.h, C.c_void_p(ptr), n, N.TK_HOST, off.ctypes.data, nb, k, int(canonical),
+                                    min_count, C.byref(h)), "tk_count_bins")
+    try:
+        tl, km = C.c_uint64(), C.c_uint64()
+        ctx.check(ctx.lib.tk_bins_info(h, C.byref(tl), C.byref(km)), "tk_bins_info")
+        offs = np.zeros(nb + 1, dtype=np.uint64)
+        ctx.check(ctx.lib.tk_bins_dump_offsets(h, offs.ctypes.data), "tk_bins_dump_offsets")
+        buf = np.zeros(max(tl.value, 1), dtype=np.uint8)
+        ctx.check(ctx.lib.tk_bins_dump_text(h, buf.ctypes.data, buf.size), "tk_bins_dump_text")
+        return buf[:tl.value].tobytes(), offs, km.value
+    finally:
+        ctx.lib.tk_bins_free(h)
+
+
 # ---------------------------------------------------------------- text formats
 
 def format_histo(hist: np.ndarray, low: int = 1, high: int = 10000, full: bool = False) -> bytes:
