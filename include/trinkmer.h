@@ -214,6 +214,58 @@ int tk_bins_dump_offsets(const tk_bins *bins, uint64_t *offsets);
 int tk_bins_dump_text(const tk_bins *bins, char *dst, uint64_t cap);
 void tk_bins_free(tk_bins *bins);
 
+/* ------------------------------------------------------------- serving
+ * A resident job server: `slots` worker slots, each with its own context and
+ * stream, and an HBM admission budget (0 = 80% of the free memory).  A queued
+ * job starts as soon as a slot is free and its memory estimate fits what the
+ * running jobs leave of the budget, so jobs arriving while others run are
+ * admitted as slots and memory free up and their work overlaps on the GPU.
+ * Each job computes what the plain calls compute (a result does not depend on
+ * the other jobs).  The reference's nearest equivalent is ParaFly's process
+ * fan-out (Trinity:3652) and the two concurrent stats processes of
+ * util/insilico_read_normalization.pl:853-854.
+ *
+ * Job kinds and outputs (tk_job_output `which`):
+ *   TK_JOB_COUNT      text = reads; 0: dump text (count >= min_count, key order), 1: histo u64[10002]
+ *                     (tk_table_histo bins for low 1, high 10000)
+ *   TK_JOB_NORMALIZE  text = left mates, text2 = right mates; counted together (canonical when
+ *                     `canonical`), then coverage of each: 0..2 left median u32 / mean f32 / stdev f32,
+ *                     3..5 the same for the right mates, 6/7 left accession offset u64 / length u32
+ *                     into text, 8/9 the same for the right mates into text2
+ *   TK_JOB_R2T        text = reads, text2 = bundle; 0: rec i32, 1: hits u32, 2: nwin u32,
+ *                     3/4 accession offset u64 / length u32 into text, 5: read starts u64[n+1] in
+ *                     6: the packed upper-cased sequences, 7: component id u64 per bundle record
+ * Input buffers are host memory owned by the caller and must stay valid until
+ * the job has completed (tk_server_wait). */
+#define TK_JOB_COUNT 1
+#define TK_JOB_NORMALIZE 2
+#define TK_JOB_R2T 3
+
+typedef struct tk_job_spec {
+    int kind;
+    int k;
+    int canonical;
+    int strand;
+    uint32_t min_count;
+    const char *text;
+    uint64_t len;
+    const char *text2;
+    uint64_t len2;
+} tk_job_spec;
+
+typedef struct tk_server tk_server;
+int tk_server_create(int device, int slots, uint64_t hbm_budget, tk_server **out);
+int tk_server_submit(tk_server *server, const tk_job_spec *spec, uint64_t *job_id);
+/* Blocks until the job is done; latency = submit -> done, queued = submit -> start. */
+int tk_server_wait(tk_server *server, uint64_t job_id, int *status, uint64_t *latency_ns, uint64_t *queued_ns);
+/* Output buffer `which` of a completed job (valid until tk_job_release). */
+int tk_job_output(tk_server *server, uint64_t job_id, int which, const void **data, uint64_t *bytes);
+const char *tk_job_error(tk_server *server, uint64_t job_id);
+int tk_job_release(tk_server *server, uint64_t job_id);
+int tk_server_stats(tk_server *server, uint64_t *budget, uint64_t *in_use, int *max_concurrent);
+/* Waits for queued and running jobs, then stops the workers. */
+void tk_server_destroy(tk_server *server);
+
 #ifdef __cplusplus
 }
 #endif

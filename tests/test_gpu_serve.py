@@ -1,0 +1,70 @@
+"""The job server: a mix of counting, normalization and assignment jobs of
+different sizes, submitted together, runs concurrently and every result is
+bit-identical to the same job run alone through the plain calls."""
+import numpy as np
+import pytest
+
+from trinityrnaseq_gb300 import native as N
+from trinityrnaseq_gb300 import synth
+from trinityrnaseq_gb300.serve import Server, plain_run
+
+pytestmark = pytest.mark.gpu
+
+
+def same(a, b):
+    if isinstance(a, (bytes, bytearray)):
+        return a == b
+    if isinstance(a, tuple):
+        return all(same(x, y) for x, y in zip(a, b))
+    a, b = np.asarray(a), np.asarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def job_mix():
+    jobs = []
+    for i, n in enumerate((2000, 40000, 5000, 120000)):
+        jobs.append((N.TK_JOB_COUNT, synth.transcriptome_reads(seed=100 + i, n_reads=n).tobytes(), b"", 1 + (i % 2)))
+    for i, n in enumerate((3000, 30000)):
+        l, r = synth.gene_pairs(seed=200 + i, n_genes=300, n_pairs=n, fastq=bool(i % 2))
+        jobs.append((N.TK_JOB_NORMALIZE, l.tobytes(), r.tobytes(), 1))
+    b, r = synth.bundle_reads(seed=300, n_contigs=800, n_components=250, max_per_component=10, n_pairs=20000)
+    jobs.append((N.TK_JOB_R2T, r.tobytes(), b.tobytes(), 1))
+    return jobs
+
+
+def submit(srv, kind, t1, t2, mc):
+    if kind == N.TK_JOB_COUNT:
+        return srv.submit_count(t1, min_count=mc)
+    if kind == N.TK_JOB_NORMALIZE:
+        return srv.submit_normalize(t1, t2)
+    return srv.submit_r2t(t1, t2)
+
+
+@pytest.mark.parametrize("slots,budget", [(4, 0), (3, 64 << 20)])
+def test_served_equals_alone(ctx, slots, budget):
+    jobs = job_mix()
+    alone = [plain_run(ctx, k, t1, t2, min_count=mc) for k, t1, t2, mc in jobs]
+    with Server(ctx.device, slots=slots, hbm_budget=budget) as srv:
+        ids = [submit(srv, *j) for j in jobs]
+        for jid, (kind, *_), want in zip(ids, jobs, alone):
+            st, lat, q = srv.wait(jid)
+            assert st == 0, srv.error(jid)
+            assert lat >= q >= 0
+            assert same(srv.result(jid, kind), want)
+            srv.release(jid)
+        bud, in_use, maxc = srv.stats()
+        assert in_use == 0
+        if budget == 0:
+            assert maxc > 1          # jobs overlapped on the GPU
+        else:
+            assert maxc >= 1         # a tight budget admits jobs as memory frees up
+
+
+def test_bad_job_fails_alone(ctx):
+    with Server(ctx.device, slots=2) as srv:
+        bad = srv.submit_count(b"@r\nACGT\n+\nII\n@x\n")   # truncated FASTQ
+        good = srv.submit_count(synth.transcriptome_reads(seed=7, n_reads=1000).tobytes())
+        st, _, _ = srv.wait(bad)
+        assert st == N.TK_E_PARSE
+        st2, _, _ = srv.wait(good)
+        assert st2 == 0

@@ -82,6 +82,27 @@ SIGNATURES = {
 }
 
 
+TK_JOB_COUNT, TK_JOB_NORMALIZE, TK_JOB_R2T = 1, 2, 3
+
+
+class JobSpec(C.Structure):
+    _fields_ = [("kind", C.c_int), ("k", C.c_int), ("canonical", C.c_int), ("strand", C.c_int),
+                ("min_count", C.c_uint32), ("text", C.c_void_p), ("len", C.c_uint64), ("text2", C.c_void_p),
+                ("len2", C.c_uint64)]
+
+
+SIGNATURES.update({
+    "tk_server_create": (C.c_int, [C.c_int, C.c_int, u64, P(vp)]),
+    "tk_server_submit": (C.c_int, [vp, P(JobSpec), P(u64)]),
+    "tk_server_wait": (C.c_int, [vp, u64, P(C.c_int), P(u64), P(u64)]),
+    "tk_job_output": (C.c_int, [vp, u64, C.c_int, P(vp), P(u64)]),
+    "tk_job_error": (C.c_char_p, [vp, u64]),
+    "tk_job_release": (C.c_int, [vp, u64]),
+    "tk_server_stats": (C.c_int, [vp, P(u64), P(u64), P(C.c_int)]),
+    "tk_server_destroy": (None, [vp]),
+})
+
+
 class TrinkmerError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str = ""):
         self.status = status

@@ -132,6 +132,44 @@ inline bool parse_u64(const char *s, uint64_t *v) {
     return true;
 }
 
+// fastaToKmerCoverageStats rows "acc\tmedian\tmean\tstdev\n" (%g, a C++ ostream's default)
+inline std::vector<std::string> format_stats_rows(const char *text, const uint64_t *noff, const uint32_t *nlen,
+                                                  const uint32_t *med, const float *mean, const float *sd,
+                                                  uint64_t n, int threads) {
+    return format_parallel(n, threads, [&](uint64_t lo, uint64_t hi, std::string &s) {
+        s.reserve((hi - lo) * 48);
+        char line[128];
+        for (uint64_t i = lo; i < hi; i++) {
+            s.append(text + noff[i], nlen[i]);
+            int L = std::snprintf(line, sizeof(line), "\t%u\t%g\t%g\n", med[i], (double)mean[i], (double)sd[i]);
+            s.append(line, (size_t)L);
+        }
+    });
+}
+
+// readsToComponents rows "comp\t>acc\tpct\tSEQ\n"; reads without a component
+// or below min_pct percent are left out
+inline std::vector<std::string> format_r2t_rows(const char *text, const uint64_t *noff, const uint32_t *nlen,
+                                                const uint64_t *roff, const char *seq, const int32_t *rec,
+                                                const uint32_t *hits, const uint32_t *nwin, const uint64_t *comp,
+                                                int min_pct, uint64_t n, int threads) {
+    return format_parallel(n, threads, [&](uint64_t lo, uint64_t hi, std::string &s) {
+        char head[64];
+        for (uint64_t i = lo; i < hi; i++) {
+            if (rec[i] < 0 || nwin[i] == 0) continue;
+            uint32_t pct = (uint32_t)((100ull * hits[i]) / nwin[i]);
+            if (min_pct > 0 && pct < (uint32_t)min_pct) continue;
+            int L = std::snprintf(head, sizeof(head), "%llu\t>", (unsigned long long)comp[(size_t)rec[i]]);
+            s.append(head, (size_t)L);
+            s.append(text + noff[i], nlen[i]);
+            L = std::snprintf(head, sizeof(head), "\t%u\t", pct);
+            s.append(head, (size_t)L);
+            s.append(seq + roff[i], roff[i + 1] - roff[i] - 1);
+            s.push_back('\n');
+        }
+    });
+}
+
 inline tk_ctx *open_ctx() {
     tk_ctx *ctx = nullptr;
     int dev = 0;
