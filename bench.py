@@ -294,8 +294,145 @@ def run_gpu(args, dist, world, rank, local):
         }
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args)
+        del pipe
+        if args.bins and world == 1:
+            out["batched"] = batched_bench(ctx, args)
+        if args.jobs and world == 1:
+            out["served"] = served_bench(ctx, args)
     ctx.close()
     return out
+
+
+# ---------------------------------------------------------------- batched and served
+
+def batched_bench(ctx, args):
+    """Per-bin counting + dump of power-law read bins (alpha 1.8, 50..200,000
+    reads, 100 nt, 1% error, each from its own 1-20-transcript locus): one
+    batched call (tk_count_bins) against one plain count + dump per bin,
+    both from host FASTA to host dump text."""
+    from trinityrnaseq_gb300 import KmerTable, synth
+    from trinityrnaseq_gb300.kmer import count_bins
+    t0 = time.time()
+    text, off, nreads = synth.power_law_bins(seed=SEED + 7, n_bins=args.bins, alpha=1.8, min_reads=50,
+                                             max_reads=200_000, read_len=100, err=0.01)
+    log(f"batched: {args.bins} bins, {int(nreads.sum())} reads ({text.nbytes / 1e9:.2f} GB) in {time.time() - t0:.1f}s")
+    t = text.tobytes()
+    count_bins(ctx, t[:int(off[min(50, args.bins)])], off[:min(50, args.bins) + 1], K, True, 1)   # warm-up (autotune)
+    tb = time.time()
+    dump, toff, kmers = count_bins(ctx, t, off, K, True, 1)
+    t_batched = time.time() - tb
+    # plain: one count + dump per bin, the way ParaFly runs one Trinity per bin
+    tp = time.time()
+    same = True
+    for b in range(args.bins):
+        bt = t[int(off[b]):int(off[b + 1])]
+        tab = KmerTable(ctx, K, True)
+        tab.count_text(bt)
+        d = tab.dump_fasta(1)
+        tab.free()
+        if b % 97 == 0:
+            same &= d == dump[int(toff[b]):int(toff[b + 1])]
+    t_plain = time.time() - tp
+    return {"workload": f"{args.bins} power-law bins (alpha 1.8, 50..200000 reads), 100 nt, 1% error; "
+                        "count + dump -L 1 per bin, host FASTA in, host dump text out",
+            "reads": int(nreads.sum()), "kmers": int(kmers), "batched_s": t_batched, "plain_s": t_plain,
+            "batched_kmers_per_s": kmers / t_batched, "plain_kmers_per_s": kmers / t_plain,
+            "batched_reads_per_s": float(nreads.sum()) / t_batched, "plain_reads_per_s": float(nreads.sum()) / t_plain,
+            "speedup_vs_plain": t_plain / t_batched, "sampled_bins_identical": bool(same)}
+
+
+def served_bench(ctx, args):
+    """A seeded Poisson stream of jobs (60% count, 30% normalize, 10% read-to-
+    component; reads log-uniform in [10k, max]) through the job server at
+    0.5x, 1x and 1.5x the measured plain capacity (the same jobs run one
+    after another through the plain calls).  Reports p50/p99 latency and
+    jobs/s; every served result is compared with its plain result."""
+    import numpy as np
+    from trinityrnaseq_gb300 import native as N
+    from trinityrnaseq_gb300 import synth
+    from trinityrnaseq_gb300.serve import Server, plain_run
+    rng = np.random.default_rng(SEED + 11)
+    t0 = time.time()
+    jobs = []
+    bundle, r2t_reads = synth.bundle_reads(seed=SEED + 12, n_contigs=20000, n_components=6000, max_per_component=40,
+                                           n_pairs=max(args.job_max_reads // 2, 5000))
+    bundle = bundle.tobytes()
+    r2t_reads = r2t_reads.tobytes()
+    rec_len = r2t_reads.index(b"\n>") + 1
+    for i in range(args.jobs):
+        u = rng.random()
+        nr = int(np.exp(rng.uniform(np.log(10_000), np.log(args.job_max_reads))))
+        if u < 0.6:
+            txt = synth.transcriptome_reads(seed=SEED + 1000 + i, n_reads=nr, read_len=int(rng.integers(76, 151)),
+                                            err=float(rng.uniform(0.005, 0.01))).tobytes()
+            jobs.append((N.TK_JOB_COUNT, txt, b"", nr))
+        elif u < 0.9:
+            l, r = synth.gene_pairs(seed=SEED + 1000 + i, n_genes=2000, n_pairs=max(nr // 2, 1), fastq=False,
+                                    err=float(rng.uniform(0.005, 0.01)))
+            jobs.append((N.TK_JOB_NORMALIZE, l.tobytes(), r.tobytes(), nr))
+        else:
+            n_take = min(nr, len(r2t_reads) // rec_len)
+            jobs.append((N.TK_JOB_R2T, r2t_reads[:n_take * rec_len], bundle, n_take))
+    # job inputs live in pinned host memory for both the plain and the served runs
+    import torch
+
+    def pinned(b: bytes):
+        if not b:
+            return b
+        t = torch.empty(len(b), dtype=torch.uint8).pin_memory()
+        t.numpy()[:] = np.frombuffer(b, dtype=np.uint8)
+        return t.numpy()
+
+    jobs = [(k, pinned(a), pinned(b), n) for k, a, b, n in jobs]
+    log(f"served: {len(jobs)} jobs generated in {time.time() - t0:.1f}s")
+    # plain capacity: the jobs one after another through the plain calls
+    tp = time.time()
+    alone = [plain_run(ctx, k, a, b) for k, a, b, _ in jobs]
+    t_plain = time.time() - tp
+    capacity = len(jobs) / t_plain
+    total_reads = sum(j[3] for j in jobs)
+
+    def same(a, b):
+        if isinstance(a, (bytes, bytearray)):
+            return a == b
+        if isinstance(a, tuple):
+            return all(same(x, y) for x, y in zip(a, b))
+        a, b = np.asarray(a), np.asarray(b)
+        return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+    levels = {}
+    for load in (0.5, 1.0, 1.5, float("inf")):
+        # inf: every job submitted at once (the server's saturated throughput)
+        gaps = rng.exponential(1.0 / (capacity * load), size=len(jobs)) if load != float("inf") else [0.0] * len(jobs)
+        with Server(ctx.device, slots=args.slots, hbm_budget=int(args.budget_gb * 1e9)) as srv:
+            start = time.time()
+            ids = []
+            t_next = start
+            for (kind, a, b, _), g in zip(jobs, gaps):
+                t_next += g
+                while time.time() < t_next:
+                    time.sleep(min(0.0005, max(0.0, t_next - time.time())))
+                ids.append(srv.submit_count(a) if kind == N.TK_JOB_COUNT else
+                           srv.submit_normalize(a, b) if kind == N.TK_JOB_NORMALIZE else srv.submit_r2t(a, b))
+            lat, sts = [], []
+            for jid in ids:
+                st, l_ms, _ = srv.wait(jid)
+                sts.append(st)
+                lat.append(l_ms)
+            wall = time.time() - start
+            ok = all(s == 0 for s in sts)
+            for jid, (kind, *_), want in zip(ids, jobs, alone):
+                ok = ok and same(srv.result(jid, kind), want)
+                srv.release(jid)
+            maxc = srv.stats()[2]
+        lat.sort()
+        levels[f"{load}x"] = {"offered_jobs_per_s": capacity * load, "jobs_per_s": len(jobs) / wall,
+                              "reads_per_s": total_reads / wall, "p50_ms": lat[len(lat) // 2],
+                              "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_concurrent": maxc,
+                              "bit_exact_vs_plain": bool(ok)}
+    return {"workload": f"{len(jobs)} jobs (60% count, 30% normalize, 10% read-to-component), reads log-uniform "
+                        f"10k..{args.job_max_reads}, Poisson arrivals; {args.slots} slots, {args.budget_gb} GB budget",
+            "plain_jobs_per_s": capacity, "plain_reads_per_s": total_reads / t_plain, "levels": levels}
 
 
 # ---------------------------------------------------------------- CPU arms
@@ -371,6 +508,11 @@ def main():
     ap.add_argument("--pairs", type=int, default=FULL_PAIRS)
     ap.add_argument("--cpu-pairs", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--bins", type=int, default=5000, help="batched-bins comparison (0 = skip)")
+    ap.add_argument("--jobs", type=int, default=200, help="served-stream comparison (0 = skip)")
+    ap.add_argument("--job-max-reads", type=int, default=2_000_000)
+    ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
