@@ -425,10 +425,12 @@ def served_bench(ctx, args):
                 ok = ok and same(srv.result(jid, kind), want)
                 srv.release(jid)
             maxc = srv.stats()[2]
+            nbatched = srv.batched_jobs()
         lat.sort()
         levels[f"{load}x"] = {"offered_jobs_per_s": capacity * load, "jobs_per_s": len(jobs) / wall,
                               "reads_per_s": total_reads / wall, "p50_ms": lat[len(lat) // 2],
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_concurrent": maxc,
+                              "jobs_in_batched_passes": nbatched,
                               "bit_exact_vs_plain": bool(ok)}
     return {"workload": f"{len(jobs)} jobs (60% count, 30% normalize, 10% read-to-component), reads log-uniform "
                         f"10k..{args.job_max_reads}, Poisson arrivals; {args.slots} slots, {args.budget_gb} GB budget",

@@ -207,6 +207,12 @@ void tk_r2t_free(tk_r2t *r2t);
 typedef struct tk_bins tk_bins;
 int tk_count_bins(tk_ctx *ctx, const char *text, uint64_t len, int where, const uint64_t *bin_off,
                   uint32_t n_bins, int k, int canonical, uint32_t min_count, tk_bins **out);
+/* The same with a minimum count per bin (min_counts[n_bins]) and, when
+ * `histos` is not NULL, each bin's tk_table_histo(1, 10000) histogram
+ * (histos[b * 10002 + i]).  Bins may be FASTQ. */
+int tk_count_bins_ex(tk_ctx *ctx, const char *text, uint64_t len, int where, const uint64_t *bin_off,
+                     uint32_t n_bins, int k, int canonical, const uint32_t *min_counts, uint64_t *histos,
+                     tk_bins **out);
 /* total dump bytes and k-mer windows counted */
 int tk_bins_info(const tk_bins *bins, uint64_t *text_len, uint64_t *kmers);
 /* n_bins + 1 byte offsets of each bin's dump in the text */
@@ -263,6 +269,11 @@ int tk_job_output(tk_server *server, uint64_t job_id, int which, const void **da
 const char *tk_job_error(tk_server *server, uint64_t job_id);
 int tk_job_release(tk_server *server, uint64_t job_id);
 int tk_server_stats(tk_server *server, uint64_t *budget, uint64_t *in_use, int *max_concurrent);
+/* Count jobs that ran inside a batched pass: a free slot takes the first
+ * queued job that fits and, for a count job, every later queued count job
+ * with the same k, strandedness and input format (up to 64 jobs / 256 MB)
+ * as the bins of one tk_count_bins_ex pass. */
+int tk_server_batched_jobs(tk_server *server, uint64_t *jobs);
 /* Waits for queued and running jobs, then stops the workers. */
 void tk_server_destroy(tk_server *server);
 

@@ -60,6 +60,25 @@ def test_served_equals_alone(ctx, slots, budget):
             assert maxc >= 1         # a tight budget admits jobs as memory frees up
 
 
+def test_queued_count_jobs_are_batched(ctx):
+    """Count jobs queued behind a running one run as bins of one batched pass,
+    with per-job minimum counts and histograms equal to their solo runs."""
+    jobs = []
+    for i in range(12):
+        txt = synth.transcriptome_reads(seed=500 + i, n_reads=1500 + 700 * i, fastq=bool(i % 3 == 0)).tobytes()
+        if i == 4:
+            txt = txt[:-1]          # no trailing newline
+        jobs.append((txt, 1 + (i % 3)))
+    alone = [plain_run(ctx, N.TK_JOB_COUNT, t, min_count=mc) for t, mc in jobs]
+    with Server(ctx.device, slots=1) as srv:
+        ids = [srv.submit_count(t, min_count=mc) for t, mc in jobs]
+        for jid, want in zip(ids, alone):
+            st, _, _ = srv.wait(jid)
+            assert st == 0, srv.error(jid)
+            assert same(srv.result(jid, N.TK_JOB_COUNT), want)
+        assert srv.batched_jobs() > 0
+
+
 def test_bad_job_fails_alone(ctx):
     with Server(ctx.device, slots=2) as srv:
         bad = srv.submit_count(b"@r\nACGT\n+\nII\n@x\n")   # truncated FASTQ

@@ -144,10 +144,14 @@ __global__ void k_bin_count(const uint8_t *__restrict__ seq, uint64_t n, int k, 
     }
 }
 
-// every occupied slot with count >= min_count, keyed (bin << 2k) | key
+constexpr uint64_t BIN_HISTO = 10002;   // jellyfish histo bins for low 1, high 10000
+
+// every occupied slot with count >= its bin's minimum, keyed (bin << 2k) | key;
+// with `histo`, also every occupied slot's count into its bin's histogram
 __global__ void k_bin_compact(const Slot *__restrict__ slots, uint64_t cap, const uint64_t *__restrict__ base,
-                              uint32_t n_bins, int k, uint32_t min_count, uint64_t *__restrict__ okeys,
-                              uint32_t *__restrict__ ovals, unsigned long long *__restrict__ n_out) {
+                              uint32_t n_bins, int k, const uint32_t *__restrict__ min_count,
+                              uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals,
+                              unsigned long long *__restrict__ n_out, unsigned long long *__restrict__ histo) {
     const unsigned lane = lane_id();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x; b0 < cap; b0 += stride) {
@@ -156,17 +160,28 @@ __global__ void k_bin_compact(const Slot *__restrict__ slots, uint64_t cap, cons
         v.x = EMPTY_KEY;
         v.y = 0;
         if (i < cap) v = __ldcs(reinterpret_cast<const ulonglong2 *>(&slots[i]));
-        bool sel = v.x != EMPTY_KEY && (uint32_t)v.y >= min_count;
+        const bool occ = v.x != EMPTY_KEY;
+        const uint64_t bin = occ ? bin_of(base, n_bins, i) : 0;
+        const uint32_t c = (uint32_t)v.y;
+        bool sel = occ && c >= min_count[bin];
+        if (histo) {
+            // warp-merged increments: equal (bin, bucket) lanes add once
+            const uint64_t cell = occ ? bin * BIN_HISTO + (c > 10000u ? 10001u : c) : ~0ULL;
+            const unsigned act = __ballot_sync(0xffffffffu, occ);
+            if (occ) {
+                const unsigned peers = __match_any_sync(act, cell);
+                if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&histo[cell], (unsigned long long)__popc(peers));
+            }
+        }
         unsigned m = __ballot_sync(0xffffffffu, sel);
         if (!m) continue;
         unsigned long long wb = 0;
         if (lane == 0) wb = atomicAdd(n_out, (unsigned long long)__popc(m));
         wb = __shfl_sync(0xffffffffu, wb, 0);
         if (sel) {
-            uint64_t bin = bin_of(base, n_bins, i);
             uint64_t o = wb + __popc(m & ((1u << lane) - 1u));
             okeys[o] = (bin << (2 * k)) | v.x;
-            ovals[o] = (uint32_t)v.y;
+            ovals[o] = c;
         }
     }
 }
@@ -268,7 +283,8 @@ static void launch_count(tk_ctx *c, int block, const uint8_t *seq, uint64_t n, i
 }
 
 static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const uint64_t *bin_off_h, uint32_t n_bins,
-                    int k, int canonical, uint32_t min_count, double load, tk_bins *out) {
+                    int k, int canonical, const uint32_t *min_counts_h, uint64_t *histos_h, double load,
+                    tk_bins *out) {
     // 1. parse everything once
     tk_reads r;
     r.ctx = c;
@@ -293,7 +309,6 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
         if (!e && len) e = cuda_check(c, cudaMemcpyAsync(r.d_text, text, len, cudaMemcpyHostToDevice, c->stream), "bins h2d");
     }
     if (!e) e = parse_reads(c, &r);
-    if (!e && r.format == TK_FMT_FASTQ) e = set_err(c, TK_E_PARSE, "bins must be FASTA");
     uint64_t *d_bin_off = nullptr, *d_seq0 = nullptr;
     if (!e) e = alloc((void **)&d_bin_off, (n_bins + 1) * 8, "bin offsets");
     if (!e) e = alloc((void **)&d_seq0, (n_bins + 2) * 8, "bin starts");
@@ -435,7 +450,15 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
     uint32_t *v0 = nullptr, *v1 = nullptr;
     unsigned long long *d_n = nullptr;
     unsigned long long hn = 0;
+    uint32_t *d_minc = nullptr;
+    unsigned long long *d_histo = nullptr;
     if (!e) e = alloc((void **)&d_n, 8, "bins n");
+    if (!e) e = alloc((void **)&d_minc, n_bins * 4, "bin minimum counts");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(d_minc, min_counts_h, n_bins * 4, cudaMemcpyHostToDevice, c->stream), "min counts");
+    if (!e && histos_h) {
+        e = alloc((void **)&d_histo, (uint64_t)n_bins * BIN_HISTO * 8, "bin histograms");
+        if (!e) cudaMemsetAsync(d_histo, 0, (uint64_t)n_bins * BIN_HISTO * 8, c->stream);
+    }
     // occupied slots <= min(windows, slots)
     const uint64_t upper = std::max<uint64_t>(1, std::min<uint64_t>(kmers, total));
     if (!e) e = alloc((void **)&k0, upper * 8, "bin keys");
@@ -446,10 +469,14 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
         cudaMemsetAsync(d_n, 0, 8, c->stream);
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COMPACT, &ev);
-        k_bin_compact<<<(unsigned)c->sm_count * 8, 256, 0, c->stream>>>(slots, total, d_base, n_bins, k, min_count, k0, v0, d_n);
+        k_bin_compact<<<(unsigned)c->sm_count * 8, 256, 0, c->stream>>>(slots, total, d_base, n_bins, k, d_minc, k0, v0,
+                                                                        d_n, d_histo);
         c->launches++;
         prof_end(c, TK_KID_COMPACT, ev, total);
         e = cuda_check(c, cudaMemcpyAsync(&hn, d_n, 8, cudaMemcpyDeviceToHost, c->stream), "bins n d2h");
+        if (!e && d_histo)
+            e = cuda_check(c, cudaMemcpyAsync(histos_h, d_histo, (uint64_t)n_bins * BIN_HISTO * 8, cudaMemcpyDeviceToHost,
+                                              c->stream), "bin histograms d2h");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "bins compact sync");
     }
     bool in_tmp = false;
@@ -514,9 +541,10 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
 
 extern "C" {
 
-int tk_count_bins(tk_ctx *ctx, const char *text, uint64_t len, int where, const uint64_t *bin_off, uint32_t n_bins,
-                  int k, int canonical, uint32_t min_count, tk_bins **out) {
-    if (!ctx || !out || !bin_off || n_bins == 0 || (!text && len)) return TK_E_INVAL;
+int tk_count_bins_ex(tk_ctx *ctx, const char *text, uint64_t len, int where, const uint64_t *bin_off,
+                     uint32_t n_bins, int k, int canonical, const uint32_t *min_counts, uint64_t *histos,
+                     tk_bins **out) {
+    if (!ctx || !out || !bin_off || !min_counts || n_bins == 0 || (!text && len)) return TK_E_INVAL;
     *out = nullptr;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return tk::set_err(ctx, TK_E_CUDA, "cudaSetDevice");
     if (k < 1 || k > tk::MAX_K) return tk::set_err(ctx, TK_E_INVAL, "k must be in 1..31");
@@ -528,13 +556,20 @@ int tk_count_bins(tk_ctx *ctx, const char *text, uint64_t len, int where, const 
     z->ctx = ctx;
     z->n_bins = n_bins;
     z->k = k;
-    int e = tk::bins_run(ctx, text, len, where, bin_off, n_bins, k, canonical, min_count ? min_count : 1, 0.6, z);
+    int e = tk::bins_run(ctx, text, len, where, bin_off, n_bins, k, canonical, min_counts, histos, 0.6, z);
     if (e) {
         delete z;
         return e;
     }
     *out = z;
     return TK_OK;
+}
+
+int tk_count_bins(tk_ctx *ctx, const char *text, uint64_t len, int where, const uint64_t *bin_off, uint32_t n_bins,
+                  int k, int canonical, uint32_t min_count, tk_bins **out) {
+    if (n_bins == 0) return TK_E_INVAL;
+    std::vector<uint32_t> mc(n_bins, min_count ? min_count : 1);
+    return tk_count_bins_ex(ctx, text, len, where, bin_off, n_bins, k, canonical, mc.data(), nullptr, out);
 }
 
 int tk_bins_info(const tk_bins *z, uint64_t *text_len, uint64_t *kmers) {

@@ -53,6 +53,7 @@ struct tk_server {
     int slots = 0;
     int running = 0;
     int max_running = 0;
+    uint64_t batched_jobs = 0;               // jobs that ran inside a batched pass
 };
 
 namespace {
@@ -96,6 +97,67 @@ int run_count(tk_ctx *c, Job &j) {
         j.out.push_back(as_bytes(hist));
     }
     return e;
+}
+
+// first non-whitespace byte of a job's text ('>' FASTA, '@' FASTQ)
+char text_format(const tk_job_spec &s) {
+    for (uint64_t i = 0; i < s.len; i++) {
+        char ch = s.text[i];
+        if (ch != ' ' && ch != '\t' && ch != '\n' && ch != '\r') return ch;
+    }
+    return 0;
+}
+
+// Several count jobs as the bins of one batched pass (tk_count_bins_ex): one
+// parse, one persistent counting launch, one dump formatting for all of them.
+// The texts are copied straight into one device buffer, a newline between
+// jobs whose text does not end with one.
+int run_count_batch(tk_ctx *c, std::vector<Job *> &batch) {
+    const uint32_t n = (uint32_t)batch.size();
+    std::vector<uint64_t> off(n + 1);
+    std::vector<uint32_t> minc(n);
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const tk_job_spec &s = batch[i]->spec;
+        off[i] = total;
+        total += s.len + ((s.len && s.text[s.len - 1] != '\n') ? 1 : 0);
+        minc[i] = s.min_count ? s.min_count : 1;
+    }
+    off[n] = total;
+    char *d_text = nullptr;
+    int e = tk::dmalloc(c, (void **)&d_text, total + 64, "batched count text");
+    static const char nl = '\n';
+    for (uint32_t i = 0; !e && i < n; i++) {
+        const tk_job_spec &s = batch[i]->spec;
+        if (s.len) e = tk::cuda_check(c, cudaMemcpyAsync(d_text + off[i], s.text, s.len, cudaMemcpyHostToDevice, c->stream), "batch h2d");
+        if (!e && off[i] + s.len < off[i + 1])
+            e = tk::cuda_check(c, cudaMemcpyAsync(d_text + off[i] + s.len, &nl, 1, cudaMemcpyHostToDevice, c->stream), "batch sep");
+    }
+    std::vector<uint64_t> histos((size_t)n * 10002);
+    tk_bins *bins = nullptr;
+    if (!e) e = tk_count_bins_ex(c, d_text, total, TK_DEVICE, off.data(), n, batch[0]->spec.k, batch[0]->spec.canonical,
+                                 minc.data(), histos.data(), &bins);
+    uint64_t tlen = 0;
+    std::vector<uint64_t> toff(n + 1);
+    std::vector<char> text;
+    if (!e) e = tk_bins_info(bins, &tlen, nullptr);
+    if (!e) e = tk_bins_dump_offsets(bins, toff.data());
+    if (!e) {
+        text.resize(tlen);
+        e = tk_bins_dump_text(bins, text.data(), tlen);
+    }
+    if (bins) tk_bins_free(bins);
+    if (d_text) tk::dfree(c, d_text);
+    if (e) return e;
+    for (uint32_t i = 0; i < n; i++) {
+        Job &j = *batch[i];
+        j.out.clear();
+        j.out.emplace_back(text.begin() + (long)toff[i], text.begin() + (long)toff[i + 1]);
+        std::vector<char> h(10002 * 8);
+        std::memcpy(h.data(), histos.data() + (size_t)i * 10002, h.size());
+        j.out.push_back(std::move(h));
+    }
+    return TK_OK;
 }
 
 int run_normalize(tk_ctx *c, Job &j) {
@@ -167,11 +229,14 @@ int run_r2t(tk_ctx *c, Job &j) {
     return e;
 }
 
+constexpr size_t BATCH_JOBS = 64;
+constexpr uint64_t BATCH_BYTES = 256ULL << 20;
+
 void worker_loop(tk_server *s) {
     tk_ctx *c = nullptr;
     int ce = tk_ctx_create(s->device, &c);
     for (;;) {
-        Job *j = nullptr;
+        std::vector<Job *> batch;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             for (;;) {
@@ -184,36 +249,72 @@ void worker_loop(tk_server *s) {
                 for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
                     uint64_t need = std::min((*it)->est, s->budget);
                     if (s->in_use + need <= s->budget) {
-                        j = *it;
+                        Job *j = *it;
                         s->queue.erase(it);
                         s->in_use += need;
                         j->est = need;
+                        batch.push_back(j);
                         break;
                     }
                 }
-                if (j) break;
+                if (!batch.empty()) break;
                 s->cv_work.wait(lk);
+            }
+            // continuous batching: later count jobs of the same kind of input
+            // join this one in a single batched pass while memory allows
+            Job *head = batch[0];
+            if (head->spec.kind == TK_JOB_COUNT && head->spec.len < BATCH_BYTES) {
+                uint64_t bytes = head->spec.len;
+                const char fmt = text_format(head->spec);
+                for (auto it = s->queue.begin(); it != s->queue.end() && batch.size() < BATCH_JOBS;) {
+                    Job *j = *it;
+                    const tk_job_spec &q = j->spec;
+                    uint64_t need = std::min(j->est, s->budget);
+                    if (q.kind == TK_JOB_COUNT && q.k == head->spec.k && q.canonical == head->spec.canonical &&
+                        bytes + q.len <= BATCH_BYTES && text_format(q) == fmt && s->in_use + need <= s->budget) {
+                        it = s->queue.erase(it);
+                        s->in_use += need;
+                        j->est = need;
+                        bytes += q.len;
+                        batch.push_back(j);
+                    } else {
+                        ++it;
+                    }
+                }
             }
             s->running++;
             s->max_running = std::max(s->max_running, s->running);
         }
-        j->t_start = clk::now();
-        int e = ce;
-        if (!e) {
-            switch (j->spec.kind) {
-            case TK_JOB_COUNT: e = run_count(c, *j); break;
-            case TK_JOB_NORMALIZE: e = run_normalize(c, *j); break;
-            case TK_JOB_R2T: e = run_r2t(c, *j); break;
-            default: e = TK_E_INVAL;
+        const auto t_start = clk::now();
+        for (Job *j : batch) j->t_start = t_start;
+        std::vector<int> st(batch.size(), ce);
+        if (!ce) {
+            int be = batch.size() > 1 ? run_count_batch(c, batch) : -1;
+            for (size_t i = 0; i < batch.size(); i++) {
+                if (be == TK_OK) { st[i] = TK_OK; continue; }
+                Job &j = *batch[i];        // alone, or the batch failed: one by one
+                j.out.clear();
+                switch (j.spec.kind) {
+                case TK_JOB_COUNT: st[i] = run_count(c, j); break;
+                case TK_JOB_NORMALIZE: st[i] = run_normalize(c, j); break;
+                case TK_JOB_R2T: st[i] = run_r2t(c, j); break;
+                default: st[i] = TK_E_INVAL;
+                }
+                if (st[i]) j.error = tk_ctx_last_error(c);
             }
         }
         {
             std::lock_guard<std::mutex> lk(s->mu);
-            j->t_done = clk::now();
-            j->status = e;
-            if (e) j->error = c ? tk_ctx_last_error(c) : "no CUDA context";
-            s->in_use -= j->est;
+            const auto t_done = clk::now();
+            for (size_t i = 0; i < batch.size(); i++) {
+                Job *j = batch[i];
+                j->t_done = t_done;
+                j->status = st[i];
+                if (st[i] && j->error.empty()) j->error = c ? tk_ctx_last_error(c) : "no CUDA context";
+                s->in_use -= j->est;
+            }
             s->running--;
+            s->batched_jobs += batch.size() > 1 ? batch.size() : 0;
         }
         s->cv_done.notify_all();
         s->cv_work.notify_all();
@@ -315,6 +416,13 @@ int tk_server_stats(tk_server *s, uint64_t *budget, uint64_t *in_use, int *max_c
     if (budget) *budget = s->budget;
     if (in_use) *in_use = s->in_use;
     if (max_concurrent) *max_concurrent = s->max_running;
+    return TK_OK;
+}
+
+int tk_server_batched_jobs(tk_server *s, uint64_t *jobs) {
+    if (!s || !jobs) return TK_E_INVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *jobs = s->batched_jobs;
     return TK_OK;
 }
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "tk_r2t_assign": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
     "tk_r2t_free": (None, [vp]),
     "tk_count_bins": (C.c_int, [vp, vp, u64, C.c_int, vp, u32, C.c_int, C.c_int, u32, P(vp)]),
+    "tk_count_bins_ex": (C.c_int, [vp, vp, u64, C.c_int, vp, u32, C.c_int, C.c_int, vp, vp, P(vp)]),
     "tk_bins_info": (C.c_int, [vp, P(u64), P(u64)]),
     "tk_bins_dump_offsets": (C.c_int, [vp, vp]),
     "tk_bins_dump_text": (C.c_int, [vp, vp, u64]),
@@ -100,6 +101,7 @@ SIGNATURES.update({
     "tk_job_release": (C.c_int, [vp, u64]),
     "tk_server_stats": (C.c_int, [vp, P(u64), P(u64), P(C.c_int)]),
     "tk_server_destroy": (None, [vp]),
+    "tk_server_batched_jobs": (C.c_int, [vp, P(u64)]),
 })
 
 

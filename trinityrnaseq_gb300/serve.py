@@ -81,6 +81,11 @@ class Server:
         N.check(self.lib.tk_job_release(self.h, jid), "tk_job_release")
         self._keep.pop(jid, None)
 
+    def batched_jobs(self) -> int:
+        n = C.c_uint64()
+        N.check(self.lib.tk_server_batched_jobs(self.h, C.byref(n)), "tk_server_batched_jobs")
+        return n.value
+
     def stats(self) -> Tuple[int, int, int]:
         b, u, m = C.c_uint64(), C.c_uint64(), C.c_int()
         N.check(self.lib.tk_server_stats(self.h, C.byref(b), C.byref(u), C.byref(m)), "tk_server_stats")
