@@ -427,7 +427,9 @@ def served_bench(ctx, args):
             maxc = srv.stats()[2]
             nbatched = srv.batched_jobs()
         lat.sort()
-        levels[f"{load}x"] = {"offered_jobs_per_s": capacity * load, "jobs_per_s": len(jobs) / wall,
+        name = "burst" if load == float("inf") else f"{load}x"
+        levels[name] = {"offered_jobs_per_s": capacity * load if load != float("inf") else None,
+                        "jobs_per_s": len(jobs) / wall,
                               "reads_per_s": total_reads / wall, "p50_ms": lat[len(lat) // 2],
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_concurrent": maxc,
                               "jobs_in_batched_passes": nbatched,

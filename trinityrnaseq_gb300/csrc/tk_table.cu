@@ -254,28 +254,45 @@ __global__ void k_occupied(const Slot *__restrict__ slots, uint64_t cap, unsigne
     if (lane_id() == 0 && n) atomicAdd(out, (unsigned long long)n);
 }
 
-// K3: keys with count >= min_count, warp-aggregated append (order is fixed by the sort that follows)
-__global__ void k_compact(const Slot *__restrict__ slots, uint64_t cap, uint32_t min_count, uint64_t *__restrict__ okeys,
-                          uint32_t *__restrict__ ovals, unsigned long long *__restrict__ n_out) {
-    const unsigned lane = lane_id();
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < cap; base += stride) {
-        uint64_t i = base + threadIdx.x;
-        ulonglong2 v;
-        v.x = EMPTY_KEY;
-        v.y = 0;
-        if (i < cap) v = __ldcs(reinterpret_cast<const ulonglong2 *>(&slots[i]));
-        bool sel = v.x != EMPTY_KEY && (uint32_t)v.y >= min_count;
-        unsigned m = __ballot_sync(0xffffffffu, sel);
-        if (!m) continue;
-        unsigned long long wbase = 0;
-        if (lane == 0) wbase = atomicAdd(n_out, (unsigned long long)__popc(m));
-        wbase = __shfl_sync(0xffffffffu, wbase, 0);
-        if (sel) {
-            uint64_t o = wbase + __popc(m & ((1u << lane) - 1u));
-            okeys[o] = v.x;
-            ovals[o] = (uint32_t)v.y;
+// K3: keys with count >= min_count.  A block takes a chunk of CP_ITEMS slots
+// per thread, ranks its selected slots with a block scan and reserves their
+// output range with one atomicAdd per chunk (a per-warp counter atomic on one
+// address serialises in L2 on a 2G-slot table).  Output order is fixed by the
+// sort that follows.
+constexpr int CP_ITEMS = 16;
+
+__global__ void __launch_bounds__(256) k_compact(const Slot *__restrict__ slots, uint64_t cap, uint32_t min_count,
+                                                 uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals,
+                                                 unsigned long long *__restrict__ n_out) {
+    __shared__ uint32_t sm[256 / 32 + 1];
+    __shared__ unsigned long long s_base;
+    const uint64_t chunk = (uint64_t)blockDim.x * CP_ITEMS;
+    for (uint64_t base = (uint64_t)blockIdx.x * chunk; base < cap; base += (uint64_t)gridDim.x * chunk) {
+        ulonglong2 v[CP_ITEMS];
+        uint32_t nsel = 0;
+#pragma unroll
+        for (int j = 0; j < CP_ITEMS; j++) {
+            const uint64_t i = base + (uint64_t)j * blockDim.x + threadIdx.x;   // coalesced, striped
+            v[j].x = EMPTY_KEY;
+            v[j].y = 0;
+            if (i < cap) v[j] = __ldcs(reinterpret_cast<const ulonglong2 *>(&slots[i]));
+            nsel += v[j].x != EMPTY_KEY && (uint32_t)v[j].y >= min_count;
         }
+        uint32_t tot;
+        uint32_t pre = block_excl_scan<uint32_t>(nsel, sm, &tot);
+        if (tot == 0) continue;                   // uniform over the block
+        if (threadIdx.x == 0) s_base = atomicAdd(n_out, (unsigned long long)tot);
+        __syncthreads();
+        uint64_t o = s_base + pre;
+#pragma unroll
+        for (int j = 0; j < CP_ITEMS; j++) {
+            if (v[j].x != EMPTY_KEY && (uint32_t)v[j].y >= min_count) {
+                okeys[o] = v[j].x;
+                ovals[o] = (uint32_t)v[j].y;
+                o++;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -315,21 +332,39 @@ __global__ void k_dump_len(const uint32_t *__restrict__ cnt, uint64_t n, int k, 
     if (i < n) len[i] = 3u + dec_digits(cnt[i]) + (uint32_t)k;
 }
 
-// K4 pass 2: write one record per thread
-__global__ void k_dump_write(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ cnt,
-                             const uint64_t *__restrict__ off, uint64_t n, int k, char *__restrict__ out) {
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    char *p = out + off[i];
-    uint32_t c = cnt[i];
-    uint32_t nd = dec_digits(c);
-    p[0] = '>';
-    for (int d = (int)nd; d >= 1; d--) { p[d] = (char)('0' + c % 10); c /= 10; }
-    p[nd + 1] = '\n';
-    uint64_t key = keys[i];
-    char *q = p + nd + 2;
-    for (int j = 0; j < k; j++) q[j] = "ACGT"[(key >> (2 * (k - 1 - j))) & 3];
-    q[k] = '\n';
+// K4 pass 2: each lane formats one record into its warp's shared-memory
+// buffer, then the warp stores the 32 records' bytes contiguously (every store
+// instruction covers 32 consecutive bytes).
+constexpr int DW_THREADS = 256;
+constexpr int DW_WARP_BYTES = 32 * (3 + 10 + MAX_K);
+
+__global__ void __launch_bounds__(DW_THREADS) k_dump_write(const uint64_t *__restrict__ keys,
+                                                          const uint32_t *__restrict__ cnt,
+                                                          const uint64_t *__restrict__ off, uint64_t n, int k,
+                                                          uint64_t total, char *__restrict__ out) {
+    __shared__ char buf[DW_THREADS / 32][DW_WARP_BYTES];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint64_t i0 = (uint64_t)blockIdx.x * DW_THREADS + warp * 32;   // first record of this warp
+    if (i0 >= n) return;
+    const uint64_t i = i0 + lane;
+    const uint64_t w0 = off[i0];
+    char *p = buf[warp];
+    if (i < n) {
+        p += off[i] - w0;
+        uint32_t c = cnt[i];
+        uint32_t nd = dec_digits(c);
+        p[0] = '>';
+        for (int d = (int)nd; d >= 1; d--) { p[d] = (char)('0' + c % 10); c /= 10; }
+        p[nd + 1] = '\n';
+        uint64_t key = keys[i];
+        char *q = p + nd + 2;
+        for (int j = 0; j < k; j++) q[j] = "ACGT"[(key >> (2 * (k - 1 - j))) & 3];
+        q[k] = '\n';
+    }
+    __syncwarp();
+    const uint64_t last = min(i0 + 32, n);
+    const uint64_t w1 = last < n ? off[last] : total;
+    for (uint64_t b = lane; b < w1 - w0; b += 32) out[w0 + b] = buf[warp][b];
 }
 
 // dump records parsed as reads: name = decimal count, sequence = k-mer
@@ -690,7 +725,8 @@ int table_sorted_pairs(tk_table *t, uint32_t min_count, uint64_t **keys_out, uin
         cudaMemsetAsync(d_n, 0, 8, c->stream);
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COMPACT, &ev);
-        k_compact<<<stream_grid(c, t->capacity, 256), 256, 0, c->stream>>>(t->t.slots, t->capacity, min_count, k0, v0, d_n);
+        k_compact<<<stream_grid(c, (t->capacity + CP_ITEMS - 1) / CP_ITEMS, 256), 256, 0, c->stream>>>(
+            t->t.slots, t->capacity, min_count, k0, v0, d_n);
         c->launches++;
         prof_end(c, TK_KID_COMPACT, ev, t->capacity);
         e = cuda_check(c, cudaMemcpyAsync(&hn, d_n, 8, cudaMemcpyDeviceToHost, c->stream), "compact n");
@@ -741,7 +777,7 @@ int format_dump(tk_ctx *c, const uint64_t *keys, const uint32_t *cnt, uint64_t n
     char *text = nullptr;
     if (!e) e = dmalloc(c, (void **)&text, total, "dump text");
     if (!e) {
-        k_dump_write<<<grid_for(n, 256), 256, 0, c->stream>>>(keys, cnt, offs, n, k, text);
+        k_dump_write<<<grid_for(n, DW_THREADS), DW_THREADS, 0, c->stream>>>(keys, cnt, offs, n, k, total, text);
         c->launches++;
         e = check_launch(c, "dump write");
     }
