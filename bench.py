@@ -198,13 +198,13 @@ class GpuPipeline:
                                      device=not e2e)
             if e2e:
                 d2h += 12 * rs.n_reads
-        windows = table.info()[1]
+        _, windows, capacity = table.info()
         reads = rl.n_reads + rr.n_reads
         packed = rl.n_bases + rl.n_reads + rr.n_bases + rr.n_reads
         table.free()
         rl.free()
         rr.free()
-        return windows, reads, h2d, d2h, packed
+        return windows, reads, h2d, d2h, packed, capacity
 
 
 def timed(pipe, stream, steps, e2e, dist):
@@ -247,7 +247,7 @@ def run_gpu(args, dist, world, rank, local):
     ms, res = timed(pipe, stream, args.steps, False, dist)
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
-    prof = {k: ctx.profile(k) for k in ("parse", "hll", "count", "compact", "sort", "dump", "coverage")}
+    prof = {k: ctx.profile(k) for k in ("parse", "hll", "scatter", "count", "compact", "sort", "dump", "coverage")}
     ctx.set_profiling(False)
     # end-to-end timed region (host FASTQ in, dump text + stats out)
     ms_e2e, res_e2e = timed(pipe, stream, args.steps, True, dist)
@@ -258,16 +258,46 @@ def run_gpu(args, dist, world, rank, local):
     tot_reads = dist.sum(reads)
     out = None
     if rank == 0:
-        # K2 algorithmic bytes: one 32-byte sector per k-mer occurrence plus one
-        # byte per packed base it streams; one count pass covers both mate files
-        count_ms, count_launches, count_units = prof["count"]
-        per_launch_units = count_units / max(count_launches, 1)
-        per_launch_ms = count_ms / max(count_launches, 1)
-        packed_per_launch = res[0][4] * args.steps / max(count_launches, 1)
-        alg_bytes = 32.0 * per_launch_units + packed_per_launch
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         peak = peaks.get("hbm_gbs", 6800.0)
-        achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+        packed = res[0][4]
+        capacity = res[0][5]
+        # random-access ceilings of this GPU, measured here: CAS + red.add pairs
+        # into one L2-resident 32 MB slice (the insert), and random 8-byte loads
+        # into a table the size of this run's (the coverage lookups)
+        ceil_insert = ctx.random_access_rate(32 << 20, atomics=True)
+        ceil_lookup = ctx.random_access_rate(capacity * 16, atomics=False)
+        per_step = {k: (v[0] / args.steps, v[1] / args.steps) for k, v in prof.items()}
+
+        def kernel_roofline(name, kid, alg_bytes_per_step, accesses_per_step, ceiling, what):
+            ms_step, launches_step = per_step[kid]
+            launches_step = max(launches_step, 1)
+            ms_launch = ms_step / launches_step
+            alg_launch = alg_bytes_per_step / launches_step
+            achieved = alg_launch / (ms_launch / 1e3) / 1e9 if ms_launch > 0 else 0.0
+            r = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                 "frac": achieved / peak, "traffic": None,
+                 "peak_source": "hbm_gbs of MEASURED_PEAKS.json (of measured)" if peaks else "fallback 6.8 TB/s",
+                 "alg_bytes_per_launch": alg_launch, "ms_per_launch": ms_launch, "launches_per_step": launches_step,
+                 "ms_per_step": ms_step}
+            if accesses_per_step:
+                rate = accesses_per_step / (ms_step / 1e3)
+                r["random_access"] = {"what": what, "achieved_per_s": rate, "ceiling_per_s": ceiling,
+                                      "frac": rate / ceiling if ceiling else None}
+            return r
+        # algorithmic bytes per k-mer occurrence (w) and per packed base (b):
+        # scatter b + 8w (bases in, keys out); insert 8w + 32w (keys in, one
+        # 32-byte slot sector per occurrence); coverage b + 32w + 12 per read
+        kernels = {
+            "coverage": kernel_roofline("k_coverage (per-read k-mer coverage stats)", "coverage",
+                                        packed + 32.0 * windows + 12.0 * reads, windows, ceil_lookup,
+                                        "random 16-byte slot lookups vs random 8-byte loads into a table of this size"),
+            "insert": kernel_roofline("k_part_step (partitioned count insert)", "count", 40.0 * windows, windows,
+                                      ceil_insert, "CAS+red.add inserts vs CAS+red.add pairs into a 32 MB slice"),
+            "scatter": kernel_roofline("k_part_scatter (k-mers into hash buckets)", "scatter",
+                                       packed + 8.0 * windows, 0, None, None),
+        }
+        top = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
         out = {
             "metric": METRIC, "value": tot_windows / t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -283,12 +313,9 @@ def run_gpu(args, dist, world, rank, local):
             "e2e": {"value": tot_windows / t_e2e, "unit": UNIT, "reads_per_s": tot_reads / t_e2e,
                     "ms_per_step": t_e2e * 1e3, "h2d_bytes_per_step": res_e2e[0][2],
                     "d2h_bytes_per_step": res_e2e[0][3]},
-            "roofline": {"bound": "hbm", "kernel": "k_count (canonical k-mer count insert)",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
-                         "alg_bytes_per_launch": alg_bytes, "kmers_per_launch": per_launch_units,
-                         "ms_per_launch": per_launch_ms, "traffic": None},
-            "kernels_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
+            "roofline": kernels[top],
+            "roofline_kernels": kernels,
+            "kernels_ms_per_step": {k: v[0] for k, v in per_step.items()},
             "gpu_launches": launches,
             "clocks": clk,
         }

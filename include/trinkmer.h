@@ -59,7 +59,8 @@ extern "C" {
 #define TK_KID_R2T_BUILD 8    /* bundle k-mer -> record table */
 #define TK_KID_R2T_ASSIGN 9   /* read -> component vote */
 #define TK_KID_BINS 10        /* batched per-bin counting */
-#define TK_KID_NUM 11        /* number of kernel classes */
+#define TK_KID_SCATTER 11     /* k-mers into hash-partition buckets (count pass 1) */
+#define TK_KID_NUM 12         /* number of kernel classes */
 
 typedef struct tk_ctx tk_ctx;
 typedef struct tk_reads tk_reads;
@@ -87,6 +88,11 @@ int tk_ctx_reset_profile(tk_ctx *ctx);
 uint64_t tk_ctx_kernel_launches(const tk_ctx *ctx);
 /* Bytes of device memory currently free / total on the context's GPU. */
 int tk_ctx_mem_info(tk_ctx *ctx, uint64_t *free_bytes, uint64_t *total_bytes);
+/* Measured random-access ceiling of this GPU: independent random 8-byte
+ * accesses per second into a table of about table_bytes (loads, or with
+ * atomics != 0 the CAS probe + red.add pair of a count insert).  The
+ * roofline denominator for the hash-table kernels. */
+int tk_ctx_random_access_rate(tk_ctx *ctx, uint64_t table_bytes, int atomics, double *accesses_per_s);
 /* Probe limit of the hash tables before a key is sent to the overflow list
  * and the table grows (jellyfish count -p/--reprobes; default 4096). */
 int tk_ctx_set_reprobes(tk_ctx *ctx, int max_probes);

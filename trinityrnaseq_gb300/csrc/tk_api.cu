@@ -112,6 +112,32 @@ static int stage_in(tk_ctx *c, const void *src, uint64_t bytes, int where, void 
     return TK_OK;
 }
 
+// Random-access ceiling probe: independent random 8-byte accesses to the key
+// words of a table of 16-byte slots (loads, or CAS + red.add as the count
+// insert does), four in flight per thread.  Every index is masked into the
+// table, so the probe stays in bounds for any size.
+__global__ void k_random_probe(unsigned long long *tab, uint64_t mask, uint64_t n_access, int atomics,
+                               unsigned long long *sink) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t acc = 0;
+    for (uint64_t i = tid * 4; i < n_access; i += nth * 4) {
+        unsigned long long v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            unsigned long long *p = tab + 2 * (mix64(i + j) & mask);
+            if (atomics) {
+                v[j] = atomicCAS(p, 0xFFFFFFFFFFFFFFFEULL, 0ULL);
+                atomicAdd(reinterpret_cast<unsigned int *>(p + 1), 1u);
+            } else {
+                v[j] = __ldcg(p);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc += v[j];
+    }
+    if (acc == 0x123456789ULL) sink[0] = acc;
+}
+
 // drops the cached dump text once the table's contents change
 static void dump_invalidate(tk_table *t) {
     if (t->d_dump) dfree(t->ctx, t->d_dump);
@@ -246,6 +272,40 @@ int tk_ctx_set_reprobes(tk_ctx *c, int max_probes) {
     if (max_probes < 1) return TK_E_INVAL;
     c->max_probes = max_probes;
     return TK_OK;
+}
+
+int tk_ctx_random_access_rate(tk_ctx *c, uint64_t table_bytes, int atomics, double *accesses_per_s) {
+    CHECK_CTX(c);
+    if (!accesses_per_s || table_bytes < 4096) return TK_E_INVAL;
+    uint64_t slots = 1;
+    while (slots * 2 * 16 <= table_bytes) slots <<= 1;
+    unsigned long long *tab = nullptr, *sink = nullptr;
+    TK_TRY(dmalloc(c, (void **)&tab, slots * 16, "probe table"));
+    int e = dmalloc(c, (void **)&sink, 8, "probe sink");
+    const uint64_t n = 1ULL << 27;
+    const unsigned grid = (unsigned)c->sm_count * 8;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (!e) {
+        cudaMemsetAsync(tab, 0, slots * 16, c->stream);
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        k_random_probe<<<grid, 256, 0, c->stream>>>(tab, slots - 1, n, atomics, sink);   // warm-up
+        cudaEventRecord(a, c->stream);
+        for (int r = 0; r < 3; r++) k_random_probe<<<grid, 256, 0, c->stream>>>(tab, slots - 1, n, atomics, sink);
+        cudaEventRecord(b, c->stream);
+        c->launches += 4;
+        e = cuda_check(c, cudaEventSynchronize(b), "probe sync");
+    }
+    if (!e) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        *accesses_per_s = 3.0 * (double)n / (ms / 1e3);
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    dfree(c, tab);
+    if (sink) dfree(c, sink);
+    return e;
 }
 
 int tk_ctx_mem_info(tk_ctx *c, uint64_t *free_bytes, uint64_t *total_bytes) {

@@ -27,6 +27,12 @@ constexpr int HLL_P = 12;
 constexpr int HLL_M = 1 << HLL_P;
 constexpr int NBUCKETS = 1 << BUCKET_BITS;
 constexpr int INS_PER_THREAD = 2;
+// bucket passes: one 512-thread block per SM; each block stages up to
+// SC_BUF keys per bucket in shared memory between flushes
+constexpr int SC_THREADS = 512;
+constexpr int SC_BUF = 24;                                       // a multiple of 4 (whole 32-byte sectors)
+constexpr int SC_BUCKETS_PER_WARP = NBUCKETS / (SC_THREADS / 32);
+constexpr size_t SC_SMEM = (size_t)NBUCKETS * SC_BUF * 8 + (size_t)NBUCKETS * 8 + (size_t)NBUCKETS * 4;
 constexpr uint64_t INS_CHUNK = (uint64_t)CT_THREADS * INS_PER_THREAD;
 enum NextMode { NEXT_NONE = 0, NEXT_FILL = 1, NEXT_PREFETCH = 2 };
 
@@ -78,19 +84,22 @@ __device__ __forceinline__ void thread_windows(const uint8_t *__restrict__ seq, 
 // Pass 1a: k-mers per (hash bucket, column) and the HLL sketch of the batch.
 // hist is bucket-major with `cols` columns per bucket; read set s uses the
 // columns [col0, col0 + gridDim.x), one per block: hist[bucket * cols + col0 + block].
+// Each count is rounded up to a multiple of 4 keys, so every (bucket, column)
+// region of the key buffer starts on a 32-byte sector; pass 1b pads the
+// rounding with EMPTY_KEY, which the insert skips.
 template <bool CANON>
-__global__ void __launch_bounds__(CT_THREADS) k_part_hist(const uint8_t *__restrict__ seq, uint64_t n, int k,
+__global__ void __launch_bounds__(SC_THREADS) k_part_hist(const uint8_t *__restrict__ seq, uint64_t n, int k,
                                                          uint32_t *__restrict__ hist, uint64_t cols, uint64_t col0,
                                                          uint32_t *__restrict__ regs,
                                                          unsigned long long *__restrict__ windows_out) {
     __shared__ uint32_t sh[NBUCKETS];
     __shared__ uint32_t sreg[HLL_M];
-    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) sh[i] = 0;
-    for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS) sreg[i] = 0;
+    for (int i = threadIdx.x; i < NBUCKETS; i += SC_THREADS) sh[i] = 0;
+    for (int i = threadIdx.x; i < HLL_M; i += SC_THREADS) sreg[i] = 0;
     __syncthreads();
     uint32_t windows = 0;
-    const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
-    for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
+    const uint64_t stride = (uint64_t)gridDim.x * SC_THREADS * CT_SPAN;
+    for (uint64_t base = (uint64_t)blockIdx.x * SC_THREADS * CT_SPAN; base < n; base += stride) {
         const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
         thread_windows<CANON>(seq, p0, p0 < n, k, [&](uint64_t key) {
             uint64_t h = mix64(key);
@@ -102,33 +111,75 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_hist(const uint8_t *__restr
         });
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) hist[(uint64_t)i * cols + col0 + blockIdx.x] = sh[i];
-    for (int i = threadIdx.x; i < HLL_M; i += CT_THREADS)
+    for (int i = threadIdx.x; i < NBUCKETS; i += SC_THREADS) hist[(uint64_t)i * cols + col0 + blockIdx.x] = (sh[i] + 3u) & ~3u;
+    for (int i = threadIdx.x; i < HLL_M; i += SC_THREADS)
         if (sreg[i]) atomicMax(&regs[i], sreg[i]);
     windows = warp_sum(windows);
     if (lane_id() == 0 && windows) atomicAdd(windows_out, (unsigned long long)windows);
 }
 
-// Pass 1b: the same windows, written bucket-major into the key buffer at the
-// offsets of the scanned histogram (same grid, same tiles as pass 1a).
+// Pass 1b: the same windows (same grid, same tiles as pass 1a), written
+// bucket-major into the key buffer.  A random 8-byte store leaves its 32-byte
+// sector partly written, and L2 then reads the sector from DRAM before it can
+// write it back; so the keys of a tile are staged per bucket in shared memory
+// and leave the block as whole, aligned sectors.  Per bucket the block keeps
+// gpos (where its next staged key goes; a multiple of 4 keys) and cnt (keys
+// staged, including up to 3 carried over from the previous tile).  A key
+// ranked past SC_BUF in one tile (a bucket flooded by a repeat) is stored
+// directly at its final position.  After each tile the warp that owns a
+// bucket writes its whole sectors and moves the 0-3 key remainder to the
+// front; at the end the remainders go out padded with EMPTY_KEY.
 template <bool CANON>
-__global__ void __launch_bounds__(CT_THREADS) k_part_scatter(const uint8_t *__restrict__ seq, uint64_t n, int k,
-                                                            const uint64_t *__restrict__ offs, uint64_t cols,
-                                                            uint64_t col0, uint64_t *__restrict__ keys) {
-    __shared__ unsigned long long sbase[NBUCKETS];   // region start of (bucket, this block)
-    __shared__ uint32_t scur[NBUCKETS];              // keys written to it so far
-    for (int i = threadIdx.x; i < NBUCKETS; i += CT_THREADS) {
-        sbase[i] = offs[(uint64_t)i * cols + col0 + blockIdx.x];
-        scur[i] = 0;
+__global__ void __launch_bounds__(SC_THREADS, 1) k_part_scatter(const uint8_t *__restrict__ seq, uint64_t n, int k,
+                                                               const uint64_t *__restrict__ offs, uint64_t cols,
+                                                               uint64_t col0, uint64_t *__restrict__ keys) {
+    extern __shared__ __align__(16) unsigned char sc_smem[];
+    uint64_t *buf = reinterpret_cast<uint64_t *>(sc_smem);                       // [NBUCKETS][SC_BUF]
+    unsigned long long *gpos = reinterpret_cast<unsigned long long *>(buf + (size_t)NBUCKETS * SC_BUF);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(gpos + NBUCKETS);
+    for (int i = threadIdx.x; i < NBUCKETS; i += SC_THREADS) {
+        gpos[i] = offs[(uint64_t)i * cols + col0 + blockIdx.x];
+        cnt[i] = 0;
     }
     __syncthreads();
-    const uint64_t stride = (uint64_t)gridDim.x * CT_THREADS * CT_SPAN;
-    for (uint64_t base = (uint64_t)blockIdx.x * CT_THREADS * CT_SPAN; base < n; base += stride) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * SC_THREADS * CT_SPAN;
+    for (uint64_t base = (uint64_t)blockIdx.x * SC_THREADS * CT_SPAN; base < n; base += stride) {
         const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
         thread_windows<CANON>(seq, p0, p0 < n, k, [&](uint64_t key) {
             const uint32_t b = (uint32_t)(mix64(key) >> (64 - BUCKET_BITS));
-            keys[sbase[b] + atomicAdd(&scur[b], 1u)] = key;
+            const uint32_t r = atomicAdd(&cnt[b], 1u);
+            if (r < SC_BUF) buf[b * SC_BUF + r] = key;
+            else keys[gpos[b] + r] = key;
         });
+        __syncthreads();
+        for (int i = 0; i < SC_BUCKETS_PER_WARP; i++) {
+            const int b = warp * SC_BUCKETS_PER_WARP + i;
+            const uint32_t nk = cnt[b];
+            const uint32_t full = nk & ~3u;
+            const uint64_t g = gpos[b];
+            const uint64_t *bb = buf + (size_t)b * SC_BUF;
+            if (lane < min(full, (uint32_t)SC_BUF)) keys[g + lane] = bb[lane];
+            const uint32_t tail = nk - full;
+            uint64_t v = 0;
+            if (lane < tail) {
+                const uint32_t idx = full + lane;
+                v = idx < SC_BUF ? bb[idx] : __ldcg(keys + g + idx);
+            }
+            __syncwarp();
+            if (lane < tail) buf[(size_t)b * SC_BUF + lane] = v;
+            if (lane == 0) {
+                cnt[b] = tail;
+                gpos[b] = g + full;
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+    for (int i = 0; i < SC_BUCKETS_PER_WARP; i++) {
+        const int b = warp * SC_BUCKETS_PER_WARP + i;
+        const uint32_t nk = cnt[b];
+        if (nk && lane < 4) keys[gpos[b] + lane] = lane < nk ? buf[(size_t)b * SC_BUF + lane] : EMPTY_KEY;
     }
 }
 
@@ -550,12 +601,12 @@ int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *le
     if (total_len == 0) return TK_OK;
     // the two passes over each read array use one fixed grid, so every tile
     // goes to the same block (histogram column) in both
+    const uint64_t tile = (uint64_t)SC_THREADS * CT_SPAN;
     std::vector<unsigned> grids(nsets);
     std::vector<uint64_t> col0(nsets);
     uint64_t cols = 0;
     for (int s = 0; s < nsets; s++) {
-        grids[s] = (unsigned)std::max<uint64_t>(
-            1, std::min<uint64_t>((lens[s] + CT_THREADS * CT_SPAN - 1) / (CT_THREADS * CT_SPAN), (uint64_t)c->sm_count * 6));
+        grids[s] = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((lens[s] + tile - 1) / tile, (uint64_t)c->sm_count));
         col0[s] = cols;
         cols += grids[s];
     }
@@ -572,21 +623,24 @@ int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *le
         prof_begin(c, TK_KID_HLL, &ev);
         for (int s = 0; s < nsets; s++) {
             if (t->canonical)
-                k_part_hist<true><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
+                k_part_hist<true><<<grids[s], SC_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
                                                                           t->d_hll, t->d_counters + 1);
             else
-                k_part_hist<false><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
+                k_part_hist<false><<<grids[s], SC_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
                                                                            t->d_hll, t->d_counters + 1);
             c->launches++;
         }
         prof_end(c, TK_KID_HLL, ev, total_len);
         e = check_launch(c, "bucket histogram");
     }
-    if (!e) e = scan_excl_u32_to_u64(c, hist, offs, cells, &windows);   // synchronises
+    uint64_t padded = 0;   // key-buffer entries: the windows plus the EMPTY_KEY padding of every region
+    if (!e) e = scan_excl_u32_to_u64(c, hist, offs, cells, &padded);   // synchronises
     if (!e) {
-        cudaMemcpyAsync(offs + cells, &windows, 8, cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(offs + cells, &padded, 8, cudaMemcpyHostToDevice, c->stream);
         std::vector<uint32_t> regs(HLL_M);
         e = cuda_check(c, cudaMemcpyAsync(regs.data(), t->d_hll, HLL_M * 4, cudaMemcpyDeviceToHost, c->stream), "hll d2h");
+        if (!e) e = cuda_check(c, cudaMemcpyAsync(&windows, t->d_counters + 1, 8, cudaMemcpyDeviceToHost, c->stream),
+                               "window count d2h");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "hll sync");
         if (!e) {
             double est = hll_estimate(regs.data());
@@ -595,18 +649,26 @@ int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *le
             else if (want > t->capacity) e = table_rehash(t, want);
         }
     }
-    if (!e && windows) e = dmalloc(c, (void **)&keys, windows * 8, "bucketed k-mers");
+    if (!e && windows) e = dmalloc(c, (void **)&keys, padded * 8, "bucketed k-mers");
     if (!e && windows) {
-        prof_begin(c, TK_KID_COUNT, &ev);
         // pass 1b: k-mers into their buckets
-        for (int s = 0; s < nsets; s++) {
+        static_assert(SC_SMEM <= 227 * 1024, "bucket staging exceeds shared memory");
+        e = cuda_check(c, cudaFuncSetAttribute(k_part_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SC_SMEM),
+                       "scatter smem");
+        if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_part_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)SC_SMEM), "scatter smem");
+        prof_begin(c, TK_KID_SCATTER, &ev);
+        for (int s = 0; !e && s < nsets; s++) {
             if (t->canonical)
-                k_part_scatter<true><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
+                k_part_scatter<true><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
             else
-                k_part_scatter<false><<<grids[s], CT_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
+                k_part_scatter<false><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
             c->launches++;
         }
-        e = overflow_reset(t);
+        prof_end(c, TK_KID_SCATTER, ev, windows);
+        if (!e) e = check_launch(c, "bucket scatter");
+        if (!e) e = overflow_reset(t);
+        prof_begin(c, TK_KID_COUNT, &ev);
         // pass 2: one launch per partition, slice p+1 prepared while p is filled
         const int nparts = 1 << t->t.pbits;
         const int mode = t->fresh ? NEXT_FILL : (t->t.pbits > 0 ? NEXT_PREFETCH : NEXT_NONE);

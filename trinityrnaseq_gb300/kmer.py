@@ -90,6 +90,13 @@ class Context:
     def set_reprobes(self, n: int) -> None:
         self.check(self.lib.tk_ctx_set_reprobes(self.h, int(n)), "tk_ctx_set_reprobes")
 
+    def random_access_rate(self, table_bytes: int, atomics: bool = False) -> float:
+        """Measured random 8-byte accesses/s into a table of about table_bytes."""
+        r = C.c_double()
+        self.check(self.lib.tk_ctx_random_access_rate(self.h, table_bytes, int(atomics), C.byref(r)),
+                   "tk_ctx_random_access_rate")
+        return r.value
+
     def mem_info(self) -> Tuple[int, int]:
         f, t = C.c_uint64(), C.c_uint64()
         self.check(self.lib.tk_ctx_mem_info(self.h, C.byref(f), C.byref(t)), "tk_ctx_mem_info")

@@ -29,7 +29,7 @@ TK_FMT_NONE, TK_FMT_FASTA, TK_FMT_FASTQ = 0, 1, 2
 
 KID = {
     "parse": 0, "hll": 1, "count": 2, "compact": 3, "sort": 4, "dump": 5, "load": 6,
-    "coverage": 7, "r2t_build": 8, "r2t_assign": 9, "bins": 10,
+    "coverage": 7, "r2t_build": 8, "r2t_assign": 9, "bins": 10, "scatter": 11,
 }
 
 u64, u32, i32, vp = C.c_uint64, C.c_uint32, C.c_int32, C.c_void_p
@@ -50,6 +50,7 @@ SIGNATURES = {
     "tk_ctx_kernel_launches": (u64, [vp]),
     "tk_ctx_mem_info": (C.c_int, [vp, P(u64), P(u64)]),
     "tk_ctx_set_reprobes": (C.c_int, [vp, C.c_int]),
+    "tk_ctx_random_access_rate": (C.c_int, [vp, u64, C.c_int, P(C.c_double)]),
     "tk_reads_parse": (C.c_int, [vp, vp, u64, C.c_int, P(vp)]),
     "tk_reads_info": (C.c_int, [vp, P(u64), P(u64), P(u32), P(C.c_int)]),
     "tk_reads_names": (C.c_int, [vp, vp, vp]),
