@@ -75,6 +75,33 @@ def test_stats_long_and_odd_reads(ctx, oracle, golden):
     assert_stats(got, oracle.cov_values(text, keys, counts, 25, True))
 
 
+def window_class_reads(seed, k, n_per_len=3):
+    """Reads whose window counts straddle every per-lane register class of the
+    warp path (1, 2, 4, 8 values per lane) and the long-read path, a third of
+    them with an N."""
+    rnd = np.random.default_rng(seed)
+    nwins = [0, 1, 2, 31, 32, 33, 63, 64, 65, 76, 127, 128, 129, 200, 255, 256, 257, 300]
+    out = []
+    for nw in nwins:
+        for i in range(n_per_len):
+            L = max(1, nw + k - 1) if nw else max(1, k - 1 - i)
+            s = rnd.choice(np.frombuffer(b"ACGT", dtype=np.uint8), L)
+            if i == 2:
+                s[rnd.integers(0, L)] = ord("N")
+            out.append(b">w%d_%d\n" % (nw, i) + s.tobytes() + b"\n")
+    return b"".join(out)
+
+
+@pytest.mark.parametrize("k", [1, 7, 17, 25, 31])
+@pytest.mark.parametrize("ds", [True, False])
+def test_stats_every_window_class_and_k(ctx, oracle, k, ds):
+    text = window_class_reads(k, k)
+    catalogue = text + window_class_reads(100 + k, k)
+    keys, counts = oracle.count(catalogue, k, ds)
+    rs, got = stats_gpu(ctx, catalogue, text, k, ds)
+    assert_stats(got, oracle.cov_values(text, keys, counts, k, ds))
+
+
 def test_stats_parity_1M_reads(ctx, oracle):
     text = synth.transcriptome_reads(seed=1, n_reads=1_000_000).tobytes()
     keys, counts = oracle.count(text, 25, True)

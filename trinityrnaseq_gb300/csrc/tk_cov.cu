@@ -22,15 +22,21 @@ namespace tk {
 constexpr int CV_THREADS = 256;
 constexpr uint32_t CV_WARP_MAX = 256;   // windows handled by the warp path
 
+// Integer statistics of one read, uniform over the warp.
+struct ReadSums {
+    uint32_t cnt, med;
+    uint64_t sum, hi, lo;
+};
+constexpr uint32_t LONG_READ = 0xFFFFFFFFu;   // cnt of a read left to the long-read pass
+
 template <int S, bool CANON>
-__device__ __forceinline__ void cov_warp_read(DevTable t, const uint8_t *__restrict__ seq, uint64_t start, uint32_t nwin,
-                                              int k, uint64_t r, uint32_t *__restrict__ median, float *__restrict__ mean,
-                                              float *__restrict__ stdev) {
+__device__ __forceinline__ ReadSums cov_warp_read(DevTable t, const uint8_t *__restrict__ seq, uint64_t start,
+                                                  uint32_t nwin, int k, uint64_t *words) {
     const uint32_t span = (nwin + 31) / 32;
     uint32_t v[S];
     uint32_t cnt = 0;
     uint64_t sum = 0, hi = 0, lo = 0;
-    lane_windows<S, CANON>(seq, start, nwin, span, k, [&](int j, bool valid, uint64_t key) {
+    auto body = [&](int j, bool valid, uint64_t key) {
         uint32_t c = PAD_VAL;
         if (valid) {
             c = tbl_get(t, key, 1u);
@@ -42,38 +48,81 @@ __device__ __forceinline__ void cov_warp_read(DevTable t, const uint8_t *__restr
             lo = nlo;
         }
         v[j] = c;
-    });
-    cnt = warp_sum(cnt);
-    sum = warp_sum(sum);
+    };
+    if (!lane_windows_packed<S, CANON>(seq, start, nwin, span, k, words, body))
+        lane_windows<S, CANON>(seq, start, nwin, span, k, body);
+    ReadSums rs;
+    rs.cnt = warp_sum(cnt);
+    rs.sum = warp_sum(sum);
     warp_sum_u128(hi, lo);
+    rs.hi = hi;
+    rs.lo = lo;
     warp_bitonic_sort<S>(v);
-    uint32_t med = cnt ? warp_elem<S>(v, cnt / 2) : 0u;
-    if (lane_id() == 0) {
-        float m, s;
-        finish_stats(cnt, sum, hi, lo, &m, &s);
-        median[r] = med;
-        mean[r] = m;
-        stdev[r] = s;
+    rs.med = rs.cnt ? warp_elem<S>(v, rs.cnt / 2) : 0u;
+    return rs;
+}
+
+// One warp, 32 consecutive reads [r0, r0 + 32): the warp computes each read's
+// sums in turn and lane i keeps read r0 + i's; then every lane finishes its own
+// read.  The floating-point finish runs on the FP64 pipe, whose cost is per
+// warp instruction whatever the number of active lanes, so finishing 32 reads
+// in one pass costs what one read alone would.  Reads with more than
+// CV_WARP_MAX windows are appended to long_list (or, with no list, left to a
+// separate pass) and not written here.
+template <bool CANON>
+__device__ __forceinline__ void cov_warp_chunk(DevTable t, const uint8_t *__restrict__ seq,
+                                               const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k, uint64_t r0,
+                                               uint32_t *__restrict__ median, float *__restrict__ mean,
+                                               float *__restrict__ stdev, uint32_t *__restrict__ long_list,
+                                               unsigned long long *__restrict__ long_n, ReadSums *__restrict__ held,
+                                               uint64_t *words) {
+    const unsigned lane = lane_id();
+    const uint32_t nr = n_reads - r0 < 32 ? (uint32_t)(n_reads - r0) : 32u;
+    for (uint32_t i = 0; i < nr; i++) {
+        const uint64_t r = r0 + i;
+        const uint64_t start = rd_off[r];
+        const uint64_t L = rd_off[r + 1] - start - 1;
+        const uint32_t nwin = L >= (uint64_t)k ? (uint32_t)(L - k + 1) : 0u;
+        ReadSums rs;
+        bool is_long = false;
+        if (nwin <= 32) rs = cov_warp_read<1, CANON>(t, seq, start, nwin, k, words);
+        else if (nwin <= 64) rs = cov_warp_read<2, CANON>(t, seq, start, nwin, k, words);
+        else if (nwin <= 128) rs = cov_warp_read<4, CANON>(t, seq, start, nwin, k, words);
+        else if (nwin <= CV_WARP_MAX) rs = cov_warp_read<8, CANON>(t, seq, start, nwin, k, words);
+        else {
+            is_long = true;
+            if (long_list && lane == 0) long_list[atomicAdd(long_n, 1ULL)] = (uint32_t)r;
+        }
+        if (lane == 0) {
+            if (is_long) rs.cnt = LONG_READ;
+            held[i] = rs;
+        }
+    }
+    __syncwarp();
+    const ReadSums mine = held[lane < nr ? lane : 0];
+    __syncwarp();
+    if (lane < nr && mine.cnt != LONG_READ) {
+        float m, sd;
+        finish_stats(mine.cnt, mine.sum, mine.hi, mine.lo, &m, &sd);
+        median[r0 + lane] = mine.med;
+        mean[r0 + lane] = m;
+        stdev[r0 + lane] = sd;
     }
 }
 
 template <bool CANON>
-__global__ void __launch_bounds__(CV_THREADS) k_coverage(DevTable t, const uint8_t *__restrict__ seq,
+__global__ void __launch_bounds__(CV_THREADS, 4) k_coverage(DevTable t, const uint8_t *__restrict__ seq,
                                                         const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
                                                         uint32_t *__restrict__ median, float *__restrict__ mean,
                                                         float *__restrict__ stdev, uint32_t *__restrict__ long_list,
                                                         unsigned long long *__restrict__ long_n) {
+    __shared__ ReadSums held[CV_THREADS];
+    __shared__ uint64_t words[CV_THREADS / 32][12];
     const uint64_t warps = (uint64_t)gridDim.x * (CV_THREADS / 32);
-    for (uint64_t r = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); r < n_reads; r += warps) {
-        const uint64_t start = rd_off[r];
-        const uint64_t L = rd_off[r + 1] - start - 1;
-        const uint32_t nwin = L >= (uint64_t)k ? (uint32_t)(L - k + 1) : 0u;
-        if (nwin <= 32) cov_warp_read<1, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-        else if (nwin <= 64) cov_warp_read<2, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-        else if (nwin <= 128) cov_warp_read<4, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-        else if (nwin <= CV_WARP_MAX) cov_warp_read<8, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-        else if (lane_id() == 0) long_list[atomicAdd(long_n, 1ULL)] = (uint32_t)r;
-    }
+    const uint64_t chunks = (n_reads + 31) / 32;
+    for (uint64_t ch = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); ch < chunks; ch += warps)
+        cov_warp_chunk<CANON>(t, seq, rd_off, n_reads, k, ch * 32, median, mean, stdev, long_list, long_n,
+                              held + (threadIdx.x & ~31u), words[threadIdx.x >> 5]);
 }
 
 // long reads: one block per read, `slab` = this block's scratch (n2max values)
@@ -158,8 +207,9 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
         }
     }
     if (!e) {
+        const uint64_t chunks = (n + 31) / 32;
         const unsigned grid = (unsigned)std::max<uint64_t>(
-            1, std::min<uint64_t>((n + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
+            1, std::min<uint64_t>((chunks + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COVERAGE, &ev);
         if (t->canonical)
@@ -225,20 +275,17 @@ static __device__ __align__(16) Slot g_noalloc_empty[2] = {{EMPTY_KEY, 0u, 0u}, 
 
 // short reads only (<= 256 windows); longer reads are left to k_coverage_long_slab
 template <bool CANON>
-__global__ void __launch_bounds__(CV_THREADS) k_coverage_short(DevTable t, const uint8_t *__restrict__ seq,
+__global__ void __launch_bounds__(CV_THREADS, 4) k_coverage_short(DevTable t, const uint8_t *__restrict__ seq,
                                                               const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
                                                               uint32_t *__restrict__ median, float *__restrict__ mean,
                                                               float *__restrict__ stdev) {
+    __shared__ ReadSums held[CV_THREADS];
+    __shared__ uint64_t words[CV_THREADS / 32][12];
     const uint64_t warps = (uint64_t)gridDim.x * (CV_THREADS / 32);
-    for (uint64_t r = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); r < n_reads; r += warps) {
-        const uint64_t start = rd_off[r];
-        const uint64_t L = rd_off[r + 1] - start - 1;
-        const uint32_t nwin = L >= (uint64_t)k ? (uint32_t)(L - k + 1) : 0u;
-        if (nwin <= 32) cov_warp_read<1, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-        else if (nwin <= 64) cov_warp_read<2, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-        else if (nwin <= 128) cov_warp_read<4, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-        else if (nwin <= CV_WARP_MAX) cov_warp_read<8, CANON>(t, seq, start, nwin, k, r, median, mean, stdev);
-    }
+    const uint64_t chunks = (n_reads + 31) / 32;
+    for (uint64_t ch = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); ch < chunks; ch += warps)
+        cov_warp_chunk<CANON>(t, seq, rd_off, n_reads, k, ch * 32, median, mean, stdev, nullptr, nullptr,
+                              held + (threadIdx.x & ~31u), words[threadIdx.x >> 5]);
 }
 
 // reads with more than 256 windows, one block per read, found by a strided scan
@@ -339,8 +386,9 @@ int coverage_stats_noalloc(tk_table *t, const tk_reads *rd, uint32_t *d_median, 
     if (n == 0) return TK_OK;
     DevTable dt = t->t;
     if (t->capacity == 0) dt = tbl_empty(empty);
+    const uint64_t chunks = (n + 31) / 32;
     const unsigned grid = (unsigned)std::max<uint64_t>(
-        1, std::min<uint64_t>((n + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
+        1, std::min<uint64_t>((chunks + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
     if (t->canonical)
         k_coverage_short<true><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
                                                                    d_stdev);

@@ -58,6 +58,73 @@ __device__ __forceinline__ void lane_windows(const uint8_t *__restrict__ seq, ui
     }
 }
 
+// Reverse complement of a k-mer in 2-bit A<C<G<T code (the low 2k bits):
+// complement every base, then reverse the order of the 2-bit groups.
+__device__ __forceinline__ uint64_t kmer_revcomp(uint64_t fw, int k) {
+    uint64_t x = __brevll(~fw);   // group order reversed, the two bits of each group swapped
+    x = ((x >> 1) & 0x5555555555555555ULL) | ((x & 0x5555555555555555ULL) << 1);
+    return x >> (64 - 2 * k);
+}
+
+// Packed form of lane_windows for reads made of A/C/G/T only (the common
+// case): the warp first writes the read as a 2-bit, first-base-most-
+// significant bit string into `words` (per-warp shared memory, 12 words),
+// then lane l cuts each of its k-mers out of two words with one funnel shift,
+// with no k-1 base priming per lane.  Returns false, having called f for no
+// window, when the read holds any other character or has no window; the
+// caller then uses lane_windows.
+template <int S, bool CANON, typename F>
+__device__ __forceinline__ bool lane_windows_packed(const uint8_t *__restrict__ seq, uint64_t start, uint32_t nwin,
+                                                    uint32_t span, int k, uint64_t *words, F &&f) {
+    constexpr int ROUNDS = (32 * S + 30 + 127) / 128;   // 128 bases per round cover nwin + k - 1 <= 32*S + 30
+    static_assert(ROUNDS * 4 <= 12 && S + 1 <= ROUNDS * 4, "packed word buffer");
+    if (nwin == 0) return false;
+    const unsigned lane = lane_id();
+    const uint32_t L = nwin + (uint32_t)k - 1;
+    uint8_t *bytes = reinterpret_cast<uint8_t *>(words);
+    bool bad = false;
+    __syncwarp();
+#pragma unroll
+    for (int rd = 0; rd < ROUNDS; rd++) {
+        const uint32_t g = (uint32_t)rd * 32 + lane;   // bases 4g .. 4g+3
+        uint32_t byte = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t p = 4 * g + i;
+            if (p < L) {
+                const uint32_t c = base_code(__ldg(seq + start + p));
+                bad |= c > 3;
+                byte |= (c & 3u) << (6 - 2 * i);
+            }
+        }
+        bytes[(g & ~7u) + (7u - (g & 7u))] = (uint8_t)byte;   // group 8q+i -> byte 7-i of word q
+    }
+    if (__any_sync(0xffffffffu, bad)) return false;
+    __syncwarp();
+    const uint64_t kmask = (1ULL << (2 * k)) - 1;
+    const uint32_t w0 = lane * span;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+        const uint32_t w = w0 + j;
+        const bool in = (uint32_t)j < span && w < nwin;
+        uint64_t key = 0;
+        if (in) {
+            const uint32_t q = w >> 5, off = 2 * (w & 31);
+            uint64_t x = words[q];
+            if (off) x = (x << off) | (words[q + 1] >> (64 - off));
+            const uint64_t fw = (x >> (64 - 2 * k)) & kmask;
+            if (CANON) {
+                const uint64_t rc = kmer_revcomp(fw, k);
+                key = rc < fw ? rc : fw;
+            } else {
+                key = fw;
+            }
+        }
+        f(j, in, key);
+    }
+    return true;
+}
+
 template <int S>
 __device__ __forceinline__ void warp_bitonic_sort(uint32_t (&v)[S]) {
     const unsigned lane = lane_id();
