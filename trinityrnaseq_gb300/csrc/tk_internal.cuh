@@ -88,7 +88,7 @@ __host__ __device__ __forceinline__ uint64_t tbl_next(const DevTable &t, uint64_
 // slot and returns the resident key otherwise.  On GB300 a CAS probe followed
 // by red.add runs ~1.3x faster than a load probe followed by red.add on an
 // L2-resident table, and 2-8x faster when the table is not L2-resident (the
-// load + red pair to one line thrashes).  See the design doc section 4.
+// load + red pair to one line thrashes).
 __device__ __forceinline__ unsigned long long tbl_claim(Slot *slot, uint64_t key) {
     unsigned long long cur = atomicCAS(&slot->key, EMPTY_KEY, (unsigned long long)key);
     return cur == EMPTY_KEY ? (unsigned long long)key : cur;
