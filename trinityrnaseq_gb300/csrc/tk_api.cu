@@ -384,6 +384,7 @@ void tk_reads_free(tk_reads *r) {
     cudaSetDevice(c->device);
     if (r->own_text) dfree(c, r->d_text);
     dfree(c, r->d_seq_alloc);
+    if (r->d_pack_alloc) dfree(c, r->d_pack_alloc);
     dfree(c, r->d_rd_off);
     dfree(c, r->d_name_off);
     dfree(c, r->d_name_len);
@@ -442,23 +443,19 @@ int tk_table_add_reads(tk_table *t, const tk_reads *r) {
     CHECK_CTX(c);
     if (r->ctx != c) return set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
     dump_invalidate(t);
-    return table_count_seq(t, r->d_seq, r->seq_len);
+    return table_count_seq(t, r);
 }
 
 int tk_table_add_reads_multi(tk_table *t, const tk_reads *const *sets, uint32_t n_sets) {
     if (!t || (!sets && n_sets)) return TK_E_INVAL;
     tk_ctx *c = t->ctx;
     CHECK_CTX(c);
-    std::vector<const uint8_t *> seqs(n_sets);
-    std::vector<uint64_t> lens(n_sets);
     for (uint32_t i = 0; i < n_sets; i++) {
         if (!sets[i]) return set_err(c, TK_E_INVAL, "tk_table_add_reads_multi: null read set");
         if (sets[i]->ctx != c) return set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
-        seqs[i] = sets[i]->d_seq;
-        lens[i] = sets[i]->seq_len;
     }
     dump_invalidate(t);
-    return table_count_many(t, seqs.data(), lens.data(), (int)n_sets);
+    return table_count_many(t, sets, (int)n_sets);
 }
 
 int tk_table_count_text(tk_table *t, const char *text, uint64_t len, int where) {

@@ -298,6 +298,7 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
     auto cleanup = [&]() {
         for (void *p : tmp) dfree(c, p);
         if (r.d_seq_alloc) dfree(c, r.d_seq_alloc);
+        if (r.d_pack_alloc) dfree(c, r.d_pack_alloc);
         if (r.d_rd_off) dfree(c, r.d_rd_off);
         if (r.d_name_off) dfree(c, r.d_name_off);
         if (r.d_name_len) dfree(c, r.d_name_len);

@@ -5,7 +5,11 @@
 //                   by one '\n' separator, 64 bytes of '\n' padding on both
 //                   sides; `rd_off[r]` = first base of read r (n+1 entries);
 //                   `name_off/name_len` = accession (first header token) in
-//                   the device copy of the input text.
+//                   the device copy of the input text.  The same positions
+//                   as 2-bit codes: `codes[j]` holds positions 32j..32j+31
+//                   (A0 C1 G2 T3, first position in the top bits) and bit
+//                   31-i of `inv[j]` is set when position 32j+i is not
+//                   A/C/G/T; word -1 exists (all positions invalid).
 //  * k-mer table  : open addressing, linear probing, 16-byte slots
 //                   {u64 key; u32 value; u32 pad} so a probe touches one
 //                   32-byte DRAM sector; capacity a power of two; empty key
@@ -230,6 +234,9 @@ struct tk_reads {
     uint64_t *d_rd_off = nullptr;           // n_reads + 1
     uint64_t *d_name_off = nullptr;         // n_reads
     uint32_t *d_name_len = nullptr;         // n_reads
+    uint64_t *d_pack_alloc = nullptr;       // codes and inv, one allocation
+    const uint64_t *d_codes = nullptr;      // word 0 of the 2-bit codes (word -1 exists)
+    const uint32_t *d_inv = nullptr;        // word 0 of the invalid-position bits (word -1 exists)
 };
 
 struct tk_table {
@@ -280,8 +287,8 @@ int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int 
 int table_alloc(tk_table *t, uint64_t capacity);
 int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val);
 int table_rehash(tk_table *t, uint64_t new_capacity);
-int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len);
-int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *lens, int nsets);
+int table_count_seq(tk_table *t, const tk_reads *r);
+int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets);
 }  // namespace tk
 
 #define TK_TRY(x) do { int _e = (x); if (_e) return _e; } while (0)

@@ -357,7 +357,53 @@ __global__ void k_names(ParseGeom g, const uint64_t *__restrict__ hdr_line, cons
     atomicMax(max_len, (uint32_t)(L > 0xFFFFFFFFull ? 0xFFFFFFFFull : L));
 }
 
+// The packed read array as 2-bit codes and invalid-position bits: thread j
+// converts positions 32j .. 32j+31 (j = -1 .. n_words-1; the 64 '\n' bytes
+// around `seq` make word -1 all invalid).  Per 4-byte group: the code of
+// A/C/G/T is ((c >> 1) & 3) ^ (its bit 1 moved to bit 0); the group is valid
+// where its bytes equal the letters those codes name.
+__global__ void k_pack_codes(const uint8_t *__restrict__ seq, int64_t n_words, uint64_t *__restrict__ codes,
+                             uint32_t *__restrict__ inv) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - 1;
+    if (j >= n_words) return;
+    const uint4 *v = reinterpret_cast<const uint4 *>(seq + 32 * j);
+    const uint4 a = v[0], b = v[1];
+    const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    uint64_t code = 0;
+    uint32_t bad = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        uint32_t x = (w[q] >> 1) & 0x03030303u;
+        x ^= (x >> 1) & 0x01010101u;   // byte b: code of position 4q+b
+        // the letter each code names, compared with the byte itself
+        const uint32_t sel = (x & 3u) | ((x >> 4) & 0x30u) | ((x >> 8) & 0x300u) | ((x >> 12) & 0x3000u);
+        const uint32_t d = w[q] ^ __byte_perm(0x54474341u, 0u, sel);
+        const uint32_t nz = (d | ((d & 0x7F7F7F7Fu) + 0x7F7F7F7Fu)) & 0x80808080u;   // bit 7 of each differing byte
+        const uint32_t nib = (((nz >> 7) * 0x08040201u) >> 24) & 0xFu;                  // position 4q at bit 3
+        const uint32_t byte = ((x << 6) & 0xC0u) | ((x >> 4) & 0x30u) | ((x >> 14) & 0x0Cu) | ((x >> 24) & 0x03u);
+        code = (code << 8) | byte;
+        bad = (bad << 4) | nib;
+    }
+    codes[j] = code;
+    inv[j] = bad;
+}
+
 static inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// Builds r->d_codes / r->d_inv from r->d_seq (after the last write to seq).
+static int pack_reads(tk_ctx *c, tk_reads *r) {
+    const int64_t n_words = (int64_t)((r->seq_len + 31) / 32) + 1;
+    const uint64_t code_words = (uint64_t)n_words + 1;          // incl. word -1
+    const uint64_t inv_words = ((uint64_t)n_words + 1 + 1) & ~1ULL;
+    TK_TRY(dmalloc(c, (void **)&r->d_pack_alloc, code_words * 8 + inv_words * 4, "2-bit codes"));
+    uint64_t *codes = r->d_pack_alloc + 1;
+    uint32_t *inv = reinterpret_cast<uint32_t *>(r->d_pack_alloc + code_words) + 1;
+    k_pack_codes<<<grid_for((uint64_t)n_words + 1, 256), 256, 0, c->stream>>>(r->d_seq, n_words, codes, inv);
+    c->launches++;
+    r->d_codes = codes;
+    r->d_inv = inv;
+    return check_launch(c, "2-bit codes");
+}
 
 int parse_reads(tk_ctx *c, tk_reads *r) {
     const char *text = r->d_text;
@@ -490,6 +536,7 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
                                                                    r->d_name_off, r->d_name_len, d_maxlen);
             c->launches++;
         }
+        if (!e) e = pack_reads(c, r);
         if (!e) e = cuda_check(c, cudaMemcpyAsync(&r->max_len, d_maxlen, 4, cudaMemcpyDeviceToHost, c->stream), "maxlen d2h");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "parse sync");
     }

@@ -36,48 +36,54 @@ constexpr size_t SC_SMEM = (size_t)NBUCKETS * SC_BUF * 8 + (size_t)NBUCKETS * 8 
 constexpr uint64_t INS_CHUNK = (uint64_t)CT_THREADS * INS_PER_THREAD;
 enum NextMode { NEXT_NONE = 0, NEXT_FILL = 1, NEXT_PREFETCH = 2 };
 
-struct Window64 {
-    uint32_t w[16];
-    __device__ __forceinline__ uint32_t get(int i) const { return (w[i >> 2] >> ((i & 3) * 8)) & 0xFFu; }
-};
-
-// bytes [p0 - 32, p0 + 32) of the padded seq array (p0 is a multiple of 32)
-__device__ __forceinline__ Window64 load_window(const uint8_t *__restrict__ seq, uint64_t p0, bool active) {
-    Window64 b;
-    if (active) {
-        const uint4 *v = reinterpret_cast<const uint4 *>(seq + p0 - 32);
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            uint4 x = __ldg(v + i);
-            b.w[4 * i] = x.x; b.w[4 * i + 1] = x.y; b.w[4 * i + 2] = x.z; b.w[4 * i + 3] = x.w;
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < 16; i++) b.w[i] = 0x0A0A0A0Au;
-    }
-    return b;
-}
-
-// Calls f(key) for every valid window ending in [p0, p0 + 32) of the padded
-// packed-read array (the 64 bytes [p0-32, p0+32) cover the k-1 bases before).
+// Windows of the 2-bit code form of a packed read array.  A thread owns the
+// 32 window end positions [32w, 32w + 32); the 64 positions [32w - 32, 32w + 32)
+// (code words w-1 and w, invalid bits likewise) hold every base those windows
+// use (k <= 31).  Each window is cut out of the 128-bit code pair with one
+// funnel shift, its reverse complement out of the pair's reverse complement,
+// and it is valid when none of its k positions has its invalid bit set.
+// Calls f(key) for every valid window, in position order.
 template <bool CANON, typename F>
-__device__ __forceinline__ void thread_windows(const uint8_t *__restrict__ seq, uint64_t p0, bool active, int k, F &&f) {
-    const uint64_t kmask = (1ULL << (2 * k)) - 1;
-    const int shift = 2 * (k - 1);
-    Window64 b = load_window(seq, p0, active);
-    uint64_t fw = 0, rc = 0;
-    int run = 0;
+__device__ __forceinline__ void thread_windows(const uint64_t *__restrict__ codes, const uint32_t *__restrict__ inv,
+                                               uint64_t w, bool active, int k, F &&f) {
+    uint64_t hi = 0, lo = 0, m = ~0ULL;
+    if (active) {
+        hi = __ldg(codes + w - 1);
+        lo = __ldg(codes + w);
+        m = ((uint64_t)__ldg(inv + w - 1) << 32) | __ldg(inv + w);
+    }
+    // bit b of `bad`: some position among bits b .. b+k-1 of m (position
+    // 32w - 32 + x sits at bit 63 - x) is not A/C/G/T
+    uint64_t bad = 0, span = m;
+    int sh = 0;
 #pragma unroll
-    for (int j = 0; j < 64; j++) {
-        uint32_t c = base_code(b.get(j));
-        if (c > 3) {
-            run = 0;
-        } else {
-            fw = ((fw << 2) | c) & kmask;
-            rc = (rc >> 2) | ((uint64_t)(3u - c) << shift);
-            run++;
+    for (int l = 0; l < 5; l++) {
+        if (k & (1 << l)) {
+            bad |= span >> sh;
+            sh += 1 << l;
         }
-        if (j >= 32 && run >= k) f((CANON && rc < fw) ? rc : fw);
+        span |= span >> (1 << l);
+    }
+    // reverse complement of the 64 positions: complement, then reverse the
+    // order of the 2-bit groups
+    uint64_t rhi = __brevll(~lo), rlo = __brevll(~hi);
+    rhi = ((rhi >> 1) & 0x5555555555555555ULL) | ((rhi & 0x5555555555555555ULL) << 1);
+    rlo = ((rlo >> 1) & 0x5555555555555555ULL) | ((rlo & 0x5555555555555555ULL) << 1);
+    const uint64_t kmask = (1ULL << (2 * k)) - 1;
+#pragma unroll
+    for (int i = 0; i < 32; i++) {
+        if ((bad >> (31 - i)) & 1ULL) continue;
+        // forward: the window ends at position 32 + i of the 64
+        const int s = 62 - 2 * i;
+        const uint64_t fw = (s ? ((lo >> s) | (hi << (64 - s))) : lo) & kmask;
+        uint64_t key = fw;
+        if (CANON) {
+            // reverse complement: it ends where the window starts, 33 + i - k
+            const int r = 66 + 2 * i - 2 * k;   // 4 .. 126
+            const uint64_t rc = (r >= 64 ? (rhi >> (r - 64)) : ((rlo >> r) | (rhi << (64 - r)))) & kmask;
+            key = rc < fw ? rc : fw;
+        }
+        f(key);
     }
 }
 
@@ -88,7 +94,8 @@ __device__ __forceinline__ void thread_windows(const uint8_t *__restrict__ seq, 
 // region of the key buffer starts on a 32-byte sector; pass 1b pads the
 // rounding with EMPTY_KEY, which the insert skips.
 template <bool CANON>
-__global__ void __launch_bounds__(SC_THREADS) k_part_hist(const uint8_t *__restrict__ seq, uint64_t n, int k,
+__global__ void __launch_bounds__(SC_THREADS) k_part_hist(const uint64_t *__restrict__ codes,
+                                                          const uint32_t *__restrict__ inv, uint64_t n, int k,
                                                          uint32_t *__restrict__ hist, uint64_t cols, uint64_t col0,
                                                          uint32_t *__restrict__ regs,
                                                          unsigned long long *__restrict__ windows_out) {
@@ -101,7 +108,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_part_hist(const uint8_t *__restr
     const uint64_t stride = (uint64_t)gridDim.x * SC_THREADS * CT_SPAN;
     for (uint64_t base = (uint64_t)blockIdx.x * SC_THREADS * CT_SPAN; base < n; base += stride) {
         const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
-        thread_windows<CANON>(seq, p0, p0 < n, k, [&](uint64_t key) {
+        thread_windows<CANON>(codes, inv, p0 >> 5, p0 < n, k, [&](uint64_t key) {
             uint64_t h = mix64(key);
             atomicAdd(&sh[h >> (64 - BUCKET_BITS)], 1u);
             uint32_t idx = (uint32_t)(h & (HLL_M - 1));
@@ -130,7 +137,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_part_hist(const uint8_t *__restr
 // bucket writes its whole sectors and moves the 0-3 key remainder to the
 // front; at the end the remainders go out padded with EMPTY_KEY.
 template <bool CANON>
-__global__ void __launch_bounds__(SC_THREADS, 1) k_part_scatter(const uint8_t *__restrict__ seq, uint64_t n, int k,
+__global__ void __launch_bounds__(SC_THREADS, 1) k_part_scatter(const uint64_t *__restrict__ codes,
+                                                               const uint32_t *__restrict__ inv, uint64_t n, int k,
                                                                const uint64_t *__restrict__ offs, uint64_t cols,
                                                                uint64_t col0, uint64_t *__restrict__ keys) {
     extern __shared__ __align__(16) unsigned char sc_smem[];
@@ -146,7 +154,7 @@ __global__ void __launch_bounds__(SC_THREADS, 1) k_part_scatter(const uint8_t *_
     const uint64_t stride = (uint64_t)gridDim.x * SC_THREADS * CT_SPAN;
     for (uint64_t base = (uint64_t)blockIdx.x * SC_THREADS * CT_SPAN; base < n; base += stride) {
         const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
-        thread_windows<CANON>(seq, p0, p0 < n, k, [&](uint64_t key) {
+        thread_windows<CANON>(codes, inv, p0 >> 5, p0 < n, k, [&](uint64_t key) {
             const uint32_t b = (uint32_t)(mix64(key) >> (64 - BUCKET_BITS));
             const uint32_t r = atomicAdd(&cnt[b], 1u);
             if (r < SC_BUF) buf[b * SC_BUF + r] = key;
@@ -594,10 +602,11 @@ static uint64_t pow2_at_least(uint64_t x) {
 
 // Counts every window of one or more packed read arrays into the table in a
 // single partitioned pass (the table is touched once for all of them).
-int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *lens, int nsets) {
+int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
     tk_ctx *c = t->ctx;
     uint64_t total_len = 0;
-    for (int s = 0; s < nsets; s++) total_len += lens[s];
+    std::vector<uint64_t> lens(nsets);
+    for (int s = 0; s < nsets; s++) total_len += (lens[s] = sets[s]->seq_len);
     if (total_len == 0) return TK_OK;
     // the two passes over each read array use one fixed grid, so every tile
     // goes to the same block (histogram column) in both
@@ -623,11 +632,11 @@ int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *le
         prof_begin(c, TK_KID_HLL, &ev);
         for (int s = 0; s < nsets; s++) {
             if (t->canonical)
-                k_part_hist<true><<<grids[s], SC_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
-                                                                          t->d_hll, t->d_counters + 1);
+                k_part_hist<true><<<grids[s], SC_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
+                                                                          hist, cols, col0[s], t->d_hll, t->d_counters + 1);
             else
-                k_part_hist<false><<<grids[s], SC_THREADS, 0, c->stream>>>(seqs[s], lens[s], t->k, hist, cols, col0[s],
-                                                                           t->d_hll, t->d_counters + 1);
+                k_part_hist<false><<<grids[s], SC_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
+                                                                           hist, cols, col0[s], t->d_hll, t->d_counters + 1);
             c->launches++;
         }
         prof_end(c, TK_KID_HLL, ev, total_len);
@@ -660,9 +669,11 @@ int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *le
         prof_begin(c, TK_KID_SCATTER, &ev);
         for (int s = 0; !e && s < nsets; s++) {
             if (t->canonical)
-                k_part_scatter<true><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
+                k_part_scatter<true><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s],
+                                                                                  t->k, offs, cols, col0[s], keys);
             else
-                k_part_scatter<false><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(seqs[s], lens[s], t->k, offs, cols, col0[s], keys);
+                k_part_scatter<false><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s],
+                                                                                   t->k, offs, cols, col0[s], keys);
             c->launches++;
         }
         prof_end(c, TK_KID_SCATTER, ev, windows);
@@ -713,9 +724,7 @@ int table_count_many(tk_table *t, const uint8_t *const *seqs, const uint64_t *le
     return drain_overflow(t);
 }
 
-int table_count_seq(tk_table *t, const uint8_t *d_seq, uint64_t seq_len) {
-    return table_count_many(t, &d_seq, &seq_len, 1);
-}
+int table_count_seq(tk_table *t, const tk_reads *r) { return table_count_many(t, &r, 1); }
 
 static int table_distinct(tk_table *t) {
     tk_ctx *c = t->ctx;
