@@ -174,8 +174,7 @@ class GpuPipeline:
         kmer, t = self.kmer, self.torch
         ctx = self.ctx
         if e2e:
-            rl = kmer.ReadSet(ctx, self.h_left.numpy())
-            rr = kmer.ReadSet(ctx, self.h_right.numpy())
+            rl, rr = kmer.ReadSet.parse_many(ctx, [self.h_left.numpy(), self.h_right.numpy()])
             h2d = self.h_left.numel() + self.h_right.numel()
         else:
             rl = kmer.ReadSet(ctx, self.d_left.data_ptr(), self.d_left.numel(), device=True)
@@ -190,7 +189,8 @@ class GpuPipeline:
         if e2e:
             if self.out["dump_host"] is None or self.out["dump_host"].numel() < dump_len:
                 self.out["dump_host"] = t.empty(int(dump_len * 1.1) + 16, dtype=t.uint8).pin_memory()
-            table.dump_fasta_into(MIN_COUNT, self.out["dump_host"].data_ptr(), self.out["dump_host"].numel())
+            # the text's download overlaps the coverage pass; synchronised below
+            table.dump_fasta_into_async(MIN_COUNT, self.out["dump_host"].data_ptr(), self.out["dump_host"].numel())
             d2h += dump_len
         for side, rs in (("l", rl), ("r", rr)):
             bufs = self.out[side + ("_host" if e2e else "_dev")]
@@ -198,6 +198,8 @@ class GpuPipeline:
                                      device=not e2e)
             if e2e:
                 d2h += 12 * rs.n_reads
+        if e2e:
+            ctx.synchronize()
         _, windows, capacity = table.info()
         reads = rl.n_reads + rr.n_reads
         packed = rl.n_bases + rl.n_reads + rr.n_bases + rr.n_reads

@@ -105,6 +105,15 @@ int tk_ctx_set_reprobes(tk_ctx *ctx, int max_probes);
  * set.  The text is copied to the device when where == TK_HOST; a TK_DEVICE
  * text must stay valid while the read set lives. */
 int tk_reads_parse(tk_ctx *ctx, const char *text, uint64_t len, int where, tk_reads **out);
+/* Parses n texts into n read sets (out[i] from texts[i]).  With TK_HOST every
+ * upload is queued on the context's copy stream first and text i is parsed as
+ * soon as its own upload lands, so the uploads of the later texts overlap the
+ * parsing of the earlier ones (page-locked host memory lets them run
+ * concurrently).  Replaces the one-file-at-a-time read loading of the tools
+ * above (no counterpart in the reference's interface: each of its tools reads
+ * its FASTA itself).  On error no read set is returned. */
+int tk_reads_parse_many(tk_ctx *ctx, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
+                        tk_reads **out);
 int tk_reads_info(const tk_reads *reads, uint64_t *n_reads, uint64_t *n_bases,
                   uint32_t *max_len, int *format);
 /* Host copies: accession offset/length into the parsed text (n_reads each). */
@@ -145,6 +154,12 @@ int tk_table_dump(tk_table *table, uint32_t min_count, int where, uint64_t *keys
  * (until the table changes). */
 int tk_table_dump_fasta(tk_table *table, uint32_t min_count, int where, char *out, uint64_t cap,
                         uint64_t *len_out);
+/* tk_table_dump_fasta into host memory without waiting for the copy: the text
+ * is formatted on the GPU, then copied to `out` on the context's copy stream
+ * while later work on the context runs.  `out` (page-locked for the copy to
+ * overlap) holds the text once tk_ctx_synchronize returns; freeing or changing
+ * the table before then is safe.  *len_out is set at once. */
+int tk_table_dump_fasta_async(tk_table *table, uint32_t min_count, char *out, uint64_t cap, uint64_t *len_out);
 /* Adds (key, count) pairs (a stored database, or another table's dump). */
 int tk_table_load_pairs(tk_table *table, const uint64_t *keys, const uint32_t *counts,
                         uint64_t n, int where);

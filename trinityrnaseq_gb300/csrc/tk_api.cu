@@ -139,7 +139,22 @@ __global__ void k_random_probe(unsigned long long *tab, uint64_t mask, uint64_t 
 }
 
 // drops the cached dump text once the table's contents change
+// the context's copy stream, created on first use
+static cudaStream_t copy_stream(tk_ctx *c) {
+    if (!c->copy_stream && cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        c->copy_stream = nullptr;
+        cudaGetLastError();
+    }
+    return c->copy_stream;
+}
+
 static void dump_invalidate(tk_table *t) {
+    if (t->dump_copy_done) {
+        // the device text is freed in stream order after its host copy ends
+        cudaStreamWaitEvent(t->ctx->stream, t->dump_copy_done, 0);
+        cudaEventDestroy(t->dump_copy_done);
+        t->dump_copy_done = nullptr;
+    }
     if (t->d_dump) dfree(t->ctx, t->d_dump);
     t->d_dump = nullptr;
     t->dump_len = 0;
@@ -223,6 +238,10 @@ void tk_ctx_destroy(tk_ctx *c) {
 static void ctx_release_now(tk_ctx *c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
     for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : c->free_events) cudaEventDestroy(e);
     cudaFree(c->d_err);
@@ -238,6 +257,7 @@ void *tk_ctx_stream(tk_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 int tk_ctx_synchronize(tk_ctx *c) {
     CHECK_CTX(c);
+    if (c->copy_stream) TK_CUDA(c, cudaStreamSynchronize(c->copy_stream));
     return cuda_check(c, cudaStreamSynchronize(c->stream), "synchronize");
 }
 
@@ -340,6 +360,76 @@ int tk_reads_parse(tk_ctx *c, const char *text, uint64_t len, int where, tk_read
     }
     *out = r;
     return TK_OK;
+}
+
+int tk_reads_parse_many(tk_ctx *c, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
+                        tk_reads **out) {
+    CHECK_CTX(c);
+    if (!out || (!texts && n) || (!lens && n)) return set_err(c, TK_E_INVAL, "tk_reads_parse_many: null argument");
+    for (uint32_t i = 0; i < n; i++) {
+        out[i] = nullptr;
+        if (!texts[i] && lens[i]) return set_err(c, TK_E_INVAL, "tk_reads_parse_many: null text");
+    }
+    cudaStream_t cs = where == TK_HOST ? copy_stream(c) : nullptr;
+    if (!cs) {
+        // device texts (or no copy stream): one after another
+        for (uint32_t i = 0; i < n; i++) {
+            int e = tk_reads_parse(c, texts[i], lens[i], where, &out[i]);
+            if (e) {
+                for (uint32_t j = 0; j < i; j++) { tk_reads_free(out[j]); out[j] = nullptr; }
+                return e;
+            }
+        }
+        return TK_OK;
+    }
+    // every upload is queued on the copy stream up front; text i is parsed on
+    // the main stream as soon as its own upload has landed, while the later
+    // ones are still in flight
+    std::vector<char *> dev(n, nullptr);
+    std::vector<cudaEvent_t> landed(n, nullptr);
+    int e = TK_OK;
+    for (uint32_t i = 0; i < n && !e; i++) e = dmalloc(c, (void **)&dev[i], lens[i] + 64, "staged input");
+    cudaEvent_t allocated = nullptr;
+    if (!e) e = cuda_check(c, cudaEventCreateWithFlags(&allocated, cudaEventDisableTiming), "event");
+    if (!e) e = cuda_check(c, cudaEventRecord(allocated, c->stream), "event record");
+    if (!e) e = cuda_check(c, cudaStreamWaitEvent(cs, allocated, 0), "copy stream wait");
+    for (uint32_t i = 0; i < n && !e; i++) {
+        e = cuda_check(c, cudaEventCreateWithFlags(&landed[i], cudaEventDisableTiming), "event");
+        if (!e && lens[i]) e = cuda_check(c, cudaMemcpyAsync(dev[i], texts[i], lens[i], cudaMemcpyHostToDevice, cs), "h2d");
+        if (!e) e = cuda_check(c, cudaEventRecord(landed[i], cs), "event record");
+    }
+    uint32_t made = 0;
+    for (uint32_t i = 0; i < n && !e; i++) {
+        e = cuda_check(c, cudaStreamWaitEvent(c->stream, landed[i], 0), "parse wait");
+        if (e) break;
+        tk_reads *r = new (std::nothrow) tk_reads();
+        if (!r) {
+            e = TK_E_OOM;
+            break;
+        }
+        r->ctx = c;
+        ctx_acquire(c);
+        r->text_len = lens[i];
+        r->d_text = dev[i];
+        r->own_text = true;
+        dev[i] = nullptr;
+        out[i] = r;
+        made = i + 1;
+        e = parse_reads(c, r);
+    }
+    if (e) {
+        cudaStreamSynchronize(cs);
+        for (uint32_t j = 0; j < made; j++) { tk_reads_free(out[j]); out[j] = nullptr; }
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        if (dev[i]) {
+            if (landed[i] || allocated) cudaStreamWaitEvent(c->stream, landed[i] ? landed[i] : allocated, 0);
+            dfree(c, dev[i]);
+        }
+        if (landed[i]) cudaEventDestroy(landed[i]);
+    }
+    if (allocated) cudaEventDestroy(allocated);
+    return e;
 }
 
 int tk_reads_info(const tk_reads *r, uint64_t *n_reads, uint64_t *n_bases, uint32_t *max_len, int *format) {
@@ -502,10 +592,9 @@ int tk_table_dump(tk_table *t, uint32_t min_count, int where, uint64_t *keys, ui
     return e;
 }
 
-int tk_table_dump_fasta(tk_table *t, uint32_t min_count, int where, char *out, uint64_t cap, uint64_t *len_out) {
-    if (!t || !len_out) return TK_E_INVAL;
+// builds (or reuses) the device text of the dump at min_count
+static int dump_build(tk_table *t, uint32_t min_count) {
     tk_ctx *c = t->ctx;
-    CHECK_CTX(c);
     if (!t->dump_valid || t->dump_min != min_count) {
         dump_invalidate(t);
         uint64_t *dk = nullptr;
@@ -523,6 +612,14 @@ int tk_table_dump_fasta(tk_table *t, uint32_t min_count, int where, char *out, u
         t->dump_min = min_count;
         t->dump_valid = true;
     }
+    return TK_OK;
+}
+
+int tk_table_dump_fasta(tk_table *t, uint32_t min_count, int where, char *out, uint64_t cap, uint64_t *len_out) {
+    if (!t || !len_out) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    TK_TRY(dump_build(t, min_count));
     *len_out = t->dump_len;
     int e = TK_OK;
     if (out) {
@@ -532,6 +629,28 @@ int tk_table_dump_fasta(tk_table *t, uint32_t min_count, int where, char *out, u
             e = cuda_check(c, cudaMemcpyAsync(out, t->d_dump, t->dump_len, kind, c->stream), "dump text copy");
     }
     if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "dump text sync");
+    return e;
+}
+
+int tk_table_dump_fasta_async(tk_table *t, uint32_t min_count, char *out, uint64_t cap, uint64_t *len_out) {
+    if (!t || !len_out) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    TK_TRY(dump_build(t, min_count));
+    *len_out = t->dump_len;
+    if (!out) return TK_OK;
+    if (cap < t->dump_len) return set_err(c, TK_E_RANGE, "tk_table_dump_fasta_async: buffer smaller than the dump");
+    if (!t->dump_len) return TK_OK;
+    cudaStream_t cs = copy_stream(c);
+    if (!cs) return tk_table_dump_fasta(t, min_count, TK_HOST, out, cap, len_out);
+    cudaEvent_t built = nullptr;
+    TK_CUDA(c, cudaEventCreateWithFlags(&built, cudaEventDisableTiming));
+    int e = cuda_check(c, cudaEventRecord(built, c->stream), "event record");
+    if (!e) e = cuda_check(c, cudaStreamWaitEvent(cs, built, 0), "copy stream wait");
+    cudaEventDestroy(built);
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(out, t->d_dump, t->dump_len, cudaMemcpyDeviceToHost, cs), "dump d2h");
+    if (!e && !t->dump_copy_done) e = cuda_check(c, cudaEventCreateWithFlags(&t->dump_copy_done, cudaEventDisableTiming), "event");
+    if (!e) e = cuda_check(c, cudaEventRecord(t->dump_copy_done, cs), "event record");
     return e;
 }
 
@@ -573,7 +692,7 @@ void tk_table_free(tk_table *t) {
     dfree(c, t->d_ovf);
     dfree(c, t->d_counters);
     dfree(c, t->d_hll);
-    dfree(c, t->d_dump);
+    dump_invalidate(t);
     delete t;
     ctx_release(c);
 }

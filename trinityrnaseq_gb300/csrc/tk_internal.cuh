@@ -201,6 +201,9 @@ struct tk_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // host <-> device copies that overlap the work on `stream` (created on
+    // first use; tk_ctx_synchronize waits for both streams)
+    cudaStream_t copy_stream = nullptr;
     uint32_t *d_err = nullptr;             // tk::DE_COUNT words
     std::string last_error;
     // profiling (CUDA events on `stream` around the hot kernels)
@@ -256,6 +259,7 @@ struct tk_table {
     bool fresh = false;                     // slots not yet written (see table_alloc_geom)
     // last formatted dump (valid until the table changes)
     char *d_dump = nullptr;
+    cudaEvent_t dump_copy_done = nullptr;   // an asynchronous host copy of d_dump in flight
     uint64_t dump_len = 0;
     uint32_t dump_min = 0;
     bool dump_valid = false;

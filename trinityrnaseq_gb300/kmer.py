@@ -122,10 +122,33 @@ class ReadSet:
         self._keep = keep if device else None   # a host text is copied; a device text is aliased
         self._host_text = None if device else text
         ctx.check(self.lib.tk_reads_parse(ctx.h, C.c_void_p(ptr), n, where, C.byref(h)), "tk_reads_parse")
+        self._adopt(h)
+
+    def _adopt(self, h) -> None:
         self.h = h
         nr, nb, ml, fm = C.c_uint64(), C.c_uint64(), C.c_uint32(), C.c_int()
-        ctx.check(self.lib.tk_reads_info(h, C.byref(nr), C.byref(nb), C.byref(ml), C.byref(fm)), "tk_reads_info")
+        self.ctx.check(self.lib.tk_reads_info(h, C.byref(nr), C.byref(nb), C.byref(ml), C.byref(fm)), "tk_reads_info")
         self.n_reads, self.n_bases, self.max_len, self.format = nr.value, nb.value, ml.value, fm.value
+
+    @classmethod
+    def parse_many(cls, ctx: Context, texts: list) -> list:
+        """Host texts -> read sets, the upload of each text overlapping the
+        parse of the ones before it (tk_reads_parse_many)."""
+        n = len(texts)
+        ptrs, lens, keep = (C.c_void_p * n)(), (C.c_uint64 * n)(), []
+        for i, t in enumerate(texts):
+            ptr, ln, k = _host_ptr(t)
+            ptrs[i], lens[i] = ptr, ln
+            keep.append(k)
+        hs = (C.c_void_p * n)()
+        ctx.check(ctx.lib.tk_reads_parse_many(ctx.h, ptrs, lens, n, N.TK_HOST, hs), "tk_reads_parse_many")
+        out = []
+        for i in range(n):
+            rs = cls.__new__(cls)
+            rs.ctx, rs.lib, rs._keep, rs._host_text = ctx, ctx.lib, None, texts[i]
+            rs._adopt(C.c_void_p(hs[i]))
+            out.append(rs)
+        return out
 
     def free(self) -> None:
         if getattr(self, "h", None):
@@ -232,6 +255,14 @@ class KmerTable:
         m = C.c_uint64()
         self.ctx.check(self.lib.tk_table_dump_fasta(self.h, min_count, N.TK_DEVICE if device else N.TK_HOST,
                                                     C.c_void_p(ptr), cap, C.byref(m)), "tk_table_dump_fasta")
+        return m.value
+
+    def dump_fasta_into_async(self, min_count: int, ptr: int, cap: int) -> int:
+        """Starts the copy of the dump text to host memory at ``ptr`` on the
+        context's copy stream; the text is there after ``Context.synchronize``."""
+        m = C.c_uint64()
+        self.ctx.check(self.lib.tk_table_dump_fasta_async(self.h, min_count, C.c_void_p(ptr), cap, C.byref(m)),
+                       "tk_table_dump_fasta_async")
         return m.value
 
     def dump_fasta(self, min_count: int = 1) -> bytes:

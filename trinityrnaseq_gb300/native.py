@@ -52,6 +52,7 @@ SIGNATURES = {
     "tk_ctx_set_reprobes": (C.c_int, [vp, C.c_int]),
     "tk_ctx_random_access_rate": (C.c_int, [vp, u64, C.c_int, P(C.c_double)]),
     "tk_reads_parse": (C.c_int, [vp, vp, u64, C.c_int, P(vp)]),
+    "tk_reads_parse_many": (C.c_int, [vp, P(vp), P(u64), u32, C.c_int, P(vp)]),
     "tk_reads_info": (C.c_int, [vp, P(u64), P(u64), P(u32), P(C.c_int)]),
     "tk_reads_names": (C.c_int, [vp, vp, vp]),
     "tk_reads_offsets": (C.c_int, [vp, vp]),
@@ -65,6 +66,7 @@ SIGNATURES = {
     "tk_table_histo": (C.c_int, [vp, u64, u64, vp]),
     "tk_table_dump": (C.c_int, [vp, u32, C.c_int, vp, vp, u64, P(u64)]),
     "tk_table_dump_fasta": (C.c_int, [vp, u32, C.c_int, vp, u64, P(u64)]),
+    "tk_table_dump_fasta_async": (C.c_int, [vp, u32, vp, u64, P(u64)]),
     "tk_table_load_pairs": (C.c_int, [vp, vp, vp, u64, C.c_int]),
     "tk_table_load_dump_fasta": (C.c_int, [vp, vp, u64, C.c_int]),
     "tk_table_free": (None, [vp]),
