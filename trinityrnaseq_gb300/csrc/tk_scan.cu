@@ -139,53 +139,92 @@ __global__ void k_rs_hist(const uint64_t *__restrict__ keys, uint64_t n, int shi
     for (int i = threadIdx.x; i < RS_BINS; i += RS_THREADS) hist[(uint64_t)i * ntiles + blockIdx.x] = h[i];
 }
 
-// stable scatter: items of a tile are ranked round by round (striped), and
-// within a round by warp then lane, which is input order.
-__global__ void k_rs_scatter(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                             uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals, uint64_t n, int shift,
-                             const uint64_t *__restrict__ offs, uint64_t ntiles) {
-    constexpr int NW = RS_THREADS / 32;
-    __shared__ uint32_t wcnt[NW][RS_BINS];   // per warp digit counts, then their prefix over warps
-    __shared__ uint32_t rtot[RS_BINS];       // this round's count per digit
-    __shared__ uint32_t run[RS_BINS];        // items of each digit already placed by this tile
-    __shared__ uint64_t gbase[RS_BINS];
+// Stable scatter of one 4096-item tile.  Warp w ranks its 512 consecutive
+// items in 16 rounds of 32 (match.any inside a round, a per-warp running count
+// per digit in shared memory); a scan over (digit, warp) turns the ranks into
+// positions of a digit-sorted tile, which is laid out in shared memory and then
+// leaves as one run per digit, consecutive threads storing consecutive items
+// (runs of ~16 keys instead of one scattered 8-byte store per item).
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_PER_LANE = RS_TILE / RS_THREADS;   // rounds per warp
+constexpr size_t RS_SMEM = (size_t)RS_WARPS * RS_BINS * 4 + RS_BINS * 4 + RS_BINS * 8 + RS_TILE * 8 + RS_TILE * 4;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t *__restrict__ keys,
+                                                          const uint32_t *__restrict__ vals,
+                                                          uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals,
+                                                          uint64_t n, int shift, const uint64_t *__restrict__ offs,
+                                                          uint64_t ntiles) {
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    uint64_t *skey = reinterpret_cast<uint64_t *>(rs_smem);                              // [RS_TILE]
+    unsigned long long *gbase = reinterpret_cast<unsigned long long *>(skey + RS_TILE);  // [RS_BINS]
+    uint32_t *sval = reinterpret_cast<uint32_t *>(gbase + RS_BINS);                      // [RS_TILE]
+    uint32_t *wcnt = sval + RS_TILE;                                                     // [RS_WARPS][RS_BINS]
+    uint32_t *dstart = wcnt + RS_WARPS * RS_BINS;                                        // [RS_BINS]
+    __shared__ uint32_t scan_sm[RS_WARPS + 1];
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < RS_BINS; i += RS_THREADS) {
-        run[i] = 0;
-        gbase[i] = offs[(uint64_t)i * ntiles + blockIdx.x];
-    }
-    const uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
+    for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) wcnt[i] = 0;
+    for (int i = threadIdx.x; i < RS_BINS; i += RS_THREADS) gbase[i] = offs[(uint64_t)i * ntiles + blockIdx.x];
+    __syncthreads();
+    const uint64_t tile0 = (uint64_t)blockIdx.x * RS_TILE;
+    const uint64_t base = tile0 + (uint64_t)warp * (RS_TILE / RS_WARPS);
     const unsigned lt_mask = (1u << lane) - 1u;
-    for (int r = 0; r < RS_ROUNDS; r++) {
-        for (int i = threadIdx.x; i < NW * RS_BINS; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
-        __syncthreads();
-        uint64_t idx = base + (uint64_t)r * RS_THREADS + threadIdx.x;
-        bool valid = idx < n;
-        uint64_t key = valid ? keys[idx] : 0;
-        uint32_t val = valid ? vals[idx] : 0;
-        uint32_t d = valid ? (uint32_t)((key >> shift) & (RS_BINS - 1)) : (uint32_t)RS_BINS;
-        unsigned peers = __match_any_sync(0xffffffffu, d);
-        uint32_t wrank = __popc(peers & lt_mask);
-        if (valid && wrank == 0) wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        for (int dd = threadIdx.x; dd < RS_BINS; dd += RS_THREADS) {
-            uint32_t acc = 0;
+    uint32_t *mycnt = wcnt + warp * RS_BINS;
+    uint64_t k[RS_PER_LANE];
+    uint32_t v[RS_PER_LANE], pos[RS_PER_LANE];
 #pragma unroll
-            for (int w = 0; w < NW; w++) {
-                uint32_t cnt = wcnt[w][dd];
-                wcnt[w][dd] = acc;
-                acc += cnt;
-            }
-            rtot[dd] = acc;
+    for (int r = 0; r < RS_PER_LANE; r++) {
+        const uint64_t idx = base + (uint64_t)r * 32 + lane;
+        const bool valid = idx < n;
+        k[r] = valid ? keys[idx] : 0;
+        v[r] = valid ? vals[idx] : 0;
+        const uint32_t d = valid ? (uint32_t)((k[r] >> shift) & (RS_BINS - 1)) : (uint32_t)RS_BINS;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & lt_mask);
+        const uint32_t cur = valid ? mycnt[d] : 0u;
+        pos[r] = cur + rank;
+        __syncwarp();
+        if (valid && rank == 0) mycnt[d] = cur + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: earlier warps' counts (stable order), and the digit's start in the tile
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_THREADS) {
+        uint32_t acc = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) {
+            const uint32_t c = wcnt[w * RS_BINS + d];
+            wcnt[w * RS_BINS + d] = acc;
+            acc += c;
         }
+        dstart[d] = acc;   // the digit's total for now
+    }
+    __syncthreads();
+    static_assert(RS_BINS == RS_THREADS, "one digit per thread in the scan");
+    {
+        uint32_t tot;
+        const uint32_t ex = block_excl_scan<uint32_t>(dstart[threadIdx.x], scan_sm, &tot);
         __syncthreads();
-        if (valid) {
-            uint64_t pos = gbase[d] + run[d] + wcnt[warp][d] + wrank;
-            okeys[pos] = key;
-            ovals[pos] = val;
+        dstart[threadIdx.x] = ex;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_PER_LANE; r++) {
+        const uint64_t idx = base + (uint64_t)r * 32 + lane;
+        if (idx < n) {
+            const uint32_t d = (uint32_t)((k[r] >> shift) & (RS_BINS - 1));
+            const uint32_t lp = dstart[d] + mycnt[d] + pos[r];
+            skey[lp] = k[r];
+            sval[lp] = v[r];
         }
-        __syncthreads();
-        for (int dd = threadIdx.x; dd < RS_BINS; dd += RS_THREADS) run[dd] += rtot[dd];
+    }
+    __syncthreads();
+    const uint32_t m = n - tile0 < (uint64_t)RS_TILE ? (uint32_t)(n - tile0) : (uint32_t)RS_TILE;
+    for (uint32_t i = threadIdx.x; i < m; i += RS_THREADS) {
+        const uint64_t key = skey[i];
+        const uint32_t d = (uint32_t)((key >> shift) & (RS_BINS - 1));
+        const uint64_t o = gbase[d] + (i - dstart[d]);
+        okeys[o] = key;
+        ovals[o] = sval[i];
     }
 }
 
@@ -199,6 +238,8 @@ int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int 
     TK_TRY(dmalloc(c, (void **)&hist, ntiles * RS_BINS * sizeof(uint32_t), "radix hist"));
     int e = dmalloc(c, (void **)&offs, ntiles * RS_BINS * sizeof(uint64_t), "radix offsets");
     if (e) { dfree(c, hist); return e; }
+    if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_rs_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM),
+                           "radix scatter smem");
     uint64_t *ka = keys, *kb = tmp_keys;
     uint32_t *va = vals, *vb = tmp_vals;
     for (int shift = 0; shift < bits && !e; shift += RS_BITS) {
@@ -206,7 +247,7 @@ int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int 
         c->launches++;
         e = scan_excl_u32_to_u64(c, hist, offs, ntiles * RS_BINS, nullptr);
         if (e) break;
-        k_rs_scatter<<<(unsigned)ntiles, RS_THREADS, 0, c->stream>>>(ka, va, kb, vb, n, shift, offs, ntiles);
+        k_rs_scatter<<<(unsigned)ntiles, RS_THREADS, RS_SMEM, c->stream>>>(ka, va, kb, vb, n, shift, offs, ntiles);
         c->launches++;
         e = check_launch(c, "radix scatter");
         uint64_t *tk_ = ka; ka = kb; kb = tk_;
