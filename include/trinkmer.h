@@ -80,7 +80,9 @@ const char *tk_ctx_last_error(const tk_ctx *ctx);
 /* The context's cudaStream_t, as an opaque pointer. */
 void *tk_ctx_stream(tk_ctx *ctx);
 int tk_ctx_synchronize(tk_ctx *ctx);
-/* CUDA-event timing of the hot kernels on the context's stream. */
+/* CUDA-event timing of the hot kernels on the context's stream: per kernel
+ * class, the milliseconds between events recorded around its launches, the
+ * number of kernels launched inside those brackets, and its work units. */
 int tk_ctx_set_profiling(tk_ctx *ctx, int on);
 int tk_ctx_profile(tk_ctx *ctx, int kid, double *ms, uint64_t *launches, uint64_t *units);
 int tk_ctx_reset_profile(tk_ctx *ctx);

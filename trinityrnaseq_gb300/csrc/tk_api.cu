@@ -65,18 +65,19 @@ static cudaEvent_t take_event(tk_ctx *c) {
 }
 
 void prof_begin(tk_ctx *c, int kid, cudaEvent_t *ev) {
-    (void)kid;
     *ev = nullptr;
     if (!c->prof) return;
     *ev = take_event(c);
     cudaEventRecord(*ev, c->stream);
+    if (kid >= 0 && kid < TK_KID_NUM) c->prof_open[kid] = c->launches;
 }
 
 void prof_end(tk_ctx *c, int kid, cudaEvent_t ev, uint64_t units) {
     if (!c->prof || !ev) return;
     cudaEvent_t b = take_event(c);
     cudaEventRecord(b, c->stream);
-    c->pending.push_back({ev, b, kid, units});
+    const uint64_t n = (kid >= 0 && kid < TK_KID_NUM) ? c->launches - c->prof_open[kid] : 0;
+    c->pending.push_back({ev, b, kid, units, n});
 }
 
 void prof_add_units(tk_ctx *c, int kid, uint64_t units) {
@@ -90,7 +91,7 @@ static int prof_fold(tk_ctx *c) {
         float ms = 0;
         cudaEventElapsedTime(&ms, p.a, p.b);
         c->prof_ms[p.kid] += ms;
-        c->prof_launches[p.kid] += 1;
+        c->prof_launches[p.kid] += p.launches;
         c->prof_units[p.kid] += p.units;
         c->free_events.push_back(p.a);
         c->free_events.push_back(p.b);

@@ -195,6 +195,7 @@ struct tk_prof_rec {
     cudaEvent_t a, b;
     int kid;
     uint64_t units;
+    uint64_t launches;   // kernels launched between the two events
 };
 
 struct tk_ctx {
@@ -214,6 +215,7 @@ struct tk_ctx {
     uint64_t prof_launches[TK_KID_NUM] = {0};
     uint64_t prof_units[TK_KID_NUM] = {0};
     uint64_t launches = 0;                  // every kernel launched by the library
+    uint64_t prof_open[TK_KID_NUM] = {0};   // `launches` when each class's bracket opened
     int max_probes = 4096;
     int sm_count = 152;
     // read sets, tables and bundles alive on this context; tk_ctx_destroy

@@ -102,46 +102,52 @@ __global__ void k_bounds(const char *__restrict__ text, uint64_t len, unsigned l
     }
 }
 
-// ---- A1: newlines per tile
-__global__ void k_tile_newlines(ParseGeom g, uint32_t *__restrict__ tile_nl) {
+// Bit i set when byte p+i (p = this thread's first byte) is a '\n' inside
+// [S, E).  Per 4-byte word the equal bytes are found with the exact
+// zero-byte test and their top bits gathered by one multiply.
+__device__ __forceinline__ uint32_t newline_bits(const ParseGeom &g, const Bytes32 &b, uint64_t p) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const uint32_t v = b.w[q] ^ 0x0A0A0A0Au;
+        const uint32_t z = ~((((v & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | v)) & 0x80808080u;   // bit 7 of each '\n' byte
+        m |= ((((z >> 7) * 0x00204081u) >> 21) & 0xFu) << (4 * q);                     // byte b -> bit b
+    }
+    if (p < g.S) m &= g.S - p >= 32 ? 0u : ~0u << (g.S - p);
+    if (p + 32 > g.E) m &= g.E <= p ? 0u : (g.E - p >= 32 ? ~0u : (1u << (g.E - p)) - 1u);
+    return m;
+}
+
+// ---- A1: newlines per tile, and each thread's newline bits for A2
+__global__ void k_tile_newlines(ParseGeom g, uint32_t *__restrict__ tile_nl, uint32_t *__restrict__ nl_bits) {
     __shared__ uint32_t sm[PT_THREADS / 32 + 1];
     uint64_t p = g.A + (uint64_t)blockIdx.x * PT_TILE + (uint64_t)threadIdx.x * PT_BYTES;
     Bytes32 b = load32(g.text, g.len, p, g.vec);
-    uint32_t n = 0;
-#pragma unroll
-    for (int i = 0; i < PT_BYTES; i++) {
-        uint64_t q = p + i;
-        n += (q >= g.S && q < g.E && b.get(i) == '\n');
-    }
+    const uint32_t m = newline_bits(g, b, p);
+    nl_bits[(uint64_t)blockIdx.x * PT_THREADS + threadIdx.x] = m;
     uint32_t tot;
-    block_excl_scan<uint32_t>(n, sm, &tot);
+    block_excl_scan<uint32_t>(__popc(m), sm, &tot);
     if (threadIdx.x == 0) tile_nl[blockIdx.x] = tot;
 }
 
-// ---- A2: line ends
-__global__ void k_line_ends(ParseGeom g, const uint64_t *__restrict__ tile_line0, uint64_t *__restrict__ line_end) {
+// ---- A2: line ends, from the newline bits (1/8 of the text's bytes)
+__global__ void k_line_ends(ParseGeom g, const uint32_t *__restrict__ nl_bits, const uint64_t *__restrict__ tile_line0,
+                            uint64_t *__restrict__ line_end) {
     __shared__ uint32_t sm[PT_THREADS / 32 + 1];
-    uint64_t p = g.A + (uint64_t)blockIdx.x * PT_TILE + (uint64_t)threadIdx.x * PT_BYTES;
-    Bytes32 b = load32(g.text, g.len, p, g.vec);
-    uint32_t n = 0;
-#pragma unroll
-    for (int i = 0; i < PT_BYTES; i++) {
-        uint64_t q = p + i;
-        n += (q >= g.S && q < g.E && b.get(i) == '\n');
-    }
+    const uint64_t p = g.A + (uint64_t)blockIdx.x * PT_TILE + (uint64_t)threadIdx.x * PT_BYTES;
+    uint32_t m = nl_bits[(uint64_t)blockIdx.x * PT_THREADS + threadIdx.x];
     uint32_t tot;
-    uint64_t line = tile_line0[blockIdx.x] + block_excl_scan<uint32_t>(n, sm, &tot);
-    if (n == 0) return;
-#pragma unroll
-    for (int i = 0; i < PT_BYTES; i++) {
-        uint64_t q = p + i;
-        if (q >= g.S && q < g.E && b.get(i) == '\n') line_end[line++] = q;
+    uint64_t line = tile_line0[blockIdx.x] + block_excl_scan<uint32_t>(__popc(m), sm, &tot);
+    while (m) {
+        line_end[line++] = p + (uint32_t)(__ffs(m) - 1);
+        m &= m - 1;
     }
 }
 
 // ---- L: line kinds.  FASTQ errors record the first offending line.
 __global__ void k_line_kinds(ParseGeom g, const uint64_t *__restrict__ line_end, uint64_t n_lines, int fastq,
-                             uint8_t *__restrict__ kind, uint32_t *__restrict__ is_hdr, uint32_t *__restrict__ err) {
+                             uint8_t *__restrict__ kind, uint32_t *__restrict__ is_hdr, uint32_t *__restrict__ len,
+                             uint32_t *__restrict__ err) {
     uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n_lines) return;
     uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
@@ -167,27 +173,21 @@ __global__ void k_line_kinds(ParseGeom g, const uint64_t *__restrict__ line_end,
     }
     kind[j] = kd;
     is_hdr[j] = h;
+    // fast path: bytes the line emits if sequence lines hold no whitespace
+    // besides their newline (checked while copying); k_line_records clears
+    // lines that precede the first record
+    len[j] = kd == LK_SEQ ? (uint32_t)(le - ls) : 0u;
 }
 
 // record index per line (~0 before the first header) and header line per record
 __global__ void k_line_records(const uint32_t *__restrict__ is_hdr, uint64_t *__restrict__ line_rec_io, uint64_t n_lines,
-                               uint64_t *__restrict__ hdr_line) {
+                               uint64_t *__restrict__ hdr_line, uint32_t *__restrict__ len) {
     uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n_lines) return;
     uint64_t incl = line_rec_io[j] + is_hdr[j];   // exclusive scan + own flag
     if (is_hdr[j]) hdr_line[incl - 1] = j;
     line_rec_io[j] = incl == 0 ? ~0ULL : incl - 1;
-}
-
-// ---- fast path, L2: bytes each line would emit if sequence lines hold no
-// whitespace besides their newline (checked while copying)
-__global__ void k_line_lengths(ParseGeom g, const uint64_t *__restrict__ line_end, const uint8_t *__restrict__ kind,
-                               const uint64_t *__restrict__ line_rec, uint64_t n_lines, uint32_t *__restrict__ len) {
-    uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_lines) return;
-    uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
-    uint64_t le = line_end[j];
-    len[j] = (kind[j] == LK_SEQ && line_rec[j] != ~0ULL) ? (uint32_t)(le - ls) : 0u;
+    if (incl == 0) len[j] = 0u;
 }
 
 // ---- fast path, copy.  A warp takes 32 consecutive lines: lane l loads line
@@ -221,22 +221,38 @@ __global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end,
         }
         unsigned todo = __ballot_sync(0xffffffffu, len > 0);
         while (todo) {
-            const int l = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const uint64_t s0 = __shfl_sync(0xffffffffu, src, l);
-            const uint64_t d0 = __shfl_sync(0xffffffffu, dst, l);
-            const uint32_t n = __shfl_sync(0xffffffffu, len, l);
-            for (uint32_t q = lane; q < n; q += 128) {
-                uint32_t c[4];
+            // four lines at a time: all their loads are in flight before any store
+            uint64_t s0[4], d0[4];
+            uint32_t n[4], nmax = 0;
 #pragma unroll
-                for (int u = 0; u < 4; u++) c[u] = q + 32 * u < n ? (uint8_t)g.text[s0 + q + 32 * u] : (uint32_t)'A';
+            for (int b = 0; b < 4; b++) {
+                const int l = todo ? __ffs(todo) - 1 : 0;
+                const bool have = todo != 0;
+                todo &= todo - 1;
+                s0[b] = __shfl_sync(0xffffffffu, src, l);
+                d0[b] = __shfl_sync(0xffffffffu, dst, l);
+                n[b] = have ? __shfl_sync(0xffffffffu, len, l) : 0u;
+                nmax = max(nmax, n[b]);
+            }
+            for (uint32_t q0 = 0; q0 < nmax; q0 += 128) {
+                uint32_t c[4][4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if (q + 32 * u < n) {
-                        ws |= is_ws(c[u]);
-                        seq[d0 + q + 32 * u] = (uint8_t)((c[u] >= 'a' && c[u] <= 'z') ? c[u] - 32u : c[u]);
+                for (int b = 0; b < 4; b++)
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const uint32_t q = q0 + 32 * u + lane;
+                        c[b][u] = q < n[b] ? (uint8_t)g.text[s0[b] + q] : (uint32_t)'A';
                     }
-                }
+#pragma unroll
+                for (int b = 0; b < 4; b++)
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const uint32_t q = q0 + 32 * u + lane;
+                        if (q < n[b]) {
+                            ws |= is_ws(c[b][u]);
+                            seq[d0[b] + q] = (uint8_t)((c[b][u] >= 'a' && c[b][u] <= 'z') ? c[b][u] - 32u : c[b][u]);
+                        }
+                    }
             }
         }
     }
@@ -430,7 +446,7 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
     const int fastq = r->format == TK_FMT_FASTQ;
 
     uint64_t n_tiles = g.S >= g.E ? 0 : (g.E - g.A + PT_TILE - 1) / PT_TILE;
-    uint32_t *tile_nl = nullptr, *tile_em = nullptr, *is_hdr = nullptr;
+    uint32_t *tile_nl = nullptr, *tile_em = nullptr, *is_hdr = nullptr, *nl_bits = nullptr;
     uint64_t *tile_line0 = nullptr, *tile_emit0 = nullptr, *line_end = nullptr, *line_rec = nullptr, *hdr_line = nullptr;
     uint32_t *line_len = nullptr;
     uint64_t *line_out = nullptr;
@@ -447,12 +463,13 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
         if (n_tiles == 0) break;
         if ((e = alloc((void **)&tile_nl, n_tiles * 4, "tile newlines"))) break;
         if ((e = alloc((void **)&tile_line0, (n_tiles + 1) * 8, "tile lines"))) break;
-        k_tile_newlines<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_nl);
+        if ((e = alloc((void **)&nl_bits, n_tiles * PT_THREADS * 4, "newline bits"))) break;
+        k_tile_newlines<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_nl, nl_bits);
         c->launches++;
         if ((e = scan_excl_u32_to_u64(c, tile_nl, tile_line0, n_tiles, &n_nl))) break;
         n_lines = n_nl + 1;
         if ((e = alloc((void **)&line_end, n_lines * 8, "line ends"))) break;
-        k_line_ends<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, line_end);
+        k_line_ends<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, nl_bits, tile_line0, line_end);
         c->launches++;
         if ((e = cuda_check(c, cudaMemcpyAsync(line_end + n_nl, &g.E, 8, cudaMemcpyHostToDevice, c->stream), "line end"))) break;
         if (fastq && (n_lines & 3) != 0) {
@@ -462,10 +479,12 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
         if ((e = alloc((void **)&kind, n_lines, "line kinds"))) break;
         if ((e = alloc((void **)&is_hdr, n_lines * 4, "header flags"))) break;
         if ((e = alloc((void **)&line_rec, n_lines * 8, "line records"))) break;
+        if ((e = alloc((void **)&line_len, n_lines * 4, "line lengths"))) break;
         if ((e = cuda_check(c, cudaMemsetAsync(c->d_err, 0, DE_COUNT * 4, c->stream), "err reset"))) break;
         uint32_t big = 0xFFFFFFFFu;
         cudaMemcpyAsync(c->d_err + DE_PARSE + 1, &big, 4, cudaMemcpyHostToDevice, c->stream);
-        k_line_kinds<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(g, line_end, n_lines, fastq, kind, is_hdr, c->d_err);
+        k_line_kinds<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(g, line_end, n_lines, fastq, kind, is_hdr, line_len,
+                                                                     c->d_err);
         c->launches++;
         uint32_t herr[2] = {0, 0};
         if ((e = cuda_check(c, cudaMemcpyAsync(herr, c->d_err + DE_PARSE, 8, cudaMemcpyDeviceToHost, c->stream), "err d2h"))) break;
@@ -475,13 +494,9 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
             break;
         }
         if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
-        k_line_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(is_hdr, line_rec, n_lines, hdr_line);
+        k_line_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(is_hdr, line_rec, n_lines, hdr_line, line_len);
         c->launches++;
-        // fast path: emitted bytes per line assuming no whitespace inside sequence lines
-        if ((e = alloc((void **)&line_len, n_lines * 4, "line lengths"))) break;
         if ((e = alloc((void **)&line_out, (n_lines + 1) * 8, "line outputs"))) break;
-        k_line_lengths<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(g, line_end, kind, line_rec, n_lines, line_len);
-        c->launches++;
         if ((e = scan_excl_u32_to_u64(c, line_len, line_out, n_lines, &n_emit))) break;
     } while (0);
     if (e) {
