@@ -12,7 +12,10 @@ median/mean/stdev coverage of each mate file (fastaToKmerCoverageStats).
 
 value  = k-mer occurrences counted / step time, inputs resident in HBM
 e2e    = the same through the C ABI from pinned host FASTQ, with the dump text
-         and the statistics copied back to the host inside the timed region
+         and the statistics copied back to the host inside the timed region;
+         each mate file goes up in record-aligned pieces so that one piece is
+         parsed while the next uploads, and the dump's download overlaps the
+         coverage pass
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--pairs P]
 """
@@ -38,6 +41,7 @@ SEED = 20240
 K = 25
 MIN_COUNT = 2           # the catalogue fastaToKmerCoverageStats reads (util/insilico_read_normalization.pl:45)
 L2_BYTES = 129 * 2**20
+E2E_PIECES = 2          # record-aligned pieces per mate file on the end-to-end path
 
 
 def log(*a):
@@ -174,17 +178,27 @@ class GpuPipeline:
         kmer, t = self.kmer, self.torch
         ctx = self.ctx
         if e2e:
-            rl, rr = kmer.ReadSet.parse_many(ctx, [self.h_left.numpy(), self.h_right.numpy()])
+            # each mate's FASTQ in record-aligned pieces: a piece is parsed while
+            # the next one uploads (the split reads only bytes near each cut)
+            pieces = []
+            for h in (self.h_left, self.h_right):
+                a = h.numpy()
+                cuts = kmer.split_records(a, E2E_PIECES)
+                pieces += [a[cuts[i]:cuts[i + 1]] for i in range(E2E_PIECES)]
+            sets = kmer.ReadSet.parse_many(ctx, pieces)
+            left_sets, right_sets = sets[:E2E_PIECES], sets[E2E_PIECES:]
             h2d = self.h_left.numel() + self.h_right.numel()
         else:
-            rl = kmer.ReadSet(ctx, self.d_left.data_ptr(), self.d_left.numel(), device=True)
-            rr = kmer.ReadSet(ctx, self.d_right.data_ptr(), self.d_right.numel(), device=True)
+            left_sets = [kmer.ReadSet(ctx, self.d_left.data_ptr(), self.d_left.numel(), device=True)]
+            right_sets = [kmer.ReadSet(ctx, self.d_right.data_ptr(), self.d_right.numel(), device=True)]
             h2d = 0
         table = kmer.KmerTable(ctx, K, True)
-        table.add_many([rl, rr])
+        table.add_many(left_sets + right_sets)
         hist = table.histo(1, 10000)
         dump_len = table.dump_fasta_len(MIN_COUNT)
-        self._alloc_out(rl.n_reads, rr.n_reads)
+        n_left = sum(r.n_reads for r in left_sets)
+        n_right = sum(r.n_reads for r in right_sets)
+        self._alloc_out(n_left, n_right)
         d2h = hist.nbytes
         if e2e:
             if self.out["dump_host"] is None or self.out["dump_host"].numel() < dump_len:
@@ -192,20 +206,27 @@ class GpuPipeline:
             # the text's download overlaps the coverage pass; synchronised below
             table.dump_fasta_into_async(MIN_COUNT, self.out["dump_host"].data_ptr(), self.out["dump_host"].numel())
             d2h += dump_len
-        for side, rs in (("l", rl), ("r", rr)):
-            bufs = self.out[side + ("_host" if e2e else "_dev")]
-            kmer.coverage_stats_into(table, rs, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(),
-                                     device=not e2e)
+        for side, group in (("l", left_sets), ("r", right_sets)):
+            bufs = self.out[side + "_dev"]
+            first = 0
+            for rs in group:
+                kmer.coverage_stats_into(table, rs, bufs[0].data_ptr() + 4 * first, bufs[1].data_ptr() + 4 * first,
+                                         bufs[2].data_ptr() + 4 * first, device=True)
+                first += rs.n_reads
             if e2e:
-                d2h += 12 * rs.n_reads
+                # the statistics go down once per mate, queued on the context's
+                # stream after its coverage passes
+                for h, d in zip(self.out[side + "_host"], bufs):
+                    h[:first].copy_(d[:first], non_blocking=True)
+                d2h += 12 * first
         if e2e:
             ctx.synchronize()
-        _, windows, capacity = table.info()
-        reads = rl.n_reads + rr.n_reads
-        packed = rl.n_bases + rl.n_reads + rr.n_bases + rr.n_reads
+        _, windows, capacity = table.info(distinct=False)
+        reads = n_left + n_right
+        packed = sum(r.n_bases + r.n_reads for r in left_sets + right_sets)
         table.free()
-        rl.free()
-        rr.free()
+        for r in left_sets + right_sets:
+            r.free()
         return windows, reads, h2d, d2h, packed, capacity
 
 

@@ -116,6 +116,14 @@ int tk_reads_parse(tk_ctx *ctx, const char *text, uint64_t len, int where, tk_re
  * its FASTA itself).  On error no read set is returned. */
 int tk_reads_parse_many(tk_ctx *ctx, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
                         tk_reads **out);
+/* Host-only: n_chunks + 1 offsets (cuts[0] = 0, cuts[n_chunks] = len,
+ * non-decreasing) that split a FASTA or FASTQ host text into n_chunks pieces
+ * of about equal size, each cut at the start of a record ('>' line; for FASTQ
+ * an '@' line whose next-but-one line starts with '+').  The pieces parse to
+ * the same reads, in order, as the whole text; with tk_reads_parse_many the
+ * upload of one piece overlaps the parse of the one before.  Only the bytes
+ * around each cut are read.  No counterpart in the reference. */
+int tk_split_records(const char *text, uint64_t len, uint32_t n_chunks, uint64_t *cuts);
 int tk_reads_info(const tk_reads *reads, uint64_t *n_reads, uint64_t *n_bases,
                   uint32_t *max_len, int *format);
 /* Host copies: accession offset/length into the parsed text (n_reads each). */
@@ -141,6 +149,8 @@ int tk_table_add_reads(tk_table *table, const tk_reads *reads);
  * jellyfish counts `cat left.fa right.fa`, Trinity:1641). */
 int tk_table_add_reads_multi(tk_table *table, const tk_reads *const *sets, uint32_t n_sets);
 int tk_table_count_text(tk_table *table, const char *text, uint64_t len, int where);
+/* distinct k-mers (a scan of the table; pass NULL to skip it), occurrences
+ * added, slots. */
 int tk_table_info(tk_table *table, uint64_t *distinct, uint64_t *total, uint64_t *capacity);
 /* hist[0] = keys with count < low, hist[1 + c - low] for low <= c <= high,
  * hist[high - low + 2] = keys with count > high (high - low + 3 entries). */

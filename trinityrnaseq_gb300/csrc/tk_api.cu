@@ -7,6 +7,7 @@
 #include "tk_internal.cuh"
 
 #include <algorithm>
+#include <cctype>
 #include <cstring>
 #include <new>
 
@@ -36,21 +37,96 @@ int cuda_check(tk_ctx *c, cudaError_t e, const char *what) {
 
 int check_launch(tk_ctx *c, const char *what) { return cuda_check(c, cudaGetLastError(), what); }
 
+// Large blocks (tables, bucketed k-mers, texts, dump buffers) come from
+// cudaMalloc and, once freed, stay with the context for the next request of
+// about the same size.  Carving them out of the stream-ordered pool instead
+// left the pool's mapping fragmented after a few rounds of differently sized
+// requests, and the random-access kernels on a table placed in it ran 10%
+// slower (insert) to 45% slower (histogram and dump) from then on.  A freed
+// block may still be in use by work queued on the context's stream; it is only
+// handed out again to work queued on that same stream, after it.  Blocks
+// cached by all contexts of the process are capped at BIG_CACHE_MAX.
+constexpr size_t BIG_BLOCK = 256ull << 20;
+constexpr size_t BIG_CACHE_MAX = 96ull << 30;
+static std::atomic<size_t> g_big_cached{0};
+
+static void big_release(tk_ctx *c) {
+    if (c->big_free.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    for (auto &b : c->big_free) {
+        cudaFree(b.first);
+        g_big_cached -= b.second;
+    }
+    c->big_free.clear();
+}
+
+static int alloc_error(tk_ctx *c, cudaError_t e, size_t bytes, const char *what) {
+    cudaGetLastError();
+    return set_err(c, e == cudaErrorMemoryAllocation ? TK_E_OOM : TK_E_CUDA,
+                   std::string("device allocation of ") + std::to_string(bytes) + " bytes for " + what + ": " +
+                       cudaGetErrorString(e));
+}
+
 int dmalloc(tk_ctx *c, void **p, size_t bytes, const char *what) {
     *p = nullptr;
+    if (bytes >= BIG_BLOCK) {
+        int best = -1;
+        for (size_t i = 0; i < c->big_free.size(); i++) {
+            const size_t sz = c->big_free[i].second;
+            if (sz >= bytes && sz - bytes <= bytes / 2 && (best < 0 || sz < c->big_free[best].second)) best = (int)i;
+        }
+        if (best >= 0) {
+            *p = c->big_free[best].first;
+            const size_t sz = c->big_free[best].second;
+            c->big_free.erase(c->big_free.begin() + best);
+            g_big_cached -= sz;
+            c->big_used[*p] = sz;
+            return TK_OK;
+        }
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e == cudaErrorMemoryAllocation) {
+            // give back what this context caches and what the pool holds, then retry
+            cudaGetLastError();
+            big_release(c);
+            cudaStreamSynchronize(c->stream);
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+            e = cudaMalloc(p, bytes);
+        }
+        if (e != cudaSuccess) {
+            *p = nullptr;
+            return alloc_error(c, e, bytes, what);
+        }
+        c->big_used[*p] = bytes;
+        return TK_OK;
+    }
     cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, c->stream);
     if (e != cudaSuccess) {
-        cudaGetLastError();
         *p = nullptr;
-        return set_err(c, e == cudaErrorMemoryAllocation ? TK_E_OOM : TK_E_CUDA,
-                       std::string("device allocation of ") + std::to_string(bytes) + " bytes for " + what + ": " +
-                           cudaGetErrorString(e));
+        return alloc_error(c, e, bytes, what);
     }
     return TK_OK;
 }
 
 void dfree(tk_ctx *c, void *p) {
-    if (p) cudaFreeAsync(p, c->stream);
+    if (!p) return;
+    auto it = c->big_used.find(p);
+    if (it == c->big_used.end()) {
+        cudaFreeAsync(p, c->stream);
+        return;
+    }
+    const size_t sz = it->second;
+    c->big_used.erase(it);
+    if (g_big_cached + sz > BIG_CACHE_MAX) {
+        // over the cap: free it once the work queued before it is done
+        cudaStreamSynchronize(c->stream);
+        if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+        cudaFree(p);
+        return;
+    }
+    g_big_cached += sz;
+    c->big_free.push_back({p, sz});
 }
 
 static cudaEvent_t take_event(tk_ctx *c) {
@@ -239,6 +315,9 @@ void tk_ctx_destroy(tk_ctx *c) {
 static void ctx_release_now(tk_ctx *c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    big_release(c);
+    for (auto &b : c->big_used) cudaFree(b.first);   // none once every handle is freed
+    c->big_used.clear();
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamDestroy(c->copy_stream);
@@ -431,6 +510,54 @@ int tk_reads_parse_many(tk_ctx *c, const char *const *texts, const uint64_t *len
     }
     if (allocated) cudaEventDestroy(allocated);
     return e;
+}
+
+// ---- record-aligned split of a host text (host code only)
+
+// true when a FASTQ record starts at p (p is a line start holding '@'): the
+// line after its sequence line starts with '+'.  A quality line that starts
+// with '@' is followed by a header and a sequence line, so it fails the test.
+static bool fastq_record_at(const char *t, uint64_t len, uint64_t p) {
+    const void *e1 = std::memchr(t + p, '\n', len - p);
+    if (!e1) return false;
+    const uint64_t s2 = (uint64_t)((const char *)e1 - t) + 1;
+    if (s2 >= len) return false;
+    const void *e2 = std::memchr(t + s2, '\n', len - s2);
+    if (!e2) return false;
+    const uint64_t s3 = (uint64_t)((const char *)e2 - t) + 1;
+    return s3 < len && t[s3] == '+';
+}
+
+int tk_split_records(const char *text, uint64_t len, uint32_t n_chunks, uint64_t *cuts) {
+    if (!cuts || n_chunks == 0 || (!text && len)) return TK_E_INVAL;
+    uint64_t first = 0;
+    while (first < len && std::isspace((unsigned char)text[first])) first++;
+    const char mark = first < len && text[first] == '@' ? '@' : '>';
+    cuts[0] = 0;
+    uint64_t prev = 0;
+    for (uint32_t i = 1; i < n_chunks; i++) {
+        uint64_t p = std::max<uint64_t>(prev, len / n_chunks * i);
+        uint64_t cut = len;
+        while (p < len) {
+            // the next line start at or after p
+            if (p > 0 && text[p - 1] != '\n') {
+                const void *nl = std::memchr(text + p, '\n', len - p);
+                if (!nl) break;
+                p = (uint64_t)((const char *)nl - text) + 1;
+                continue;
+            }
+            if (p > first && text[p] == mark && (mark == '>' || fastq_record_at(text, len, p))) {
+                cut = p;
+                break;
+            }
+            const void *nl = std::memchr(text + p, '\n', len - p);
+            if (!nl) break;
+            p = (uint64_t)((const char *)nl - text) + 1;
+        }
+        cuts[i] = prev = cut;
+    }
+    cuts[n_chunks] = len;
+    return TK_OK;
 }
 
 int tk_reads_info(const tk_reads *r, uint64_t *n_reads, uint64_t *n_bases, uint32_t *max_len, int *format) {

@@ -19,6 +19,8 @@
 #include <stdint.h>
 #include <atomic>
 #include <string>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/trinkmer.h"
@@ -216,6 +218,9 @@ struct tk_ctx {
     uint64_t prof_units[TK_KID_NUM] = {0};
     uint64_t launches = 0;                  // every kernel launched by the library
     uint64_t prof_open[TK_KID_NUM] = {0};   // `launches` when each class's bracket opened
+    // blocks of >= 256 MB: cudaMalloc'd once and kept for reuse (see dmalloc)
+    std::vector<std::pair<void *, size_t>> big_free;
+    std::unordered_map<void *, size_t> big_used;
     int max_probes = 4096;
     int sm_count = 152;
     // read sets, tables and bundles alive on this context; tk_ctx_destroy

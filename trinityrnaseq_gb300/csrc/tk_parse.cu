@@ -26,9 +26,8 @@ constexpr uint64_t PT_TILE = (uint64_t)PT_THREADS * PT_BYTES;
 
 enum LineKind : uint8_t { LK_SKIP = 0, LK_HDR = 1, LK_SEQ = 2 };
 
-__device__ __forceinline__ bool is_ws(uint32_t c) {
-    return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\f' || c == '\v';
-}
+// ' ', '\t', '\n', '\v', '\f', '\r' (9..13)
+__device__ __forceinline__ bool is_ws(uint32_t c) { return c == ' ' || c - 9u < 5u; }
 
 struct Bytes32 {
     uint32_t w[8];
@@ -250,7 +249,7 @@ __global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end,
                         const uint32_t q = q0 + 32 * u + lane;
                         if (q < n[b]) {
                             ws |= is_ws(c[b][u]);
-                            seq[d0[b] + q] = (uint8_t)((c[b][u] >= 'a' && c[b][u] <= 'z') ? c[b][u] - 32u : c[b][u]);
+                            seq[d0[b] + q] = (uint8_t)(c[b][u] - 'a' < 26u ? c[b][u] - 32u : c[b][u]);
                         }
                     }
             }

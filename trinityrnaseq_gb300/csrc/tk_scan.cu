@@ -118,7 +118,7 @@ int scan_excl_u32_to_u64(tk_ctx *c, const uint32_t *in, uint64_t *out, uint64_t 
 // ------------------------------------------------------------------ radix sort
 
 constexpr int RS_THREADS = 256;
-constexpr int RS_ROUNDS = 16;                 // items per thread per tile
+constexpr int RS_ROUNDS = 8;                  // items per thread per tile
 constexpr int RS_BITS = 8;
 constexpr int RS_BINS = 1 << RS_BITS;
 constexpr uint64_t RS_TILE = (uint64_t)RS_THREADS * RS_ROUNDS;
@@ -139,12 +139,12 @@ __global__ void k_rs_hist(const uint64_t *__restrict__ keys, uint64_t n, int shi
     for (int i = threadIdx.x; i < RS_BINS; i += RS_THREADS) hist[(uint64_t)i * ntiles + blockIdx.x] = h[i];
 }
 
-// Stable scatter of one 4096-item tile.  Warp w ranks its 512 consecutive
-// items in 16 rounds of 32 (match.any inside a round, a per-warp running count
+// Stable scatter of one 2048-item tile.  Warp w ranks its 256 consecutive
+// items in 8 rounds of 32 (match.any inside a round, a per-warp running count
 // per digit in shared memory); a scan over (digit, warp) turns the ranks into
 // positions of a digit-sorted tile, which is laid out in shared memory and then
 // leaves as one run per digit, consecutive threads storing consecutive items
-// (runs of ~16 keys instead of one scattered 8-byte store per item).
+// (runs of ~8 keys instead of one scattered 8-byte store per item).
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_PER_LANE = RS_TILE / RS_THREADS;   // rounds per warp
 constexpr size_t RS_SMEM = (size_t)RS_WARPS * RS_BINS * 4 + RS_BINS * 4 + RS_BINS * 8 + RS_TILE * 8 + RS_TILE * 4;

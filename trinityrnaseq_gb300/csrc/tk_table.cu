@@ -31,7 +31,9 @@ constexpr int INS_PER_THREAD = 1;
 // SC_BUF keys per bucket in shared memory between flushes
 constexpr int SC_THREADS = 512;
 constexpr int SC_BUF = 24;                                       // a multiple of 4 (whole 32-byte sectors)
+static_assert(SC_BUF % 4 == 0 && SC_BUF <= 32, "a half-warp flushes a bucket in two 16-key stores");
 constexpr int SC_BUCKETS_PER_WARP = NBUCKETS / (SC_THREADS / 32);
+static_assert((NBUCKETS / (SC_THREADS / 32)) % 2 == 0, "buckets are flushed in pairs");
 constexpr size_t SC_SMEM = (size_t)NBUCKETS * SC_BUF * 8 + (size_t)NBUCKETS * 8 + (size_t)NBUCKETS * 4;
 constexpr uint64_t INS_CHUNK = (uint64_t)CT_THREADS * INS_PER_THREAD;
 enum NextMode { NEXT_NONE = 0, NEXT_FILL = 1, NEXT_PREFETCH = 2 };
@@ -161,22 +163,26 @@ __global__ void __launch_bounds__(SC_THREADS, 1) k_part_scatter(const uint64_t *
             else keys[gpos[b] + r] = key;
         });
         __syncthreads();
-        for (int i = 0; i < SC_BUCKETS_PER_WARP; i++) {
-            const int b = warp * SC_BUCKETS_PER_WARP + i;
+        // two buckets per step, one per half-warp
+        const unsigned hl = lane & 15u;
+        for (int i = 0; i < SC_BUCKETS_PER_WARP; i += 2) {
+            const int b = warp * SC_BUCKETS_PER_WARP + i + (int)(lane >> 4);
             const uint32_t nk = cnt[b];
             const uint32_t full = nk & ~3u;
             const uint64_t g = gpos[b];
             const uint64_t *bb = buf + (size_t)b * SC_BUF;
-            if (lane < min(full, (uint32_t)SC_BUF)) keys[g + lane] = bb[lane];
+            const uint32_t nb = min(full, (uint32_t)SC_BUF);
+            if (hl < nb) keys[g + hl] = bb[hl];
+            if (hl + 16 < nb) keys[g + hl + 16] = bb[hl + 16];
             const uint32_t tail = nk - full;
             uint64_t v = 0;
-            if (lane < tail) {
-                const uint32_t idx = full + lane;
+            if (hl < tail) {
+                const uint32_t idx = full + hl;
                 v = idx < SC_BUF ? bb[idx] : __ldcg(keys + g + idx);
             }
             __syncwarp();
-            if (lane < tail) buf[(size_t)b * SC_BUF + lane] = v;
-            if (lane == 0) {
+            if (hl < tail) buf[(size_t)b * SC_BUF + hl] = v;
+            if (hl == 0) {
                 cnt[b] = tail;
                 gpos[b] = g + full;
             }
@@ -750,8 +756,10 @@ static int table_distinct(tk_table *t) {
 }
 
 int table_info(tk_table *t, uint64_t *distinct, uint64_t *total, uint64_t *capacity) {
-    TK_TRY(table_distinct(t));
-    if (distinct) *distinct = t->distinct;
+    if (distinct) {
+        TK_TRY(table_distinct(t));   // a scan of the table, only when asked for
+        *distinct = t->distinct;
+    }
     if (total) *total = t->total;
     if (capacity) *capacity = t->capacity;
     return TK_OK;

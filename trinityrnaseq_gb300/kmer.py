@@ -33,6 +33,18 @@ def _host_ptr(buf: Buffer) -> Tuple[int, int, object]:
     raise TypeError(f"unsupported buffer type {type(buf)}")
 
 
+def split_records(text: Buffer, n_chunks: int) -> list:
+    """n_chunks + 1 record-aligned cut offsets of a host FASTA/FASTQ text
+    (tk_split_records; host code, no GPU needed)."""
+    lib = N.load()
+    ptr, n, keep = _host_ptr(text)
+    cuts = (C.c_uint64 * (n_chunks + 1))()
+    st = lib.tk_split_records(C.c_void_p(ptr), n, n_chunks, cuts)
+    if st != N.TK_OK:
+        raise N.TrinkmerError(st, "tk_split_records")
+    return list(cuts)
+
+
 class Context:
     """A CUDA device context with its own stream (tk_ctx)."""
 
@@ -223,10 +235,13 @@ class KmerTable:
         ptr, n, keep = _host_ptr(text)
         self.ctx.check(self.lib.tk_table_count_text(self.h, C.c_void_p(ptr), n, N.TK_HOST), "tk_table_count_text")
 
-    def info(self) -> Tuple[int, int, int]:
+    def info(self, distinct: bool = True) -> Tuple[int, int, int]:
+        """(distinct k-mers, occurrences added, slots); distinct=False skips the
+        table scan that counts distinct k-mers and reports -1."""
         d, t, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        self.ctx.check(self.lib.tk_table_info(self.h, C.byref(d), C.byref(t), C.byref(c)), "tk_table_info")
-        return d.value, t.value, c.value
+        self.ctx.check(self.lib.tk_table_info(self.h, C.byref(d) if distinct else None, C.byref(t), C.byref(c)),
+                       "tk_table_info")
+        return (d.value if distinct else -1), t.value, c.value
 
     def histo(self, low: int = 1, high: int = 10000) -> np.ndarray:
         h = np.zeros(high - low + 3, dtype=np.uint64)
