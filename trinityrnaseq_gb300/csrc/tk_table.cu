@@ -276,6 +276,201 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_step(const uint64_t *__rest
     }
 }
 
+// ---- pass 2 by ranges (slices of at least 2^SR_BITS slots).  Per partition
+// p the keys are regrouped by the 4096-slot range of the slice their home slot
+// falls in (k_sr_hist, k_sr_scatter), and one block per range then
+// builds that range in shared memory (k_sr_build): it loads the range (all
+// empty on a fresh table), inserts the range's keys with shared-memory CAS
+// and add, and writes the range back whole.  A key whose probe run reaches the
+// end of its range (its chain goes on into the next range, which another block
+// owns) is merged into a small per-block table and then appended with its
+// multiplicity to a deferred list that is inserted into the global table once
+// every range is written; the global probe order (home, home+1, ... wrapping
+// in the slice) is the one every reader uses, so the layout is an ordinary
+// linear-probing table.  Global atomics drop from two per occurrence to the
+// deferred keys alone, and a fresh slice needs no separate fill.
+constexpr int SR_BITS = 12;
+constexpr int SR_SLOTS = 1 << SR_BITS;
+constexpr int SR_THREADS = 1024;        // regrouping passes (2 blocks per SM: few per-block range counts)
+constexpr int SR_BUILD_THREADS = 512;
+constexpr int SR_MINI = 256;
+constexpr size_t SR_SMEM = (size_t)(SR_SLOTS + SR_MINI) * sizeof(Slot);
+
+__device__ __forceinline__ uint32_t key_range(const DevTable &t, uint64_t key) {
+    return (uint32_t)((mix64(key) & t.lmask) >> SR_BITS);
+}
+
+// Keys [ps, pe) split evenly over the blocks.  Per block, keys per range
+// (counts[range * gridDim.x + block]) and, summed over blocks, per range
+// (totals, zeroed beforehand).
+__global__ void __launch_bounds__(SR_THREADS) k_sr_hist(const uint64_t *__restrict__ keys, uint64_t ps, uint64_t pe,
+                                                       DevTable t, uint32_t nsub, uint32_t *__restrict__ counts,
+                                                       uint32_t *__restrict__ totals) {
+    extern __shared__ uint32_t sr_h[];
+    for (uint32_t i = threadIdx.x; i < nsub; i += SR_THREADS) sr_h[i] = 0;
+    __syncthreads();
+    const uint64_t chunk = (pe - ps + gridDim.x - 1) / gridDim.x;
+    const uint64_t lo = ps + (uint64_t)blockIdx.x * chunk, hi = min(pe, lo + chunk);
+    for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += 4 * SR_THREADS) {
+        uint64_t k4[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint64_t i = i0 + (uint64_t)u * SR_THREADS;
+            k4[u] = i < hi ? __ldcs(keys + i) : EMPTY_KEY;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (k4[u] != EMPTY_KEY) atomicAdd(&sr_h[key_range(t, k4[u])], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nsub; i += SR_THREADS) {
+        counts[(uint64_t)i * gridDim.x + blockIdx.x] = sr_h[i];
+        if (sr_h[i]) atomicAdd(&totals[i], sr_h[i]);
+    }
+}
+
+// exclusive prefix of totals[0..nsub) into out[0..nsub) (block-wide scan;
+// thread t sums a run of consecutive ranges)
+__device__ __forceinline__ void range_starts(const uint32_t *__restrict__ totals, uint32_t nsub, uint64_t *out) {
+    __shared__ uint64_t sm[SR_THREADS / 32 + 1];
+    const uint32_t per = (nsub + SR_THREADS - 1) / SR_THREADS;
+    const uint32_t lo = min(nsub, threadIdx.x * per), hi = min(nsub, lo + per);
+    uint64_t sum = 0;
+    for (uint32_t j = lo; j < hi; j++) sum += totals[j];
+    uint64_t tot;
+    uint64_t run = block_excl_scan<uint64_t>(sum, sm, &tot);
+    for (uint32_t j = lo; j < hi; j++) {
+        out[j] = run;
+        run += totals[j];
+    }
+    __syncthreads();
+}
+
+// The same keys into range order: each block reserves its share of every
+// range with one atomic on the range's cursor, then places its keys there.
+__global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__restrict__ keys, uint64_t ps, uint64_t pe,
+                                                          DevTable t, uint32_t nsub, const uint32_t *__restrict__ counts,
+                                                          const uint32_t *__restrict__ totals,
+                                                          unsigned long long *__restrict__ cursor,
+                                                          uint64_t *__restrict__ range_keys) {
+    extern __shared__ unsigned long long sr_base[];   // [nsub] this block's first position per range
+    uint32_t *sr_cur = reinterpret_cast<uint32_t *>(sr_base + nsub);   // [nsub] keys placed so far
+    range_starts(totals, nsub, reinterpret_cast<uint64_t *>(sr_base));
+    for (uint32_t i = threadIdx.x; i < nsub; i += SR_THREADS) {
+        const uint32_t mine = counts[(uint64_t)i * gridDim.x + blockIdx.x];
+        if (mine) sr_base[i] += atomicAdd(&cursor[i], (unsigned long long)mine);
+        sr_cur[i] = 0;
+    }
+    __syncthreads();
+    const uint64_t chunk = (pe - ps + gridDim.x - 1) / gridDim.x;
+    const uint64_t lo = ps + (uint64_t)blockIdx.x * chunk, hi = min(pe, lo + chunk);
+    for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += 4 * SR_THREADS) {
+        uint64_t k4[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint64_t i = i0 + (uint64_t)u * SR_THREADS;
+            k4[u] = i < hi ? __ldcs(keys + i) : EMPTY_KEY;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (k4[u] == EMPTY_KEY) continue;
+            const uint32_t r = key_range(t, k4[u]);
+            range_keys[sr_base[r] + atomicAdd(&sr_cur[r], 1u)] = k4[u];
+        }
+    }
+}
+
+// shared-memory probe from `loc` up to `end`; adds `inc` where the key lives
+// or lands.  A slot's key never changes once set, so a plain load that sees the
+// key (most occurrences repeat a key already placed) needs only the add; an
+// empty slot is claimed with CAS.  Returns false if the probe ran off the end.
+__device__ __forceinline__ bool smem_add(Slot *tab, uint32_t loc, uint32_t end, uint64_t key, uint32_t inc) {
+    for (; loc < end; loc++) {
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&tab[loc].key);
+        if (cur == EMPTY_KEY) cur = atomicCAS(&tab[loc].key, EMPTY_KEY, (unsigned long long)key);
+        if (cur == EMPTY_KEY || cur == key) {
+            atomicAdd(&tab[loc].val, inc);
+            return true;
+        }
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *__restrict__ range_keys,
+                                                        const uint32_t *__restrict__ totals, uint32_t nsub, int p,
+                                                        DevTable t, int fresh, uint32_t *__restrict__ next_totals,
+                                                        unsigned long long *__restrict__ next_cursor,
+                                                        uint64_t *__restrict__ defer_keys, uint32_t *__restrict__ defer_cnt,
+                                                        uint64_t defer_cap, unsigned long long *__restrict__ defer_n) {
+    extern __shared__ __align__(16) unsigned char sr_smem[];
+    Slot *tab = reinterpret_cast<Slot *>(sr_smem);
+    Slot *mini = tab + SR_SLOTS;
+    __shared__ uint64_t ab[2];
+    const uint32_t r = blockIdx.x;
+    if (r == 0) {
+        // the next partition's range counters (their last users finished before this launch)
+        for (uint32_t i = threadIdx.x; i < nsub; i += SR_BUILD_THREADS) {
+            next_totals[i] = 0;
+            next_cursor[i] = 0;
+        }
+    }
+    {
+        // this range's keys: [start, start + total) of the range-ordered buffer
+        uint64_t sum = 0;
+        for (uint32_t i = threadIdx.x; i < r; i += SR_BUILD_THREADS) sum += totals[i];
+        sum = warp_sum(sum);
+        __shared__ uint64_t part[SR_BUILD_THREADS / 32];
+        if (lane_id() == 0) part[threadIdx.x >> 5] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t a = 0;
+            for (int w = 0; w < SR_BUILD_THREADS / 32; w++) a += part[w];
+            ab[0] = a;
+            ab[1] = a + totals[r];
+        }
+    }
+    ulonglong2 *g = reinterpret_cast<ulonglong2 *>(t.slots + ((uint64_t)p << t.lbits) + ((uint64_t)r << SR_BITS));
+    ulonglong2 *st = reinterpret_cast<ulonglong2 *>(tab);
+    ulonglong2 e;
+    e.x = EMPTY_KEY;
+    e.y = 0;
+    for (int i = threadIdx.x; i < SR_SLOTS; i += SR_BUILD_THREADS) st[i] = fresh ? e : g[i];
+    for (int i = threadIdx.x; i < SR_MINI; i += SR_BUILD_THREADS) reinterpret_cast<ulonglong2 *>(mini)[i] = e;
+    __syncthreads();
+    const uint64_t a = ab[0], b = ab[1];
+    for (uint64_t i0 = a + threadIdx.x; i0 < b; i0 += 4 * SR_BUILD_THREADS) {
+        uint64_t k4[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint64_t i = i0 + (uint64_t)u * SR_BUILD_THREADS;
+            k4[u] = i < b ? __ldcs(range_keys + i) : EMPTY_KEY;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint64_t key = k4[u];
+            if (key == EMPTY_KEY || smem_add(tab, (uint32_t)(mix64(key) & (SR_SLOTS - 1)), SR_SLOTS, key, 1u)) continue;
+            // the probe left the range: count it in the per-block table, or defer it singly
+            const uint32_t m = (uint32_t)(mix64(key ^ 0x5851F42D4C957F2DULL) & (SR_MINI - 1));
+            if (smem_add(mini, m, SR_MINI, key, 1u) || (m && smem_add(mini, 0, m, key, 1u))) continue;
+            const unsigned long long j = atomicAdd(defer_n, 1ULL);
+            if (j < defer_cap) {
+                defer_keys[j] = key;
+                defer_cnt[j] = 1u;
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < SR_SLOTS; i += SR_BUILD_THREADS) g[i] = st[i];
+    for (int i = threadIdx.x; i < SR_MINI; i += SR_BUILD_THREADS) {
+        if (mini[i].key == EMPTY_KEY) continue;
+        const unsigned long long j = atomicAdd(defer_n, 1ULL);
+        if (j < defer_cap) {
+            defer_keys[j] = mini[i].key;
+            defer_cnt[j] = mini[i].val;
+        }
+    }
+}
+
 __global__ void k_rehash(const Slot *__restrict__ old, uint64_t old_cap, DevTable t, int max_probes,
                          uint64_t *__restrict__ ovf_keys, uint32_t *__restrict__ ovf_cnt, uint64_t ovf_cap,
                          unsigned long long *__restrict__ counters) {
@@ -606,6 +801,107 @@ static uint64_t pow2_at_least(uint64_t x) {
     return p;
 }
 
+// Pass 2 with global atomics, one partition after another: a launch prepares
+// slice p (fills a fresh slice, or prefetches a filled one to L2), then a
+// launch CAS-probes and adds partition p's keys into it.  Preparing slice p+1
+// inside the insert of p instead (the writes of one slice competing in L2 with
+// the atomics on the other) measured ~12% slower.
+static int count_by_atomics(tk_table *t, const uint64_t *keys, const uint64_t *offs, uint64_t cols) {
+    tk_ctx *c = t->ctx;
+    const int nparts = 1 << t->t.pbits;
+    const int mode = t->fresh ? NEXT_FILL : (t->t.pbits > 0 ? NEXT_PREFETCH : NEXT_NONE);
+    const unsigned igrid = (unsigned)c->sm_count * 8;
+    for (int p = 0; p < nparts; p++) {
+        if (mode != NEXT_NONE) {
+            k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(keys, offs, cols, -1, p, t->t, mode, c->max_probes,
+                                                             t->d_ovf, (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
+                                                             t->d_counters);
+            c->launches++;
+        }
+        k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(keys, offs, cols, p, -1, t->t, mode, c->max_probes, t->d_ovf,
+                                                         (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap, t->d_counters);
+        c->launches++;
+    }
+    return check_launch(c, "count insert");
+}
+
+// Pass 2 by ranges on a fresh table (see k_sr_build).  *done is false when
+// the deferred list overran its capacity: the table is then emptied again and
+// the caller counts with count_by_atomics instead, so nothing is lost.
+static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *offs, uint64_t cols, bool *done) {
+    tk_ctx *c = t->ctx;
+    *done = false;
+    const int nparts = 1 << t->t.pbits;
+    const uint32_t nsub = 1u << (t->t.lbits - SR_BITS);
+    const uint64_t bpp = (uint64_t)(NBUCKETS >> t->t.pbits);
+    // partition boundaries on the host: the first offset of each partition's buckets
+    std::vector<uint64_t> pb(nparts + 1);
+    TK_CUDA(c, cudaMemcpy2DAsync(pb.data(), 8, offs, bpp * cols * 8, 8, nparts + 1, cudaMemcpyDeviceToHost, c->stream));
+    TK_CUDA(c, cudaStreamSynchronize(c->stream));
+    uint64_t max_part = 0;
+    for (int p = 0; p < nparts; p++) max_part = std::max(max_part, pb[p + 1] - pb[p]);
+    const unsigned G = (unsigned)c->sm_count * 2;   // blocks of the regrouping passes
+    const uint64_t cells = (uint64_t)nsub * G;
+    const uint64_t defer_cap = std::max<uint64_t>(1u << 16, std::min<uint64_t>(pb[nparts] / 64, 1u << 24));
+    uint64_t *range_keys = nullptr, *defer_keys = nullptr;
+    uint32_t *counts = nullptr, *defer_cnt = nullptr, *totals = nullptr;
+    unsigned long long *defer_n = nullptr, *cursor = nullptr;
+    int e = dmalloc(c, (void **)&range_keys, std::max<uint64_t>(max_part, 1) * 8, "range keys");
+    if (!e) e = dmalloc(c, (void **)&counts, cells * 4, "range counts");
+    if (!e) e = dmalloc(c, (void **)&totals, 2ull * nsub * 4, "range totals");
+    if (!e) e = dmalloc(c, (void **)&cursor, 2ull * nsub * 8, "range cursors");
+    if (!e) e = dmalloc(c, (void **)&defer_keys, defer_cap * 8, "deferred keys");
+    if (!e) e = dmalloc(c, (void **)&defer_cnt, defer_cap * 4, "deferred counts");
+    if (!e) e = dmalloc(c, (void **)&defer_n, 8, "deferred count");
+    if (!e) e = cuda_check(c, cudaMemsetAsync(defer_n, 0, 8, c->stream), "defer reset");
+    if (!e) e = cuda_check(c, cudaMemsetAsync(totals, 0, 2ull * nsub * 4, c->stream), "totals reset");
+    if (!e) e = cuda_check(c, cudaMemsetAsync(cursor, 0, 2ull * nsub * 8, c->stream), "cursor reset");
+    if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_sr_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SR_SMEM),
+                           "range build smem");
+    for (int p = 0; !e && p < nparts; p++) {
+        const uint64_t ps = pb[p], pe = pb[p + 1];
+        uint32_t *tot = totals + (uint64_t)(p & 1) * nsub, *tot_next = totals + (uint64_t)((p + 1) & 1) * nsub;
+        unsigned long long *cur = cursor + (uint64_t)(p & 1) * nsub, *cur_next = cursor + (uint64_t)((p + 1) & 1) * nsub;
+        if (pe > ps) {
+            k_sr_hist<<<G, SR_THREADS, nsub * 4, c->stream>>>(keys, ps, pe, t->t, nsub, counts, tot);
+            k_sr_scatter<<<G, SR_THREADS, nsub * 12, c->stream>>>(keys, ps, pe, t->t, nsub, counts, tot, cur, range_keys);
+            c->launches += 2;
+        }
+        k_sr_build<<<nsub, SR_BUILD_THREADS, SR_SMEM, c->stream>>>(range_keys, tot, nsub, p, t->t, 1, tot_next, cur_next,
+                                                             defer_keys, defer_cnt, defer_cap, defer_n);
+        c->launches++;
+    }
+    unsigned long long nd = 0;
+    if (!e) e = check_launch(c, "range build");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(&nd, defer_n, 8, cudaMemcpyDeviceToHost, c->stream), "defer d2h");
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "defer sync");
+    if (!e && nd > defer_cap) {
+        // the deferred list overran: empty the table again and count with atomics
+        k_fill_empty<<<stream_grid(c, t->capacity, 256), 256, 0, c->stream>>>(t->t.slots, t->capacity, 0);
+        c->launches++;
+        t->fresh = false;
+        e = check_launch(c, "table refill");
+    } else if (!e) {
+        t->fresh = false;
+        if (nd) {
+            k_insert_pairs<<<stream_grid(c, nd, 256), 256, 0, c->stream>>>(defer_keys, defer_cnt, nd, t->t, c->max_probes,
+                                                                            t->d_ovf, (uint32_t *)(t->d_ovf + t->ovf_cap),
+                                                                            t->ovf_cap, t->d_counters);
+            c->launches++;
+            e = check_launch(c, "deferred insert");
+        }
+        if (!e) *done = true;
+    }
+    dfree(c, range_keys);
+    dfree(c, counts);
+    dfree(c, totals);
+    dfree(c, cursor);
+    dfree(c, defer_keys);
+    dfree(c, defer_cnt);
+    dfree(c, defer_n);
+    return e;
+}
+
 // Counts every window of one or more packed read arrays into the table in a
 // single partitioned pass (the table is touched once for all of them).
 int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
@@ -686,25 +982,9 @@ int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
         if (!e) e = check_launch(c, "bucket scatter");
         if (!e) e = overflow_reset(t);
         prof_begin(c, TK_KID_COUNT, &ev);
-        // pass 2: one launch per partition, slice p+1 prepared while p is filled
-        const int nparts = 1 << t->t.pbits;
-        const int mode = t->fresh ? NEXT_FILL : (t->t.pbits > 0 ? NEXT_PREFETCH : NEXT_NONE);
-        // Slice p is prepared by a launch of its own just before partition p is
-        // inserted: preparing slice p+1 inside the insert of p (the writes of
-        // one slice competing in L2 with the atomics on the other) measured
-        // ~12% slower.
-        const unsigned igrid = (unsigned)c->sm_count * 8;
-        for (int p = 0; !e && p < nparts; p++) {
-            if (mode != NEXT_NONE) {
-                k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(keys, offs, cols, -1, p, t->t, mode, c->max_probes,
-                                                                 t->d_ovf, (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
-                                                                 t->d_counters);
-                c->launches++;
-            }
-            k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(keys, offs, cols, p, -1, t->t, mode, c->max_probes, t->d_ovf,
-                                                             (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap, t->d_counters);
-            c->launches++;
-        }
+        bool done = false;
+        if (!e && t->fresh && t->t.lbits >= SR_BITS) e = count_by_ranges(t, keys, offs, cols, &done);
+        if (!e && !done) e = count_by_atomics(t, keys, offs, cols);
         prof_end(c, TK_KID_COUNT, ev, windows);
         if (!e) e = check_launch(c, "count insert");
         if (!e) t->fresh = false;
