@@ -161,3 +161,26 @@ def test_bad_dump_is_an_error(ctx):
     with pytest.raises(native.TrinkmerError) as ei:
         t.load_dump_fasta(b">3\nACGTACGTACGTACGTACGTACGTA\n>x\nACGTACGTACGTACGTACGTACGTA\n")
     assert ei.value.status == native.TK_E_PARSE
+
+
+def test_range_build_fallback_when_deferred_list_overruns(native_built, oracle):
+    """A fresh table is built range by range in shared memory; keys whose probe
+    leaves their range are deferred.  With the deferred list capped at one
+    entry the build overruns it, the table is emptied and counted with global
+    atomics instead: the result must not change."""
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np, sys\n"
+        "from trinityrnaseq_gb300 import Context, KmerTable, synth\n"
+        "left, right = synth.gene_pairs(seed=41, n_genes=2000, n_pairs=300000, fastq=False)\n"
+        "t = KmerTable(Context(0), 25, True)\n"
+        "t.count_text(left.tobytes() + right.tobytes())\n"
+        "sys.stdout.buffer.write(t.dump_fasta(1))\n")
+    env = dict(os.environ, TRINKMER_DEFER_CAP="1")
+    capped = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, timeout=600)
+    assert capped.returncode == 0, capped.stderr[-2000:]
+    left, right = synth.gene_pairs(seed=41, n_genes=2000, n_pairs=300000, fastq=False)
+    keys, counts = oracle.count(left.tobytes() + right.tobytes(), 25, True)
+    assert capped.stdout == oracle.dump(keys, counts, 25, 1)

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 namespace tk {
 
@@ -842,7 +843,8 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     for (int p = 0; p < nparts; p++) max_part = std::max(max_part, pb[p + 1] - pb[p]);
     const unsigned G = (unsigned)c->sm_count * 2;   // blocks of the regrouping passes
     const uint64_t cells = (uint64_t)nsub * G;
-    const uint64_t defer_cap = std::max<uint64_t>(1u << 16, std::min<uint64_t>(pb[nparts] / 64, 1u << 24));
+    uint64_t defer_cap = std::max<uint64_t>(1u << 16, std::min<uint64_t>(pb[nparts] / 64, 1u << 24));
+    if (const char *v = getenv("TRINKMER_DEFER_CAP")) defer_cap = std::max<uint64_t>(1, strtoull(v, nullptr, 10));   // tests: force the fallback
     uint64_t *range_keys = nullptr, *defer_keys = nullptr;
     uint32_t *counts = nullptr, *defer_cnt = nullptr, *totals = nullptr;
     unsigned long long *defer_n = nullptr, *cursor = nullptr;
