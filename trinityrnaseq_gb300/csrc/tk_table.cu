@@ -302,8 +302,8 @@ __device__ __forceinline__ uint32_t key_range(const DevTable &t, uint64_t key) {
 }
 
 // Keys [ps, pe) split evenly over the blocks.  Per block, keys per range
-// (counts[range * gridDim.x + block]) and, summed over blocks, per range
-// (totals, zeroed beforehand).
+// (counts[range * gridDim.x + block]) and, summed over blocks after rounding
+// each up to a multiple of 4, per range (totals, zeroed beforehand).
 __global__ void __launch_bounds__(SR_THREADS) k_sr_hist(const uint64_t *__restrict__ keys, uint64_t ps, uint64_t pe,
                                                        DevTable t, uint32_t nsub, uint32_t *__restrict__ counts,
                                                        uint32_t *__restrict__ totals) {
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_sr_hist(const uint64_t *__restri
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < nsub; i += SR_THREADS) {
         counts[(uint64_t)i * gridDim.x + blockIdx.x] = sr_h[i];
-        if (sr_h[i]) atomicAdd(&totals[i], sr_h[i]);
+        if (sr_h[i]) atomicAdd(&totals[i], (sr_h[i] + 3u) & ~3u);   // each block's run padded to whole sectors
     }
 }
 
@@ -347,20 +347,42 @@ __device__ __forceinline__ void range_starts(const uint32_t *__restrict__ totals
     __syncthreads();
 }
 
-// The same keys into range order: each block reserves its share of every
-// range with one atomic on the range's cursor, then places its keys there.
+// The same keys into range order.  Each block reserves its share of every
+// range (rounded up to whole 32-byte sectors) with one atomic on the range's
+// cursor, counting-sorts its chunk by range in shared memory, and writes each
+// range's run as whole sectors, the rounding filled with EMPTY_KEY (the build
+// skips it).  Scattered single-key stores instead cost one L2 request per key.
+constexpr int SRS_MAX = 12288;   // keys of one block's chunk (the host sizes the grid to fit)
+static inline size_t SRS_SMEM(uint32_t nsub) { return (size_t)SRS_MAX * 8 + (size_t)nsub * 16; }
+
 __global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__restrict__ keys, uint64_t ps, uint64_t pe,
                                                           DevTable t, uint32_t nsub, const uint32_t *__restrict__ counts,
                                                           const uint32_t *__restrict__ totals,
                                                           unsigned long long *__restrict__ cursor,
                                                           uint64_t *__restrict__ range_keys) {
-    extern __shared__ unsigned long long sr_base[];   // [nsub] this block's first position per range
-    uint32_t *sr_cur = reinterpret_cast<uint32_t *>(sr_base + nsub);   // [nsub] keys placed so far
-    range_starts(totals, nsub, reinterpret_cast<uint64_t *>(sr_base));
-    for (uint32_t i = threadIdx.x; i < nsub; i += SR_THREADS) {
-        const uint32_t mine = counts[(uint64_t)i * gridDim.x + blockIdx.x];
-        if (mine) sr_base[i] += atomicAdd(&cursor[i], (unsigned long long)mine);
-        sr_cur[i] = 0;
+    extern __shared__ __align__(16) unsigned char srs_smem[];
+    uint64_t *skeys = reinterpret_cast<uint64_t *>(srs_smem);                          // [SRS_MAX]
+    unsigned long long *gbase = reinterpret_cast<unsigned long long *>(skeys + SRS_MAX);  // [nsub]
+    uint32_t *lstart = reinterpret_cast<uint32_t *>(gbase + nsub);                      // [nsub]
+    uint32_t *lcur = lstart + nsub;                                                      // [nsub]
+    __shared__ uint32_t sm[SR_THREADS / 32 + 1];
+    range_starts(totals, nsub, reinterpret_cast<uint64_t *>(gbase));
+    // this block's run of every range, and where its keys sit in shared memory
+    const uint32_t per = (nsub + SR_THREADS - 1) / SR_THREADS;
+    const uint32_t lo_r = min(nsub, threadIdx.x * per), hi_r = min(nsub, lo_r + per);
+    uint32_t sum = 0;
+    for (uint32_t r = lo_r; r < hi_r; r++) {
+        const uint32_t mine = counts[(uint64_t)r * gridDim.x + blockIdx.x];
+        if (mine) gbase[r] += atomicAdd(&cursor[r], (unsigned long long)((mine + 3u) & ~3u));
+        lcur[r] = mine;
+        sum += mine;
+    }
+    uint32_t tot;
+    uint32_t run = block_excl_scan<uint32_t>(sum, sm, &tot);
+    for (uint32_t r = lo_r; r < hi_r; r++) {
+        lstart[r] = run;
+        run += lcur[r];
+        lcur[r] = 0;
     }
     __syncthreads();
     const uint64_t chunk = (pe - ps + gridDim.x - 1) / gridDim.x;
@@ -376,8 +398,17 @@ __global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__res
         for (int u = 0; u < 4; u++) {
             if (k4[u] == EMPTY_KEY) continue;
             const uint32_t r = key_range(t, k4[u]);
-            range_keys[sr_base[r] + atomicAdd(&sr_cur[r], 1u)] = k4[u];
+            skeys[lstart[r] + atomicAdd(&lcur[r], 1u)] = k4[u];
         }
+    }
+    __syncthreads();
+    // one warp per range at a time: consecutive lanes store consecutive keys
+    const unsigned lane = lane_id();
+    for (uint32_t r = threadIdx.x >> 5; r < nsub; r += SR_THREADS / 32) {
+        const uint32_t n = lcur[r], n4 = (n + 3u) & ~3u;
+        const uint64_t g = gbase[r];
+        const uint32_t l0 = lstart[r];
+        for (uint32_t j = lane; j < n4; j += 32) range_keys[g + j] = j < n ? skeys[l0 + j] : EMPTY_KEY;
     }
 }
 
@@ -841,14 +872,17 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     TK_CUDA(c, cudaStreamSynchronize(c->stream));
     uint64_t max_part = 0;
     for (int p = 0; p < nparts; p++) max_part = std::max(max_part, pb[p + 1] - pb[p]);
-    const unsigned G = (unsigned)c->sm_count * 2;   // blocks of the regrouping passes
+    // blocks of the regrouping passes: two per SM, more if a block's chunk
+    // would not fit in the scatter's shared memory
+    const unsigned G = (unsigned)std::max<uint64_t>((uint64_t)c->sm_count * 2, (max_part + SRS_MAX - 1) / SRS_MAX);
     const uint64_t cells = (uint64_t)nsub * G;
     uint64_t defer_cap = std::max<uint64_t>(1u << 16, std::min<uint64_t>(pb[nparts] / 64, 1u << 24));
     if (const char *v = getenv("TRINKMER_DEFER_CAP")) defer_cap = std::max<uint64_t>(1, strtoull(v, nullptr, 10));   // tests: force the fallback
     uint64_t *range_keys = nullptr, *defer_keys = nullptr;
     uint32_t *counts = nullptr, *defer_cnt = nullptr, *totals = nullptr;
     unsigned long long *defer_n = nullptr, *cursor = nullptr;
-    int e = dmalloc(c, (void **)&range_keys, std::max<uint64_t>(max_part, 1) * 8, "range keys");
+    // a partition's keys plus the sector rounding of every (range, block) run
+    int e = dmalloc(c, (void **)&range_keys, (max_part + 3 * cells + 1) * 8, "range keys");
     if (!e) e = dmalloc(c, (void **)&counts, cells * 4, "range counts");
     if (!e) e = dmalloc(c, (void **)&totals, 2ull * nsub * 4, "range totals");
     if (!e) e = dmalloc(c, (void **)&cursor, 2ull * nsub * 8, "range cursors");
@@ -860,13 +894,15 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     if (!e) e = cuda_check(c, cudaMemsetAsync(cursor, 0, 2ull * nsub * 8, c->stream), "cursor reset");
     if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_sr_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SR_SMEM),
                            "range build smem");
+    if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_sr_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)SRS_SMEM(nsub)), "range scatter smem");
     for (int p = 0; !e && p < nparts; p++) {
         const uint64_t ps = pb[p], pe = pb[p + 1];
         uint32_t *tot = totals + (uint64_t)(p & 1) * nsub, *tot_next = totals + (uint64_t)((p + 1) & 1) * nsub;
         unsigned long long *cur = cursor + (uint64_t)(p & 1) * nsub, *cur_next = cursor + (uint64_t)((p + 1) & 1) * nsub;
         if (pe > ps) {
             k_sr_hist<<<G, SR_THREADS, nsub * 4, c->stream>>>(keys, ps, pe, t->t, nsub, counts, tot);
-            k_sr_scatter<<<G, SR_THREADS, nsub * 12, c->stream>>>(keys, ps, pe, t->t, nsub, counts, tot, cur, range_keys);
+            k_sr_scatter<<<G, SR_THREADS, SRS_SMEM(nsub), c->stream>>>(keys, ps, pe, t->t, nsub, counts, tot, cur, range_keys);
             c->launches += 2;
         }
         k_sr_build<<<nsub, SR_BUILD_THREADS, SR_SMEM, c->stream>>>(range_keys, tot, nsub, p, t->t, 1, tot_next, cur_next,
@@ -1071,6 +1107,13 @@ int table_histo(tk_table *t, uint64_t low, uint64_t high, uint64_t *hist) {
     if (!e) e = cuda_check(c, cudaMemcpyAsync(hist, d, nb * 8, cudaMemcpyDeviceToHost, c->stream), "histo d2h");
     if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "histo sync");
     dfree(c, d);
+    if (!e) {
+        // every occupied slot fell in one bin: the bins add up to the distinct k-mers
+        uint64_t distinct = 0;
+        for (uint64_t i = 0; i < nb; i++) distinct += hist[i];
+        t->distinct = distinct;
+        t->distinct_valid = true;
+    }
     return e;
 }
 
