@@ -277,9 +277,10 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_step(const uint64_t *__rest
     }
 }
 
-// ---- pass 2 by ranges (slices of at least 2^SR_BITS slots).  Per partition
-// p the keys are regrouped by the 4096-slot range of the slice their home slot
-// falls in (k_sr_hist, k_sr_scatter), and one block per range then
+// ---- pass 2 by ranges (slices of at least 2^SR_MIN_LBITS slots).  Per
+// partition p the keys are regrouped by the range of the slice their home slot
+// falls in (a slice is cut into about three ranges per SM, so that the build
+// runs as one wave; k_sr_hist, k_sr_scatter), and one block per range then
 // builds that range in shared memory (k_sr_build): it loads the range (all
 // empty on a fresh table), inserts the range's keys with shared-memory CAS
 // and add, and writes the range back whole.  A key whose probe run reaches the
@@ -290,15 +291,24 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_step(const uint64_t *__rest
 // in the slice) is the one every reader uses, so the layout is an ordinary
 // linear-probing table.  Global atomics drop from two per occurrence to the
 // deferred keys alone, and a fresh slice needs no separate fill.
-constexpr int SR_BITS = 12;
-constexpr int SR_SLOTS = 1 << SR_BITS;
+constexpr int SR_MIN_LBITS = 12;        // slices below 4096 slots keep the atomic path
+constexpr int SR_MAX_SLOTS = 4600;      // slots of one range in shared memory (3 blocks per SM)
 constexpr int SR_THREADS = 1024;        // regrouping passes (2 blocks per SM: few per-block range counts)
 constexpr int SR_BUILD_THREADS = 512;
-constexpr int SR_MINI = 256;
-constexpr size_t SR_SMEM = (size_t)(SR_SLOTS + SR_MINI) * sizeof(Slot);
+constexpr int SR_MINI = 64;
+constexpr size_t SR_SMEM = (size_t)(SR_MAX_SLOTS + SR_MINI) * sizeof(Slot);
 
-__device__ __forceinline__ uint32_t key_range(const DevTable &t, uint64_t key) {
-    return (uint32_t)((mix64(key) & t.lmask) >> SR_BITS);
+// A slice of 2^lbits slots is cut into nsub ranges: slot s belongs to range
+// floor(s * nsub / 2^lbits), so range r is [ceil(r 2^lbits / nsub),
+// ceil((r+1) 2^lbits / nsub)).
+__device__ __forceinline__ uint32_t slot_range(const DevTable &t, uint64_t s, uint32_t nsub) {
+    return (uint32_t)((s * nsub) >> t.lbits);
+}
+__device__ __forceinline__ uint64_t range_first(const DevTable &t, uint32_t r, uint32_t nsub) {
+    return (((uint64_t)r << t.lbits) + nsub - 1) / nsub;
+}
+__device__ __forceinline__ uint32_t key_range(const DevTable &t, uint64_t key, uint32_t nsub) {
+    return slot_range(t, mix64(key) & t.lmask, nsub);
 }
 
 // Keys [ps, pe) split evenly over the blocks.  Per block, keys per range
@@ -321,7 +331,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_sr_hist(const uint64_t *__restri
         }
 #pragma unroll
         for (int u = 0; u < 4; u++)
-            if (k4[u] != EMPTY_KEY) atomicAdd(&sr_h[key_range(t, k4[u])], 1u);
+            if (k4[u] != EMPTY_KEY) atomicAdd(&sr_h[key_range(t, k4[u], nsub)], 1u);
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < nsub; i += SR_THREADS) {
@@ -397,7 +407,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__res
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             if (k4[u] == EMPTY_KEY) continue;
-            const uint32_t r = key_range(t, k4[u]);
+            const uint32_t r = key_range(t, k4[u], nsub);
             skeys[lstart[r] + atomicAdd(&lcur[r], 1u)] = k4[u];
         }
     }
@@ -436,9 +446,11 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
                                                         uint64_t defer_cap, unsigned long long *__restrict__ defer_n) {
     extern __shared__ __align__(16) unsigned char sr_smem[];
     Slot *tab = reinterpret_cast<Slot *>(sr_smem);
-    Slot *mini = tab + SR_SLOTS;
+    Slot *mini = tab + SR_MAX_SLOTS;
     __shared__ uint64_t ab[2];
     const uint32_t r = blockIdx.x;
+    const uint64_t r0 = range_first(t, r, nsub);
+    const uint32_t len = (uint32_t)(range_first(t, r + 1, nsub) - r0);   // <= SR_MAX_SLOTS (host checks)
     if (r == 0) {
         // the next partition's range counters (their last users finished before this launch)
         for (uint32_t i = threadIdx.x; i < nsub; i += SR_BUILD_THREADS) {
@@ -461,12 +473,12 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
             ab[1] = a + totals[r];
         }
     }
-    ulonglong2 *g = reinterpret_cast<ulonglong2 *>(t.slots + ((uint64_t)p << t.lbits) + ((uint64_t)r << SR_BITS));
+    ulonglong2 *g = reinterpret_cast<ulonglong2 *>(t.slots + ((uint64_t)p << t.lbits) + r0);
     ulonglong2 *st = reinterpret_cast<ulonglong2 *>(tab);
     ulonglong2 e;
     e.x = EMPTY_KEY;
     e.y = 0;
-    for (int i = threadIdx.x; i < SR_SLOTS; i += SR_BUILD_THREADS) st[i] = fresh ? e : g[i];
+    for (uint32_t i = threadIdx.x; i < len; i += SR_BUILD_THREADS) st[i] = fresh ? e : g[i];
     for (int i = threadIdx.x; i < SR_MINI; i += SR_BUILD_THREADS) reinterpret_cast<ulonglong2 *>(mini)[i] = e;
     __syncthreads();
     const uint64_t a = ab[0], b = ab[1];
@@ -480,7 +492,7 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const uint64_t key = k4[u];
-            if (key == EMPTY_KEY || smem_add(tab, (uint32_t)(mix64(key) & (SR_SLOTS - 1)), SR_SLOTS, key, 1u)) continue;
+            if (key == EMPTY_KEY || smem_add(tab, (uint32_t)((mix64(key) & t.lmask) - r0), len, key, 1u)) continue;
             // the probe left the range: count it in the per-block table, or defer it singly
             const uint32_t m = (uint32_t)(mix64(key ^ 0x5851F42D4C957F2DULL) & (SR_MINI - 1));
             if (smem_add(mini, m, SR_MINI, key, 1u) || (m && smem_add(mini, 0, m, key, 1u))) continue;
@@ -492,7 +504,7 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < SR_SLOTS; i += SR_BUILD_THREADS) g[i] = st[i];
+    for (uint32_t i = threadIdx.x; i < len; i += SR_BUILD_THREADS) g[i] = st[i];
     for (int i = threadIdx.x; i < SR_MINI; i += SR_BUILD_THREADS) {
         if (mini[i].key == EMPTY_KEY) continue;
         const unsigned long long j = atomicAdd(defer_n, 1ULL);
@@ -864,7 +876,11 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     tk_ctx *c = t->ctx;
     *done = false;
     const int nparts = 1 << t->t.pbits;
-    const uint32_t nsub = 1u << (t->t.lbits - SR_BITS);
+    // ranges per slice: one wave of three build blocks per SM, more if a range
+    // would not fit in shared memory
+    const uint64_t slice = 1ULL << t->t.lbits;
+    uint32_t nsub = (uint32_t)std::min<uint64_t>(slice / 1024, (uint64_t)c->sm_count * 3);
+    nsub = (uint32_t)std::max<uint64_t>(nsub, (slice + SR_MAX_SLOTS - 1) / SR_MAX_SLOTS);
     const uint64_t bpp = (uint64_t)(NBUCKETS >> t->t.pbits);
     // partition boundaries on the host: the first offset of each partition's buckets
     std::vector<uint64_t> pb(nparts + 1);
@@ -1021,7 +1037,7 @@ int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
         if (!e) e = overflow_reset(t);
         prof_begin(c, TK_KID_COUNT, &ev);
         bool done = false;
-        if (!e && t->fresh && t->t.lbits >= SR_BITS) e = count_by_ranges(t, keys, offs, cols, &done);
+        if (!e && t->fresh && t->t.lbits >= SR_MIN_LBITS) e = count_by_ranges(t, keys, offs, cols, &done);
         if (!e && !done) e = count_by_atomics(t, keys, offs, cols);
         prof_end(c, TK_KID_COUNT, ev, windows);
         if (!e) e = check_launch(c, "count insert");
