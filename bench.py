@@ -285,10 +285,12 @@ def run_gpu(args, dist, world, rank, local):
         peak = peaks.get("hbm_gbs", 6800.0)
         packed = res[0][4]
         capacity = res[0][5]
-        # random-access ceilings of this GPU, measured here: CAS + red.add pairs
-        # into one L2-resident 32 MB slice (the insert), and random 8-byte loads
-        # into a table the size of this run's (the coverage lookups)
-        ceil_insert = ctx.random_access_rate(32 << 20, atomics=True)
+        # random-access ceilings of this GPU, measured here at this run's table
+        # footprint: CAS + red.add pairs (what a per-occurrence insert costs) and
+        # random 8-byte loads (the coverage lookups); plus CAS + red.add pairs
+        # into one L2-resident 32 MB slice
+        ceil_insert = ctx.random_access_rate(capacity * 16, atomics=True)
+        ceil_slice = ctx.random_access_rate(32 << 20, atomics=True)
         ceil_lookup = ctx.random_access_rate(capacity * 16, atomics=False)
         per_step = {k: (v[0] / args.steps, v[1] / args.steps) for k, v in prof.items()}
 
@@ -315,11 +317,13 @@ def run_gpu(args, dist, world, rank, local):
             "coverage": kernel_roofline("k_coverage (per-read k-mer coverage stats)", "coverage",
                                         packed + 32.0 * windows + 12.0 * reads, windows, ceil_lookup,
                                         "random 16-byte slot lookups vs random 8-byte loads into a table of this size"),
-            "insert": kernel_roofline("k_part_step (partitioned count insert)", "count", 40.0 * windows, windows,
-                                      ceil_insert, "CAS+red.add inserts vs CAS+red.add pairs into a 32 MB slice"),
+            "insert": kernel_roofline("k_sr_hist + k_sr_scatter + k_sr_build (count by table ranges)", "count",
+                                      40.0 * windows, windows, ceil_insert,
+                                      "k-mer occurrences counted vs random CAS+red.add pairs into a table of this size"),
             "scatter": kernel_roofline("k_part_scatter (k-mers into hash buckets)", "scatter",
                                        packed + 8.0 * windows, 0, None, None),
         }
+        kernels["insert"]["random_access"]["l2_slice_ceiling_per_s"] = ceil_slice
         top = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
         out = {
             "metric": METRIC, "value": tot_windows / t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
