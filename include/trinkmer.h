@@ -124,6 +124,24 @@ int tk_reads_parse_many(tk_ctx *ctx, const char *const *texts, const uint64_t *l
  * upload of one piece overlaps the parse of the one before.  Only the bytes
  * around each cut are read.  No counterpart in the reference. */
 int tk_split_records(const char *text, uint64_t len, uint32_t n_chunks, uint64_t *cuts);
+/* FASTQ -> FASTA read prep (the conversion Trinity runs before counting:
+ * `seqtk-trinity seq -A -R {1,2} [-r]`, Trinity:2745-2805; its executable spec
+ * is util/support_scripts/fastQ_to_fastA.pl:60-118).  For a read set parsed
+ * from FASTQ: ">name[/1|/2][/append]\nSEQUENCE\n" per record, the name the
+ * header's first field, "/1" or "/2" from a Casava "1:"/"2:" comment, the
+ * sequence line as written (case kept; only the header loses CRs).  append
+ * = -1 adds nothing, N >= 0 adds "/N" (the script's -a N), with
+ * TK_FA_IF_MISSING only to names not already ending in /1 or /2 (what
+ * seqtk-trinity -R N is for).  TK_FA_REVCOMP reverse-complements
+ * (PerlLib/Nuc_translator.pm:286-292).  A poorly formed record (sequence
+ * empty or "0", quality blank or of another length) fails with TK_E_PARSE
+ * unless TK_FA_IGNORE_DIRTY skips it.  out == NULL reports the length only;
+ * the text is kept with the read set for the next call with the same
+ * options. */
+#define TK_FA_REVCOMP 1
+#define TK_FA_IGNORE_DIRTY 2
+#define TK_FA_IF_MISSING 4
+int tk_reads_to_fasta(tk_reads *reads, int append, int flags, int where, char *out, uint64_t cap, uint64_t *len_out);
 int tk_reads_info(const tk_reads *reads, uint64_t *n_reads, uint64_t *n_bases,
                   uint32_t *max_len, int *format);
 /* Host copies: accession offset/length into the parsed text (n_reads each). */

@@ -741,4 +741,109 @@ int orc_records(const char *text, size_t len, char **out, size_t *out_len) {
     return 0;
 }
 
+/* ---- FASTQ -> FASTA prep: util/support_scripts/fastQ_to_fastA.pl:60-118,
+ * the executable spec of Trinity's `seqtk-trinity seq -A -R N [-r]`
+ * (Trinity:2745-2805).  Line by line: a line starting with '@' (after its CRs
+ * are removed) opens a record of it and the next three lines; every other
+ * line is skipped.  Only the header loses its CRs; the other lines lose just
+ * their "\n".  A record is clean when the sequence is non-empty and not "0",
+ * the third line starts with '+', the quality line holds a non-space byte and
+ * is as long as the sequence (fastQ_to_fastA.pl:86-88).  Name = first
+ * whitespace-separated field of the header without '@' (empty if the header
+ * starts with whitespace); "/1" or "/2" is added when more fields follow, the
+ * name does not already end in /1 or /2, and the next field starts "1:" or
+ * "2:" (Casava 1.8, :95-97); then "/append" when append >= 0 (the -a option),
+ * or with ORC_FA_IF_MISSING only when the name does not already end in /1 or
+ * /2; ORC_FA_REV reverse-complements the sequence with
+ * PerlLib/Nuc_translator.pm:286-292's letter map.  A poorly formed record
+ * fails the call (ORC_E_PARSE, *bad = 1-based record number) unless
+ * ORC_FA_IGNORE_DIRTY skips it. */
+static int pl_ws(unsigned char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\f' || c == '\v'; }
+
+static unsigned char rc_letter(unsigned char c) {
+    static const char from[] = "ACGTacgtyrkmYRKMUu", to[] = "TGCAtgcarymkRYMKAa";
+    for (int i = 0; from[i]; i++)
+        if ((unsigned char)from[i] == c) return (unsigned char)to[i];
+    return c;
+}
+
+static int fa_ends_12(const char *n, size_t l) { return l >= 2 && n[l - 2] == '/' && (n[l - 1] == '1' || n[l - 1] == '2'); }
+
+int orc_fastq_to_fasta(const char *text, size_t len, int append, int flags, char **out, size_t *out_len, uint64_t *bad) {
+    sbuf_t o = {0};
+    size_t p = 0;
+    uint64_t rec = 0;
+    char *hdr = NULL;
+    size_t hcap = 0;
+    *bad = 0;
+    while (p < len) {
+        /* one line [p, e) and the next line start q */
+        const char *nl = memchr(text + p, '\n', len - p);
+        size_t e = nl ? (size_t)(nl - text) : len, q = nl ? e + 1 : len;
+        /* the header candidate without CRs */
+        size_t hl = 0;
+        if (hcap < e - p + 1) { hcap = e - p + 64; free(hdr); hdr = malloc(hcap); if (!hdr) { free(o.b); return ORC_E_OOM; } }
+        for (size_t i = p; i < e; i++) if (text[i] != '\r') hdr[hl++] = text[i];
+        if (!(hl > 0 && hdr[0] == '@')) { p = q; continue; }
+        rec++;
+        /* the next three lines (absent at end of input) */
+        size_t ls[3], le[3];
+        int have[3];
+        size_t r = q;
+        for (int j = 0; j < 3; j++) {
+            have[j] = r < len;
+            const char *m = have[j] ? memchr(text + r, '\n', len - r) : NULL;
+            ls[j] = r;
+            le[j] = have[j] ? (m ? (size_t)(m - text) : len) : r;
+            r = have[j] ? (m ? le[j] + 1 : len) : r;
+        }
+        p = r;
+        size_t sl = le[0] - ls[0], ql = le[2] - ls[2];
+        int clean = have[0] && have[1] && have[2] && sl > 0 && !(sl == 1 && text[ls[0]] == '0') &&
+                    le[1] > ls[1] && text[ls[1]] == '+' && ql == sl;
+        if (clean) {
+            int ns = 0;
+            for (size_t i = ls[2]; i < le[2]; i++) if (!pl_ws((unsigned char)text[i])) { ns = 1; break; }
+            clean = ns;
+        }
+        if (!clean) {
+            if (flags & ORC_FA_IGNORE_DIRTY) continue;
+            free(hdr); free(o.b);
+            *bad = rec;
+            return ORC_E_PARSE;
+        }
+        /* name: first field of the header after '@'; the second decides Casava */
+        size_t a = 1, b = 1;
+        while (b < hl && !pl_ws((unsigned char)hdr[b])) b++;
+        size_t f2 = b;
+        while (f2 < hl && pl_ws((unsigned char)hdr[f2])) f2++;
+        int more = f2 < hl;
+        char suffix[32];
+        int sfx = 0;
+        if (more && !fa_ends_12(hdr + a, b - a) && f2 + 1 < hl && (hdr[f2] == '1' || hdr[f2] == '2') && hdr[f2 + 1] == ':')
+            sfx = snprintf(suffix, sizeof suffix, "/%c", hdr[f2]);
+        if (append >= 0) {
+            int ends = fa_ends_12(hdr + a, b - a) || sfx;
+            if (!(flags & ORC_FA_IF_MISSING) || !ends) sfx += snprintf(suffix + sfx, sizeof suffix - sfx, "/%d", append);
+        }
+        if (sb_reserve(&o, 4 + (b - a) + sfx + sl)) { free(hdr); free(o.b); return ORC_E_OOM; }
+        o.b[o.n++] = '>';
+        memcpy(o.b + o.n, hdr + a, b - a); o.n += b - a;
+        memcpy(o.b + o.n, suffix, sfx); o.n += sfx;
+        o.b[o.n++] = '\n';
+        if (flags & ORC_FA_REV)
+            for (size_t i = 0; i < sl; i++) o.b[o.n++] = (char)rc_letter((unsigned char)text[le[0] - 1 - i]);
+        else {
+            memcpy(o.b + o.n, text + ls[0], sl);
+            o.n += sl;
+        }
+        o.b[o.n++] = '\n';
+    }
+    free(hdr);
+    if (!o.b) { o.b = malloc(1); if (!o.b) return ORC_E_OOM; }
+    *out = o.b;
+    *out_len = o.n;
+    return 0;
+}
+
 void orc_free(void *p) { free(p); }

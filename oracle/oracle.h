@@ -78,6 +78,16 @@ int orc_r2t_values(const char *reads, size_t rlen, const char *bundle,
 /* "acc\tsequence\n" per parsed record (the parse the other calls use). */
 int orc_records(const char *text, size_t len, char **out, size_t *out_len);
 
+/* FASTQ -> FASTA as util/support_scripts/fastQ_to_fastA.pl prints it (see
+ * oracle.c): append >= 0 adds "/append" (-a), flags ORC_FA_*; on a poorly
+ * formed record returns ORC_E_PARSE with *bad = its 1-based number unless
+ * ORC_FA_IGNORE_DIRTY. */
+#define ORC_FA_REV 1
+#define ORC_FA_IGNORE_DIRTY 2
+#define ORC_FA_IF_MISSING 4
+int orc_fastq_to_fasta(const char *text, size_t len, int append, int flags, char **out, size_t *out_len,
+                       uint64_t *bad);
+
 void orc_free(void *p);
 
 #ifdef __cplusplus

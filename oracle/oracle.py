@@ -33,6 +33,7 @@ def load() -> C.CDLL:
     lib = C.CDLL(str(LIB))
     vp, u64, P = C.c_void_p, C.c_uint64, C.POINTER
     lib.orc_count.argtypes = [vp, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int, P(vp), P(vp), P(u64)]
+    lib.orc_fastq_to_fasta.argtypes = [vp, C.c_size_t, C.c_int, C.c_int, P(vp), P(C.c_size_t), P(u64)]
     lib.orc_histo.argtypes = [vp, u64, u64, u64, vp]
     lib.orc_histo.restype = None
     lib.orc_dump.argtypes = [vp, vp, u64, C.c_int, C.c_uint32, P(vp), P(C.c_size_t)]
@@ -73,6 +74,22 @@ def _take_bytes(ptr: C.c_void_p, n: int) -> bytes:
     b = C.string_at(ptr, n) if n else b""
     lib.orc_free(ptr)
     return b
+
+
+FA_REV, FA_IGNORE_DIRTY, FA_IF_MISSING = 1, 2, 4
+
+
+def fastq_to_fasta(text: bytes, append: int = -1, flags: int = 0) -> bytes:
+    """FASTQ -> FASTA as util/support_scripts/fastQ_to_fastA.pl prints it;
+    raises ValueError(record number) on a poorly formed record unless
+    FA_IGNORE_DIRTY."""
+    lib = load()
+    p, n, bad = C.c_void_p(), C.c_size_t(), C.c_uint64()
+    st = lib.orc_fastq_to_fasta(text, len(text), append, flags, C.byref(p), C.byref(n), C.byref(bad))
+    if st == -4:
+        raise ValueError(bad.value)
+    _chk(st, "fastq_to_fasta")
+    return _take_bytes(p, n.value)
 
 
 def records(text: bytes) -> bytes:

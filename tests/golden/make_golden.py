@@ -3,7 +3,7 @@
 Perl code (run here, where the reference checkout and Perl are available; the
 fixtures are committed so nothing at test time needs the reference).
 
-    python tests/golden/make_golden.py /path/to/trinityrnaseq
+    python tests/golden/make_golden.py /path/to/trinityrnaseq [--prep-only]
 
 What each fixture pins:
   edge.fa / bulk.fa          inputs (edge cases: multi-line records, lower case,
@@ -15,6 +15,10 @@ What each fixture pins:
                              mode (each window and its reverse complement)
   edge.fq / edge.fastQ_to_fastA.fa
                              FASTQ records through util/support_scripts/fastQ_to_fastA.pl
+  prep.fq / prep*.fa         the FASTQ->FASTA prep through fastQ_to_fastA.pl with no
+                             option, -a 1, --rev, -a 2 --rev (Casava comments, CR, IUPAC)
+  prep_dirty.fq / prep_dirty.ignore.fa
+                             poorly formed records, --ignore_dirty
   left.fa right.fa           200 seeded read pairs (2x100)
   left.stats right.stats     the oracle's fastaToKmerCoverageStats tables, sorted
                              as util/insilico_read_normalization.pl:865-892 does
@@ -80,6 +84,38 @@ def edge_fastq() -> bytes:
     return "".join(out).encode()
 
 
+def prep_fastq() -> bytes:
+    """FASTQ for the FASTQ->FASTA prep: Casava comments (1:/2: appended, 3: not,
+    names already ending in /1 left alone), tab and multiple separators, lower
+    case, N and IUPAC letters, CRLF line ends and a CR inside a line."""
+    rnd = random.Random(17)
+    heads = ["r0 1:N:0:ACGT", "r1 2:Y:18:ATCACG", "r2/1 2:N:0:ACGT", "r3 3:N:0:ACGT", "r4\t1:N:0:ACGT", "r5",
+             "r6  2:N:0", "r7/2", "r8 x 1:N", "r9 1:N:0:ACGT extra words"]
+    out = []
+    for i in range(40):
+        L = rnd.randint(1, 90)
+        alpha = "ACGT" if i % 4 else "ACGTNacgtnyrkmYRKMUu"
+        seq = "".join(rnd.choice(alpha) for _ in range(L))
+        hdr = heads[i % len(heads)].replace("r", "r%d_" % i, 1)
+        qual = "".join(rnd.choice("!#5?I@") for _ in range(L))
+        if i % 9 == 4:
+            out.append(f"@{hdr}\r\n{seq}\r\n+\r\n{qual}\r\n")
+        elif i % 13 == 6:
+            cut = L // 2
+            out.append(f"@{hdr}\n{seq[:cut]}\r{seq[cut:]}\n+{hdr}\n{qual[:cut]}\r{qual[cut:]}\n")
+        else:
+            out.append(f"@{hdr}\n{seq}\n+\n{qual}\n")
+    return "".join(out).encode()
+
+
+def prep_dirty_fastq() -> bytes:
+    """Records fastQ_to_fastA.pl calls poorly formed: quality shorter or longer
+    than the sequence, a blank quality line."""
+    recs = ["@ok1\nACGTACGT\n+\nIIIIIIII\n", "@short 1:N\nACGTACGT\n+\nIIII\n", "@ok2 2:N\nGGGCCC\n+\nIIIIII\n",
+            "@long\nACG\n+\nIIIII\n", "@blank\nACGT\n+\n\n", "@ok3\nTTTT\n+\nIIII\n"]
+    return "".join(recs).encode()
+
+
 def perl(ref: Path, script: str, *args, stdin=None) -> bytes:
     env = dict(os.environ, LC_ALL="C")
     return subprocess.run(["perl", str(ref / script), *map(str, args)], check=True, stdout=subprocess.PIPE,
@@ -100,9 +136,27 @@ def sorted_stats(text: bytes) -> bytes:
     return head + b"\n" + b"".join(l + b"\n" for l in body)
 
 
+def make_prep(ref: Path) -> None:
+    """The FASTQ->FASTA prep fixtures (util/support_scripts/fastQ_to_fastA.pl)."""
+    fq = HERE / "prep.fq"
+    fq.write_bytes(prep_fastq())
+    script = "util/support_scripts/fastQ_to_fastA.pl"
+    (HERE / "prep.fa").write_bytes(perl(ref, script, "-I", fq))
+    (HERE / "prep.a1.fa").write_bytes(perl(ref, script, "-I", fq, "-a", 1))
+    (HERE / "prep.rev.fa").write_bytes(perl(ref, script, "-I", fq, "--rev"))
+    (HERE / "prep.a2rev.fa").write_bytes(perl(ref, script, "-I", fq, "-a", 2, "--rev"))
+    dq = HERE / "prep_dirty.fq"
+    dq.write_bytes(prep_dirty_fastq())
+    (HERE / "prep_dirty.ignore.fa").write_bytes(perl(ref, script, "-I", dq, "--ignore_dirty"))
+
+
 def main() -> None:
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     HERE.mkdir(exist_ok=True)
+    if len(sys.argv) > 2 and sys.argv[2] == "--prep-only":
+        make_prep(ref)
+        return
+    make_prep(ref)
     edge = edge_fasta()
     (HERE / "edge.fa").write_bytes(edge)
     bulk = synth.transcriptome_reads(seed=11, n_transcripts=50, n_reads=300, read_len=76).tobytes()

@@ -94,3 +94,18 @@ def test_r2t_first_record_owns_shared_kmer(oracle):
     r = (">q1\n" + shared + "\n").encode()
     rows = oracle.r2t(r, b, 25, False, 0).decode().split("\t")
     assert rows[0] == "7" and rows[1] == ">q1" and rows[2] == "100"
+
+
+@pytest.mark.parametrize("fixture,append,flags", [
+    ("prep.fa", -1, 0), ("prep.a1.fa", 1, 0), ("prep.rev.fa", -1, 1), ("prep.a2rev.fa", 2, 1)])
+def test_fastq_to_fasta_matches_reference_script(oracle, golden, fixture, append, flags):
+    """util/support_scripts/fastQ_to_fastA.pl output (no option, -a 1, --rev, -a 2 --rev)."""
+    assert oracle.fastq_to_fasta((golden / "prep.fq").read_bytes(), append, flags) == (golden / fixture).read_bytes()
+
+
+def test_fastq_to_fasta_dirty_records(oracle, golden):
+    dirty = (golden / "prep_dirty.fq").read_bytes()
+    assert oracle.fastq_to_fasta(dirty, -1, oracle.FA_IGNORE_DIRTY) == (golden / "prep_dirty.ignore.fa").read_bytes()
+    with pytest.raises(ValueError) as e:
+        oracle.fastq_to_fasta(dirty)
+    assert e.value.args[0] == 2     # the script dies on the second record

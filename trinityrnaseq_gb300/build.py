@@ -27,12 +27,14 @@ LIB = PKG / "lib"
 BIN = PKG / "bin"
 INCLUDE = ROOT / "include"
 
-CUDA_SOURCES = ["tk_api.cu", "tk_scan.cu", "tk_parse.cu", "tk_table.cu", "tk_cov.cu", "tk_r2t.cu", "tk_bins.cu", "tk_server.cu"]
+CUDA_SOURCES = ["tk_api.cu", "tk_scan.cu", "tk_parse.cu", "tk_table.cu", "tk_cov.cu", "tk_r2t.cu", "tk_bins.cu", "tk_server.cu",
+                "tk_fasta.cu"]
 TOOL_SOURCES = {
     "jellyfish": ["jellyfish.cpp"],
     "fastaToKmerCoverageStats": ["fastaToKmerCoverageStats.cpp"],
     "ReadsToTranscripts": ["ReadsToTranscripts.cpp"],
     "trinkmerd": ["trinkmerd.cpp"],
+    "seqtk-trinity": ["seqtk_trinity.cpp"],
 }
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -560,6 +560,32 @@ int tk_split_records(const char *text, uint64_t len, uint32_t n_chunks, uint64_t
     return TK_OK;
 }
 
+int tk_reads_to_fasta(tk_reads *r, int append, int flags, int where, char *out, uint64_t cap, uint64_t *len_out) {
+    if (!r || !len_out) return TK_E_INVAL;
+    tk_ctx *c = r->ctx;
+    CHECK_CTX(c);
+    if (r->format != TK_FMT_FASTQ && r->n_reads)
+        return set_err(c, TK_E_INVAL, "tk_reads_to_fasta: the read set was not parsed from FASTQ");
+    if (flags & ~(TK_FA_REVCOMP | TK_FA_IGNORE_DIRTY | TK_FA_IF_MISSING))
+        return set_err(c, TK_E_INVAL, "tk_reads_to_fasta: unknown flag");
+    if (append < -1) return set_err(c, TK_E_INVAL, "tk_reads_to_fasta: append must be -1 (none) or >= 0");
+    if (!r->d_fasta || r->fasta_append != append || r->fasta_flags != flags) {
+        if (r->d_fasta) dfree(c, r->d_fasta);
+        r->d_fasta = nullptr;
+        r->fasta_flags = -1;
+        TK_TRY(reads_fasta(r, append, flags, &r->d_fasta, &r->fasta_len));
+        r->fasta_append = append;
+        r->fasta_flags = flags;
+    }
+    *len_out = r->fasta_len;
+    if (!out) return TK_OK;
+    if (cap < r->fasta_len) return set_err(c, TK_E_RANGE, "tk_reads_to_fasta: buffer smaller than the text");
+    if (r->fasta_len)
+        TK_CUDA(c, cudaMemcpyAsync(out, r->d_fasta, r->fasta_len,
+                                   where == TK_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "fasta copy");
+}
+
 int tk_reads_info(const tk_reads *r, uint64_t *n_reads, uint64_t *n_bases, uint32_t *max_len, int *format) {
     if (!r) return TK_E_INVAL;
     if (n_reads) *n_reads = r->n_reads;
@@ -603,6 +629,7 @@ void tk_reads_free(tk_reads *r) {
     if (r->own_text) dfree(c, r->d_text);
     dfree(c, r->d_seq_alloc);
     if (r->d_pack_alloc) dfree(c, r->d_pack_alloc);
+    if (r->d_fasta) dfree(c, r->d_fasta);
     dfree(c, r->d_rd_off);
     dfree(c, r->d_name_off);
     dfree(c, r->d_name_len);

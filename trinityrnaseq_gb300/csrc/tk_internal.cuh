@@ -244,6 +244,9 @@ struct tk_reads {
     uint64_t *d_rd_off = nullptr;           // n_reads + 1
     uint64_t *d_name_off = nullptr;         // n_reads
     uint32_t *d_name_len = nullptr;         // n_reads
+    char *d_fasta = nullptr;                // last FASTA conversion (tk_reads_to_fasta)
+    uint64_t fasta_len = 0;
+    int fasta_append = 0, fasta_flags = -1;
     uint64_t *d_pack_alloc = nullptr;       // codes and inv, one allocation
     const uint64_t *d_codes = nullptr;      // word 0 of the 2-bit codes (word -1 exists)
     const uint32_t *d_inv = nullptr;        // word 0 of the invalid-position bits (word -1 exists)
@@ -299,6 +302,7 @@ int table_alloc(tk_table *t, uint64_t capacity);
 int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val);
 int table_rehash(tk_table *t, uint64_t new_capacity);
 int table_count_seq(tk_table *t, const tk_reads *r);
+int reads_fasta(tk_reads *r, int append, int flags, char **d_text, uint64_t *text_len);
 int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets);
 }  // namespace tk
 

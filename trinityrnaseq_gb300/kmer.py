@@ -197,6 +197,20 @@ class ReadSet:
         self.ctx.check(self.lib.tk_reads_copy_seq(self.h, buf.ctypes.data, n), "tk_reads_copy_seq")
         return buf[:n].tobytes()
 
+    def to_fasta(self, append: int = -1, revcomp: bool = False, ignore_dirty: bool = False,
+                 if_missing: bool = False) -> bytes:
+        """FASTQ read set -> FASTA text (tk_reads_to_fasta; the read prep of
+        util/support_scripts/fastQ_to_fastA.pl / seqtk-trinity seq -A)."""
+        flags = (N.TK_FA_REVCOMP if revcomp else 0) | (N.TK_FA_IGNORE_DIRTY if ignore_dirty else 0) | \
+                (N.TK_FA_IF_MISSING if if_missing else 0)
+        n = C.c_uint64()
+        self.ctx.check(self.lib.tk_reads_to_fasta(self.h, append, flags, N.TK_HOST, None, 0, C.byref(n)),
+                       "tk_reads_to_fasta")
+        buf = np.zeros(max(n.value, 1), dtype=np.uint8)
+        self.ctx.check(self.lib.tk_reads_to_fasta(self.h, append, flags, N.TK_HOST, buf.ctypes.data, buf.size,
+                                                  C.byref(n)), "tk_reads_to_fasta")
+        return buf[:n.value].tobytes()
+
     def sequences(self) -> list:
         off = self.offsets().tolist()
         s = self.packed()

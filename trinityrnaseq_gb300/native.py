@@ -27,6 +27,8 @@ TK_DEVICE = 1
 
 TK_FMT_NONE, TK_FMT_FASTA, TK_FMT_FASTQ = 0, 1, 2
 
+TK_FA_REVCOMP, TK_FA_IGNORE_DIRTY, TK_FA_IF_MISSING = 1, 2, 4
+
 KID = {
     "parse": 0, "hll": 1, "count": 2, "compact": 3, "sort": 4, "dump": 5, "load": 6,
     "coverage": 7, "r2t_build": 8, "r2t_assign": 9, "bins": 10, "scatter": 11,
@@ -54,6 +56,7 @@ SIGNATURES = {
     "tk_reads_parse": (C.c_int, [vp, vp, u64, C.c_int, P(vp)]),
     "tk_reads_parse_many": (C.c_int, [vp, P(vp), P(u64), u32, C.c_int, P(vp)]),
     "tk_split_records": (C.c_int, [vp, u64, u32, P(u64)]),
+    "tk_reads_to_fasta": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, vp, u64, P(u64)]),
     "tk_reads_info": (C.c_int, [vp, P(u64), P(u64), P(u32), P(C.c_int)]),
     "tk_reads_names": (C.c_int, [vp, vp, vp]),
     "tk_reads_offsets": (C.c_int, [vp, vp]),
