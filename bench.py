@@ -349,12 +349,75 @@ def run_gpu(args, dist, world, rank, local):
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args)
         del pipe
+        if args.prep and world == 1:
+            out["prep"] = prep_bench(ctx, left, args)
         if args.bins and world == 1:
             out["batched"] = batched_bench(ctx, args)
         if args.jobs and world == 1:
             out["served"] = served_bench(ctx, args)
     ctx.close()
     return out
+
+
+# ---------------------------------------------------------------- read prep
+
+def prep_bench(ctx, fastq, args):
+    """FASTQ -> FASTA read prep of one mate file (the `seqtk-trinity seq -A -R 1`
+    conversion Trinity runs before counting): parse + convert on the GPU, with
+    the FASTQ resident in HBM (device) and from pinned host memory to a pinned
+    host FASTA (e2e), against the oracle's restatement of fastQ_to_fastA.pl on
+    one host core (both tools are single-threaded) over a 1M-record sample."""
+    import torch
+    from trinityrnaseq_gb300 import kmer
+    from oracle import oracle as O
+    dev = torch.device(f"cuda:{ctx.device}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    h_in = torch.from_numpy(fastq).pin_memory()
+    d_in = h_in.to(dev)
+    n_bytes = h_in.numel()
+    opts = dict(append=1, if_missing=True)
+
+    def run(e2e, out):
+        rs = kmer.ReadSet(ctx, h_in.numpy()) if e2e else kmer.ReadSet(ctx, d_in.data_ptr(), n_bytes, device=True)
+        n = rs.fasta_len(**opts)
+        if out is not None:
+            rs.fasta_into(out.data_ptr(), out.numel(), device=not e2e, **opts)
+        reads = rs.n_reads
+        rs.free()
+        return n, reads
+
+    n_out, reads = run(False, None)
+    d_out = torch.empty(n_out + 16, dtype=torch.uint8, device=dev)
+    h_out = torch.empty(n_out + 16, dtype=torch.uint8).pin_memory()
+    res = {}
+    for mode, out in (("device", d_out), ("e2e", h_out)):
+        for _ in range(args.warmup):
+            run(mode == "e2e", out)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for _ in range(args.steps):
+                run(mode == "e2e", out)
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        s = ev[0].elapsed_time(ev[1]) / 1e3 / args.steps
+        res[mode] = {"reads_per_s": reads / s, "input_gb_per_s": n_bytes / s / 1e9, "ms": s * 1e3}
+    # bit-exact check and CPU time on a 1M-record sample
+    cut = kmer.split_records(fastq, max(1, reads // 1_000_000))[1]
+    sample = fastq[:cut].tobytes()
+    t0 = time.time()
+    want = O.fastq_to_fasta(sample, 1, O.FA_IF_MISSING)
+    cpu_s = time.time() - t0
+    rs = kmer.ReadSet(ctx, sample)
+    same = rs.to_fasta(**opts) == want
+    n_sample = rs.n_reads
+    rs.free()
+    return {"workload": f"{reads} FASTQ records (2x100 left mates, {n_bytes / 1e9:.2f} GB) -> FASTA, names /1",
+            "records": reads, "fasta_bytes": n_out, **res,
+            "cpu": {"reads_per_s": n_sample / cpu_s, "cores": 1, "kind": "port",
+                    "sample": f"first {n_sample} records; the oracle's restatement of fastQ_to_fastA.pl"},
+            "bit_exact_vs_oracle_sample": same}
 
 
 # ---------------------------------------------------------------- batched and served
@@ -566,6 +629,7 @@ def main():
     ap.add_argument("--pairs", type=int, default=FULL_PAIRS)
     ap.add_argument("--cpu-pairs", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--prep", type=int, default=1, help="FASTQ->FASTA read prep leg (0 = skip)")
     ap.add_argument("--bins", type=int, default=5000, help="batched-bins comparison (0 = skip)")
     ap.add_argument("--jobs", type=int, default=200, help="served-stream comparison (0 = skip)")
     ap.add_argument("--job-max-reads", type=int, default=2_000_000)

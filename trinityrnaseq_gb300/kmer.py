@@ -197,19 +197,36 @@ class ReadSet:
         self.ctx.check(self.lib.tk_reads_copy_seq(self.h, buf.ctypes.data, n), "tk_reads_copy_seq")
         return buf[:n].tobytes()
 
+    @staticmethod
+    def _fa_flags(revcomp: bool, ignore_dirty: bool, if_missing: bool) -> int:
+        return (N.TK_FA_REVCOMP if revcomp else 0) | (N.TK_FA_IGNORE_DIRTY if ignore_dirty else 0) | \
+               (N.TK_FA_IF_MISSING if if_missing else 0)
+
+    def fasta_len(self, append: int = -1, revcomp: bool = False, ignore_dirty: bool = False,
+                  if_missing: bool = False) -> int:
+        """Converts on the device (kept with the read set); returns the FASTA size."""
+        n = C.c_uint64()
+        self.ctx.check(self.lib.tk_reads_to_fasta(self.h, append, self._fa_flags(revcomp, ignore_dirty, if_missing),
+                                                  N.TK_HOST, None, 0, C.byref(n)), "tk_reads_to_fasta")
+        return n.value
+
+    def fasta_into(self, ptr: int, cap: int, append: int = -1, revcomp: bool = False, ignore_dirty: bool = False,
+                   if_missing: bool = False, device: bool = False) -> int:
+        """The FASTA text into a caller buffer (host or device address)."""
+        n = C.c_uint64()
+        self.ctx.check(self.lib.tk_reads_to_fasta(self.h, append, self._fa_flags(revcomp, ignore_dirty, if_missing),
+                                                  N.TK_DEVICE if device else N.TK_HOST, C.c_void_p(ptr), cap,
+                                                  C.byref(n)), "tk_reads_to_fasta")
+        return n.value
+
     def to_fasta(self, append: int = -1, revcomp: bool = False, ignore_dirty: bool = False,
                  if_missing: bool = False) -> bytes:
         """FASTQ read set -> FASTA text (tk_reads_to_fasta; the read prep of
         util/support_scripts/fastQ_to_fastA.pl / seqtk-trinity seq -A)."""
-        flags = (N.TK_FA_REVCOMP if revcomp else 0) | (N.TK_FA_IGNORE_DIRTY if ignore_dirty else 0) | \
-                (N.TK_FA_IF_MISSING if if_missing else 0)
-        n = C.c_uint64()
-        self.ctx.check(self.lib.tk_reads_to_fasta(self.h, append, flags, N.TK_HOST, None, 0, C.byref(n)),
-                       "tk_reads_to_fasta")
-        buf = np.zeros(max(n.value, 1), dtype=np.uint8)
-        self.ctx.check(self.lib.tk_reads_to_fasta(self.h, append, flags, N.TK_HOST, buf.ctypes.data, buf.size,
-                                                  C.byref(n)), "tk_reads_to_fasta")
-        return buf[:n.value].tobytes()
+        n = self.fasta_len(append, revcomp, ignore_dirty, if_missing)
+        buf = np.zeros(max(n, 1), dtype=np.uint8)
+        m = self.fasta_into(buf.ctypes.data, buf.size, append, revcomp, ignore_dirty, if_missing)
+        return buf[:m].tobytes()
 
     def sequences(self) -> list:
         off = self.offsets().tolist()
