@@ -111,7 +111,7 @@ __device__ __forceinline__ void cov_warp_chunk(DevTable t, const uint8_t *__rest
 }
 
 template <bool CANON>
-__global__ void __launch_bounds__(CV_THREADS, 4) k_coverage(DevTable t, const uint8_t *__restrict__ seq,
+__global__ void __launch_bounds__(CV_THREADS, 6) k_coverage(DevTable t, const uint8_t *__restrict__ seq,
                                                         const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
                                                         uint32_t *__restrict__ median, float *__restrict__ mean,
                                                         float *__restrict__ stdev, uint32_t *__restrict__ long_list,

@@ -95,22 +95,29 @@ __device__ __forceinline__ void thread_windows(const uint64_t *__restrict__ code
 // columns [col0, col0 + gridDim.x), one per block: hist[bucket * cols + col0 + block].
 // Each count is rounded up to a multiple of 4 keys, so every (bucket, column)
 // region of the key buffer starts on a 32-byte sector; pass 1b pads the
-// rounding with EMPTY_KEY, which the insert skips.
+// rounding with EMPTY_KEY, which the insert skips.  Pass 1b's block of
+// SC_THREADS owns tiles b, b+G, b+2G, ... (G blocks); this pass covers the same
+// tiles with two tiles at a time per block (HIST_THREADS = 2 x SC_THREADS), for
+// twice the resident warps (pass 1b is held to one block per SM by its
+// shared-memory staging).
+constexpr int HIST_THREADS = 2 * SC_THREADS;
 template <bool CANON>
-__global__ void __launch_bounds__(SC_THREADS) k_part_hist(const uint64_t *__restrict__ codes,
-                                                          const uint32_t *__restrict__ inv, uint64_t n, int k,
-                                                         uint32_t *__restrict__ hist, uint64_t cols, uint64_t col0,
-                                                         uint32_t *__restrict__ regs,
-                                                         unsigned long long *__restrict__ windows_out) {
+__global__ void __launch_bounds__(HIST_THREADS) k_part_hist(const uint64_t *__restrict__ codes,
+                                                           const uint32_t *__restrict__ inv, uint64_t n, int k,
+                                                           uint32_t *__restrict__ hist, uint64_t cols, uint64_t col0,
+                                                           uint32_t *__restrict__ regs,
+                                                           unsigned long long *__restrict__ windows_out) {
     __shared__ uint32_t sh[NBUCKETS];
     __shared__ uint32_t sreg[HLL_M];
-    for (int i = threadIdx.x; i < NBUCKETS; i += SC_THREADS) sh[i] = 0;
-    for (int i = threadIdx.x; i < HLL_M; i += SC_THREADS) sreg[i] = 0;
+    for (int i = threadIdx.x; i < NBUCKETS; i += HIST_THREADS) sh[i] = 0;
+    for (int i = threadIdx.x; i < HLL_M; i += HIST_THREADS) sreg[i] = 0;
     __syncthreads();
     uint32_t windows = 0;
-    const uint64_t stride = (uint64_t)gridDim.x * SC_THREADS * CT_SPAN;
-    for (uint64_t base = (uint64_t)blockIdx.x * SC_THREADS * CT_SPAN; base < n; base += stride) {
-        const uint64_t p0 = base + (uint64_t)threadIdx.x * CT_SPAN;
+    const uint64_t tile = (uint64_t)SC_THREADS * CT_SPAN;
+    const uint32_t half = threadIdx.x / SC_THREADS, t = threadIdx.x % SC_THREADS;
+    for (uint64_t base = ((uint64_t)blockIdx.x + (uint64_t)half * gridDim.x) * tile; base < n;
+         base += 2ull * gridDim.x * tile) {
+        const uint64_t p0 = base + (uint64_t)t * CT_SPAN;
         thread_windows<CANON>(codes, inv, p0 >> 5, p0 < n, k, [&](uint64_t key) {
             uint64_t h = mix64(key);
             atomicAdd(&sh[h >> (64 - BUCKET_BITS)], 1u);
@@ -121,8 +128,8 @@ __global__ void __launch_bounds__(SC_THREADS) k_part_hist(const uint64_t *__rest
         });
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < NBUCKETS; i += SC_THREADS) hist[(uint64_t)i * cols + col0 + blockIdx.x] = (sh[i] + 3u) & ~3u;
-    for (int i = threadIdx.x; i < HLL_M; i += SC_THREADS)
+    for (int i = threadIdx.x; i < NBUCKETS; i += HIST_THREADS) hist[(uint64_t)i * cols + col0 + blockIdx.x] = (sh[i] + 3u) & ~3u;
+    for (int i = threadIdx.x; i < HLL_M; i += HIST_THREADS)
         if (sreg[i]) atomicMax(&regs[i], sreg[i]);
     windows = warp_sum(windows);
     if (lane_id() == 0 && windows) atomicAdd(windows_out, (unsigned long long)windows);
@@ -279,8 +286,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_step(const uint64_t *__rest
 
 // ---- pass 2 by ranges (slices of at least 2^SR_MIN_LBITS slots).  Per
 // partition p the keys are regrouped by the range of the slice their home slot
-// falls in (a slice is cut into about three ranges per SM, so that the build
-// runs as one wave; k_sr_hist, k_sr_scatter), and one block per range then
+// falls in (a slice is cut into SR_BUILD_PER_SM ranges per SM, so that the
+// build runs as one wave; k_sr_hist, k_sr_scatter), and one block per range then
 // builds that range in shared memory (k_sr_build): it loads the range (all
 // empty on a fresh table), inserts the range's keys with shared-memory CAS
 // and add, and writes the range back whole.  A key whose probe run reaches the
@@ -292,11 +299,12 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_step(const uint64_t *__rest
 // linear-probing table.  Global atomics drop from two per occurrence to the
 // deferred keys alone, and a fresh slice needs no separate fill.
 constexpr int SR_MIN_LBITS = 12;        // slices below 4096 slots keep the atomic path
-constexpr int SR_MAX_SLOTS = 4600;      // slots of one range in shared memory (3 blocks per SM)
+constexpr int SR_BUILD_PER_SM = 4;      // build blocks resident per SM: the slice is cut into one wave of ranges
+constexpr int SR_MAX_SLOTS = 4600;      // slots of one range in shared memory (12 bytes each)
 constexpr int SR_THREADS = 1024;        // regrouping passes (2 blocks per SM: few per-block range counts)
 constexpr int SR_BUILD_THREADS = 512;
 constexpr int SR_MINI = 64;
-constexpr size_t SR_SMEM = (size_t)(SR_MAX_SLOTS + SR_MINI) * sizeof(Slot);
+constexpr size_t SR_SMEM = (size_t)(SR_MAX_SLOTS + SR_MINI) * 12;
 
 // A slice of 2^lbits slots is cut into nsub ranges: slot s belongs to range
 // floor(s * nsub / 2^lbits), so range r is [ceil(r 2^lbits / nsub),
@@ -422,16 +430,19 @@ __global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__res
     }
 }
 
-// shared-memory probe from `loc` up to `end`; adds `inc` where the key lives
-// or lands.  A slot's key never changes once set, so a plain load that sees the
-// key (most occurrences repeat a key already placed) needs only the add; an
-// empty slot is claimed with CAS.  Returns false if the probe ran off the end.
-__device__ __forceinline__ bool smem_add(Slot *tab, uint32_t loc, uint32_t end, uint64_t key, uint32_t inc) {
+// Shared-memory probe from `loc` up to `end` in a table kept as separate key
+// and count arrays (8-byte keys: a warp's random probes hit half as many banks
+// per slot as 16-byte slots would); adds `inc` where the key lives or lands.
+// A slot's key never changes once set, so a plain load that sees the key (most
+// occurrences repeat a key already placed) needs only the add; an empty slot
+// is claimed with CAS.  Returns false if the probe ran off the end.
+__device__ __forceinline__ bool smem_add(unsigned long long *keys, uint32_t *vals, uint32_t loc, uint32_t end,
+                                         uint64_t key, uint32_t inc) {
     for (; loc < end; loc++) {
-        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&tab[loc].key);
-        if (cur == EMPTY_KEY) cur = atomicCAS(&tab[loc].key, EMPTY_KEY, (unsigned long long)key);
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&keys[loc]);
+        if (cur == EMPTY_KEY) cur = atomicCAS(&keys[loc], EMPTY_KEY, (unsigned long long)key);
         if (cur == EMPTY_KEY || cur == key) {
-            atomicAdd(&tab[loc].val, inc);
+            atomicAdd(&vals[loc], inc);
             return true;
         }
     }
@@ -445,8 +456,10 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
                                                         uint64_t *__restrict__ defer_keys, uint32_t *__restrict__ defer_cnt,
                                                         uint64_t defer_cap, unsigned long long *__restrict__ defer_n) {
     extern __shared__ __align__(16) unsigned char sr_smem[];
-    Slot *tab = reinterpret_cast<Slot *>(sr_smem);
-    Slot *mini = tab + SR_MAX_SLOTS;
+    unsigned long long *tkey = reinterpret_cast<unsigned long long *>(sr_smem);   // [SR_MAX_SLOTS]
+    unsigned long long *mkey = tkey + SR_MAX_SLOTS;                                // [SR_MINI]
+    uint32_t *tval = reinterpret_cast<uint32_t *>(mkey + SR_MINI);                 // [SR_MAX_SLOTS]
+    uint32_t *mval = tval + SR_MAX_SLOTS;                                          // [SR_MINI]
     __shared__ uint64_t ab[2];
     const uint32_t r = blockIdx.x;
     const uint64_t r0 = range_first(t, r, nsub);
@@ -474,12 +487,20 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
         }
     }
     ulonglong2 *g = reinterpret_cast<ulonglong2 *>(t.slots + ((uint64_t)p << t.lbits) + r0);
-    ulonglong2 *st = reinterpret_cast<ulonglong2 *>(tab);
-    ulonglong2 e;
-    e.x = EMPTY_KEY;
-    e.y = 0;
-    for (uint32_t i = threadIdx.x; i < len; i += SR_BUILD_THREADS) st[i] = fresh ? e : g[i];
-    for (int i = threadIdx.x; i < SR_MINI; i += SR_BUILD_THREADS) reinterpret_cast<ulonglong2 *>(mini)[i] = e;
+    for (uint32_t i = threadIdx.x; i < len; i += SR_BUILD_THREADS) {
+        if (fresh) {
+            tkey[i] = EMPTY_KEY;
+            tval[i] = 0;
+        } else {
+            const ulonglong2 v = g[i];
+            tkey[i] = v.x;
+            tval[i] = (uint32_t)v.y;
+        }
+    }
+    for (int i = threadIdx.x; i < SR_MINI; i += SR_BUILD_THREADS) {
+        mkey[i] = EMPTY_KEY;
+        mval[i] = 0;
+    }
     __syncthreads();
     const uint64_t a = ab[0], b = ab[1];
     for (uint64_t i0 = a + threadIdx.x; i0 < b; i0 += 4 * SR_BUILD_THREADS) {
@@ -492,10 +513,10 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const uint64_t key = k4[u];
-            if (key == EMPTY_KEY || smem_add(tab, (uint32_t)((mix64(key) & t.lmask) - r0), len, key, 1u)) continue;
+            if (key == EMPTY_KEY || smem_add(tkey, tval, (uint32_t)((mix64(key) & t.lmask) - r0), len, key, 1u)) continue;
             // the probe left the range: count it in the per-block table, or defer it singly
             const uint32_t m = (uint32_t)(mix64(key ^ 0x5851F42D4C957F2DULL) & (SR_MINI - 1));
-            if (smem_add(mini, m, SR_MINI, key, 1u) || (m && smem_add(mini, 0, m, key, 1u))) continue;
+            if (smem_add(mkey, mval, m, SR_MINI, key, 1u) || (m && smem_add(mkey, mval, 0, m, key, 1u))) continue;
             const unsigned long long j = atomicAdd(defer_n, 1ULL);
             if (j < defer_cap) {
                 defer_keys[j] = key;
@@ -504,13 +525,18 @@ __global__ void __launch_bounds__(SR_BUILD_THREADS) k_sr_build(const uint64_t *_
         }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < len; i += SR_BUILD_THREADS) g[i] = st[i];
+    for (uint32_t i = threadIdx.x; i < len; i += SR_BUILD_THREADS) {
+        ulonglong2 v;
+        v.x = tkey[i];
+        v.y = tval[i];
+        g[i] = v;
+    }
     for (int i = threadIdx.x; i < SR_MINI; i += SR_BUILD_THREADS) {
-        if (mini[i].key == EMPTY_KEY) continue;
+        if (mkey[i] == EMPTY_KEY) continue;
         const unsigned long long j = atomicAdd(defer_n, 1ULL);
         if (j < defer_cap) {
-            defer_keys[j] = mini[i].key;
-            defer_cnt[j] = mini[i].val;
+            defer_keys[j] = mkey[i];
+            defer_cnt[j] = mval[i];
         }
     }
 }
@@ -879,7 +905,7 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     // ranges per slice: one wave of three build blocks per SM, more if a range
     // would not fit in shared memory
     const uint64_t slice = 1ULL << t->t.lbits;
-    uint32_t nsub = (uint32_t)std::min<uint64_t>(slice / 1024, (uint64_t)c->sm_count * 3);
+    uint32_t nsub = (uint32_t)std::min<uint64_t>(slice / 1024, (uint64_t)c->sm_count * SR_BUILD_PER_SM);
     nsub = (uint32_t)std::max<uint64_t>(nsub, (slice + SR_MAX_SLOTS - 1) / SR_MAX_SLOTS);
     const uint64_t bpp = (uint64_t)(NBUCKETS >> t->t.pbits);
     // partition boundaries on the host: the first offset of each partition's buckets
@@ -988,10 +1014,10 @@ int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
         prof_begin(c, TK_KID_HLL, &ev);
         for (int s = 0; s < nsets; s++) {
             if (t->canonical)
-                k_part_hist<true><<<grids[s], SC_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
+                k_part_hist<true><<<grids[s], HIST_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
                                                                           hist, cols, col0[s], t->d_hll, t->d_counters + 1);
             else
-                k_part_hist<false><<<grids[s], SC_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
+                k_part_hist<false><<<grids[s], HIST_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
                                                                            hist, cols, col0[s], t->d_hll, t->d_counters + 1);
             c->launches++;
         }
