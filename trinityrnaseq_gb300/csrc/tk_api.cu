@@ -47,7 +47,7 @@ int check_launch(tk_ctx *c, const char *what) { return cuda_check(c, cudaGetLast
 // handed out again to work queued on that same stream, after it.  Blocks
 // cached by all contexts of the process are capped at BIG_CACHE_MAX.
 constexpr size_t BIG_BLOCK = 256ull << 20;
-constexpr size_t BIG_CACHE_MAX = 96ull << 30;
+constexpr size_t BIG_CACHE_MAX = 128ull << 30;
 static std::atomic<size_t> g_big_cached{0};
 
 static void big_release(tk_ctx *c) {

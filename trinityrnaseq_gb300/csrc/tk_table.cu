@@ -904,9 +904,10 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     const int nparts = 1 << t->t.pbits;
     // ranges per slice: one wave of three build blocks per SM, more if a range
     // would not fit in shared memory
-    const uint64_t slice = 1ULL << t->t.lbits;
-    uint32_t nsub = (uint32_t)std::min<uint64_t>(slice / 1024, (uint64_t)c->sm_count * SR_BUILD_PER_SM);
-    nsub = (uint32_t)std::max<uint64_t>(nsub, (slice + SR_MAX_SLOTS - 1) / SR_MAX_SLOTS);
+    const uint64_t slice = 1ULL << t->t.lbits, wave = (uint64_t)c->sm_count * SR_BUILD_PER_SM;
+    uint32_t nsub;
+    if (slice / 1024 < wave) nsub = (uint32_t)(slice / 1024);   // a small slice: ranges of 1024 slots
+    else nsub = (uint32_t)(wave * ((slice + wave * SR_MAX_SLOTS - 1) / (wave * SR_MAX_SLOTS)));   // whole waves
     const uint64_t bpp = (uint64_t)(NBUCKETS >> t->t.pbits);
     // partition boundaries on the host: the first offset of each partition's buckets
     std::vector<uint64_t> pb(nparts + 1);
