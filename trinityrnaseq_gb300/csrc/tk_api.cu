@@ -42,10 +42,12 @@ int check_launch(tk_ctx *c, const char *what) { return cuda_check(c, cudaGetLast
 // about the same size.  Carving them out of the stream-ordered pool instead
 // left the pool's mapping fragmented after a few rounds of differently sized
 // requests, and the random-access kernels on a table placed in it ran 10%
-// slower (insert) to 45% slower (histogram and dump) from then on.  A freed
-// block may still be in use by work queued on the context's stream; it is only
-// handed out again to work queued on that same stream, after it.  Blocks
-// cached by all contexts of the process are capped at BIG_CACHE_MAX.
+// slower (insert) to 45% slower (histogram and dump) from then on.  A request
+// takes the smallest cached block at most 1/8 larger.  A freed block may still
+// be in use by work queued on the context's stream; it is only handed out
+// again to work queued on that same stream, after it.  Blocks cached by all
+// contexts of the process are capped at BIG_CACHE_MAX; past it a context
+// frees its least recently freed blocks first.
 constexpr size_t BIG_BLOCK = 256ull << 20;
 constexpr size_t BIG_CACHE_MAX = 128ull << 30;
 static std::atomic<size_t> g_big_cached{0};
@@ -74,7 +76,7 @@ int dmalloc(tk_ctx *c, void **p, size_t bytes, const char *what) {
         int best = -1;
         for (size_t i = 0; i < c->big_free.size(); i++) {
             const size_t sz = c->big_free[i].second;
-            if (sz >= bytes && sz - bytes <= bytes / 2 && (best < 0 || sz < c->big_free[best].second)) best = (int)i;
+            if (sz >= bytes && sz - bytes <= bytes / 8 && (best < 0 || sz < c->big_free[best].second)) best = (int)i;
         }
         if (best >= 0) {
             *p = c->big_free[best].first;
@@ -118,12 +120,26 @@ void dfree(tk_ctx *c, void *p) {
     }
     const size_t sz = it->second;
     c->big_used.erase(it);
-    if (g_big_cached + sz > BIG_CACHE_MAX) {
-        // over the cap: free it once the work queued before it is done
+    if (sz > BIG_CACHE_MAX || g_big_cached + sz > BIG_CACHE_MAX) {
+        // over the cap: give back this context's least recently freed blocks
+        // (or this one, if it alone is too big) once the queued work is done
         cudaStreamSynchronize(c->stream);
         if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
-        cudaFree(p);
-        return;
+        if (sz > BIG_CACHE_MAX) {
+            cudaFree(p);
+            return;
+        }
+        size_t drop = 0;
+        while (drop < c->big_free.size() && g_big_cached + sz > BIG_CACHE_MAX) {
+            cudaFree(c->big_free[drop].first);
+            g_big_cached -= c->big_free[drop].second;
+            drop++;
+        }
+        c->big_free.erase(c->big_free.begin(), c->big_free.begin() + drop);
+        if (g_big_cached + sz > BIG_CACHE_MAX) {   // the rest is cached by other contexts
+            cudaFree(p);
+            return;
+        }
     }
     g_big_cached += sz;
     c->big_free.push_back({p, sz});
