@@ -95,6 +95,10 @@ int tk_ctx_mem_info(tk_ctx *ctx, uint64_t *free_bytes, uint64_t *total_bytes);
  * atomics != 0 the CAS probe + red.add pair of a count insert).  The
  * roofline denominator for the hash-table kernels. */
 int tk_ctx_random_access_rate(tk_ctx *ctx, uint64_t table_bytes, int atomics, double *accesses_per_s);
+/* Device blocks of 256 MB and more are kept by the context after they are
+ * freed, for the next request of about the same size (up to 128 GB cached per
+ * process, or TRINKMER_BLOCK_CACHE_GB); this gives them back to the driver. */
+int tk_ctx_trim(tk_ctx *ctx);
 /* Probe limit of the hash tables before a key is sent to the overflow list
  * and the table grows (jellyfish count -p/--reprobes; default 4096). */
 int tk_ctx_set_reprobes(tk_ctx *ctx, int max_probes);

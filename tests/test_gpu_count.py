@@ -184,3 +184,33 @@ def test_range_build_fallback_when_deferred_list_overruns(native_built, oracle):
     left, right = synth.gene_pairs(seed=41, n_genes=2000, n_pairs=300000, fastq=False)
     keys, counts = oracle.count(left.tobytes() + right.tobytes(), 25, True)
     assert capped.stdout == oracle.dump(keys, counts, 25, 1)
+
+
+def test_block_cache_trim_and_zero_cap(native_built, ctx, oracle):
+    """Large blocks are cached per context after they are freed; tk_ctx_trim
+    gives them back, and a zero cap (TRINKMER_BLOCK_CACHE_GB=0) frees them at
+    once.  Counting is unchanged either way."""
+    import os
+    import subprocess
+    import sys
+    left, right = synth.gene_pairs(seed=43, n_genes=3000, n_pairs=1_500_000, fastq=False)
+    t = KmerTable(ctx, 25, True)
+    t.count_text(left.tobytes() + right.tobytes())
+    assert t.info(distinct=False)[2] * 16 >= 256 << 20   # the table is a cached-size block
+    t.free()
+    free_before, _ = ctx.mem_info()
+    ctx.trim()
+    free_after, _ = ctx.mem_info()
+    assert free_after >= free_before
+    code = ("import sys\n"
+            "from trinityrnaseq_gb300 import Context, KmerTable, synth\n"
+            "left, right = synth.gene_pairs(seed=43, n_genes=3000, n_pairs=200000, fastq=False)\n"
+            "t = KmerTable(Context(0), 25, True)\n"
+            "t.count_text(left.tobytes() + right.tobytes())\n"
+            "sys.stdout.buffer.write(t.dump_fasta(2))\n")
+    p = subprocess.run([sys.executable, "-c", code], env=dict(os.environ, TRINKMER_BLOCK_CACHE_GB="0"),
+                       capture_output=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    left, right = synth.gene_pairs(seed=43, n_genes=3000, n_pairs=200000, fastq=False)
+    keys, counts = oracle.count(left.tobytes() + right.tobytes(), 25, True)
+    assert p.stdout == oracle.dump(keys, counts, 25, 2)

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cctype>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -49,8 +50,18 @@ int check_launch(tk_ctx *c, const char *what) { return cuda_check(c, cudaGetLast
 // contexts of the process are capped at BIG_CACHE_MAX; past it a context
 // frees its least recently freed blocks first.
 constexpr size_t BIG_BLOCK = 256ull << 20;
-constexpr size_t BIG_CACHE_MAX = 128ull << 30;
 static std::atomic<size_t> g_big_cached{0};
+
+// 128 GB, or TRINKMER_BLOCK_CACHE_GB (several processes sharing one GPU, such
+// as two coverage-statistics runs side by side, each keep their own cache)
+static size_t big_cache_max() {
+    static const size_t v = [] {
+        const char *e = getenv("TRINKMER_BLOCK_CACHE_GB");
+        return e ? (size_t)(strtod(e, nullptr) * (double)(1ull << 30)) : (size_t)(128ull << 30);
+    }();
+    return v;
+}
+#define BIG_CACHE_MAX big_cache_max()
 
 static void big_release(tk_ctx *c) {
     if (c->big_free.empty()) return;
@@ -422,6 +433,17 @@ int tk_ctx_random_access_rate(tk_ctx *c, uint64_t table_bytes, int atomics, doub
     dfree(c, tab);
     if (sink) dfree(c, sink);
     return e;
+}
+
+int tk_ctx_trim(tk_ctx *c) {
+    CHECK_CTX(c);
+    big_release(c);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) {
+        TK_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaMemPoolTrimTo(pool, 0);
+    }
+    return TK_OK;
 }
 
 int tk_ctx_mem_info(tk_ctx *c, uint64_t *free_bytes, uint64_t *total_bytes) {

@@ -109,6 +109,10 @@ class Context:
                    "tk_ctx_random_access_rate")
         return r.value
 
+    def trim(self) -> None:
+        """Gives the context's cached device blocks back to the driver (tk_ctx_trim)."""
+        self.check(self.lib.tk_ctx_trim(self.h), "tk_ctx_trim")
+
     def mem_info(self) -> Tuple[int, int]:
         f, t = C.c_uint64(), C.c_uint64()
         self.check(self.lib.tk_ctx_mem_info(self.h, C.byref(f), C.byref(t)), "tk_ctx_mem_info")

@@ -53,6 +53,7 @@ SIGNATURES = {
     "tk_ctx_mem_info": (C.c_int, [vp, P(u64), P(u64)]),
     "tk_ctx_set_reprobes": (C.c_int, [vp, C.c_int]),
     "tk_ctx_random_access_rate": (C.c_int, [vp, u64, C.c_int, P(C.c_double)]),
+    "tk_ctx_trim": (C.c_int, [vp]),
     "tk_reads_parse": (C.c_int, [vp, vp, u64, C.c_int, P(vp)]),
     "tk_reads_parse_many": (C.c_int, [vp, P(vp), P(u64), u32, C.c_int, P(vp)]),
     "tk_split_records": (C.c_int, [vp, u64, u32, P(u64)]),
