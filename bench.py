@@ -101,7 +101,9 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks.dev{device}.csv"
+        # raw samples (the JSON line carries their summary); BENCH_CLOCKS_DIR keeps them
+        import tempfile
+        self.path = Path(os.environ.get("BENCH_CLOCKS_DIR", tempfile.gettempdir())) / f"trinkmer_clocks.dev{device}.csv"
 
     def start(self):
         try:
