@@ -189,11 +189,45 @@ __global__ void k_line_records(const uint32_t *__restrict__ is_hdr, uint64_t *__
     if (incl == 0) len[j] = 0u;
 }
 
+// FASTQ: line j belongs to record j >> 2, whose header is line 4r
+__global__ void k_fastq_records(uint64_t *__restrict__ line_rec, uint64_t n_lines, uint64_t *__restrict__ hdr_line) {
+    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_lines) return;
+    line_rec[j] = j >> 2;
+    if ((j & 3) == 0) hdr_line[j >> 2] = j;
+}
+
 // ---- fast path, copy.  A warp takes 32 consecutive lines: lane l loads line
 // l's metadata (coalesced), header lines record their read's start, and then
 // the warp copies the group's sequence lines one after another, 32 bytes per
 // step with four steps in flight, upper-casing into seq.  A sequence line
 // holding whitespace sets *ws_seen and the byte-wise path redoes the emit.
+// The 4 bytes at offset so of a line of n bytes starting at text position S;
+// bytes outside the line read as 'A' (neither whitespace nor lower case).
+// Two aligned 4-byte loads and a funnel shift when the text is aligned and
+// both words lie inside it, byte loads otherwise.
+__device__ __forceinline__ uint32_t line_word(const ParseGeom &g, uint64_t S, int64_t so, uint32_t n) {
+    const int64_t a = (int64_t)S + so;
+    uint32_t x;
+    if (g.vec && a >= 0 && (uint64_t)((a & ~3LL) + 8) <= g.len) {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(g.text + (a & ~3LL));
+        x = __funnelshift_r(__ldg(p), __ldg(p + 1), 8u * (uint32_t)(a & 3));
+    } else {
+        x = 0;
+        for (int i = 0; i < 4; i++) {
+            const int64_t q = so + i;
+            const uint32_t c = (q >= 0 && q < (int64_t)n) ? (uint8_t)g.text[S + q] : 0x41u;
+            x |= c << (8 * i);
+        }
+        return x;
+    }
+    if (so >= 0 && so + 4 <= (int64_t)n) return x;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        if (so + i < 0 || so + i >= (int64_t)n) x = (x & ~(0xFFu << (8 * i))) | (0x41u << (8 * i));
+    return x;
+}
+
 __global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end, const uint8_t *__restrict__ kind,
                              const uint64_t *__restrict__ line_rec, const uint64_t *__restrict__ line_out,
                              uint64_t n_lines, uint8_t *__restrict__ seq, uint64_t *__restrict__ rd_off,
@@ -220,9 +254,10 @@ __global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end,
         }
         unsigned todo = __ballot_sync(0xffffffffu, len > 0);
         while (todo) {
-            // four lines at a time: all their loads are in flight before any store
+            // four lines at a time, one aligned 4-byte output word per lane and
+            // line: all loads are in flight before any store
             uint64_t s0[4], d0[4];
-            uint32_t n[4], nmax = 0;
+            uint32_t n[4], nw[4], wmax = 0;
 #pragma unroll
             for (int b = 0; b < 4; b++) {
                 const int l = todo ? __ffs(todo) - 1 : 0;
@@ -231,27 +266,36 @@ __global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end,
                 s0[b] = __shfl_sync(0xffffffffu, src, l);
                 d0[b] = __shfl_sync(0xffffffffu, dst, l);
                 n[b] = have ? __shfl_sync(0xffffffffu, len, l) : 0u;
-                nmax = max(nmax, n[b]);
+                nw[b] = n[b] ? (uint32_t)(((d0[b] + n[b] + 3) >> 2) - (d0[b] >> 2)) : 0u;
+                wmax = max(wmax, nw[b]);
             }
-            for (uint32_t q0 = 0; q0 < nmax; q0 += 128) {
-                uint32_t c[4][4];
+            for (uint32_t w0 = 0; w0 < wmax; w0 += 32) {
+                const uint32_t w = w0 + lane;
+                uint32_t x[4];
 #pragma unroll
                 for (int b = 0; b < 4; b++)
+                    x[b] = w < nw[b] ? line_word(g, s0[b], (int64_t)4 * w - (int64_t)(d0[b] & 3), n[b]) : 0x41414141u;
 #pragma unroll
-                    for (int u = 0; u < 4; u++) {
-                        const uint32_t q = q0 + 32 * u + lane;
-                        c[b][u] = q < n[b] ? (uint8_t)g.text[s0[b] + q] : (uint32_t)'A';
+                for (int b = 0; b < 4; b++) {
+                    if (w >= nw[b]) continue;
+                    const int64_t so = (int64_t)4 * w - (int64_t)(d0[b] & 3);   // line offset of the word's first byte
+                    const uint32_t t = x[b] & 0x7F7F7F7Fu;
+                    // bit 7 of each byte that is a-z, then of each byte that is ' ' or 9..13
+                    const uint32_t lower = (t + 0x1F1F1F1Fu) & ~(t + 0x05050505u) & ~x[b] & 0x80808080u;
+                    const uint32_t sp = x[b] ^ 0x20202020u;
+                    const uint32_t zsp = ~(((sp & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | sp) & 0x80808080u;
+                    const uint32_t rng = (t + 0x77777777u) & ~(t + 0x72727272u) & ~x[b] & 0x80808080u;
+                    ws |= (zsp | rng) != 0u;
+                    const uint32_t up = x[b] ^ (lower >> 2);
+                    uint8_t *o = seq + (d0[b] & ~3ULL) + 4ull * w;
+                    if (so >= 0 && so + 4 <= (int64_t)n[b]) {
+                        *reinterpret_cast<uint32_t *>(o) = up;
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 4; i++)
+                            if (so + i >= 0 && so + i < (int64_t)n[b]) o[i] = (uint8_t)(up >> (8 * i));
                     }
-#pragma unroll
-                for (int b = 0; b < 4; b++)
-#pragma unroll
-                    for (int u = 0; u < 4; u++) {
-                        const uint32_t q = q0 + 32 * u + lane;
-                        if (q < n[b]) {
-                            ws |= is_ws(c[b][u]);
-                            seq[d0[b] + q] = (uint8_t)(c[b][u] - 'a' < 26u ? c[b][u] - 32u : c[b][u]);
-                        }
-                    }
+                }
             }
         }
     }
@@ -487,16 +531,24 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
         c->launches++;
         uint32_t herr[2] = {0, 0};
         if ((e = cuda_check(c, cudaMemcpyAsync(herr, c->d_err + DE_PARSE, 8, cudaMemcpyDeviceToHost, c->stream), "err d2h"))) break;
-        if ((e = scan_excl_u32_to_u64(c, is_hdr, line_rec, n_lines, &n_reads))) break;  // syncs
+        if (fastq) {
+            // 4-line records: record j >> 2, header line 4r, no scan needed
+            n_reads = n_lines / 4;
+            if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
+            k_fastq_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(line_rec, n_lines, hdr_line);
+            c->launches++;
+        } else {
+            if ((e = scan_excl_u32_to_u64(c, is_hdr, line_rec, n_lines, &n_reads))) break;  // syncs
+            if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
+            k_line_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(is_hdr, line_rec, n_lines, hdr_line, line_len);
+            c->launches++;
+        }
+        if ((e = alloc((void **)&line_out, (n_lines + 1) * 8, "line outputs"))) break;
+        if ((e = scan_excl_u32_to_u64(c, line_len, line_out, n_lines, &n_emit))) break;   // syncs
         if (herr[0]) {
             e = set_err(c, TK_E_PARSE, "FASTQ input: malformed record at line " + std::to_string(herr[1]));
             break;
         }
-        if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
-        k_line_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(is_hdr, line_rec, n_lines, hdr_line, line_len);
-        c->launches++;
-        if ((e = alloc((void **)&line_out, (n_lines + 1) * 8, "line outputs"))) break;
-        if ((e = scan_excl_u32_to_u64(c, line_len, line_out, n_lines, &n_emit))) break;
     } while (0);
     if (e) {
         for (void *p : tmp) dfree(c, p);
