@@ -60,7 +60,9 @@ extern "C" {
 #define TK_KID_R2T_ASSIGN 9   /* read -> component vote */
 #define TK_KID_BINS 10        /* batched per-bin counting */
 #define TK_KID_SCATTER 11     /* k-mers into hash-partition buckets (count pass 1) */
-#define TK_KID_NUM 12         /* number of kernel classes */
+#define TK_KID_NORM 12        /* normalization: name sort, pair merge, selection */
+#define TK_KID_EXTRACT 13     /* normalization: selected FASTQ records */
+#define TK_KID_NUM 14         /* number of kernel classes */
 
 typedef struct tk_ctx tk_ctx;
 typedef struct tk_reads tk_reads;
@@ -247,6 +249,56 @@ int tk_r2t_component_ids(const tk_r2t *r2t, uint64_t *ids);
 int tk_r2t_assign(tk_r2t *r2t, const tk_reads *reads, int where, int32_t *rec,
                   uint32_t *hits, uint32_t *nwin);
 void tk_r2t_free(tk_r2t *r2t);
+
+/* ------------------------------------------------------------- normalization
+ * Replaces what util/insilico_read_normalization.pl does with the coverage
+ * statistics of the reads (Trinity:3421-3479 runs it with --pairs_together for
+ * paired reads): each side's stats table sorted by read name
+ * (`sort -k1,1` under LC_ALL=C, insilico:865-892), the two sorted tables
+ * merged by util/support_scripts/nbkc_merge_left_right_stats.pl --sorted
+ * (insilico:951-965), the rows selected by nbkc_normalize.pl --max_cov
+ * --min_cov --max_CV (insilico:972-977; a side alone, right == NULL, as
+ * insilico:917-947 does for single-end reads), and the selected reads
+ * extracted from the FASTQ input (make_normalized_reads_file,
+ * insilico:470-584).
+ *
+ * tk_norm_select takes the read sets the statistics belong to (their names;
+ * both must stay alive while the tk_norm is used) and their per-read median,
+ * mean and stdev as tk_coverage_stats writes them (`where`: TK_HOST or
+ * TK_DEVICE arrays of n_reads entries).  The tables it works on are the ones
+ * fastaToKmerCoverageStats prints (acc, "%u", "%g", "%g"), so the result is
+ * the reference scripts' output on those tables byte for byte: rows in
+ * sorted-name order, the merge's two-cursor pairing, averages through
+ * "%.1f", nbkc_normalize.pl's srand(12345) draw sequence (Perl's drand48).
+ * A mean or stdev outside [1e-17, 1.8e19) (other than 0), or a selected row
+ * with median 0 (min_cov <= 0; Perl dies dividing by it), is TK_E_INVAL. */
+typedef struct tk_norm tk_norm;
+typedef struct tk_norm_counts {
+    uint64_t rows;        /* rows nbkc_normalize.pl read (merged pairs, or reads) */
+    uint64_t selected;    /* accs printed */
+    uint64_t aberrant;    /* mean <= 0 or stdev/mean > max_CV */
+    uint64_t below_min;   /* median < min_cov */
+} tk_norm_counts;
+int tk_norm_select(tk_ctx *ctx, const tk_reads *left, const uint32_t *left_median, const float *left_mean,
+                   const float *left_stdev, const tk_reads *right, const uint32_t *right_median,
+                   const float *right_mean, const float *right_stdev, int where, int max_cov, int min_cov,
+                   int max_cv, tk_norm **out);
+/* counts and the byte length of the accs text */
+int tk_norm_info(const tk_norm *norm, tk_norm_counts *counts, uint64_t *accs_len);
+/* nbkc_normalize.pl's output: one selected acc per line (without "/1" or "/2") */
+int tk_norm_accs(const tk_norm *norm, int where, char *out, uint64_t cap);
+/* The table nbkc_normalize.pl reads: pairs.K25.stats as
+ * nbkc_merge_left_right_stats.pl writes it, or a side's sorted stats table
+ * (header row first).  out == NULL returns the length only. */
+int tk_norm_table(tk_norm *norm, int where, char *out, uint64_t cap, uint64_t *len);
+/* The FASTQ records of `fastq` whose core names the selection holds, verbatim
+ * and in input order (the name rules of PerlLib/Fastq_reader.pm:106-121 and
+ * insilico:452-466, 529-531); the text is kept in the tk_norm until the next
+ * call.  A selected name without a record in `fastq` is TK_E_PARSE (the script
+ * dies with "not all specified records have been retrieved"). */
+int tk_norm_extract(tk_norm *norm, const tk_reads *fastq, uint64_t *len);
+int tk_norm_extract_copy(const tk_norm *norm, int where, char *out, uint64_t cap);
+void tk_norm_free(tk_norm *norm);
 
 /* ------------------------------------------------------------- batched bins
  * Replaces the per-bin k-mer counting of Trinity's phase 2 (one

@@ -846,4 +846,339 @@ int orc_fastq_to_fasta(const char *text, size_t len, int append, int flags, char
     return 0;
 }
 
+/* ---------------------------------------------------------- normalization tail
+ * What util/insilico_read_normalization.pl does with the two coverage-stats
+ * tables, restated step by step on their text:
+ *   sort    head -n1 S > S.sort && tail -n +2 S | sort -k1,1 >> S.sort
+ *           (insilico_read_normalization.pl:865-892, LC_ALL=C from
+ *           PerlLib/COMMON.pm:7): rows by their first blank-delimited field,
+ *           bytewise, ties by the whole line (sort's last-resort compare);
+ *   merge   util/support_scripts/nbkc_merge_left_right_stats.pl --sorted
+ *           (insilico:951-965; script lines 89-146): two cursors, a pair when
+ *           the accs agree without their "/digit" ending, else the cursor
+ *           whose acc is string-less moves; averages printed with "%.1f";
+ *   select  util/support_scripts/nbkc_normalize.pl (insilico:972-977; script
+ *           lines 68-117): srand(12345); rows below min_cov, with mean <= 0 or
+ *           stdev/mean > max_CV are dropped, each other row draws rand(1) and
+ *           is kept when the draw is <= max_cov/median; its acc is printed
+ *           without a final "/1" or "/2".
+ * Single-end (or pairs kept apart, insilico:917-947) selects on one sorted
+ * table.  Perl's rand is drand48 (X' = 0x5DEECE66D X + 11 mod 2^48, seed
+ * (s << 16) + 0x330E, value X'/2^48); its numeric conversion of these fields
+ * is strtod's. */
+
+typedef struct { const char *p; size_t n; } span_t;
+
+static int is_blank_c(unsigned char c) { return c == ' ' || c == '\t'; }
+static int is_perl_ws(unsigned char c) { return c == ' ' || (c >= 9 && c <= 13); }
+
+static int span_cmp(span_t a, span_t b) {
+    size_t m = a.n < b.n ? a.n : b.n;
+    int r = m ? memcmp(a.p, b.p, m) : 0;
+    if (r) return r;
+    return a.n < b.n ? -1 : a.n > b.n;
+}
+
+static span_t first_field(span_t line) {
+    size_t i = 0;
+    while (i < line.n && !is_blank_c((unsigned char)line.p[i])) i++;
+    span_t f = {line.p, i};
+    return f;
+}
+
+static int cmp_stats_line(const void *x, const void *y) {
+    span_t a = *(const span_t *)x, b = *(const span_t *)y;
+    int r = span_cmp(first_field(a), first_field(b));
+    return r ? r : span_cmp(a, b);
+}
+
+/* rows of a table (after its header line), without their "\n" */
+static int table_rows(const char *t, size_t len, span_t *head, span_t **rows, size_t *n) {
+    size_t cap = 1024, k = 0, i = 0;
+    span_t *r = malloc(cap * sizeof *r);
+    if (!r) return ORC_E_OOM;
+    int have_head = 0;
+    while (i < len) {
+        size_t j = i;
+        while (j < len && t[j] != '\n') j++;
+        span_t s = {t + i, j - i};
+        if (!have_head) { *head = s; have_head = 1; }
+        else {
+            if (k == cap) {
+                cap *= 2;
+                span_t *q = realloc(r, cap * sizeof *r);
+                if (!q) { free(r); return ORC_E_OOM; }
+                r = q;
+            }
+            r[k++] = s;
+        }
+        i = j + 1;
+    }
+    if (!have_head) { free(r); return ORC_E_PARSE; }
+    *rows = r;
+    *n = k;
+    return 0;
+}
+
+/* tab-separated fields of a row; returns their number (at most max) */
+static int split_tabs(span_t line, span_t *f, int max) {
+    int k = 0;
+    size_t i = 0;
+    while (k < max) {
+        size_t j = i;
+        while (j < line.n && line.p[j] != '\t') j++;
+        f[k].p = line.p + i; f[k].n = j - i; k++;
+        if (j >= line.n) break;
+        i = j + 1;
+    }
+    return k;
+}
+
+static double num_of(span_t f) {
+    char tmp[64];
+    size_t n = f.n < sizeof tmp - 1 ? f.n : sizeof tmp - 1;
+    memcpy(tmp, f.p, n);
+    tmp[n] = 0;
+    return strtod(tmp, NULL);
+}
+
+/* acc without a final "/<digit>" when what precedes it is one or more non-space bytes */
+static span_t merge_core(span_t a) {
+    if (a.n >= 3 && a.p[a.n - 2] == '/' && a.p[a.n - 1] >= '0' && a.p[a.n - 1] <= '9') {
+        for (size_t i = 0; i + 2 < a.n; i++)
+            if (is_perl_ws((unsigned char)a.p[i])) return a;
+        a.n -= 2;
+    }
+    return a;
+}
+
+static span_t strip_12(span_t a) {
+    if (a.n >= 2 && a.p[a.n - 2] == '/' && (a.p[a.n - 1] == '1' || a.p[a.n - 1] == '2')) a.n -= 2;
+    return a;
+}
+
+static int sb_put(sbuf_t *s, const char *p, size_t n) {
+    if (sb_reserve(s, n)) return ORC_E_OOM;
+    memcpy(s->b + s->n, p, n);
+    s->n += n;
+    return 0;
+}
+
+int orc_norm(const char *left, size_t llen, const char *right, size_t rlen, int max_cov, int min_cov, int max_cv,
+             char **table, size_t *table_len, char **accs, size_t *accs_len, uint64_t counts[4]) {
+    span_t lh, rh, *lr = NULL, *rr = NULL;
+    size_t nl = 0, nr = 0;
+    sbuf_t tb = {0}, ab = {0};
+    int e = table_rows(left, llen, &lh, &lr, &nl);
+    if (!e && right) e = table_rows(right, rlen, &rh, &rr, &nr);
+    if (e) { free(lr); return e; }
+    qsort(lr, nl, sizeof *lr, cmp_stats_line);
+    if (right) qsort(rr, nr, sizeof *rr, cmp_stats_line);
+    /* the table nbkc_normalize.pl reads: the merged pairs, or the sorted stats */
+    if (right) {
+        const char *hdr = "acc\tleft_acc\tleft_median_cov\tleft_mean_cov\tleft_stdev\tright_acc\tright_median_cov\t"
+                          "right_mean_cov\tright_stdev\tmedian_cov\tmean_cov\tstdev\n";
+        e = sb_put(&tb, hdr, strlen(hdr));
+        size_t i = 0, j = 0;
+        while (!e && i < nl && j < nr) {
+            span_t a[8], b[8];
+            if (split_tabs(lr[i], a, 8) != 4 || split_tabs(rr[j], b, 8) != 4) { e = ORC_E_PARSE; break; }
+            span_t ca = merge_core(a[0]), cb = merge_core(b[0]);
+            if (span_cmp(ca, cb) != 0) {
+                if (span_cmp(a[0], b[0]) < 0) i++; else j++;
+                continue;
+            }
+            char avg[3][64];
+            for (int q = 0; q < 3; q++) snprintf(avg[q], sizeof avg[q], "%.1f", (num_of(a[q + 1]) + num_of(b[q + 1])) / 2);
+            e = sb_put(&tb, ca.p, ca.n);
+            for (int q = 0; q < 4 && !e; q++) { e = sb_put(&tb, "\t", 1); if (!e) e = sb_put(&tb, a[q].p, a[q].n); }
+            for (int q = 0; q < 4 && !e; q++) { e = sb_put(&tb, "\t", 1); if (!e) e = sb_put(&tb, b[q].p, b[q].n); }
+            for (int q = 0; q < 3 && !e; q++) { e = sb_put(&tb, "\t", 1); if (!e) e = sb_put(&tb, avg[q], strlen(avg[q])); }
+            if (!e) e = sb_put(&tb, "\n", 1);
+            i++; j++;
+        }
+    } else {
+        e = sb_put(&tb, lh.p, lh.n);
+        if (!e) e = sb_put(&tb, "\n", 1);
+        for (size_t i = 0; i < nl && !e; i++) {
+            e = sb_put(&tb, lr[i].p, lr[i].n);
+            if (!e) e = sb_put(&tb, "\n", 1);
+        }
+    }
+    free(lr);
+    free(rr);
+    /* nbkc_normalize.pl over that table, columns looked up by name */
+    uint64_t total = 0, selected = 0, aberrant = 0, below = 0;
+    if (!e) {
+        span_t th, *rows = NULL;
+        size_t n = 0;
+        e = table_rows(tb.b, tb.n, &th, &rows, &n);
+        span_t hf[16];
+        int nh = e ? 0 : split_tabs(th, hf, 16);
+        int c_acc = -1, c_med = -1, c_mean = -1, c_sd = -1;
+        for (int q = 0; q < nh; q++) {
+            span_t f = hf[q];
+            if (f.n == 3 && !memcmp(f.p, "acc", 3)) c_acc = q;
+            else if (f.n == 10 && !memcmp(f.p, "median_cov", 10)) c_med = q;
+            else if (f.n == 8 && !memcmp(f.p, "mean_cov", 8)) c_mean = q;
+            else if (f.n == 5 && !memcmp(f.p, "stdev", 5)) c_sd = q;
+        }
+        if (!e && (c_acc < 0 || c_med < 0 || c_mean < 0 || c_sd < 0)) e = ORC_E_PARSE;
+        uint64_t x = ((uint64_t)12345 << 16) | 0x330E;
+        const uint64_t mask = (1ULL << 48) - 1;
+        for (size_t i = 0; i < n && !e; i++) {
+            span_t f[16];
+            if (split_tabs(rows[i], f, 16) != nh) { e = ORC_E_PARSE; break; }
+            total++;
+            double med = num_of(f[c_med]);
+            if (med < (double)min_cov) { below++; continue; }
+            double sd = num_of(f[c_sd]), u = num_of(f[c_mean]);
+            if (u <= 0) { aberrant++; continue; }
+            double cv = sd / u;
+            if (cv > (double)max_cv) { aberrant++; continue; }
+            x = (x * 0x5DEECE66DULL + 0xB) & mask;
+            double r = ldexp((double)x, -48);
+            if (med == 0) { e = ORC_E_INVAL; break; }   /* Perl: Illegal division by zero */
+            if (r <= (double)max_cov / med) {
+                span_t a = strip_12(f[c_acc]);
+                e = sb_put(&ab, a.p, a.n);
+                if (!e) e = sb_put(&ab, "\n", 1);
+                selected++;
+            }
+        }
+        free(rows);
+    }
+    if (e) { free(tb.b); free(ab.b); return e; }
+    if (!tb.b) tb.b = malloc(1);
+    if (!ab.b) ab.b = malloc(1);
+    if (!tb.b || !ab.b) { free(tb.b); free(ab.b); return ORC_E_OOM; }
+    counts[0] = total; counts[1] = selected; counts[2] = aberrant; counts[3] = below;
+    *table = tb.b; *table_len = tb.n;
+    *accs = ab.b; *accs_len = ab.n;
+    return 0;
+}
+
+/* ------------------------------------------------------------ read extraction
+ * make_normalized_reads_file of util/insilico_read_normalization.pl:470-584
+ * for FASTQ: the accs file's non-blank lines, each without a final "/" and
+ * word character (build_selected_index, :452-466), are the wanted names; every
+ * 4-line record of the FASTQ text (PerlLib/Fastq_reader.pm:47-75) whose core
+ * name -- the header's first whitespace-delimited field without '@' and
+ * without a final "/1" or "/2" (Fastq_reader.pm:106-121), then without its
+ * first "_forward" and its first "_reverse" (insilico:529-531) -- is wanted is
+ * written out verbatim, in input order.  A malformed record, or a wanted name
+ * no record carries (insilico:556-578), is an error: ORC_E_PARSE with
+ * *missing = the number of such names. */
+
+static int is_word_c(unsigned char c) {
+    return (c >= '0' && c <= '9') || (c >= 'A' && c <= 'Z') || (c >= 'a' && c <= 'z') || c == '_';
+}
+
+typedef struct { char *p; size_t n; uint32_t hits; } want_t;
+
+static int cmp_want(const void *x, const void *y) {
+    const want_t *a = x, *b = y;
+    span_t sa = {a->p, a->n}, sb2 = {b->p, b->n};
+    return span_cmp(sa, sb2);
+}
+
+static void remove_first(char *s, size_t *n, const char *pat) {
+    size_t m = strlen(pat);
+    for (size_t i = 0; i + m <= *n; i++)
+        if (!memcmp(s + i, pat, m)) {
+            memmove(s + i, s + i + m, *n - i - m);
+            *n -= m;
+            return;
+        }
+}
+
+int orc_norm_extract(const char *fq, size_t len, const char *accs, size_t alen, char **out, size_t *out_len,
+                     uint64_t *missing) {
+    *missing = 0;
+    size_t cap = 1024, nw = 0;
+    want_t *w = malloc(cap * sizeof *w);
+    if (!w) return ORC_E_OOM;
+    int e = 0;
+    for (size_t i = 0; i < alen && !e;) {
+        size_t j = i;
+        while (j < alen && accs[j] != '\n') j++;
+        size_t n = j - i;
+        int blank = 1;
+        for (size_t q = 0; q < n; q++) if (!is_perl_ws((unsigned char)accs[i + q])) blank = 0;
+        if (!blank) {
+            if (n >= 2 && accs[i + n - 2] == '/' && is_word_c((unsigned char)accs[i + n - 1])) n -= 2;
+            if (nw == cap) {
+                cap *= 2;
+                want_t *q = realloc(w, cap * sizeof *w);
+                if (!q) { e = ORC_E_OOM; break; }
+                w = q;
+            }
+            w[nw].p = malloc(n ? n : 1);
+            if (!w[nw].p) { e = ORC_E_OOM; break; }
+            memcpy(w[nw].p, accs + i, n);
+            w[nw].n = n;
+            w[nw].hits = 0;
+            nw++;
+        }
+        i = j + 1;
+    }
+    if (!e) qsort(w, nw, sizeof *w, cmp_want);
+    /* distinct names only */
+    size_t nd = 0;
+    for (size_t i = 0; i < nw && !e; i++) {
+        if (nd && w[nd - 1].n == w[i].n && !memcmp(w[nd - 1].p, w[i].p, w[i].n)) { free(w[i].p); continue; }
+        w[nd++] = w[i];
+    }
+    sbuf_t o = {0};
+    char *name = NULL;
+    size_t name_cap = 0;
+    for (size_t pos = 0; pos < len && !e;) {
+        /* four lines, each with its "\n" when there is one */
+        size_t ls[4], le[4], p = pos;
+        int nlines = 0;
+        while (nlines < 4 && p < len) {
+            size_t q = p;
+            while (q < len && fq[q] != '\n') q++;
+            ls[nlines] = p; le[nlines] = q; nlines++;
+            p = q < len ? q + 1 : q;
+        }
+        /* split(/\n/) drops trailing empty fields: the record needs 4 */
+        int fields = nlines;
+        while (fields > 0 && le[fields - 1] == ls[fields - 1]) fields--;
+        if (fields != 4 || fq[ls[0]] != '@') { e = ORC_E_PARSE; break; }
+        size_t a = ls[0] + 1, b = a;
+        while (b < le[0] && !is_perl_ws((unsigned char)fq[b])) b++;
+        size_t n = b - a;
+        if (n + 1 > name_cap) {
+            name_cap = 2 * (n + 1);
+            char *q = realloc(name, name_cap);
+            if (!q) { e = ORC_E_OOM; break; }
+            name = q;
+        }
+        memcpy(name, fq + a, n);
+        if (n >= 3 && name[n - 2] == '/' && (name[n - 1] == '1' || name[n - 1] == '2')) n -= 2;
+        remove_first(name, &n, "_forward");
+        remove_first(name, &n, "_reverse");
+        want_t key = {name, n, 0};
+        want_t *hit = nd ? bsearch(&key, w, nd, sizeof *w, cmp_want) : NULL;
+        if (hit) {
+            hit->hits++;
+            e = sb_put(&o, fq + pos, p - pos);
+        }
+        pos = p;
+    }
+    free(name);
+    for (size_t i = 0; i < nd; i++) {
+        if (!w[i].hits) (*missing)++;
+        free(w[i].p);
+    }
+    free(w);
+    if (!e && *missing) e = ORC_E_PARSE;
+    if (e) { free(o.b); return e; }
+    if (!o.b) { o.b = malloc(1); if (!o.b) return ORC_E_OOM; }
+    *out = o.b;
+    *out_len = o.n;
+    return 0;
+}
+
 void orc_free(void *p) { free(p); }

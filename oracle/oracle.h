@@ -88,6 +88,22 @@ int orc_records(const char *text, size_t len, char **out, size_t *out_len);
 int orc_fastq_to_fasta(const char *text, size_t len, int append, int flags, char **out, size_t *out_len,
                        uint64_t *bad);
 
+/* The normalization tail of util/insilico_read_normalization.pl (see
+ * oracle.c): left/right are coverage-stats tables as fastaToKmerCoverageStats
+ * prints them (header row first, any row order); right == NULL selects on one
+ * side alone.  *table = the table nbkc_normalize.pl reads (the merged pairs
+ * from nbkc_merge_left_right_stats.pl --sorted, or the sorted stats); *accs =
+ * what nbkc_normalize.pl prints; counts = {rows, selected, aberrant, below
+ * min_cov}. */
+int orc_norm(const char *left, size_t llen, const char *right, size_t rlen, int max_cov, int min_cov, int max_cv,
+             char **table, size_t *table_len, char **accs, size_t *accs_len, uint64_t counts[4]);
+
+/* The FASTQ records whose core names the accs text selects, verbatim and in
+ * input order (make_normalized_reads_file); ORC_E_PARSE with *missing > 0
+ * when a selected name has no record. */
+int orc_norm_extract(const char *fq, size_t len, const char *accs, size_t alen, char **out, size_t *out_len,
+                     uint64_t *missing);
+
 void orc_free(void *p);
 
 #ifdef __cplusplus

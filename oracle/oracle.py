@@ -47,6 +47,9 @@ def load() -> C.CDLL:
     lib.orc_r2t_values.argtypes = [vp, C.c_size_t, vp, C.c_size_t, C.c_int, C.c_int, C.c_int, P(u64), P(vp),
                                    P(vp), P(vp)]
     lib.orc_records.argtypes = [vp, C.c_size_t, P(vp), P(C.c_size_t)]
+    lib.orc_norm.argtypes = [vp, C.c_size_t, vp, C.c_size_t, C.c_int, C.c_int, C.c_int, P(vp), P(C.c_size_t), P(vp),
+                             P(C.c_size_t), P(u64)]
+    lib.orc_norm_extract.argtypes = [vp, C.c_size_t, vp, C.c_size_t, P(vp), P(C.c_size_t), P(u64)]
     lib.orc_free.argtypes = [vp]
     lib.orc_free.restype = None
     _lib = lib
@@ -89,6 +92,34 @@ def fastq_to_fasta(text: bytes, append: int = -1, flags: int = 0) -> bytes:
     if st == -4:
         raise ValueError(bad.value)
     _chk(st, "fastq_to_fasta")
+    return _take_bytes(p, n.value)
+
+
+def norm(left_stats: bytes, right_stats=None, max_cov: int = 200, min_cov: int = 1, max_cv: int = 10000):
+    """(table, accs, counts) of the normalization tail of
+    util/insilico_read_normalization.pl over coverage-stats tables: each side
+    sorted with `sort -k1,1`, nbkc_merge_left_right_stats.pl --sorted when
+    right_stats is given, nbkc_normalize.pl.  counts = (rows, selected,
+    aberrant, below min_cov)."""
+    lib = load()
+    tp, tn, ap, an = C.c_void_p(), C.c_size_t(), C.c_void_p(), C.c_size_t()
+    cnt = (C.c_uint64 * 4)()
+    r = right_stats if right_stats is not None else None
+    _chk(lib.orc_norm(left_stats, len(left_stats), r, len(r) if r is not None else 0, max_cov, min_cov, max_cv,
+                      C.byref(tp), C.byref(tn), C.byref(ap), C.byref(an), cnt), "norm")
+    return _take_bytes(tp, tn.value), _take_bytes(ap, an.value), tuple(int(v) for v in cnt)
+
+
+def norm_extract(fastq: bytes, accs: bytes) -> bytes:
+    """The FASTQ records the accs select (make_normalized_reads_file);
+    raises ValueError(number of selected names without a record) or on a
+    malformed record (ValueError(0))."""
+    lib = load()
+    p, n, miss = C.c_void_p(), C.c_size_t(), C.c_uint64()
+    st = lib.orc_norm_extract(fastq, len(fastq), accs, len(accs), C.byref(p), C.byref(n), C.byref(miss))
+    if st == -4:
+        raise ValueError(miss.value)
+    _chk(st, "norm_extract")
     return _take_bytes(p, n.value)
 
 

@@ -25,6 +25,20 @@ What each fixture pins:
   pairs.stats                util/support_scripts/nbkc_merge_left_right_stats.pl --sorted
   normalized.accs            util/support_scripts/nbkc_normalize.pl --max_cov 3
                              --min_cov 1 --max_CV 10000 on pairs.stats
+  norm.left.stats norm.right.stats
+                             coverage-stats tables for the normalization tail
+                             (duplicates, unpaired reads, odd names, every
+                             branch of nbkc_normalize.pl)
+  norm.pairs.stats           both sorted by insilico_read_normalization.pl:880's
+                             `sort -k1,1`, then nbkc_merge_left_right_stats.pl --sorted
+  norm.pairs.c5.accs norm.pairs.c200.accs
+                             nbkc_normalize.pl on it (--max_cov 5 --min_cov 2
+                             --max_CV 1; --max_cov 200 --min_cov 1 --max_CV 10000)
+  norm.left.c5.accs          nbkc_normalize.pl on the sorted left table alone
+  norm.left.fq / norm.left.c5.fq
+                             FASTQ reads and the records make_normalized_reads_file
+                             keeps for norm.pairs.c5.accs, read by
+                             PerlLib/Fastq_reader.pm
   r2t.bundle.fa r2t.reads.fa small bundle and reads
   r2t.out.sort               the oracle's readsToComponents rows through
                              `sort -k1,1n -k3,3nr -k2,2` under LC_ALL=C (Trinity:2258)
@@ -150,13 +164,150 @@ def make_prep(ref: Path) -> None:
     (HERE / "prep_dirty.ignore.fa").write_bytes(perl(ref, script, "-I", dq, "--ignore_dirty"))
 
 
+def norm_tables():
+    """Two coverage-stats tables (as fastaToKmerCoverageStats prints them,
+    unsorted) for the normalization tail: mates named <core>/1 and <core>/2,
+    unpaired reads on either side, a left name twice, names whose core ends
+    in /1, /3 endings, no ending, an empty name, "_forward"/"_reverse" names,
+    punctuation and a high byte around '/', and values that reach every
+    branch of nbkc_normalize.pl (median 0, mean 0, stdev/mean > 1, "%.1f"
+    ties, exponent forms of "%g").  Every value has at most 6 significant
+    digits, so float32 carries it exactly to "%g"."""
+    rnd = random.Random(4242)
+
+    def val(kind):
+        if kind == 0:
+            return "0"
+        if kind == 1:
+            return "%g" % (rnd.randint(1, 400) / 4)                 # quarter steps: "%.1f" ties
+        if kind == 2:
+            return "%g" % float("%.6g" % rnd.uniform(0.001, 60))
+        if kind == 3:
+            return "%g" % float("%.6g" % rnd.uniform(1e5, 5e7))     # 1.23457e+06 forms
+        return "%g" % float("%.6g" % rnd.uniform(1e-6, 1e-4))        # 1.5e-05 forms
+
+    def row(name):
+        med = rnd.choice([0, 1, 2, 2, 3, 4, 5, 7, 9, 12, 40, 300])
+        mean = val(rnd.choice([0, 1, 1, 2, 2, 2, 3, 4]) if rnd.random() < 0.15 else rnd.choice([1, 2]))
+        sd = val(rnd.choice([0, 1, 2, 2, 3, 4]))
+        return f"{name}\t{med}\t{mean}\t{sd}\n"
+
+    cores = [f"r{i:04d}" for i in range(150)]
+    cores += ["a.b", "a", "a-x", "a0", "x/1", "y/1/2", "r_forward", "s_reverse", "t_forward_x_reverse", "z\xc3z",
+              "P", "p", "u/3", "v/a", "w_"]
+    left, right = [], []
+    for c in cores:
+        p = rnd.random()
+        if c in ("x/1", "y/1/2"):
+            left.append(c + "/1"); right.append(c + "/2")
+        elif c == "u/3":
+            left.append("u/3"); right.append("u/3")
+        elif p < 0.75:
+            left.append(c + "/1"); right.append(c + "/2")
+        elif p < 0.83:
+            left.append(c + "/1")
+        elif p < 0.91:
+            right.append(c + "/2")
+        else:
+            left.append(c); right.append(c + "/" + rnd.choice("123"))
+    left.append("r0007/1")            # a name twice
+    left.append(""); right.append("")  # empty names
+    rnd.shuffle(left)
+    rnd.shuffle(right)
+    head = "acc\tmedian_cov\tmean_cov\tstdev\n"
+    lt = (head + "".join(row(n) for n in left)).encode("latin-1")
+    rt = (head + "".join(row(n) for n in right)).encode("latin-1")
+    return lt, rt
+
+
+def norm_fastq(names, seed):
+    """FASTQ records for the extraction: each name once (headers as Trinity's
+    inputs carry them: "@core/1", "@core 1:N:0:ACGT", "@core_forward/1"),
+    and some reads no selection names."""
+    rnd = random.Random(seed)
+    out = []
+    for i, n in enumerate(names):
+        L = rnd.randint(5, 40)
+        seq = "".join(rnd.choice("ACGT") for _ in range(L))
+        qual = "".join(rnd.choice("!#5?I") for _ in range(L))
+        out.append(f"@{n}\n{seq}\n+\n{qual}\n")
+    return "".join(out).encode("latin-1")
+
+
+def sort_stats_file(path: Path, out: Path) -> None:
+    """insilico_read_normalization.pl:880's command, run as it runs it."""
+    subprocess.run(f"head -n1 '{path}' > '{out}' && tail -n +2 '{path}' | sort -k1,1 >> '{out}'", shell=True,
+                   check=True, env=dict(os.environ, LC_ALL="C"))
+
+
+def extract_perl(ref: Path, fq: Path, accs: Path) -> bytes:
+    """make_normalized_reads_file (insilico:452-466, 505-545) on one FASTQ:
+    the records are read by the reference's PerlLib/Fastq_reader.pm."""
+    code = (r"use lib '%s/PerlLib'; use Fastq_reader; my %%idx;"
+            r" open(my $f, $ARGV[1]) or die; while (my $l = <$f>) { chomp $l; next unless $l =~ /\S/;"
+            r" $l =~ s|/\w$||; $idx{$l} = 0; } close $f;"
+            r" my $r = new Fastq_reader($ARGV[0]); while (my $s = $r->next()) { my $a = $s->get_core_read_name();"
+            r" $a =~ s/_forward//; $a =~ s/_reverse//; if (exists $idx{$a}) { $idx{$a}++;"
+            r" print $s->get_fastq_record(); } }"
+            r' my @m = grep { !$idx{$_} } keys %%idx; die "missing @m" if @m;' % ref)
+    return subprocess.run(["perl", "-e", code, str(fq), str(accs)], check=True, stdout=subprocess.PIPE).stdout
+
+
+def make_norm(ref: Path) -> None:
+    """The normalization-tail fixtures (insilico_read_normalization.pl:865-985,
+    470-584) from the reference's own scripts."""
+    lt, rt = norm_tables()
+    lp, rp = HERE / "norm.left.stats", HERE / "norm.right.stats"
+    lp.write_bytes(lt)
+    rp.write_bytes(rt)
+    ls, rs = HERE / "_norm.left.sort", HERE / "_norm.right.sort"
+    sort_stats_file(lp, ls)
+    sort_stats_file(rp, rs)
+    pairs = perl(ref, "util/support_scripts/nbkc_merge_left_right_stats.pl", "--left", ls, "--right", rs, "--sorted")
+    (HERE / "norm.pairs.stats").write_bytes(pairs)
+    pp = HERE / "norm.pairs.stats"
+    for tag, args in (("c5", (5, 2, 1)), ("c200", (200, 1, 10000))):
+        acc = perl(ref, "util/support_scripts/nbkc_normalize.pl", "--stats_file", pp, "--max_cov", args[0],
+                   "--min_cov", args[1], "--max_CV", args[2])
+        (HERE / f"norm.pairs.{tag}.accs").write_bytes(acc)
+    single = perl(ref, "util/support_scripts/nbkc_normalize.pl", "--stats_file", ls, "--max_cov", 5, "--min_cov", 2,
+                  "--max_CV", 1)
+    (HERE / "norm.left.c5.accs").write_bytes(single)
+    # extraction: FASTQ headers for every left read (named as the reads were
+    # before the FASTQ->FASTA prep added /1), plus reads nothing selects
+    lnames = [l.split(b"\t", 1)[0].decode("latin-1") for l in lt.split(b"\n")[1:] if l]
+    heads = []
+    for i, n in enumerate(sorted(set(lnames))):
+        core = n[:-2] if len(n) >= 3 and n[-2] == "/" and n[-1] in "12" else n
+        if not core or core != core.strip():
+            continue
+        if i % 5 == 1 and not core.endswith(("/1", "/2")):
+            heads.append(f"{core} 1:N:0:ACGT")
+        else:
+            heads.append(f"{core}/1")
+    # reads nothing selects; and "x", "y" (the accs of x/1/1 and y/1/2/1,
+    # whose own records have the core names x/1 and y/1/2) carried by reads of
+    # their own, without which the script dies ("not all specified records
+    # have been retrieved")
+    heads += ["extra1/1", "extra2/1 1:N:0", "x/2", "y 2:N:0"]
+    fq = HERE / "norm.left.fq"
+    fq.write_bytes(norm_fastq(heads, 99))
+    (HERE / "norm.left.c5.fq").write_bytes(extract_perl(ref, fq, HERE / "norm.pairs.c5.accs"))
+    ls.unlink()
+    rs.unlink()
+
+
 def main() -> None:
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     HERE.mkdir(exist_ok=True)
     if len(sys.argv) > 2 and sys.argv[2] == "--prep-only":
         make_prep(ref)
         return
+    if len(sys.argv) > 2 and sys.argv[2] == "--norm-only":
+        make_norm(ref)
+        return
     make_prep(ref)
+    make_norm(ref)
     edge = edge_fasta()
     (HERE / "edge.fa").write_bytes(edge)
     bulk = synth.transcriptome_reads(seed=11, n_transcripts=50, n_reads=300, read_len=76).tobytes()

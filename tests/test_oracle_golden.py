@@ -109,3 +109,58 @@ def test_fastq_to_fasta_dirty_records(oracle, golden):
     with pytest.raises(ValueError) as e:
         oracle.fastq_to_fasta(dirty)
     assert e.value.args[0] == 2     # the script dies on the second record
+
+
+# ---- normalization tail: the oracle against the reference scripts' own output
+
+@pytest.mark.parametrize("args,fixture,counts", [
+    ((5, 2, 1), "norm.pairs.c5.accs", (133, 49, 49, 14)),
+    ((200, 1, 10000), "norm.pairs.c200.accs", (133, 99, 30, 4)),
+])
+def test_norm_pairs_matches_reference_scripts(oracle, golden, args, fixture, counts):
+    """sort -k1,1 | nbkc_merge_left_right_stats.pl --sorted | nbkc_normalize.pl
+    (insilico_read_normalization.pl:865-985); counts as the script's stderr
+    summary printed them."""
+    table, accs, cnt = oracle.norm((golden / "norm.left.stats").read_bytes(), (golden / "norm.right.stats").read_bytes(),
+                                   *args)
+    assert table == (golden / "norm.pairs.stats").read_bytes()
+    assert accs == (golden / fixture).read_bytes()
+    assert cnt == counts
+
+
+def test_norm_single_matches_reference_script(oracle, golden):
+    _, accs, cnt = oracle.norm((golden / "norm.left.stats").read_bytes(), None, 5, 2, 1)
+    assert accs == (golden / "norm.left.c5.accs").read_bytes()
+    assert cnt == (149, 55, 44, 29)
+
+
+def test_norm_reproduces_earlier_pair_fixture(oracle, golden):
+    table, accs, _ = oracle.norm((golden / "left.stats").read_bytes(), (golden / "right.stats").read_bytes(), 3, 1,
+                                 10000)
+    assert table == (golden / "pairs.stats").read_bytes()
+    assert accs == (golden / "normalized.accs").read_bytes()
+
+
+def test_norm_extract_matches_reference(oracle, golden):
+    """make_normalized_reads_file with PerlLib/Fastq_reader.pm (insilico:470-584)."""
+    fq = (golden / "norm.left.fq").read_bytes()
+    assert oracle.norm_extract(fq, (golden / "norm.pairs.c5.accs").read_bytes()) == \
+        (golden / "norm.left.c5.fq").read_bytes()
+    # a selected name without a record: the script dies
+    recs = fq.split(b"\n")
+    drop = [i for i in range(0, len(recs) - 1, 4) if recs[i].startswith(b"@x/2")][0]
+    short = b"\n".join(recs[:drop] + recs[drop + 4:])
+    with pytest.raises(ValueError) as e:
+        oracle.norm_extract(short, (golden / "norm.pairs.c5.accs").read_bytes())
+    assert str(e.value) == "1"
+
+
+def test_drand48_is_perls_rand(oracle):
+    """srand(12345); rand(1) x3 as perl 5.38 printed them (%.17g)."""
+    a, c, m = 0x5DEECE66D, 0xB, (1 << 48) - 1
+    x = (12345 << 16) | 0x330E
+    got = []
+    for _ in range(3):
+        x = (a * x + c) & m
+        got.append(x / 2 ** 48)
+    assert ["%.17g" % v for v in got] == ["0.22532851279629895", "0.91918306853355602", "0.20684125324818226"]

@@ -5,8 +5,8 @@ Drop-in replacements for the three native tools Trinity drives on this path
 ``fastaToKmerCoverageStats`` and Chrysalis' ``ReadsToTranscripts`` -- built on
 hand-written sm_103a CUDA kernels behind the C ABI in ``include/trinkmer.h``.
 """
-from .kmer import (Context, KmerTable, ReadSet, ReadsToTranscripts, coverage_stats, format_histo, format_r2t,
-                   format_stats)
+from .kmer import (Context, KmerTable, Normalization, ReadSet, ReadsToTranscripts, coverage_stats, format_histo,
+                   format_r2t, format_stats)
 
-__all__ = ["Context", "KmerTable", "ReadSet", "ReadsToTranscripts", "coverage_stats", "format_histo",
-           "format_stats", "format_r2t"]
+__all__ = ["Context", "KmerTable", "Normalization", "ReadSet", "ReadsToTranscripts", "coverage_stats",
+           "format_histo", "format_stats", "format_r2t"]

@@ -1023,4 +1023,103 @@ void tk_r2t_free(tk_r2t *z) {
     ctx_release(c);
 }
 
+// ------------------------------------------------------------------ normalization
+
+int tk_norm_select(tk_ctx *c, const tk_reads *left, const uint32_t *left_median, const float *left_mean,
+                   const float *left_stdev, const tk_reads *right, const uint32_t *right_median,
+                   const float *right_mean, const float *right_stdev, int where, int max_cov, int min_cov,
+                   int max_cv, tk_norm **out) {
+    if (!out) return TK_E_INVAL;
+    *out = nullptr;
+    CHECK_CTX(c);
+    if (!left || left->ctx != c || (right && right->ctx != c))
+        return set_err(c, TK_E_INVAL, "tk_norm_select: read sets of another context");
+    if (where != TK_HOST && where != TK_DEVICE) return set_err(c, TK_E_INVAL, "tk_norm_select: where");
+    if (left->n_reads && (!left_median || !left_mean || !left_stdev))
+        return set_err(c, TK_E_INVAL, "tk_norm_select: left statistics missing");
+    if (right && right->n_reads && (!right_median || !right_mean || !right_stdev))
+        return set_err(c, TK_E_INVAL, "tk_norm_select: right statistics missing");
+    if (left->n_reads > 0xFFFFFFFFull || (right && right->n_reads > 0xFFFFFFFFull))
+        return set_err(c, TK_E_INVAL, "tk_norm_select: more than 2^32 reads on a side");
+    tk_norm *nm = new (std::nothrow) tk_norm();
+    if (!nm) return TK_E_OOM;
+    nm->ctx = c;
+    nm->pairs = right != nullptr;
+    nm->max_cov = max_cov;
+    nm->min_cov = min_cov;
+    nm->max_cv = max_cv;
+    ctx_acquire(c);
+    const tk_reads *reads[2] = {left, right};
+    const uint32_t *med[2] = {left_median, right_median};
+    const float *mean[2] = {left_mean, right_mean};
+    const float *sd[2] = {left_stdev, right_stdev};
+    int e = norm_select(nm, reads, med, mean, sd, where);
+    if (e) {
+        tk_norm_free(nm);
+        return e;
+    }
+    *out = nm;
+    return TK_OK;
+}
+
+int tk_norm_info(const tk_norm *nm, tk_norm_counts *counts, uint64_t *accs_len) {
+    if (!nm) return TK_E_INVAL;
+    if (counts) *counts = nm->counts;
+    if (accs_len) *accs_len = nm->accs_len;
+    return TK_OK;
+}
+
+static int norm_copy_out(tk_ctx *c, const char *src, uint64_t len, int where, char *out, uint64_t cap,
+                         const char *what) {
+    if (!out && len) return set_err(c, TK_E_INVAL, std::string(what) + ": no buffer");
+    if (cap < len) return set_err(c, TK_E_RANGE, std::string(what) + ": buffer smaller than the text");
+    if (len)
+        TK_CUDA(c, cudaMemcpyAsync(out, src, len, where == TK_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                   c->stream));
+    return cuda_check(c, cudaStreamSynchronize(c->stream), what);
+}
+
+int tk_norm_accs(const tk_norm *nm, int where, char *out, uint64_t cap) {
+    if (!nm) return TK_E_INVAL;
+    tk_ctx *c = nm->ctx;
+    CHECK_CTX(c);
+    return norm_copy_out(c, nm->d_accs, nm->accs_len, where, out, cap, "tk_norm_accs");
+}
+
+int tk_norm_table(tk_norm *nm, int where, char *out, uint64_t cap, uint64_t *len) {
+    if (!nm) return TK_E_INVAL;
+    tk_ctx *c = nm->ctx;
+    CHECK_CTX(c);
+    TK_TRY(norm_table(nm));
+    if (len) *len = nm->table_len;
+    if (!out) return TK_OK;
+    return norm_copy_out(c, nm->d_table, nm->table_len, where, out, cap, "tk_norm_table");
+}
+
+int tk_norm_extract(tk_norm *nm, const tk_reads *fastq, uint64_t *len) {
+    if (!nm || !fastq) return TK_E_INVAL;
+    tk_ctx *c = nm->ctx;
+    CHECK_CTX(c);
+    if (fastq->ctx != c) return set_err(c, TK_E_INVAL, "tk_norm_extract: read set of another context");
+    TK_TRY(norm_extract(nm, fastq));
+    if (len) *len = nm->ext_len;
+    return TK_OK;
+}
+
+int tk_norm_extract_copy(const tk_norm *nm, int where, char *out, uint64_t cap) {
+    if (!nm) return TK_E_INVAL;
+    tk_ctx *c = nm->ctx;
+    CHECK_CTX(c);
+    return norm_copy_out(c, nm->d_ext, nm->ext_len, where, out, cap, "tk_norm_extract_copy");
+}
+
+void tk_norm_free(tk_norm *nm) {
+    if (!nm) return;
+    tk_ctx *c = nm->ctx;
+    cudaSetDevice(c->device);
+    norm_release(nm);
+    delete nm;
+    ctx_release(c);
+}
+
 }  // extern "C"

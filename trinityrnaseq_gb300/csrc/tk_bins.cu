@@ -266,8 +266,6 @@ struct tk_bins {
 
 namespace tk {
 int parse_reads(tk_ctx *c, tk_reads *r);
-int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int bits, uint64_t *tmp_keys,
-                     uint32_t *tmp_vals, bool *result_in_tmp);
 
 // block sizes the count kernel is tuned over, per context (0 = not tuned yet)
 static int g_tuned_block[64];

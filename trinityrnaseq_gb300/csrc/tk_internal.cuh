@@ -284,6 +284,51 @@ struct tk_r2t {
     std::vector<uint64_t> comp_id;          // per bundle record
 };
 
+namespace tk {
+// One read's coverage statistics as the stats tables carry them: the median,
+// mean and stdev printed "%u", "%g", "%g", and the numbers Perl reads back.
+struct NormVal {
+    double mean, sd;        // the values of the "%g" texts
+    uint32_t med;
+    uint32_t gmean, gsd;    // their 6 significant digits (0 for a zero)
+    int8_t xmean, xsd;      // their decimal exponents
+    uint8_t sfx_len;        // length of "\t%u\t%g\t%g"
+    uint8_t pad;
+};
+
+// One side's reads in the order of its sorted stats table.
+struct NormSide {
+    uint64_t n = 0;
+    const char *text = nullptr;     // device text the names point into
+    NormVal *val = nullptr;         // read order
+    uint32_t *perm = nullptr;       // sorted position -> read
+    uint64_t *h0 = nullptr, *h1 = nullptr, *off = nullptr;   // sorted: first 16 name bytes, name offset
+    uint32_t *len = nullptr, *core = nullptr;                 // sorted: name length, without "/<digit>"
+};
+}  // namespace tk
+
+struct tk_norm {
+    tk_ctx *ctx = nullptr;
+    bool pairs = false;
+    int max_cov = 0, min_cov = 0, max_cv = 0;
+    tk::NormSide side[2];
+    uint64_t n_rows = 0;
+    uint32_t *row_l = nullptr, *row_r = nullptr;   // pairs: sorted positions of each merged row
+    uint64_t *row_n = nullptr;                     // pairs: 10 x the three "%.1f" averages per row
+    uint64_t *acc_off = nullptr;                   // n_rows + 1: each row's line in d_accs (empty if not kept)
+    char *d_accs = nullptr;
+    uint64_t accs_len = 0;
+    tk_norm_counts counts{};
+    char *d_table = nullptr;
+    uint64_t table_len = 0;
+    char *d_ext = nullptr;                         // last extraction
+    uint64_t ext_len = 0;
+    uint32_t *d_hash = nullptr;                    // selected names: row index per slot, ~0 empty
+    uint8_t *d_keydup = nullptr;                   // per row: its name is another row's, or empty
+    uint64_t hash_mask = 0;
+    uint64_t n_keys = 0;
+};
+
 // host helpers shared by the translation units
 namespace tk {
 int set_err(tk_ctx *c, int code, const std::string &msg);
@@ -297,13 +342,18 @@ int check_launch(tk_ctx *c, const char *what);
 int scan_excl_u64(tk_ctx *c, const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *total_host);
 int scan_excl_u32_to_u64(tk_ctx *c, const uint32_t *in, uint64_t *out, uint64_t n, uint64_t *total_host);
 int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int bits,
-                     uint64_t *tmp_keys, uint32_t *tmp_vals, bool *result_in_tmp);
+                     uint64_t *tmp_keys, uint32_t *tmp_vals, bool *result_in_tmp, int first_bit = 0);
 int table_alloc(tk_table *t, uint64_t capacity);
 int table_alloc_init(tk_table *t, uint64_t capacity, uint32_t init_val);
 int table_rehash(tk_table *t, uint64_t new_capacity);
 int table_count_seq(tk_table *t, const tk_reads *r);
 int reads_fasta(tk_reads *r, int append, int flags, char **d_text, uint64_t *text_len);
 int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets);
+int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *const med[2],
+                const float *const mean[2], const float *const sd[2], int where);
+int norm_table(tk_norm *nm);
+int norm_extract(tk_norm *nm, const tk_reads *fq);
+void norm_release(tk_norm *nm);
 }  // namespace tk
 
 #define TK_TRY(x) do { int _e = (x); if (_e) return _e; } while (0)

@@ -228,8 +228,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t *__res
     }
 }
 
+// Sorts by key bits [first_bit, first_bit + bits), 8 bits per pass.
 int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int bits, uint64_t *tmp_keys,
-                     uint32_t *tmp_vals, bool *result_in_tmp) {
+                     uint32_t *tmp_vals, bool *result_in_tmp, int first_bit) {
     *result_in_tmp = false;
     if (n <= 1 || bits <= 0) return TK_OK;
     uint64_t ntiles = (n + RS_TILE - 1) / RS_TILE;
@@ -242,7 +243,7 @@ int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int 
                            "radix scatter smem");
     uint64_t *ka = keys, *kb = tmp_keys;
     uint32_t *va = vals, *vb = tmp_vals;
-    for (int shift = 0; shift < bits && !e; shift += RS_BITS) {
+    for (int shift = first_bit; shift < first_bit + bits && shift < 64 && !e; shift += RS_BITS) {
         k_rs_hist<<<(unsigned)ntiles, RS_THREADS, 0, c->stream>>>(ka, n, shift, hist, ntiles);
         c->launches++;
         e = scan_excl_u32_to_u64(c, hist, offs, ntiles * RS_BINS, nullptr);

@@ -390,6 +390,83 @@ class ReadsToTranscripts:
         return rec[:n], hits[:n], nwin[:n]
 
 
+class Normalization:
+    """In-silico normalization over coverage statistics (tk_norm): the sort,
+    pair merge and selection util/insilico_read_normalization.pl runs through
+    `sort -k1,1`, nbkc_merge_left_right_stats.pl --sorted and nbkc_normalize.pl,
+    and its extraction of the selected FASTQ records.
+
+    left_stats / right_stats are (median, mean, stdev) per read as
+    coverage_stats returns them (host numpy arrays), or device addresses
+    (median_ptr, mean_ptr, stdev_ptr) with device=True.  right=None selects on
+    one side alone.  The read sets must outlive this object."""
+
+    def __init__(self, ctx: Context, left: ReadSet, left_stats, right: Optional[ReadSet] = None, right_stats=None,
+                 max_cov: int = 200, min_cov: int = 1, max_cv: int = 10000, device: bool = False):
+        self.ctx, self.lib, self.h = ctx, ctx.lib, None
+        self._reads = (left, right)
+        keep = []
+
+        def ptrs(stats, n):
+            if stats is None:
+                return (None, None, None)
+            if device:
+                return tuple(C.c_void_p(int(p)) for p in stats)
+            med = np.ascontiguousarray(stats[0], dtype=np.uint32)
+            mean = np.ascontiguousarray(stats[1], dtype=np.float32)
+            sd = np.ascontiguousarray(stats[2], dtype=np.float32)
+            if not (len(med) == len(mean) == len(sd) == n):
+                raise ValueError("statistics must have one entry per read")
+            keep.extend((med, mean, sd))
+            return tuple(C.c_void_p(a.ctypes.data) for a in (med, mean, sd))
+
+        lp = ptrs(left_stats, left.n_reads)
+        rp = ptrs(right_stats, right.n_reads) if right is not None else (None, None, None)
+        h = C.c_void_p()
+        ctx.check(self.lib.tk_norm_select(ctx.h, left.h, *lp, right.h if right is not None else None, *rp,
+                                          N.TK_DEVICE if device else N.TK_HOST, max_cov, min_cov, max_cv,
+                                          C.byref(h)), "tk_norm_select")
+        self.h = h
+        cnt = (C.c_uint64 * 4)()
+        alen = C.c_uint64()
+        ctx.check(self.lib.tk_norm_info(h, cnt, C.byref(alen)), "tk_norm_info")
+        self.counts = {"rows": cnt[0], "selected": cnt[1], "aberrant": cnt[2], "below_min": cnt[3]}
+        self.accs_len = alen.value
+
+    def free(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.tk_norm_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def accs(self) -> bytes:
+        """nbkc_normalize.pl's output: the selected accs, one per line."""
+        buf = C.create_string_buffer(max(self.accs_len, 1))
+        self.ctx.check(self.lib.tk_norm_accs(self.h, N.TK_HOST, buf, self.accs_len), "tk_norm_accs")
+        return buf.raw[:self.accs_len]
+
+    def table(self) -> bytes:
+        """The table nbkc_normalize.pl reads (merged pairs or sorted stats)."""
+        n = C.c_uint64()
+        self.ctx.check(self.lib.tk_norm_table(self.h, N.TK_HOST, None, 0, C.byref(n)), "tk_norm_table")
+        buf = C.create_string_buffer(max(n.value, 1))
+        self.ctx.check(self.lib.tk_norm_table(self.h, N.TK_HOST, buf, n.value, C.byref(n)), "tk_norm_table")
+        return buf.raw[:n.value]
+
+    def extract(self, fastq: ReadSet) -> bytes:
+        """The selected records of a FASTQ read set, verbatim, in input order."""
+        n = C.c_uint64()
+        self.ctx.check(self.lib.tk_norm_extract(self.h, fastq.h, C.byref(n)), "tk_norm_extract")
+        buf = C.create_string_buffer(max(n.value, 1))
+        self.ctx.check(self.lib.tk_norm_extract_copy(self.h, N.TK_HOST, buf, n.value), "tk_norm_extract_copy")
+        return buf.raw[:n.value]
+
+
 def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool = True,
                min_count: int = 1) -> Tuple[bytes, np.ndarray, int]:
     """Per-bin k-mer dumps of back-to-back FASTA bins in one batched GPU pass

@@ -31,7 +31,7 @@ TK_FA_REVCOMP, TK_FA_IGNORE_DIRTY, TK_FA_IF_MISSING = 1, 2, 4
 
 KID = {
     "parse": 0, "hll": 1, "count": 2, "compact": 3, "sort": 4, "dump": 5, "load": 6,
-    "coverage": 7, "r2t_build": 8, "r2t_assign": 9, "bins": 10, "scatter": 11,
+    "coverage": 7, "r2t_build": 8, "r2t_assign": 9, "bins": 10, "scatter": 11, "norm": 12, "extract": 13,
 }
 
 u64, u32, i32, vp = C.c_uint64, C.c_uint32, C.c_int32, C.c_void_p
@@ -82,6 +82,13 @@ SIGNATURES = {
     "tk_r2t_component_ids": (C.c_int, [vp, vp]),
     "tk_r2t_assign": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
     "tk_r2t_free": (None, [vp]),
+    "tk_norm_select": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, P(vp)]),
+    "tk_norm_info": (C.c_int, [vp, vp, P(u64)]),
+    "tk_norm_accs": (C.c_int, [vp, C.c_int, vp, u64]),
+    "tk_norm_table": (C.c_int, [vp, C.c_int, vp, u64, P(u64)]),
+    "tk_norm_extract": (C.c_int, [vp, vp, P(u64)]),
+    "tk_norm_extract_copy": (C.c_int, [vp, C.c_int, vp, u64]),
+    "tk_norm_free": (None, [vp]),
     "tk_count_bins": (C.c_int, [vp, vp, u64, C.c_int, vp, u32, C.c_int, C.c_int, u32, P(vp)]),
     "tk_count_bins_ex": (C.c_int, [vp, vp, u64, C.c_int, vp, u32, C.c_int, C.c_int, vp, vp, P(vp)]),
     "tk_bins_info": (C.c_int, [vp, P(u64), P(u64)]),
