@@ -353,6 +353,8 @@ def run_gpu(args, dist, world, rank, local):
         del pipe
         if args.prep and world == 1:
             out["prep"] = prep_bench(ctx, left, args)
+        if args.norm and world == 1:
+            out["normalize"] = norm_bench(ctx, left, right, args)
         if args.bins and world == 1:
             out["batched"] = batched_bench(ctx, args)
         if args.jobs and world == 1:
@@ -419,6 +421,135 @@ def prep_bench(ctx, fastq, args):
             "records": reads, "fasta_bytes": n_out, **res,
             "cpu": {"reads_per_s": n_sample / cpu_s, "cores": 1, "kind": "port",
                     "sample": f"first {n_sample} records; the oracle's restatement of fastQ_to_fastA.pl"},
+            "bit_exact_vs_oracle_sample": same}
+
+
+# ---------------------------------------------------------------- normalization tail
+
+NORM_ARGS = (200, 1, 10000)   # Trinity's defaults: --max_cov 200 --min_cov 1 --max_CV 10000
+
+
+def norm_bench(ctx, left, right, args):
+    """The in-silico normalization tail on the plain-path workload: both sides'
+    stats sorted by read name, the pair merge, nbkc_normalize.pl's selection and
+    the extraction of the selected FASTQ records of both sides (tk_norm_*), with
+    the statistics resident in HBM (device); and the whole normalization of
+    util/insilico_read_normalization.pl from pinned host FASTQ to pinned host
+    normalized FASTQ (e2e: parse, prep, count, stats, tail, extraction, D2H).
+    The CPU leg times the oracle's restatement of sort + merge + selection +
+    extraction (the reference runs GNU sort and single-threaded Perl) on one
+    core over the first 1M pairs, from the stats tables."""
+    import torch
+    from trinityrnaseq_gb300 import kmer
+    from oracle import oracle as O
+    dev = torch.device(f"cuda:{ctx.device}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    h_fq = [torch.from_numpy(x).pin_memory() for x in (left, right)]
+    fq = [kmer.ReadSet(ctx, h.numpy()) for h in h_fq]
+    n = [r.n_reads for r in fq]
+    flen = [r.fasta_len(a, if_missing=True) for r, a in zip(fq, (1, 2))]
+    d_fa = [torch.empty(x + 16, dtype=torch.uint8, device=dev) for x in flen]
+    stats = [(torch.empty(m, dtype=torch.int32, device=dev), torch.empty(m, dtype=torch.float32, device=dev),
+              torch.empty(m, dtype=torch.float32, device=dev)) for m in n]
+
+    def prep_count_stats(fqs):
+        fas = []
+        for r, a, buf, ln in zip(fqs, (1, 2), d_fa, flen):
+            r.fasta_into(buf.data_ptr(), buf.numel(), append=a, if_missing=True, device=True)
+            fas.append(kmer.ReadSet(ctx, buf.data_ptr(), ln, device=True))
+        t = kmer.KmerTable(ctx, K, True)
+        t.add_many(fas)
+        for r, st in zip(fas, stats):
+            kmer.coverage_stats_into(t, r, *(x.data_ptr() for x in st))
+        t.free()
+        return fas
+
+    def tail(fas, fqs, outs=None):
+        nm = kmer.Normalization(ctx, fas[0], tuple(x.data_ptr() for x in stats[0]), fas[1],
+                                tuple(x.data_ptr() for x in stats[1]), *NORM_ARGS, device=True)
+        lens = []
+        for i, r in enumerate(fqs):
+            if outs is None:
+                lens.append(nm.extract_into(r))
+            else:
+                lens.append(nm.extract_into(r, outs[i].data_ptr(), outs[i].numel()))
+        c = nm.counts
+        nm.free()
+        return c, lens
+
+    fa = prep_count_stats(fq)
+    counts, ext = tail(fa, fq)
+    h_out = [torch.empty(x + 16, dtype=torch.uint8).pin_memory() for x in ext]
+
+    def timed_region(fn, after_warmup=None):
+        for _ in range(args.warmup):
+            fn()
+        if after_warmup:
+            after_warmup()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for _ in range(args.steps):
+                fn()
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) / 1e3 / args.steps
+
+    ctx.set_profiling(True)
+    s_dev = timed_region(lambda: tail(fa, fq), ctx.reset_profile)
+    prof = {k: ctx.profile(k) for k in ("norm", "extract")}
+    ctx.set_profiling(False)
+
+    def whole():
+        fqs = [kmer.ReadSet(ctx, h.numpy()) for h in h_fq]
+        fas = prep_count_stats(fqs)
+        tail(fas, fqs, h_out)
+        for r in fas + fqs:
+            r.free()
+
+    s_e2e = timed_region(whole)
+    for r in fa + fq:
+        r.free()
+    pairs = min(n)
+    # CPU: the oracle on the first 1M pairs, from their stats tables; and the
+    # GPU's selection of the same sample compared with it
+    m = min(1_000_000, pairs)
+    samp = []
+    for x in (left, right):
+        head = x[:min(x.nbytes, 4 * m * 512)].tobytes()   # 4-line records of < 512 bytes
+        samp.append(b"\n".join(head.split(b"\n", 4 * m)[:4 * m]) + b"\n")
+    sfq = [kmer.ReadSet(ctx, s) for s in samp]
+    sfa = [kmer.ReadSet(ctx, r.to_fasta(a, if_missing=True)) for r, a in zip(sfq, (1, 2))]
+    t = kmer.KmerTable(ctx, K, True)
+    for r in sfa:
+        t.add(r)
+    sst = [kmer.coverage_stats(t, r) for r in sfa]
+    t.free()
+    tables = [kmer.format_stats(r.accessions(), *st) for r, st in zip(sfa, sst)]
+    t0 = time.time()
+    _, accs, _ = O.norm(tables[0], tables[1], *NORM_ARGS)
+    outs = [O.norm_extract(s, accs) for s in samp]
+    cpu_s = time.time() - t0
+    nm = kmer.Normalization(ctx, sfa[0], sst[0], sfa[1], sst[1], *NORM_ARGS)
+    same = nm.accs() == accs and all(nm.extract(r) == o for r, o in zip(sfq, outs))
+    nm.free()
+    for r in sfa + sfq:
+        r.free()
+    return {"workload": f"{pairs} pairs (the plain path's reads): sort both sides' stats by name, pair merge, "
+                        f"select (--max_cov {NORM_ARGS[0]} --min_cov {NORM_ARGS[1]} --max_CV {NORM_ARGS[2]}), "
+                        "extract both sides' records",
+            "pairs": pairs, "selected": counts["selected"], "rows": counts["rows"],
+            "extracted_bytes": sum(ext),
+            "device": {"pairs_per_s": pairs / s_dev, "ms": s_dev * 1e3,
+                       "kernels_ms": {k: v[0] / args.steps for k, v in prof.items()},
+                       "launches": {k: v[1] / args.steps for k, v in prof.items()}},
+            "e2e": {"pairs_per_s": pairs / s_e2e, "ms": s_e2e * 1e3,
+                    "what": "pinned host FASTQ of both sides -> parse, prep, count, stats, tail, extraction -> "
+                            "pinned host normalized FASTQ",
+                    "h2d_bytes": sum(h.numel() for h in h_fq), "d2h_bytes": sum(ext)},
+            "cpu": {"pairs_per_s": m / cpu_s, "cores": 1, "kind": "port",
+                    "sample": f"first {m} pairs; the oracle's sort + merge + selection + extraction from stats tables"},
             "bit_exact_vs_oracle_sample": same}
 
 
@@ -645,6 +776,7 @@ def main():
     ap.add_argument("--cpu-pairs", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--prep", type=int, default=1, help="FASTQ->FASTA read prep leg (0 = skip)")
+    ap.add_argument("--norm", type=int, default=1, help="normalization-tail leg (0 = skip)")
     ap.add_argument("--bins", type=int, default=5000, help="batched-bins comparison (0 = skip)")
     ap.add_argument("--jobs", type=int, default=200, help="served-stream comparison (0 = skip)")
     ap.add_argument("--job-max-reads", type=int, default=2_000_000)

@@ -101,3 +101,74 @@ def test_tools_fail_loudly_on_bad_input(native_built, tmp_path):
                        stdout=subprocess.PIPE, stderr=subprocess.PIPE)
     assert r.returncode != 0 and b"Error" in r.stderr
     assert not (tmp_path / "mer_counts.jf").exists()
+
+
+def _shuffled(text: bytes, seed: int, drop: float) -> bytes:
+    import random
+    recs = text.split(b"\n")
+    recs = [b"\n".join(recs[i:i + 4]) + b"\n" for i in range(0, len(recs) - 1, 4)]
+    rnd = random.Random(seed)
+    rnd.shuffle(recs)
+    return b"".join(r for r in recs if rnd.random() >= drop)
+
+
+def _oracle_normalize(oracle, sides, ss, pairs_together, max_cov, min_cov, max_cv):
+    """The script's own sequence of steps, each through the oracle:
+    seqtk-trinity, jellyfish count (+ dump -L 2), fastaToKmerCoverageStats,
+    sort / merge / nbkc_normalize.pl, make_normalized_reads_file."""
+    fas = []
+    for i, (tag, fq) in enumerate(sides):
+        letter = ss[i] if i < len(ss) else ""
+        flags = oracle.FA_IF_MISSING | (oracle.FA_REV if letter == "R" else 0)
+        fas.append(oracle.fastq_to_fasta(fq, 2 if tag == "right" else 1, flags))
+    canonical = not ss
+    keys, counts = oracle.count(b"".join(fas), 25, canonical)
+    d2 = oracle.dump(keys, counts, 25, 2)
+    k2, c2 = oracle.load_dump(d2, 25, canonical)
+    stats = [oracle.cov_stats(fa, k2, c2, 25, canonical) for fa in fas]
+    if pairs_together:
+        _, accs, _ = oracle.norm(stats[0], stats[1], max_cov, min_cov, max_cv)
+        return [oracle.norm_extract(fq, accs) for _, fq in sides]
+    out = []
+    for (tag, fq), st in zip(sides, stats):
+        _, accs, _ = oracle.norm(st, None, max_cov, min_cov, max_cv)
+        out.append(oracle.norm_extract(fq, accs))
+    return out
+
+
+@pytest.mark.parametrize("ss,pairs_together,single", [("", True, False), ("RF", True, False), ("", False, False),
+                                                      ("", False, True)])
+def test_insilico_read_normalization(native_built, oracle, tmp_path, ss, pairs_together, single):
+    """bin/insilico_read_normalization with Trinity's command line
+    (Trinity:3426-3448) writes the normalized FASTQ the script's steps write."""
+    from trinityrnaseq_gb300 import synth
+    left, right = synth.gene_pairs(seed=71, n_genes=60, n_pairs=6000, fastq=True)
+    lfq, rfq = _shuffled(left.tobytes(), 1, 0.03), _shuffled(right.tobytes(), 2, 0.03)
+    (tmp_path / "reads_2.fq").write_bytes(rfq)
+    # the left reads in two files, cut at a record boundary
+    recs = lfq.split(b"\n")
+    cut = (len(recs) // 8) * 4
+    (tmp_path / "reads_1.fq").write_bytes(b"\n".join(recs[:cut]) + b"\n")
+    (tmp_path / "reads_1b.fq").write_bytes(b"\n".join(recs[cut:]))
+    out = tmp_path / "norm"
+    args = [BIN / "insilico_read_normalization", "--seqType", "fq", "--JM", "4G", "--max_cov", 30, "--min_cov", 1,
+            "--CPU", 4, "--output", out, "--max_CV", 10000]
+    if ss:
+        args += ["--SS_lib_type", ss]
+    if single:
+        args += ["--single", "reads_1.fq,reads_1b.fq"]
+        sides = [("single", lfq)]
+    else:
+        args += ["--left", "reads_1.fq,reads_1b.fq", "--right", "reads_2.fq"]
+        if pairs_together:
+            args += ["--pairs_together", "--PARALLEL_STATS"]
+        sides = [("left", lfq), ("right", rfq)]
+    r = subprocess.run([str(a) for a in args], cwd=tmp_path, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    assert r.returncode == 0, r.stderr.decode()
+    assert b"reads selected during normalization" in r.stderr
+    want = _oracle_normalize(oracle, sides, ss, pairs_together, 30, 1, 10000)
+    for (tag, _), w in zip(sides, want):
+        got = (out / f"{tag}.norm.fq").read_bytes()
+        assert got == w, tag
+        assert os.path.islink(out / f"{tag}.norm.fq")
+    assert (out / "reads_1.fq_ext_all_reads.normalized_K25_maxC30_minC1_maxCV10000.fq").exists()

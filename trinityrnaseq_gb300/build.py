@@ -35,6 +35,7 @@ TOOL_SOURCES = {
     "ReadsToTranscripts": ["ReadsToTranscripts.cpp"],
     "trinkmerd": ["trinkmerd.cpp"],
     "seqtk-trinity": ["seqtk_trinity.cpp"],
+    "insilico_read_normalization": ["insilico_read_normalization.cpp"],
 }
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

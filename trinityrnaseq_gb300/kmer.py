@@ -458,13 +458,22 @@ class Normalization:
         self.ctx.check(self.lib.tk_norm_table(self.h, N.TK_HOST, buf, n.value, C.byref(n)), "tk_norm_table")
         return buf.raw[:n.value]
 
-    def extract(self, fastq: ReadSet) -> bytes:
-        """The selected records of a FASTQ read set, verbatim, in input order."""
+    def extract_into(self, fastq: ReadSet, ptr: Optional[int] = None, cap: int = 0, device: bool = False) -> int:
+        """Runs the extraction (the text stays on the device) and returns its
+        length; with ptr, also copies it there (host, or device address)."""
         n = C.c_uint64()
         self.ctx.check(self.lib.tk_norm_extract(self.h, fastq.h, C.byref(n)), "tk_norm_extract")
-        buf = C.create_string_buffer(max(n.value, 1))
-        self.ctx.check(self.lib.tk_norm_extract_copy(self.h, N.TK_HOST, buf, n.value), "tk_norm_extract_copy")
-        return buf.raw[:n.value]
+        if ptr is not None:
+            self.ctx.check(self.lib.tk_norm_extract_copy(self.h, N.TK_DEVICE if device else N.TK_HOST,
+                                                         C.c_void_p(ptr), cap), "tk_norm_extract_copy")
+        return n.value
+
+    def extract(self, fastq: ReadSet) -> bytes:
+        """The selected records of a FASTQ read set, verbatim, in input order."""
+        n = self.extract_into(fastq)
+        buf = C.create_string_buffer(max(n, 1))
+        self.ctx.check(self.lib.tk_norm_extract_copy(self.h, N.TK_HOST, buf, n), "tk_norm_extract_copy")
+        return buf.raw[:n]
 
 
 def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool = True,
