@@ -355,6 +355,8 @@ def run_gpu(args, dist, world, rank, local):
             out["prep"] = prep_bench(ctx, left, args)
         if args.norm and world == 1:
             out["normalize"] = norm_bench(ctx, left, right, args)
+        if args.r2t and world == 1:
+            out["r2t"] = r2t_bench(ctx, args)
         if args.bins and world == 1:
             out["batched"] = batched_bench(ctx, args)
         if args.jobs and world == 1:
@@ -550,6 +552,106 @@ def norm_bench(ctx, left, right, args):
                     "h2d_bytes": sum(h.numel() for h in h_fq), "d2h_bytes": sum(ext)},
             "cpu": {"pairs_per_s": m / cpu_s, "cores": 1, "kind": "port",
                     "sample": f"first {m} pairs; the oracle's sort + merge + selection + extraction from stats tables"},
+            "bit_exact_vs_oracle_sample": same}
+
+
+# ---------------------------------------------------------------- read -> component
+
+R2T_CONTIGS, R2T_COMPONENTS = 100_000, 30_000
+
+
+def r2t_bench(ctx, args):
+    """Read -> component assignment (Chrysalis ReadsToTranscripts, Trinity:2237-2251)
+    at the R2T scale: 100,000 contigs (log-normal, median 400 nt) in 30,000
+    components of 1-40 contigs bundled as >s_<id> X-joined records, and
+    args.r2t_pairs pairs of 100 nt reads drawn from them at 1% error.  One step
+    = build the bundle k-mer table, parse the reads, vote per read; device =
+    reads FASTA resident in HBM and the per-read results left there; e2e =
+    pinned host FASTA in, per-read (record, hits, windows) copied back.  The
+    CPU leg runs the oracle with all host threads on the first 1M reads."""
+    import numpy as np
+    import torch
+    from trinityrnaseq_gb300 import kmer, synth
+    from oracle import oracle as O
+    t0 = time.time()
+    bundle, reads = synth.bundle_reads(seed=SEED + 11, n_contigs=R2T_CONTIGS, contig_median=400.0,
+                                       n_components=R2T_COMPONENTS, max_per_component=40, n_pairs=args.r2t_pairs,
+                                       read_len=100, err=0.01)
+    log(f"r2t: bundle {bundle.nbytes / 1e6:.1f} MB, reads {reads.nbytes / 1e9:.2f} GB in {time.time() - t0:.1f}s")
+    dev = torch.device(f"cuda:{ctx.device}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    b = bundle.tobytes()
+    h_reads = torch.from_numpy(reads).pin_memory()
+    d_reads = h_reads.to(dev)
+    torch.cuda.synchronize()
+    probe = kmer.ReadSet(ctx, d_reads.data_ptr(), d_reads.numel(), device=True)
+    n = probe.n_reads
+    probe.free()
+    d_out = [torch.empty(n, dtype=torch.int32, device=dev) for _ in range(3)]
+    h_out = [torch.empty(n, dtype=torch.int32).pin_memory() for _ in range(3)]
+    info = {}
+
+    def step(e2e):
+        z = kmer.ReadsToTranscripts(ctx, b, K, False)
+        rs = kmer.ReadSet(ctx, h_reads.numpy()) if e2e else kmer.ReadSet(ctx, d_reads.data_ptr(), d_reads.numel(),
+                                                                         device=True)
+        outs = h_out if e2e else d_out
+        z.assign_into(rs, *(o.data_ptr() for o in outs), device=not e2e)
+        info["kmers"] = z.n_kmers
+        rs.free()
+        z.free()
+
+    res = {}
+    for mode in ("device", "e2e"):
+        for _ in range(args.warmup):
+            step(mode == "e2e")
+        if mode == "device":
+            ctx.set_profiling(True)
+            ctx.reset_profile()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for _ in range(args.steps):
+                step(mode == "e2e")
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        s = ev[0].elapsed_time(ev[1]) / 1e3 / args.steps
+        if mode == "device":
+            prof = {k: ctx.profile(k) for k in ("parse", "r2t_build", "r2t_assign")}
+            ctx.set_profiling(False)
+        res[mode] = {"reads_per_s": n / s, "ms": s * 1e3}
+    lookups = int(h_out[2].numpy().astype(np.int64).sum())
+    assigned = int((h_out[0].numpy() >= 0).sum())
+    ms_assign = prof["r2t_assign"][0] / args.steps
+    cap = 1 << max(10, int(np.ceil(np.log2(info["kmers"] / 0.6 + 1))))
+    ceil_lookup = ctx.random_access_rate(cap * 16, atomics=False)
+    rate = lookups / (ms_assign / 1e3)
+    # CPU: the oracle with all host threads on the first 1M reads; and the
+    # GPU's votes for the same reads compared with it
+    m = min(1_000_000, n)
+    head = reads[:min(reads.nbytes, 2 * m * 256)].tobytes()
+    sample = b"\n".join(head.split(b"\n", 2 * m)[:2 * m]) + b"\n"
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    want = O.r2t_values(sample, b, K, False, threads)
+    cpu_s = time.time() - t0
+    z = kmer.ReadsToTranscripts(ctx, b, K, False)
+    rs = kmer.ReadSet(ctx, sample)
+    got = z.assign(rs)
+    same = all(np.array_equal(g, w) for g, w in zip(got, want))
+    rs.free()
+    z.free()
+    return {"workload": f"{R2T_CONTIGS} contigs in {R2T_COMPONENTS} components ({bundle.nbytes / 1e6:.0f} MB bundle, "
+                        f"{info['kmers']} bundle k-mers), {n} reads x 100 nt at 1% error "
+                        f"({reads.nbytes / 1e9:.2f} GB FASTA); build + parse + vote",
+            "reads": n, "lookups": lookups, "assigned": assigned, **res,
+            "kernels_ms": {k: v[0] / args.steps for k, v in prof.items()},
+            "e2e_bytes": {"h2d": h_reads.numel(), "d2h": 12 * n},
+            "roofline_assign": {"lookups_per_s": rate, "ceiling_per_s": ceil_lookup, "frac": rate / ceil_lookup,
+                                "what": "read k-mer lookups vs random 8-byte loads into a table of this size"},
+            "cpu": {"reads_per_s": m / cpu_s, "cores": threads, "kind": "port",
+                    "sample": f"first {m} reads; the oracle's build + vote (C, OpenMP)"},
             "bit_exact_vs_oracle_sample": same}
 
 
@@ -777,6 +879,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--prep", type=int, default=1, help="FASTQ->FASTA read prep leg (0 = skip)")
     ap.add_argument("--norm", type=int, default=1, help="normalization-tail leg (0 = skip)")
+    ap.add_argument("--r2t", type=int, default=1, help="read -> component leg (0 = skip)")
+    ap.add_argument("--r2t_pairs", type=int, default=50_000_000, help="read pairs of the read -> component leg")
     ap.add_argument("--bins", type=int, default=5000, help="batched-bins comparison (0 = skip)")
     ap.add_argument("--jobs", type=int, default=200, help="served-stream comparison (0 = skip)")
     ap.add_argument("--job-max-reads", type=int, default=2_000_000)

@@ -380,6 +380,12 @@ class ReadsToTranscripts:
         except Exception:
             pass
 
+    def assign_into(self, reads: ReadSet, rec_ptr: int, hits_ptr: int, nwin_ptr: int, device: bool = True) -> None:
+        """assign() writing n_reads entries to caller arrays (device addresses by default)."""
+        self.ctx.check(self.lib.tk_r2t_assign(self.h, reads.h, N.TK_DEVICE if device else N.TK_HOST,
+                                              C.c_void_p(rec_ptr), C.c_void_p(hits_ptr), C.c_void_p(nwin_ptr)),
+                       "tk_r2t_assign")
+
     def assign(self, reads: ReadSet) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
         n = reads.n_reads
         rec = np.zeros(max(n, 1), dtype=np.int32)
