@@ -6,10 +6,11 @@
 // is parsed like reads; every window of k A/C/G/T bases is inserted with
 // value = its record index through atomicMin, so a k-mer held by several
 // records belongs to the first of them whatever the insertion order.
-// Assign: one warp per read looks each window up, sorts the record indices
-// in registers and takes the longest run: the record with most votes, ties to
-// the smaller index.  Reads with more than 256 windows use one block and a
-// global scratch slab.
+// Assign: one warp per read packs the read's bases 2 bits each into shared
+// memory, cuts each lane's windows out of it, looks them up, sorts the record
+// indices in registers and takes the longest run: the record with most votes,
+// ties to the smaller index.  Reads with more than 256 windows use one block
+// and a global scratch slab.
 #include "tk_warp.cuh"
 
 #include <algorithm>
@@ -64,13 +65,16 @@ __global__ void __launch_bounds__(RT_THREADS) k_r2t_build(const uint8_t *__restr
 
 template <int S, bool CANON>
 __device__ __forceinline__ void r2t_warp_read(DevTable t, const uint8_t *__restrict__ seq, uint64_t start, uint32_t nwin,
-                                              int k, uint64_t r, int32_t *__restrict__ rec, uint32_t *__restrict__ hits) {
+                                              int k, uint64_t r, int32_t *__restrict__ rec, uint32_t *__restrict__ hits,
+                                              uint64_t *words) {
     const unsigned lane = lane_id();
     const uint32_t span = (nwin + 31) / 32;
     uint32_t v[S];
-    lane_windows<S, CANON>(seq, start, nwin, span, k, [&](int j, bool valid, uint64_t key) {
-        v[j] = valid ? tbl_get(t, key, PAD_VAL) : PAD_VAL;
-    });
+    auto body = [&](int j, bool valid, uint64_t key) { v[j] = valid ? tbl_get(t, key, PAD_VAL) : PAD_VAL; };
+    // k-mers cut from the read packed in shared memory; reads with another
+    // character take the byte path
+    if (!lane_windows_packed<S, CANON>(seq, start, nwin, span, k, words, body))
+        lane_windows<S, CANON>(seq, start, nwin, span, k, body);
     warp_bitonic_sort<S>(v);
     // longest run of equal values; run start indices by an inclusive max-scan
     uint32_t prev_last = __shfl_up_sync(0xffffffffu, v[S - 1], 1);
@@ -115,21 +119,24 @@ __device__ __forceinline__ void r2t_warp_read(DevTable t, const uint8_t *__restr
 }
 
 template <bool CANON>
-__global__ void __launch_bounds__(RT_THREADS) k_r2t_assign(DevTable t, const uint8_t *__restrict__ seq,
-                                                          const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
-                                                          int32_t *__restrict__ rec, uint32_t *__restrict__ hits,
-                                                          uint32_t *__restrict__ nwin_out, uint32_t *__restrict__ long_list,
-                                                          unsigned long long *__restrict__ long_n) {
+__global__ void __launch_bounds__(RT_THREADS, 6) k_r2t_assign(DevTable t, const uint8_t *__restrict__ seq,
+                                                             const uint64_t *__restrict__ rd_off, uint64_t n_reads,
+                                                             int k, int32_t *__restrict__ rec,
+                                                             uint32_t *__restrict__ hits, uint32_t *__restrict__ nwin_out,
+                                                             uint32_t *__restrict__ long_list,
+                                                             unsigned long long *__restrict__ long_n) {
+    __shared__ uint64_t words[RT_THREADS / 32][12];
+    uint64_t *w = words[threadIdx.x >> 5];
     const uint64_t warps = (uint64_t)gridDim.x * (RT_THREADS / 32);
     for (uint64_t r = (uint64_t)blockIdx.x * (RT_THREADS / 32) + (threadIdx.x >> 5); r < n_reads; r += warps) {
         const uint64_t start = rd_off[r];
         const uint64_t L = rd_off[r + 1] - start - 1;
         const uint32_t nwin = L >= (uint64_t)k ? (uint32_t)(L - k + 1) : 0u;
         if (lane_id() == 0) nwin_out[r] = nwin;
-        if (nwin <= 32) r2t_warp_read<1, CANON>(t, seq, start, nwin, k, r, rec, hits);
-        else if (nwin <= 64) r2t_warp_read<2, CANON>(t, seq, start, nwin, k, r, rec, hits);
-        else if (nwin <= 128) r2t_warp_read<4, CANON>(t, seq, start, nwin, k, r, rec, hits);
-        else if (nwin <= RT_WARP_MAX) r2t_warp_read<8, CANON>(t, seq, start, nwin, k, r, rec, hits);
+        if (nwin <= 32) r2t_warp_read<1, CANON>(t, seq, start, nwin, k, r, rec, hits, w);
+        else if (nwin <= 64) r2t_warp_read<2, CANON>(t, seq, start, nwin, k, r, rec, hits, w);
+        else if (nwin <= 128) r2t_warp_read<4, CANON>(t, seq, start, nwin, k, r, rec, hits, w);
+        else if (nwin <= RT_WARP_MAX) r2t_warp_read<8, CANON>(t, seq, start, nwin, k, r, rec, hits, w);
         else if (lane_id() == 0) long_list[atomicAdd(long_n, 1ULL)] = (uint32_t)r;
     }
 }
