@@ -114,7 +114,8 @@ __device__ bool g6(float f, uint32_t *D, int *X) {
     const int be = (int)((bits >> 23) & 0xFF);
     const uint32_t m = (bits & 0x7FFFFFu) | 0x800000u;   // normal in this range
     const int q = be - 150;
-    int x = (int)floor(log10((double)f));
+    // floor(log10 f) to within one: the binade's exponent times log10(2) ~ 1233/4096
+    int x = ((be - 127) * 1233) >> 12;
     for (int it = 0; it < 4; it++) {
         const uint64_t d = scaled_rne(m, q, 5 - x);
         if (d >= 1000000) { x++; continue; }
@@ -285,11 +286,17 @@ __device__ __forceinline__ uint64_t slot_chunk(const uint8_t *__restrict__ slots
 }
 
 __global__ void k_name_maxlen(const uint32_t *__restrict__ len, uint64_t n, uint32_t *__restrict__ out) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t v = i < n ? len[i] : 0u;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane_id() == 0 && v) atomicMax(out, v);
+    __shared__ uint32_t sm[NM_THREADS / 32];
+    uint32_t v = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        v = max(v, len[i]);
+    v = __reduce_max_sync(0xffffffffu, v);
+    if (lane_id() == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NM_THREADS / 32; w++) v = max(v, sm[w]);
+        if (v) atomicMax(out, v);
+    }
 }
 
 __global__ void k_iota(uint32_t *__restrict__ p, uint64_t n) {
@@ -541,8 +548,8 @@ __device__ __forceinline__ void row_numbers(const RowArgs &a, uint64_t p, double
 }
 
 // the row's class: 0 draws, 1 below min_cov, 2 aberrant; pairs also get their averages
-__global__ void k_norm_rows(RowArgs a, uint32_t *__restrict__ draws, unsigned long long *__restrict__ tally,
-                            uint32_t *__restrict__ err) {
+__global__ void k_norm_rows(RowArgs a, uint32_t *__restrict__ draws, double *__restrict__ ratio,
+                            unsigned long long *__restrict__ tally, uint32_t *__restrict__ err) {
     const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t below = 0, aberrant = 0;
     if (p < a.n_rows) {
@@ -565,6 +572,7 @@ __global__ void k_norm_rows(RowArgs a, uint32_t *__restrict__ draws, unsigned lo
         else {
             d = 1;
             if (med == 0.0) flag_err(err, NE_DIV0);
+            else ratio[p] = __ddiv_rn((double)a.max_cov, med);
         }
         draws[p] = d;
     }
@@ -598,7 +606,7 @@ __device__ __forceinline__ void row_acc(const RowArgs &a, const SNames &L, uint6
     *len = n;
 }
 
-__global__ void k_norm_pick(RowArgs a, SNames L, const uint32_t *__restrict__ draws,
+__global__ void k_norm_pick(RowArgs a, SNames L, const uint32_t *__restrict__ draws, const double *__restrict__ ratio,
                             const uint64_t *__restrict__ rank, uint64_t x0, uint32_t *__restrict__ out_len,
                             unsigned long long *__restrict__ tally) {
     const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -606,11 +614,9 @@ __global__ void k_norm_pick(RowArgs a, SNames L, const uint32_t *__restrict__ dr
     if (p < a.n_rows) {
         uint32_t len = 0;
         if (draws[p]) {
-            double med, u, sd;
-            row_numbers(a, p, &med, &u, &sd);
             const uint64_t x = lcg_jump(x0, rank[p] + 1);
-            const double r = __dmul_rn((double)x, 0x1p-48);
-            if (med != 0.0 && r <= __ddiv_rn((double)a.max_cov, med)) {
+            const double r = __dmul_rn((double)x, 0x1p-48);   // X / 2^48, exact
+            if (r <= ratio[p]) {
                 uint64_t o;
                 uint32_t n;
                 row_acc(a, L, p, &o, &n);
@@ -862,16 +868,47 @@ __global__ void k_extract_missing(const uint64_t *__restrict__ acc_off, uint64_t
     if (lane_id() == 0 && m) atomicAdd(missing, (unsigned long long)m);
 }
 
-// a warp per record, 32 bytes a step
-__global__ void k_extract_copy(const char *__restrict__ text, const uint64_t *__restrict__ name_off, uint64_t n,
-                               const uint64_t *__restrict__ out_off, char *__restrict__ out) {
+// The 4 bytes of a record at record offset so (record = text[a0, a0 + n));
+// bytes outside the record read as 0.  Two aligned 4-byte loads and a funnel
+// shift when the text is 4-byte aligned and both words lie inside it.
+__device__ __forceinline__ uint32_t rec_word(const char *__restrict__ text, uint64_t text_len, bool vec, uint64_t a0,
+                                             int64_t so, uint64_t n) {
+    const int64_t a = (int64_t)a0 + so;
+    if (vec && a >= 0 && (uint64_t)((a & ~3LL) + 8) <= text_len && so >= 0 && so + 4 <= (int64_t)n) {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(text + (a & ~3LL));
+        return __funnelshift_r(__ldg(p), __ldg(p + 1), 8u * (uint32_t)(a & 3));
+    }
+    uint32_t x = 0;
+    for (int i = 0; i < 4; i++) {
+        const int64_t q = so + i;
+        if (q >= 0 && q < (int64_t)n) x |= (uint32_t)(uint8_t)text[a0 + q] << (8 * i);
+    }
+    return x;
+}
+
+// a warp per record; each lane writes aligned 4-byte output words (byte
+// stores only for the words a record shares with its neighbours)
+__global__ void k_extract_copy(const char *__restrict__ text, uint64_t text_len, bool vec,
+                               const uint64_t *__restrict__ name_off, uint64_t n, const uint64_t *__restrict__ out_off,
+                               char *__restrict__ out) {
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = lane_id();
     if (warp >= n) return;
     const uint64_t o = out_off[warp], len = out_off[warp + 1] - o;
     if (!len) return;
-    const char *src = text + name_off[warp] - 1;
-    for (uint64_t q = lane; q < len; q += 32) out[o + q] = src[q];
+    const uint64_t a0 = name_off[warp] - 1;
+    const uint64_t nw = ((o + len + 3) >> 2) - (o >> 2);
+    for (uint64_t w = lane; w < nw; w += 32) {
+        const int64_t so = (int64_t)(4 * w) - (int64_t)(o & 3);
+        const uint32_t x = rec_word(text, text_len, vec, a0, so, len);
+        char *d = out + (o & ~3ULL) + 4 * w;
+        if (so >= 0 && so + 4 <= (int64_t)len) {
+            *reinterpret_cast<uint32_t *>(d) = x;
+        } else {
+            for (int i = 0; i < 4; i++)
+                if (so + i >= 0 && so + i < (int64_t)len) d[i] = (char)(x >> (8 * i));
+        }
+    }
 }
 
 // ---------------------------------------------------------------- host side
@@ -938,7 +975,8 @@ static int sort_side(tk_ctx *c, const tk_reads *r, NormSide &s) {
     TK_TRY(sc.get((void **)&d_u32, 16, "sort scalars"));
     TK_TRY(sc.get((void **)&orand, 16, "sort key bits"));
     TK_CUDA(c, cudaMemsetAsync(d_u32, 0, 16, c->stream));
-    k_name_maxlen<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(r->d_name_len, n, d_u32);
+    k_name_maxlen<<<(unsigned)std::min<uint64_t>(nm_grid(n), (uint64_t)c->sm_count * 8), NM_THREADS, 0, c->stream>>>(
+        r->d_name_len, n, d_u32);
     c->launches++;
     uint32_t maxlen = 0;
     TK_CUDA(c, cudaMemcpyAsync(&maxlen, d_u32, 4, cudaMemcpyDeviceToHost, c->stream));
@@ -1158,8 +1196,10 @@ int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *con
     TK_TRY(dmalloc(c, (void **)&nm->acc_off, (P + 1) * 8, "accs offsets"));
     uint32_t *draws = nullptr, *lens = nullptr;
     uint64_t *rank = nullptr;
+    double *ratio = nullptr;
     unsigned long long *tally = nullptr;
     TK_TRY(sc.get((void **)&draws, P * 4, "norm draws"));
+    TK_TRY(sc.get((void **)&ratio, P * 8, "norm ratios"));
     TK_TRY(sc.get((void **)&lens, P * 4, "accs lengths"));
     TK_TRY(sc.get((void **)&rank, (P + 1) * 8, "norm draw ranks"));
     TK_TRY(sc.get((void **)&tally, 32, "norm tallies"));
@@ -1168,7 +1208,7 @@ int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *con
     const SNames L = snames(nm->side[0]);
     uint64_t n_draws = 0;
     if (P) {
-        k_norm_rows<<<nm_grid(P), NM_THREADS, 0, c->stream>>>(a, draws, tally, d_err);
+        k_norm_rows<<<nm_grid(P), NM_THREADS, 0, c->stream>>>(a, draws, ratio, tally, d_err);
         c->launches++;
         TK_TRY(check_launch(c, "norm rows"));
         TK_TRY(scan_excl_u32_to_u64(c, draws, rank, P, &n_draws));
@@ -1176,7 +1216,7 @@ int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *con
         if (herr[NE_DOMAIN]) return set_err(c, TK_E_INVAL, "normalization: an average outside [0, 1e15)");
         if (herr[NE_DIV0]) return set_err(c, TK_E_INVAL, "normalization: a selected row has median 0 (min_cov <= 0)");
         const uint64_t x0 = (12345ULL << 16) | 0x330EULL;
-        k_norm_pick<<<nm_grid(P), NM_THREADS, 0, c->stream>>>(a, L, draws, rank, x0, lens, tally);
+        k_norm_pick<<<nm_grid(P), NM_THREADS, 0, c->stream>>>(a, L, draws, ratio, rank, x0, lens, tally);
         c->launches++;
         TK_TRY(check_launch(c, "norm pick"));
         TK_TRY(scan_excl_u32_to_u64(c, lens, nm->acc_off, P, &nm->accs_len));
@@ -1308,7 +1348,9 @@ int norm_extract(tk_norm *nm, const tk_reads *fq) {
     TK_TRY(dmalloc(c, (void **)&nm->d_ext, total ? total : 1, "extracted reads"));
     if (n && total) {
         TK_CUDA(c, cudaMemcpyAsync(offs + n, &total, 8, cudaMemcpyHostToDevice, c->stream));
-        k_extract_copy<<<nm_grid(n * 32), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->d_name_off, n, offs, nm->d_ext);
+        const bool vec = ((uintptr_t)fq->d_text & 3) == 0;
+        k_extract_copy<<<nm_grid(n * 32), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, vec, fq->d_name_off, n,
+                                                                       offs, nm->d_ext);
         c->launches++;
         TK_TRY(check_launch(c, "extract copy"));
     }
