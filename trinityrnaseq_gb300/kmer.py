@@ -9,12 +9,34 @@ helpers write the reference's text formats; the C++ drop-in executables under
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import weakref
 from typing import Optional, Sequence, Tuple, Union
 
 import numpy as np
 
 from . import native as N
+
+# Every live handle owner, so that interpreter exit frees read sets, tables
+# and selections before their contexts, while the CUDA runtime and any other
+# CUDA user in the process (PyTorch) are still fully up.
+_owners: "weakref.WeakSet" = weakref.WeakSet()
+_contexts: "weakref.WeakSet" = weakref.WeakSet()
+
+
+@atexit.register
+def _release_all() -> None:
+    for o in list(_owners):
+        try:
+            o.free()
+        except Exception:
+            pass
+    for c in list(_contexts):
+        try:
+            c.close()
+        except Exception:
+            pass
 
 Buffer = Union[bytes, bytearray, memoryview, np.ndarray]
 
@@ -55,6 +77,7 @@ class Context:
         N.check(st, "tk_ctx_create")
         self.h = h
         self.device = device
+        _contexts.add(self)
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -142,6 +165,7 @@ class ReadSet:
 
     def _adopt(self, h) -> None:
         self.h = h
+        _owners.add(self)
         nr, nb, ml, fm = C.c_uint64(), C.c_uint64(), C.c_uint32(), C.c_int()
         self.ctx.check(self.lib.tk_reads_info(h, C.byref(nr), C.byref(nb), C.byref(ml), C.byref(fm)), "tk_reads_info")
         self.n_reads, self.n_bases, self.max_len, self.format = nr.value, nb.value, ml.value, fm.value
@@ -246,6 +270,7 @@ class KmerTable:
         h = C.c_void_p()
         ctx.check(self.lib.tk_table_create(ctx.h, k, int(canonical), capacity, C.byref(h)), "tk_table_create")
         self.h = h
+        _owners.add(self)
 
     def free(self) -> None:
         if getattr(self, "h", None):
@@ -362,6 +387,7 @@ class ReadsToTranscripts:
         ctx.check(self.lib.tk_r2t_create(ctx.h, C.c_void_p(ptr), n, N.TK_HOST, k, int(strand), C.byref(h)),
                   "tk_r2t_create")
         self.h = h
+        _owners.add(self)
         nr, nk = C.c_uint64(), C.c_uint64()
         ctx.check(self.lib.tk_r2t_info(h, C.byref(nr), C.byref(nk)), "tk_r2t_info")
         self.n_records, self.n_kmers = nr.value, nk.value
@@ -433,6 +459,7 @@ class Normalization:
                                           N.TK_DEVICE if device else N.TK_HOST, max_cov, min_cov, max_cv,
                                           C.byref(h)), "tk_norm_select")
         self.h = h
+        _owners.add(self)
         cnt = (C.c_uint64 * 4)()
         alen = C.c_uint64()
         ctx.check(self.lib.tk_norm_info(h, cnt, C.byref(alen)), "tk_norm_info")
