@@ -1060,7 +1060,7 @@ int orc_norm(const char *left, size_t llen, const char *right, size_t rlen, int 
 
 /* ------------------------------------------------------------ read extraction
  * make_normalized_reads_file of util/insilico_read_normalization.pl:470-584
- * for FASTQ: the accs file's non-blank lines, each without a final "/" and
+ * (FASTA input: see fa_chunk below; FASTQ:) the accs file's non-blank lines, each without a final "/" and
  * word character (build_selected_index, :452-466), are the wanted names; every
  * 4-line record of the FASTQ text (PerlLib/Fastq_reader.pm:47-75) whose core
  * name -- the header's first whitespace-delimited field without '@' and
@@ -1090,6 +1090,62 @@ static void remove_first(char *s, size_t *n, const char *pat) {
             *n -= m;
             return;
         }
+}
+
+/* PerlLib/Fasta_reader.pm:45-70 on one chunk (read up to and including the
+ * next "\n>"): the '>' at its start and end dropped, control bytes other than
+ * tab and newline and bytes 0x7F-0xFF deleted, header = first line, sequence =
+ * the other lines joined with whitespace removed; written ">header\nseq\n"
+ * when its accession (first field of the header, without a final "/1" or
+ * "/2", insilico:526-527) is wanted. */
+static int fa_chunk(const char *c, size_t n, want_t *w, size_t nd, sbuf_t *o) {
+    if (n && c[0] == '>') { c++; n--; }
+    if (n && c[n - 1] == '>') n--;
+    char *hdr = malloc(n + 1), *seq = malloc(n + 1);
+    if (!hdr || !seq) { free(hdr); free(seq); return ORC_E_OOM; }
+    size_t hl = 0, sl = 0, i = 0;
+    for (; i < n && c[i] != '\n'; i++) {
+        unsigned char b = (unsigned char)c[i];
+        if (b == '\t' || (b >= 32 && b < 127)) hdr[hl++] = (char)b;
+    }
+    for (; i < n; i++) {
+        unsigned char b = (unsigned char)c[i];
+        if (b > 32 && b < 127) seq[sl++] = (char)b;
+    }
+    size_t al = 0;
+    if (hl && hdr[0] != ' ' && hdr[0] != '\t')
+        while (al < hl && hdr[al] != ' ' && hdr[al] != '\t') al++;
+    size_t kl = al;
+    if (kl >= 2 && hdr[kl - 2] == '/' && (hdr[kl - 1] == '1' || hdr[kl - 1] == '2')) kl -= 2;
+    want_t key = {hdr, kl, 0};
+    want_t *hit = nd ? bsearch(&key, w, nd, sizeof *w, cmp_want) : NULL;
+    int e = 0;
+    if (hit) {
+        hit->hits++;
+        e = sb_put(o, ">", 1);
+        if (!e) e = sb_put(o, hdr, hl);
+        if (!e) e = sb_put(o, "\n", 1);
+        if (!e) e = sb_put(o, seq, sl);
+        if (!e) e = sb_put(o, "\n", 1);
+    }
+    free(hdr);
+    free(seq);
+    return e;
+}
+
+static int has_word(const char *c, size_t n) {
+    for (size_t i = 0; i < n; i++)
+        if (is_word_c((unsigned char)c[i])) return 1;
+    return 0;
+}
+
+/* the next "\n>"-terminated chunk at *pos */
+static size_t fa_next(const char *t, size_t len, size_t *pos) {
+    size_t a = *pos, q = a;
+    while (q + 1 < len && !(t[q] == '\n' && t[q + 1] == '>')) q++;
+    size_t end = q + 1 < len ? q + 2 : len;
+    *pos = end;
+    return end - a;
 }
 
 int orc_norm_extract(const char *fq, size_t len, const char *accs, size_t alen, char **out, size_t *out_len,
@@ -1132,7 +1188,20 @@ int orc_norm_extract(const char *fq, size_t len, const char *accs, size_t alen, 
     sbuf_t o = {0};
     char *name = NULL;
     size_t name_cap = 0;
-    for (size_t pos = 0; pos < len && !e;) {
+    size_t first = 0;
+    while (first < len && is_perl_ws((unsigned char)fq[first])) first++;
+    const int fasta = first < len && fq[first] == '>';
+    for (size_t pos = 0; fasta && pos < len && !e;) {
+        /* Fasta_reader::next: a chunk without a word character is skipped once */
+        size_t a = pos, n = fa_next(fq, len, &pos);
+        if (!has_word(fq + a, n)) {
+            if (pos >= len) break;   /* the read after it finds nothing: end of input */
+            a = pos;
+            n = fa_next(fq, len, &pos);
+        }
+        e = fa_chunk(fq + a, n, w, nd, &o);
+    }
+    for (size_t pos = 0; !fasta && pos < len && !e;) {
         /* four lines, each with its "\n" when there is one */
         size_t ls[4], le[4], p = pos;
         int nlines = 0;

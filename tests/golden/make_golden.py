@@ -39,6 +39,10 @@ What each fixture pins:
                              FASTQ reads and the records make_normalized_reads_file
                              keeps for norm.pairs.c5.accs, read by
                              PerlLib/Fastq_reader.pm
+  norm.left.fa / norm.left.c5.fa
+                             the same for FASTA input, read by PerlLib/Fasta_reader.pm,
+                             for norm.pairs.c5.fa.accs (without the one name with a
+                             byte Fasta_reader deletes)
   r2t.bundle.fa r2t.reads.fa small bundle and reads
   r2t.out.sort               the oracle's readsToComponents rows through
                              `sort -k1,1n -k3,3nr -k2,2` under LC_ALL=C (Trinity:2258)
@@ -234,6 +238,30 @@ def norm_fastq(names, seed):
     return "".join(out).encode("latin-1")
 
 
+def norm_fasta(names, seed):
+    """FASTA records for the extraction from FASTA input: comments after a
+    space or tab, CRLF records, a control byte in a comment, multi-line and
+    lower-case sequences with a space and a tab inside, a blank line first."""
+    rnd = random.Random(seed)
+    out = ["\n"]
+    for i, n in enumerate(names):
+        L = rnd.randint(5, 70)
+        seq = "".join(rnd.choice("ACGTacgtN") for _ in range(L))
+        lines = [seq[j:j + 25] for j in range(0, L, 25)]
+        if i % 6 == 5:
+            lines[0] = lines[0][:3] + " " + lines[0][3:] + "\t"
+        kind = i % 4
+        if kind == 0:
+            out.append(f">{n} some comment\tmore\n" + "".join(l + "\n" for l in lines))
+        elif kind == 1:
+            out.append(f">{n}\r\n" + "".join(l + "\r\n" for l in lines))
+        elif kind == 2:
+            out.append(f">{n}\n" + "".join(l + "\n" for l in lines))
+        else:
+            out.append(f">{n} \x01ctl\n" + "".join(l + "\n" for l in lines))
+    return "".join(out).encode("latin-1")
+
+
 def sort_stats_file(path: Path, out: Path) -> None:
     """insilico_read_normalization.pl:880's command, run as it runs it."""
     subprocess.run(f"head -n1 '{path}' > '{out}' && tail -n +2 '{path}' | sort -k1,1 >> '{out}'", shell=True,
@@ -251,6 +279,19 @@ def extract_perl(ref: Path, fq: Path, accs: Path) -> bytes:
             r" print $s->get_fastq_record(); } }"
             r' my @m = grep { !$idx{$_} } keys %%idx; die "missing @m" if @m;' % ref)
     return subprocess.run(["perl", "-e", code, str(fq), str(accs)], check=True, stdout=subprocess.PIPE).stdout
+
+
+def extract_perl_fasta(ref: Path, fa: Path, accs: Path) -> bytes:
+    """make_normalized_reads_file for --seqType fa (insilico:518-545): records
+    read by the reference's PerlLib/Fasta_reader.pm."""
+    code = (r"use lib '%s/PerlLib'; use Fasta_reader; my %%idx;"
+            r" open(my $f, $ARGV[1]) or die; while (my $l = <$f>) { chomp $l; next unless $l =~ /\S/;"
+            r" $l =~ s|/\w$||; $idx{$l} = 0; } close $f;"
+            r" my $r = new Fasta_reader($ARGV[0]); while (my $s = $r->next()) { my $a = $s->get_accession();"
+            r" $a =~ s|/[12]\s*$||; if (exists $idx{$a}) { $idx{$a}++;"
+            r" print $s->get_FASTA_format(fasta_line_len => -1); } }"
+            r' my @m = grep { !$idx{$_} } keys %%idx; die "missing @m" if @m;' % ref)
+    return subprocess.run(["perl", "-e", code, str(fa), str(accs)], check=True, stdout=subprocess.PIPE).stdout
 
 
 def make_norm(ref: Path) -> None:
@@ -293,6 +334,17 @@ def make_norm(ref: Path) -> None:
     fq = HERE / "norm.left.fq"
     fq.write_bytes(norm_fastq(heads, 99))
     (HERE / "norm.left.c5.fq").write_bytes(extract_perl(ref, fq, HERE / "norm.pairs.c5.accs"))
+    # the same from FASTA input (names as the stats carry them, "x" and "y"
+    # again from reads of their own)
+    fnames = [n for n in sorted(set(lnames)) if n] + ["extra9/1", "x/2", "y"]
+    fa = HERE / "norm.left.fa"
+    fa.write_bytes(norm_fasta(fnames, 98))
+    # Fasta_reader deletes bytes 0x7F-0xFF, so no FASTA record can carry the
+    # name z\xc3z (the script dies on it): the FASTA case selects the rest
+    sel = HERE / "norm.pairs.c5.fa.accs"
+    sel.write_bytes(b"".join(l + b"\n" for l in (HERE / "norm.pairs.c5.accs").read_bytes().split(b"\n")
+                             if l and l != b"z\xc3z"))
+    (HERE / "norm.left.c5.fa").write_bytes(extract_perl_fasta(ref, fa, sel))
     ls.unlink()
     rs.unlink()
 

@@ -63,6 +63,30 @@ def test_extract_matches_reference(ctx, golden):
     assert e.value.status == native.TK_E_PARSE
 
 
+def test_extract_fasta(ctx, golden, oracle):
+    """FASTA input: the name z\xc3z loses its high byte in Fasta_reader, so
+    the full selection dies as the script does; without that pair the records
+    are those the oracle (pinned to Fasta_reader's output) extracts."""
+    lt, rt = (golden / "norm.left.stats").read_bytes(), (golden / "norm.right.stats").read_bytes()
+    fa_text = (golden / "norm.left.fa").read_bytes()
+    fa = ReadSet(ctx, fa_text)
+    lrs, ls = table_inputs(ctx, lt)
+    rrs, rs = table_inputs(ctx, rt)
+    nm = Normalization(ctx, lrs, ls, rrs, rs, 5, 2, 1)
+    with pytest.raises(native.TrinkmerError) as e:
+        nm.extract(fa)
+    assert e.value.status == native.TK_E_PARSE
+
+    def drop(t):
+        return b"".join(l + b"\n" for l in t.split(b"\n") if l and not l.startswith(b"z\xc3z"))
+    lrs2, ls2 = table_inputs(ctx, drop(lt))
+    rrs2, rs2 = table_inputs(ctx, drop(rt))
+    nm2 = Normalization(ctx, lrs2, ls2, rrs2, rs2, 5, 2, 1)
+    got = nm2.extract(fa)
+    assert got == oracle.norm_extract(fa_text, nm2.accs())
+    assert got.count(b">") == len(nm2.accs().splitlines())
+
+
 def test_earlier_pair_fixture(ctx, golden):
     lrs, ls = table_inputs(ctx, (golden / "left.stats").read_bytes())
     rrs, rs = table_inputs(ctx, (golden / "right.stats").read_bytes())

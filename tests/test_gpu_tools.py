@@ -112,15 +112,16 @@ def _shuffled(text: bytes, seed: int, drop: float) -> bytes:
     return b"".join(r for r in recs if rnd.random() >= drop)
 
 
-def _oracle_normalize(oracle, sides, ss, pairs_together, max_cov, min_cov, max_cv):
+def _oracle_normalize(oracle, sides, ss, pairs_together, max_cov, min_cov, max_cv, fasta=False):
     """The script's own sequence of steps, each through the oracle:
-    seqtk-trinity, jellyfish count (+ dump -L 2), fastaToKmerCoverageStats,
-    sort / merge / nbkc_normalize.pl, make_normalized_reads_file."""
+    seqtk-trinity (FASTQ), jellyfish count (+ dump -L 2),
+    fastaToKmerCoverageStats, sort / merge / nbkc_normalize.pl,
+    make_normalized_reads_file."""
     fas = []
     for i, (tag, fq) in enumerate(sides):
         letter = ss[i] if i < len(ss) else ""
         flags = oracle.FA_IF_MISSING | (oracle.FA_REV if letter == "R" else 0)
-        fas.append(oracle.fastq_to_fasta(fq, 2 if tag == "right" else 1, flags))
+        fas.append(fq if fasta else oracle.fastq_to_fasta(fq, 2 if tag == "right" else 1, flags))
     canonical = not ss
     keys, counts = oracle.count(b"".join(fas), 25, canonical)
     d2 = oracle.dump(keys, counts, 25, 2)
@@ -172,3 +173,34 @@ def test_insilico_read_normalization(native_built, oracle, tmp_path, ss, pairs_t
         assert got == w, tag
         assert os.path.islink(out / f"{tag}.norm.fq")
     assert (out / "reads_1.fq_ext_all_reads.normalized_K25_maxC30_minC1_maxCV10000.fq").exists()
+
+
+def _shuffled_fasta(text: bytes, seed: int, drop: float) -> bytes:
+    import random
+    recs = [b">" + r for r in text.split(b">")[1:]]
+    rnd = random.Random(seed)
+    rnd.shuffle(recs)
+    return b"".join(r for r in recs if rnd.random() >= drop)
+
+
+@pytest.mark.parametrize("pairs_together", [True, False])
+def test_insilico_read_normalization_fasta(native_built, oracle, tmp_path, pairs_together):
+    """--seqType fa: FASTA counted as it is, records extracted with
+    PerlLib/Fasta_reader.pm's rules; outputs left.norm.fa / right.norm.fa."""
+    from trinityrnaseq_gb300 import synth
+    left, right = synth.gene_pairs(seed=72, n_genes=60, n_pairs=6000, fastq=False)
+    lfa, rfa = _shuffled_fasta(left.tobytes(), 3, 0.03), _shuffled_fasta(right.tobytes(), 4, 0.03)
+    (tmp_path / "l.fa").write_bytes(lfa)
+    (tmp_path / "r.fa").write_bytes(rfa)
+    out = tmp_path / "norm"
+    args = [BIN / "insilico_read_normalization", "--seqType", "fa", "--JM", "4G", "--max_cov", 30, "--min_cov", 1,
+            "--CPU", 4, "--output", out, "--max_CV", 10000, "--left", "l.fa", "--right", "r.fa"]
+    if pairs_together:
+        args.append("--pairs_together")
+    r = subprocess.run([str(a) for a in args], cwd=tmp_path, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    assert r.returncode == 0, r.stderr.decode()
+    sides = [("left", lfa), ("right", rfa)]
+    want = _oracle_normalize(oracle, sides, "", pairs_together, 30, 1, 10000, fasta=True)
+    for (tag, _), w in zip(sides, want):
+        assert (out / f"{tag}.norm.fa").read_bytes() == w, tag
+    assert (out / "l.fa.normalized_K25_maxC30_minC1_maxCV10000.fa").exists()

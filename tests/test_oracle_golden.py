@@ -164,3 +164,16 @@ def test_drand48_is_perls_rand(oracle):
         x = (a * x + c) & m
         got.append(x / 2 ** 48)
     assert ["%.17g" % v for v in got] == ["0.22532851279629895", "0.91918306853355602", "0.20684125324818226"]
+
+
+def test_norm_extract_fasta_matches_reference(oracle, golden):
+    """make_normalized_reads_file for --seqType fa, records read by
+    PerlLib/Fasta_reader.pm (control and high bytes deleted, sequence lines
+    joined without whitespace, ">header\\nsequence\\n")."""
+    fa = (golden / "norm.left.fa").read_bytes()
+    assert oracle.norm_extract(fa, (golden / "norm.pairs.c5.fa.accs").read_bytes()) == \
+        (golden / "norm.left.c5.fa").read_bytes()
+    # z\xc3z cannot be carried by any FASTA record: the script dies on it
+    with pytest.raises(ValueError) as e:
+        oracle.norm_extract(fa, (golden / "norm.pairs.c5.accs").read_bytes())
+    assert str(e.value) == "1"

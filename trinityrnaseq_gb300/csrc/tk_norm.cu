@@ -859,6 +859,100 @@ __global__ void k_extract_find(const char *__restrict__ text, uint64_t text_len,
     rec_len[r] = len;
 }
 
+// ---- FASTA records (Fasta_reader.pm:45-70, Sequence::get_FASTA_format with
+// fasta_line_len => -1): control bytes other than tab and newline, and bytes
+// 0x7F-0xFF, are deleted; header = the first line; sequence = the other lines
+// joined without whitespace; accession = the header's first field; the record
+// is written ">header\nsequence\n".  The extraction key is the accession
+// without a final "/1" or "/2" (insilico:526-527).
+
+constexpr int FA_ACC_MAX = 256;   // accession bytes kept for the lookup
+
+__device__ __forceinline__ bool fa_hdr_keep(uint8_t c) { return c == '\t' || (c >= 32 && c < 127); }
+__device__ __forceinline__ bool fa_seq_keep(uint8_t c) { return c > 32 && c < 127; }
+
+// [a, e): record r ('>' at a); hl = end of its header line
+__device__ __forceinline__ void fa_extent(const char *__restrict__ text, uint64_t text_len,
+                                          const uint64_t *__restrict__ name_off, uint64_t n, uint64_t r, uint64_t *a,
+                                          uint64_t *hl, uint64_t *e) {
+    *a = name_off[r] - 1;
+    *e = r + 1 < n ? name_off[r + 1] - 1 : text_len;
+    uint64_t p = *a + 1;
+    while (p < *e && text[p] != '\n') p++;
+    *hl = p;
+}
+
+__global__ void k_extract_find_fa(const char *__restrict__ text, uint64_t text_len,
+                                  const uint64_t *__restrict__ name_off, uint64_t n, const char *__restrict__ accs,
+                                  const uint64_t *__restrict__ acc_off, const uint32_t *__restrict__ slots,
+                                  uint64_t mask, uint8_t *__restrict__ found, uint32_t *__restrict__ rec_len,
+                                  uint32_t *__restrict__ err) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    uint64_t a, hl, e;
+    fa_extent(text, text_len, name_off, n, r, &a, &hl, &e);
+    char acc[FA_ACC_MAX];
+    uint32_t al = 0, hk = 0;
+    bool in_acc = true;
+    for (uint64_t p = a + 1; p < hl; p++) {
+        const uint8_t c = (uint8_t)text[p];
+        if (!fa_hdr_keep(c)) continue;
+        hk++;
+        if (c == ' ' || c == '\t') in_acc = false;
+        if (in_acc) {
+            if (al == FA_ACC_MAX) {
+                flag_err(err, NE_DOMAIN);
+                in_acc = false;
+            } else {
+                acc[al++] = (char)c;
+            }
+        }
+    }
+    if (al >= 2 && acc[al - 2] == '/' && (acc[al - 1] == '1' || acc[al - 1] == '2')) al -= 2;
+    Pieces s;
+    s.k = 1;
+    s.p[0] = acc;
+    s.n[0] = al;
+    uint64_t h = pieces_hash(s) & mask;
+    bool hit = false;
+    for (uint64_t probe = 0; probe <= mask; probe++) {
+        const uint32_t cur = slots[h];
+        if (cur == ~0u) break;
+        const uint64_t co = acc_off[cur];
+        const uint32_t cn = key_len(accs, co, (uint32_t)(acc_off[cur + 1] - co - 1));
+        if (pieces_eq(s, accs + co, cn)) {
+            found[cur] = 1;
+            hit = true;
+            break;
+        }
+        h = (h + 1) & mask;
+    }
+    uint32_t len = 0;
+    if (hit) {
+        uint64_t sk = 0;
+        for (uint64_t p = hl; p < e; p++) sk += fa_seq_keep((uint8_t)text[p]);
+        len = (uint32_t)(1 + hk + 1 + sk + 1);
+    }
+    rec_len[r] = len;
+}
+
+__global__ void k_extract_write_fa(const char *__restrict__ text, uint64_t text_len,
+                                   const uint64_t *__restrict__ name_off, uint64_t n,
+                                   const uint64_t *__restrict__ out_off, char *__restrict__ out) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n || out_off[r + 1] == out_off[r]) return;
+    uint64_t a, hl, e;
+    fa_extent(text, text_len, name_off, n, r, &a, &hl, &e);
+    char *o = out + out_off[r];
+    *o++ = '>';
+    for (uint64_t p = a + 1; p < hl; p++)
+        if (fa_hdr_keep((uint8_t)text[p])) *o++ = text[p];
+    *o++ = '\n';
+    for (uint64_t p = hl; p < e; p++)
+        if (fa_seq_keep((uint8_t)text[p])) *o++ = text[p];
+    *o = '\n';
+}
+
 __global__ void k_extract_missing(const uint64_t *__restrict__ acc_off, uint64_t n_rows, const uint8_t *__restrict__ dup,
                                   const uint8_t *__restrict__ found, unsigned long long *__restrict__ missing) {
     const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1288,8 +1382,7 @@ int norm_extract(tk_norm *nm, const tk_reads *fq) {
         nm->d_ext = nullptr;
         nm->ext_len = 0;
     }
-    if (fq->format != TK_FMT_FASTQ && fq->n_reads)
-        return set_err(c, TK_E_INVAL, "tk_norm_extract: the read set was not parsed from FASTQ");
+    const bool fasta = fq->format == TK_FMT_FASTA;
     cudaEvent_t ev = nullptr;
     prof_begin(c, TK_KID_EXTRACT, &ev);
     const uint64_t P = nm->n_rows, n = fq->n_reads;
@@ -1326,9 +1419,14 @@ int norm_extract(tk_norm *nm, const tk_reads *fq) {
     TK_TRY(sc.get((void **)&offs, (n + 1) * 8, "extract offsets"));
     uint64_t total = 0;
     if (n) {
-        k_extract_find<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off, fq->d_name_len,
-                                                                  n, nm->d_accs, nm->acc_off, nm->d_hash,
-                                                                  nm->hash_mask, found, rec_len);
+        if (fasta)
+            k_extract_find_fa<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off, n,
+                                                                         nm->d_accs, nm->acc_off, nm->d_hash,
+                                                                         nm->hash_mask, found, rec_len, d_err);
+        else
+            k_extract_find<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off,
+                                                                      fq->d_name_len, n, nm->d_accs, nm->acc_off,
+                                                                      nm->d_hash, nm->hash_mask, found, rec_len);
         c->launches++;
         TK_TRY(check_launch(c, "extract find"));
         TK_TRY(scan_excl_u32_to_u64(c, rec_len, offs, n, &total));
@@ -1342,15 +1440,22 @@ int norm_extract(tk_norm *nm, const tk_reads *fq) {
     TK_CUDA(c, cudaMemcpyAsync(&missing, d_missing, 8, cudaMemcpyDeviceToHost, c->stream));
     TK_TRY(read_err(c, d_err, herr));
     if (herr[NE_HASH]) return set_err(c, TK_E_INVAL, "extract: selected-name table full");
+    if (herr[NE_DOMAIN])
+        return set_err(c, TK_E_RANGE, "extract: a FASTA accession longer than " + std::to_string(FA_ACC_MAX) + " bytes");
     if (missing)
         return set_err(c, TK_E_PARSE, "extract: not all selected records were found (missing " +
                                           std::to_string(missing) + ")");
     TK_TRY(dmalloc(c, (void **)&nm->d_ext, total ? total : 1, "extracted reads"));
     if (n && total) {
         TK_CUDA(c, cudaMemcpyAsync(offs + n, &total, 8, cudaMemcpyHostToDevice, c->stream));
-        const bool vec = ((uintptr_t)fq->d_text & 3) == 0;
-        k_extract_copy<<<nm_grid(n * 32), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, vec, fq->d_name_off, n,
-                                                                       offs, nm->d_ext);
+        if (fasta) {
+            k_extract_write_fa<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off, n,
+                                                                          offs, nm->d_ext);
+        } else {
+            const bool vec = ((uintptr_t)fq->d_text & 3) == 0;
+            k_extract_copy<<<nm_grid(n * 32), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, vec,
+                                                                           fq->d_name_off, n, offs, nm->d_ext);
+        }
         c->launches++;
         TK_TRY(check_launch(c, "extract copy"));
     }

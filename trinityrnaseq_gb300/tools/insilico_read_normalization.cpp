@@ -1,7 +1,7 @@
-// insilico_read_normalization -- drop-in for util/insilico_read_normalization.pl
-// for FASTQ reads, the command Trinity runs before assembly (Trinity:3421-3479):
+// insilico_read_normalization -- drop-in for util/insilico_read_normalization.pl,
+// the command Trinity runs before assembly (Trinity:3421-3479):
 //
-//   insilico_read_normalization --seqType fq --JM 10G --max_cov 200 --min_cov 1
+//   insilico_read_normalization --seqType fq|fa --JM 10G --max_cov 200 --min_cov 1
 //       --CPU N --output DIR --max_CV 10000 [--SS_lib_type RF]
 //       (--left a.fq[,b.fq] --right a.fq[,b.fq] [--pairs_together] [--PARALLEL_STATS]
 //        | --single s.fq[,t.fq])
@@ -17,7 +17,10 @@
 // are the script's: DIR/<base>.normalized_K25_maxC<M>_minC<m>_maxCV<V>.fq per
 // side, with DIR/left.norm.fq and DIR/right.norm.fq (or single.norm.fq)
 // symlinked to them (insilico:393-456), and the selection summary on stderr.
-// No intermediate file is written.  --seqType fa is not provided here.
+// FASTA input (--seqType fa) is counted as it is and extracted with
+// PerlLib/Fasta_reader.pm's rules (the .fa outputs); reverse-complemented
+// FASTA (an R in --SS_lib_type with fa, insilico:692-697) is not provided.
+// No intermediate file is written.
 #include "tk_tool.hpp"
 
 #include <sys/stat.h>
@@ -29,7 +32,7 @@
 using namespace tool;
 
 static void usage() {
-    std::fputs("usage: insilico_read_normalization --seqType fq --JM <n>G --max_cov <int> [--min_cov <int>]\n"
+    std::fputs("usage: insilico_read_normalization --seqType fq|fa --JM <n>G --max_cov <int> [--min_cov <int>]\n"
                "         [--max_CV <int>] [--CPU <int>] [--output <dir>] [--SS_lib_type F|R|FR|RF]\n"
                "         (--left <fq>[,<fq>...] --right <fq>[,<fq>...] [--pairs_together] | --single <fq>[,...])\n"
                "         [--left_list <file>] [--right_list <file>] [--KMER_SIZE 25] [--PARALLEL_STATS]\n"
@@ -157,16 +160,19 @@ int main(int argc, char **argv) {
             die("do not understand option: %s", a.c_str());
         }
     }
-    if (seq_type != "fq") {
+    if (seq_type != "fq" && seq_type != "fa") {
         usage();
-        die(seq_type == "fa" ? "--seqType fa is not provided by this tool" : "set --seqType to 'fq' or 'fa'");
+        die("set --seqType to 'fq' or 'fa'");
     }
+    const bool fa_in = seq_type == "fa";
     if (jm.size() < 2 || jm[0] < '0' || jm[0] > '9' || jm.find_first_not_of("0123456789.") != jm.size() - 1 ||
         jm.back() != 'G')
         die("must set --JM to number of G of RAM (ie. 10G)");
     if (!ss.empty() && ss != "R" && ss != "F" && ss != "RF" && ss != "FR")
         die("unrecognized SS_lib_type value of %s. Should be: F, R, RF, or FR", ss.c_str());
     if (ss == "R") ss = "F";   // one strand-specific end needs no reverse complement (insilico:198-203)
+    if (fa_in && ss.find('R') != std::string::npos)
+        die("reverse-complemented FASTA input (--seqType fa with an R in --SS_lib_type) is not provided by this tool");
     if (!left_list.empty()) left = read_list(left_list);
     if (!right_list.empty()) right = read_list(right_list);
     left = split_commas(left);
@@ -205,7 +211,14 @@ int main(int argc, char **argv) {
         int fmt = 0;
         uint64_t n = 0;
         check(tk_reads_info(d.fq, &n, nullptr, nullptr, &fmt), ctx, "reads info");
-        if (n && fmt != TK_FMT_FASTQ) die("%s input is not FASTQ", d.tag.c_str());
+        if (n && fmt != (fa_in ? TK_FMT_FASTA : TK_FMT_FASTQ))
+            die("%s input is not %s", d.tag.c_str(), fa_in ? "FASTA" : "FASTQ");
+        d.n = n;
+        if (fa_in) {
+            // FASTA is counted as it is (insilico:692-705 concatenates it)
+            check(tk_table_add_reads(t, d.fq), ctx, "k-mer count");
+            continue;
+        }
         // seqtk-trinity seq -A -R {1|2} [-r]: "-r" for the side whose library letter is R
         const char letter = s < ss.size() ? ss[s] : 0;
         const int flags = TK_FA_IF_MISSING | (letter == 'R' ? TK_FA_REVCOMP : 0);
@@ -216,8 +229,9 @@ int main(int argc, char **argv) {
         check(tk_reads_to_fasta(d.fq, append, flags, TK_HOST, fa.data(), fa.size(), &flen), ctx, "fastq to fasta");
         check(tk_reads_parse(ctx, fa.data(), flen, TK_HOST, &d.fa), ctx, "parse converted reads");
         check(tk_table_add_reads(t, d.fa), ctx, "k-mer count");
-        d.n = n;
     }
+    if (fa_in)
+        for (Side &d : sides) d.fa = d.fq;
     for (Side &d : sides) {
         d.med.resize(d.n ? d.n : 1);
         d.mean.resize(d.n ? d.n : 1);
@@ -259,13 +273,14 @@ int main(int argc, char **argv) {
         check(tk_norm_extract_copy(sel[s], TK_HOST, text.data(), text.size()), ctx, "capture normalized reads");
         const std::string base = d.files.size() == 1 ? base_name(d.files[0]) : base_name(d.files[0]) + "_ext_all_reads";
         const std::string name = base + ".normalized_K" + std::to_string(kmer) + "_maxC" + std::to_string(max_cov) +
-                                 "_minC" + std::to_string(min_cov) + "_maxCV" + std::to_string(max_cv) + ".fq";
+                                 "_minC" + std::to_string(min_cov) + "_maxCV" + std::to_string(max_cv) + "." +
+                                 seq_type;
         const std::string path = out_dir + "/" + name;
         FILE *f = std::fopen(path.c_str(), "wb");
         if (!f) die("cannot write to %s", path.c_str());
         if (len && std::fwrite(text.data(), 1, len, f) != len) die("cannot write to %s", path.c_str());
         std::fclose(f);
-        const std::string link = out_dir + "/" + d.tag + ".norm.fq";
+        const std::string link = out_dir + "/" + d.tag + ".norm." + seq_type;
         unlink(link.c_str());
         if (symlink(name.c_str(), link.c_str()) != 0) die("cannot link %s", link.c_str());
         outputs.push_back(path);
@@ -273,7 +288,7 @@ int main(int argc, char **argv) {
     if (sel.size() == 2 && sel[1] == sel[0]) sel[1] = nullptr;
     for (tk_norm *n : sel) tk_norm_free(n);
     for (Side &d : sides) {
-        tk_reads_free(d.fa);
+        if (d.fa != d.fq) tk_reads_free(d.fa);
         tk_reads_free(d.fq);
     }
     tk_ctx_destroy(ctx);
