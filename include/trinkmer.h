@@ -291,11 +291,14 @@ int tk_norm_accs(const tk_norm *norm, int where, char *out, uint64_t cap);
  * nbkc_merge_left_right_stats.pl writes it, or a side's sorted stats table
  * (header row first).  out == NULL returns the length only. */
 int tk_norm_table(tk_norm *norm, int where, char *out, uint64_t cap, uint64_t *len);
-/* The FASTQ records of `fastq` whose core names the selection holds, verbatim
- * and in input order (the name rules of PerlLib/Fastq_reader.pm:106-121 and
- * insilico:452-466, 529-531); the text is kept in the tk_norm until the next
- * call.  A selected name without a record in `fastq` is TK_E_PARSE (the script
- * dies with "not all specified records have been retrieved"). */
+/* The records of `fastq` whose core names the selection holds, in input
+ * order: FASTQ records verbatim (the name rules of
+ * PerlLib/Fastq_reader.pm:106-121 and insilico:452-466, 529-531), or for a
+ * FASTA read set ">header\nsequence\n" as PerlLib/Fasta_reader.pm:45-70 and
+ * Sequence::get_FASTA_format print them (insilico:518-527).  The text is kept
+ * in the tk_norm until the next call.  A selected name without a record is
+ * TK_E_PARSE (the script dies with "not all specified records have been
+ * retrieved"); a FASTA accession longer than 256 bytes is TK_E_RANGE. */
 int tk_norm_extract(tk_norm *norm, const tk_reads *fastq, uint64_t *len);
 int tk_norm_extract_copy(const tk_norm *norm, int where, char *out, uint64_t cap);
 void tk_norm_free(tk_norm *norm);
