@@ -698,8 +698,9 @@ def batched_bench(ctx, args):
 
 
 def served_bench(ctx, args):
-    """A seeded Poisson stream of jobs (60% count, 30% normalize, 10% read-to-
-    component; reads log-uniform in [10k, max]) through the job server at
+    """A seeded Poisson stream of jobs (60% count, 30% normalize -- count,
+    statistics, pair selection and extraction --, 10% read-to-component; reads
+    log-uniform in [10k, max]) through the job server at
     0.5x, 1x and 1.5x the measured plain capacity (the same jobs run one
     after another through the plain calls), after an untimed warm-up job of
     each kind per slot.  Reports p50/p99 latency and jobs/s; every served
@@ -744,13 +745,26 @@ def served_bench(ctx, args):
     log(f"served: {len(jobs)} jobs generated in {time.time() - t0:.1f}s")
     # plain capacity: the jobs one after another through the plain calls
     tp = time.time()
-    alone = [plain_run(ctx, k, a, b) for k, a, b, _ in jobs]
+    # a normalize job is the whole normalization: statistics, pair selection
+    # (Trinity's --max_cov 200 --min_cov 1 --max_CV 10000) and extraction
+    def plain(k, a, b):
+        return plain_run(ctx, "normalize_select", a, b, norm=NORM_ARGS) if k == N.TK_JOB_NORMALIZE else \
+            plain_run(ctx, k, a, b)
+
+    def submit(srv, kind, a, b):
+        if kind == N.TK_JOB_COUNT:
+            return srv.submit_count(a)
+        if kind == N.TK_JOB_NORMALIZE:
+            return srv.submit_normalize(a, b, max_cov=NORM_ARGS[0], min_cov=NORM_ARGS[1], max_cv=NORM_ARGS[2])
+        return srv.submit_r2t(a, b)
+
+    alone = [plain(k, a, b) for k, a, b, _ in jobs]
     t_plain = time.time() - tp
     capacity = len(jobs) / t_plain
     total_reads = sum(j[3] for j in jobs)
 
     def same(a, b):
-        if isinstance(a, (bytes, bytearray)):
+        if isinstance(a, (bytes, bytearray, int)):
             return a == b
         if isinstance(a, tuple):
             return all(same(x, y) for x, y in zip(a, b))
@@ -766,8 +780,7 @@ def served_bench(ctx, args):
             warm = [j for kind in (N.TK_JOB_COUNT, N.TK_JOB_NORMALIZE, N.TK_JOB_R2T)
                     for j in [x for x in jobs if x[0] == kind][:args.slots]]
             for kind, a, b, _ in warm:
-                wid = srv.submit_count(a) if kind == N.TK_JOB_COUNT else \
-                    srv.submit_normalize(a, b) if kind == N.TK_JOB_NORMALIZE else srv.submit_r2t(a, b)
+                wid = submit(srv, kind, a, b)
                 srv.wait(wid)
                 srv.release(wid)
             start = time.time()
@@ -777,8 +790,7 @@ def served_bench(ctx, args):
                 t_next += g
                 while time.time() < t_next:
                     time.sleep(min(0.0005, max(0.0, t_next - time.time())))
-                ids.append(srv.submit_count(a) if kind == N.TK_JOB_COUNT else
-                           srv.submit_normalize(a, b) if kind == N.TK_JOB_NORMALIZE else srv.submit_r2t(a, b))
+                ids.append(submit(srv, kind, a, b))
             lat, sts = [], []
             for jid in ids:
                 st, l_ms, _ = srv.wait(jid)
@@ -787,7 +799,7 @@ def served_bench(ctx, args):
             wall = time.time() - start
             ok = all(s == 0 for s in sts)
             for jid, (kind, *_), want in zip(ids, jobs, alone):
-                ok = ok and same(srv.result(jid, kind), want)
+                ok = ok and same(srv.result(jid, "normalize_select" if kind == N.TK_JOB_NORMALIZE else kind), want)
                 srv.release(jid)
             maxc = srv.stats()[2]
             nbatched = srv.batched_jobs()
@@ -799,7 +811,8 @@ def served_bench(ctx, args):
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_concurrent": maxc,
                               "jobs_in_batched_passes": nbatched,
                               "bit_exact_vs_plain": bool(ok)}
-    return {"workload": f"{len(jobs)} jobs (60% count, 30% normalize, 10% read-to-component), reads log-uniform "
+    return {"workload": f"{len(jobs)} jobs (60% count, 30% normalize with selection and extraction, "
+                        f"10% read-to-component), reads log-uniform "
                         f"10k..{args.job_max_reads}, Poisson arrivals; {args.slots} slots, {args.budget_gb} GB budget",
             "plain_jobs_per_s": capacity, "plain_reads_per_s": total_reads / t_plain, "levels": levels}
 

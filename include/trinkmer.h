@@ -347,7 +347,10 @@ void tk_bins_free(tk_bins *bins);
  *   TK_JOB_NORMALIZE  text = left mates, text2 = right mates; counted together (canonical when
  *                     `canonical`), then coverage of each: 0..2 left median u32 / mean f32 / stdev f32,
  *                     3..5 the same for the right mates, 6/7 left accession offset u64 / length u32
- *                     into text, 8/9 the same for the right mates into text2
+ *                     into text, 8/9 the same for the right mates into text2.  With max_cov >= 2 the
+ *                     pairs are also selected (tk_norm_select with max_cov, min_cov, max_cv) and
+ *                     extracted: 10 the accs text, 11 counts u64[4] (tk_norm_counts), 12/13 the
+ *                     selected left / right records (tk_norm_extract)
  *   TK_JOB_R2T        text = reads, text2 = bundle; 0: rec i32, 1: hits u32, 2: nwin u32,
  *                     3/4 accession offset u64 / length u32 into text, 5: read starts u64[n+1] in
  *                     6: the packed upper-cased sequences, 7: component id u64 per bundle record
@@ -367,6 +370,9 @@ typedef struct tk_job_spec {
     uint64_t len;
     const char *text2;
     uint64_t len2;
+    int max_cov;          /* TK_JOB_NORMALIZE: >= 2 selects and extracts (0: statistics only) */
+    int min_cov;
+    int max_cv;
 } tk_job_spec;
 
 typedef struct tk_server tk_server;

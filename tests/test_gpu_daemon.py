@@ -45,6 +45,8 @@ def test_daemon_jobs(native_built, oracle, golden, tmp_path):
         reqs = [f"COUNT 25 1 2 {both} {tmp_path}/dump.fa {tmp_path}/dump.histo",
                 f"NORMALIZE 25 1 {tmp_path}/left.fa {tmp_path}/right.fa {tmp_path}/l.stats {tmp_path}/r.stats",
                 f"R2T 25 0 0 {tmp_path}/r2t.reads.fa {tmp_path}/r2t.bundle.fa {tmp_path}/r2c.out",
+                f"SELECT 25 1 3 1 10000 {tmp_path}/left.fa {tmp_path}/right.fa {tmp_path}/l.norm.fa "
+                f"{tmp_path}/r.norm.fa {tmp_path}/sel.accs",
                 f"COUNT 25 1 1 {tmp_path}/missing.fa {tmp_path}/x.fa"]
         answers = [None] * len(reqs)
 
@@ -56,16 +58,23 @@ def test_daemon_jobs(native_built, oracle, golden, tmp_path):
             t.start()
         for t in threads:
             t.join()
-        assert all(a.startswith("OK") for a in answers[:3]), answers
-        assert answers[3].startswith("ERR")
+        assert all(a.startswith("OK") for a in answers[:4]), answers
+        assert answers[4].startswith("ERR")
         keys, counts = oracle.count(both.read_bytes(), 25, True)
         assert (tmp_path / "dump.fa").read_bytes() == oracle.dump(keys, counts, 25, 2)
         assert (tmp_path / "dump.histo").read_bytes() == format_histo(oracle.histo(counts), 1, 10000)
         assert sort_stats((tmp_path / "l.stats").read_bytes()) == (golden / "left.stats").read_bytes()
         assert sort_stats((tmp_path / "r.stats").read_bytes()) == (golden / "right.stats").read_bytes()
         assert trinity_r2t_sort((tmp_path / "r2c.out").read_bytes()) == (golden / "r2t.out.sort").read_bytes()
+        # the whole normalization: nbkc_normalize.pl's accs (the reference scripts' own output) and the
+        # records they select
+        accs = (tmp_path / "sel.accs").read_bytes()
+        assert accs == (golden / "normalized.accs").read_bytes()
+        for side in ("left", "right"):
+            assert (tmp_path / f"{side[0]}.norm.fa").read_bytes() == \
+                oracle.norm_extract((golden / f"{side}.fa").read_bytes(), accs)
         st = ask(sock, "STATS").split()
-        assert st[0] == "OK" and int(st[1]) == 3
+        assert st[0] == "OK" and int(st[1]) == 4
         assert ask(sock, "QUIT") == "OK"
         assert proc.wait(timeout=60) == 0
     finally:

@@ -87,3 +87,25 @@ def test_bad_job_fails_alone(ctx):
         assert st == N.TK_E_PARSE
         st2, _, _ = srv.wait(good)
         assert st2 == 0
+
+
+def test_served_normalization_selects_like_plain_calls(ctx):
+    """A normalize job with max_cov selects and extracts what tk_norm does
+    alone, FASTA and FASTQ mates, while other jobs share the GPU."""
+    jobs = []
+    for i, fq in enumerate((False, True)):
+        l, r = synth.gene_pairs(seed=400 + i, n_genes=200, n_pairs=20000, fastq=fq)
+        jobs.append((l.tobytes(), r.tobytes(), (5 + 20 * i, 1, 10000)))
+    want = [plain_run(ctx, "normalize_select", l, r, norm=nm) for l, r, nm in jobs]
+    with Server(ctx.device, slots=3) as srv:
+        ids = [srv.submit_normalize(l, r, max_cov=nm[0], min_cov=nm[1], max_cv=nm[2]) for l, r, nm in jobs]
+        extra = srv.submit_count(jobs[0][0])
+        for jid, w in zip(ids, want):
+            st, _, _ = srv.wait(jid)
+            assert st == 0, srv.error(jid)
+            got = srv.result(jid, "normalize_select")
+            assert got[0] == w[0] and got[1] == w[1] and got[2] == w[2] and got[3] == w[3]
+            assert got[1][1] == len(got[0].splitlines()) > 0
+            srv.release(jid)
+        assert srv.wait(extra)[0] == 0
+        srv.release(extra)

@@ -64,7 +64,7 @@ uint64_t job_estimate(const tk_job_spec &s) {
     uint64_t a = s.len, b = s.len2;
     switch (s.kind) {
     case TK_JOB_COUNT: return 32 * a + (64ULL << 20);
-    case TK_JOB_NORMALIZE: return 32 * (a + b) + (64ULL << 20);
+    case TK_JOB_NORMALIZE: return (s.max_cov >= 2 ? 40 : 32) * (a + b) + (64ULL << 20);
     case TK_JOB_R2T: return 6 * a + 48 * b + (64ULL << 20);
     default: return 64ULL << 20;
     }
@@ -188,6 +188,34 @@ int run_normalize(tk_ctx *c, Job &j) {
         names.push_back(as_bytes(nlen));
     }
     for (auto &v : names) j.out.push_back(std::move(v));
+    if (!e && s.max_cov >= 2) {
+        // the insilico selection and extraction over the statistics just computed
+        auto ptr = [&](int which) { return (const void *)j.out[which].data(); };
+        tk_norm *nm = nullptr;
+        e = tk_norm_select(c, rl, (const uint32_t *)ptr(0), (const float *)ptr(1), (const float *)ptr(2), rr,
+                           (const uint32_t *)ptr(3), (const float *)ptr(4), (const float *)ptr(5), TK_HOST,
+                           s.max_cov, s.min_cov, s.max_cv, &nm);
+        tk_norm_counts cnt{};
+        uint64_t alen = 0;
+        if (!e) e = tk_norm_info(nm, &cnt, &alen);
+        std::vector<char> accs(alen);
+        if (!e && alen) e = tk_norm_accs(nm, TK_HOST, accs.data(), alen);
+        std::vector<std::vector<char>> recs;
+        for (tk_reads *r : {rl, rr}) {
+            uint64_t n = 0;
+            if (!e) e = tk_norm_extract(nm, r, &n);
+            std::vector<char> t(n);
+            if (!e && n) e = tk_norm_extract_copy(nm, TK_HOST, t.data(), n);
+            recs.push_back(std::move(t));
+        }
+        if (nm) tk_norm_free(nm);
+        if (!e) {
+            const uint64_t cv[4] = {cnt.rows, cnt.selected, cnt.aberrant, cnt.below_min};
+            j.out.push_back(std::move(accs));
+            j.out.push_back(as_bytes(std::vector<uint64_t>(cv, cv + 4)));
+            for (auto &t : recs) j.out.push_back(std::move(t));
+        }
+    }
     if (rl) tk_reads_free(rl);
     if (rr) tk_reads_free(rr);
     if (t) tk_table_free(t);

@@ -104,7 +104,7 @@ TK_JOB_COUNT, TK_JOB_NORMALIZE, TK_JOB_R2T = 1, 2, 3
 class JobSpec(C.Structure):
     _fields_ = [("kind", C.c_int), ("k", C.c_int), ("canonical", C.c_int), ("strand", C.c_int),
                 ("min_count", C.c_uint32), ("text", C.c_void_p), ("len", C.c_uint64), ("text2", C.c_void_p),
-                ("len2", C.c_uint64)]
+                ("len2", C.c_uint64), ("max_cov", C.c_int), ("min_cov", C.c_int), ("max_cv", C.c_int)]
 
 
 SIGNATURES.update({

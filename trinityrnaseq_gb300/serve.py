@@ -33,10 +33,10 @@ class Server:
     def __exit__(self, *a):
         self.close()
 
-    def _submit(self, kind, text, text2=b"", k=25, canonical=True, strand=False, min_count=1) -> int:
+    def _submit(self, kind, text, text2=b"", k=25, canonical=True, strand=False, min_count=1, norm=(0, 0, 0)) -> int:
         p1, n1, k1 = _host_ptr(text)
         p2, n2, k2 = _host_ptr(text2)
-        spec = N.JobSpec(kind, k, int(canonical), int(strand), min_count, p1, n1, p2, n2)
+        spec = N.JobSpec(kind, k, int(canonical), int(strand), min_count, p1, n1, p2, n2, *norm)
         jid = C.c_uint64()
         N.check(self.lib.tk_server_submit(self.h, C.byref(spec), C.byref(jid)), "tk_server_submit")
         self._keep[jid.value] = (text, text2, k1, k2)   # inputs must outlive the job
@@ -45,8 +45,10 @@ class Server:
     def submit_count(self, reads, k=25, canonical=True, min_count=1) -> int:
         return self._submit(N.TK_JOB_COUNT, reads, b"", k, canonical, False, min_count)
 
-    def submit_normalize(self, left, right, k=25, canonical=True) -> int:
-        return self._submit(N.TK_JOB_NORMALIZE, left, right, k, canonical)
+    def submit_normalize(self, left, right, k=25, canonical=True, max_cov=0, min_cov=1, max_cv=10000) -> int:
+        """Coverage statistics of both mates; with max_cov >= 2 also the pair
+        selection and the selected records (outputs 10-13)."""
+        return self._submit(N.TK_JOB_NORMALIZE, left, right, k, canonical, norm=(max_cov, min_cov, max_cv))
 
     def submit_r2t(self, reads, bundle, k=25, strand=False) -> int:
         return self._submit(N.TK_JOB_R2T, reads, bundle, k, not strand, strand)
@@ -73,6 +75,9 @@ class Server:
         if kind == N.TK_JOB_NORMALIZE:
             d = (np.uint32, np.float32, np.float32, np.uint32, np.float32, np.float32)
             return tuple(self.output(jid, i, t) for i, t in enumerate(d))
+        if kind == "normalize_select":
+            return (self.output(jid, 10, None), tuple(int(v) for v in self.output(jid, 11, np.uint64)),
+                    self.output(jid, 12, None), self.output(jid, 13, None))
         return self.output(jid, 0, np.int32), self.output(jid, 1, np.uint32), self.output(jid, 2, np.uint32)
 
     def error(self, jid: int) -> str:
@@ -93,7 +98,7 @@ class Server:
         return b.value, u.value, m.value
 
 
-def plain_run(ctx, kind: int, text, text2=b"", k=25, canonical=True, strand=False, min_count=1):
+def plain_run(ctx, kind, text, text2=b"", k=25, canonical=True, strand=False, min_count=1, norm=(200, 1, 10000)):
     """The same job through the plain single-job calls (the reference point
     a served result must equal)."""
     from .kmer import KmerTable, ReadSet, ReadsToTranscripts, coverage_stats
@@ -106,5 +111,13 @@ def plain_run(ctx, kind: int, text, text2=b"", k=25, canonical=True, strand=Fals
         t = KmerTable(ctx, k, canonical)
         t.add_many([rl, rr])
         return coverage_stats(t, rl) + coverage_stats(t, rr)
+    if kind == "normalize_select":
+        from .kmer import Normalization
+        rl, rr = ReadSet(ctx, text), ReadSet(ctx, text2)
+        t = KmerTable(ctx, k, canonical)
+        t.add_many([rl, rr])
+        nm = Normalization(ctx, rl, coverage_stats(t, rl), rr, coverage_stats(t, rr), *norm)
+        c = nm.counts
+        return (nm.accs(), (c["rows"], c["selected"], c["aberrant"], c["below_min"]), nm.extract(rl), nm.extract(rr))
     z = ReadsToTranscripts(ctx, text2, k, strand)
     return z.assign(ReadSet(ctx, text))

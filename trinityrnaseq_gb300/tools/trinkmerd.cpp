@@ -12,6 +12,9 @@
 //         -> the `jellyfish dump -L min_count` text and the `jellyfish histo` file
 //   NORMALIZE <k> <ds 0|1> <left.fa> <right.fa> <left_stats_out> <right_stats_out>
 //         -> the two `fastaToKmerCoverageStats` tables (k-mers counted over both files)
+//   SELECT <k> <ds 0|1> <max_cov> <min_cov> <max_CV> <left> <right> <left_out> <right_out> <accs_out>
+//         -> the whole in-silico normalization of the pairs (util/insilico_read_normalization.pl
+//            --pairs_together): the selected records of each side and nbkc_normalize.pl's accs
 //   R2T <k> <strand 0|1> <min_pct> <reads.fa> <bundle.fasta> <out>
 //         -> the `ReadsToTranscripts` rows
 //   STATS -> OK <jobs> <p50_ms> <p99_ms> <max_concurrent>
@@ -88,7 +91,7 @@ static std::string handle(const std::string &req) {
     }
     tk_job_spec s{};
     std::vector<char> t1, t2;
-    std::string o1, o2;
+    std::string o1, o2, o3;
     int min_pct = 0;
     if (cmd == "COUNT") {
         std::string reads;
@@ -102,6 +105,15 @@ static std::string handle(const std::string &req) {
         std::string l, r;
         in >> s.k >> s.canonical >> l >> r >> o1 >> o2;
         if (!in) return "ERR usage: NORMALIZE k ds left right left_out right_out";
+        s.kind = TK_JOB_NORMALIZE;
+        if (!readable(l) || !readable(r)) return "ERR cannot read " + l + " or " + r;
+        t1 = read_file(l);
+        t2 = read_file(r);
+    } else if (cmd == "SELECT") {
+        std::string l, r;
+        in >> s.k >> s.canonical >> s.max_cov >> s.min_cov >> s.max_cv >> l >> r >> o1 >> o2 >> o3;
+        if (!in) return "ERR usage: SELECT k ds max_cov min_cov max_CV left right left_out right_out accs_out";
+        if (s.max_cov < 2) return "ERR max_cov must be at least 2";
         s.kind = TK_JOB_NORMALIZE;
         if (!readable(l) || !readable(r)) return "ERR cannot read " + l + " or " + r;
         t1 = read_file(l);
@@ -140,6 +152,13 @@ static std::string handle(const std::string &req) {
         if (!o2.empty()) {
             const uint64_t *h = out_as<uint64_t>(id, 1, &n2);
             write_chunks(o2, histo_text(h, n2), {});
+        }
+    } else if (s.kind == TK_JOB_NORMALIZE && s.max_cov >= 2) {
+        const char *accs = out_as<char>(id, 10, &n);
+        write_chunks(o3, std::string(accs, n), {});
+        for (int side = 0; side < 2; side++) {
+            const char *recs = out_as<char>(id, 12 + side, &n2);
+            write_chunks(side ? o2 : o1, std::string(recs, n2), {});
         }
     } else if (s.kind == TK_JOB_NORMALIZE) {
         const char *hdr = "acc\tmedian_cov\tmean_cov\tstdev\n";
