@@ -11,32 +11,28 @@ from __future__ import annotations
 
 import atexit
 import ctypes as C
-import weakref
 from typing import Optional, Sequence, Tuple, Union
 
 import numpy as np
 
 from . import native as N
 
-# Every live handle owner, so that interpreter exit frees read sets, tables
-# and selections before their contexts, while the CUDA runtime and any other
-# CUDA user in the process (PyTorch) are still fully up.
-_owners: "weakref.WeakSet" = weakref.WeakSet()
-_contexts: "weakref.WeakSet" = weakref.WeakSet()
+# At interpreter exit the library is not called any more: handles still alive
+# are left to the process teardown (the driver reclaims the device memory),
+# so that no CUDA state another library in the process (PyTorch) still uses
+# is released under it while that library tears down its own objects.
+_exiting = False
 
 
 @atexit.register
-def _release_all() -> None:
-    for o in list(_owners):
-        try:
-            o.free()
-        except Exception:
-            pass
-    for c in list(_contexts):
-        try:
-            c.close()
-        except Exception:
-            pass
+def _at_exit() -> None:
+    global _exiting
+    _exiting = True
+
+
+def _live() -> bool:
+    return not _exiting
+
 
 Buffer = Union[bytes, bytearray, memoryview, np.ndarray]
 
@@ -77,12 +73,11 @@ class Context:
         N.check(st, "tk_ctx_create")
         self.h = h
         self.device = device
-        _contexts.add(self)
 
     def close(self) -> None:
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and _live():
             self.lib.tk_ctx_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __enter__(self):
         return self
@@ -165,7 +160,6 @@ class ReadSet:
 
     def _adopt(self, h) -> None:
         self.h = h
-        _owners.add(self)
         nr, nb, ml, fm = C.c_uint64(), C.c_uint64(), C.c_uint32(), C.c_int()
         self.ctx.check(self.lib.tk_reads_info(h, C.byref(nr), C.byref(nb), C.byref(ml), C.byref(fm)), "tk_reads_info")
         self.n_reads, self.n_bases, self.max_len, self.format = nr.value, nb.value, ml.value, fm.value
@@ -191,7 +185,7 @@ class ReadSet:
         return out
 
     def free(self) -> None:
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and _live():
             self.lib.tk_reads_free(self.h)
             self.h = None
 
@@ -270,10 +264,9 @@ class KmerTable:
         h = C.c_void_p()
         ctx.check(self.lib.tk_table_create(ctx.h, k, int(canonical), capacity, C.byref(h)), "tk_table_create")
         self.h = h
-        _owners.add(self)
 
     def free(self) -> None:
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and _live():
             self.lib.tk_table_free(self.h)
             self.h = None
 
@@ -387,7 +380,6 @@ class ReadsToTranscripts:
         ctx.check(self.lib.tk_r2t_create(ctx.h, C.c_void_p(ptr), n, N.TK_HOST, k, int(strand), C.byref(h)),
                   "tk_r2t_create")
         self.h = h
-        _owners.add(self)
         nr, nk = C.c_uint64(), C.c_uint64()
         ctx.check(self.lib.tk_r2t_info(h, C.byref(nr), C.byref(nk)), "tk_r2t_info")
         self.n_records, self.n_kmers = nr.value, nk.value
@@ -396,7 +388,7 @@ class ReadsToTranscripts:
         self.component_ids = ids[:self.n_records]
 
     def free(self) -> None:
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and _live():
             self.lib.tk_r2t_free(self.h)
             self.h = None
 
@@ -459,7 +451,6 @@ class Normalization:
                                           N.TK_DEVICE if device else N.TK_HOST, max_cov, min_cov, max_cv,
                                           C.byref(h)), "tk_norm_select")
         self.h = h
-        _owners.add(self)
         cnt = (C.c_uint64 * 4)()
         alen = C.c_uint64()
         ctx.check(self.lib.tk_norm_info(h, cnt, C.byref(alen)), "tk_norm_info")
@@ -467,7 +458,7 @@ class Normalization:
         self.accs_len = alen.value
 
     def free(self) -> None:
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and _live():
             self.lib.tk_norm_free(self.h)
             self.h = None
 

@@ -7,7 +7,7 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 
 from . import native as N
-from .kmer import _contexts, _host_ptr
+from .kmer import _host_ptr, _live
 
 
 class Server:
@@ -19,13 +19,12 @@ class Server:
         h = C.c_void_p()
         N.check(self.lib.tk_server_create(device, slots, hbm_budget, C.byref(h)), "tk_server_create")
         self.h = h
-        _contexts.add(self)   # closed at interpreter exit if still open
         self._keep: Dict[int, object] = {}
 
     def close(self) -> None:
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and _live():
             self.lib.tk_server_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __enter__(self):
         return self
