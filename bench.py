@@ -5,17 +5,20 @@ Workload (the plain path at scale): 20,000 multi-isoform genes, 20M read
 pairs of 2x100 nt (fragment normal(300, 50), 1% substitutions, 0.01% N),
 constant-quality FASTQ, generated from a fixed seed.  One step is the plain
 pipeline the reference runs for in-silico normalization
-(util/insilico_read_normalization.pl:588-654, 816-898): parse both mates,
-canonical k=25 count of all 40M reads (jellyfish count), histogram
-(jellyfish histo), the -L 2 catalogue as text (jellyfish dump), and per-read
-median/mean/stdev coverage of each mate file (fastaToKmerCoverageStats).
+(util/insilico_read_normalization.pl:588-654, 816-985, 470-584): parse both
+mates, canonical k=25 count of all 40M reads (jellyfish count), histogram
+(jellyfish histo), the -L 2 catalogue as text (jellyfish dump), per-read
+median/mean/stdev coverage of each mate file (fastaToKmerCoverageStats), and
+the normalization to max_cov 200: both stats tables sorted by name, the pair
+merge, the seeded selection (nbkc_normalize.pl) and the selected FASTQ
+records of both mates extracted.
 
 value  = k-mer occurrences counted / step time, inputs resident in HBM
-e2e    = the same through the C ABI from pinned host FASTQ, with the dump text
-         and the statistics copied back to the host inside the timed region;
-         each mate file goes up in record-aligned pieces so that one piece is
-         parsed while the next uploads, and the dump's download overlaps the
-         coverage pass
+e2e    = the same through the C ABI from pinned host FASTQ, with the dump text,
+         the statistics and the normalized records copied back to the host
+         inside the timed region; each mate file goes up in record-aligned
+         pieces so that one piece is parsed while the next uploads, and the
+         dump's download overlaps the coverage pass and the selection
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--pairs P]
 """
@@ -42,6 +45,7 @@ K = 25
 MIN_COUNT = 2           # the catalogue fastaToKmerCoverageStats reads (util/insilico_read_normalization.pl:45)
 L2_BYTES = 129 * 2**20
 E2E_PIECES = 2          # record-aligned pieces per mate file on the end-to-end path
+NORM_ARGS = (200, 1, 10000)   # normalization: Trinity's --max_cov 200 --min_cov 1 --max_CV 10000
 
 
 def log(*a):
@@ -174,6 +178,7 @@ class GpuPipeline:
                 self.out[side + "_dev"] = [t.empty(n, dtype=t.int32, device=self.dev) for _ in range(3)]
                 self.out[side + "_host"] = [t.empty(n, dtype=t.int32).pin_memory() for _ in range(3)]
             self.out["dump_host"] = None
+            self.out["ext_host"] = None
 
     def step(self, e2e: bool):
         """One plain pipeline pass; returns (windows, reads, h2d_bytes, d2h_bytes)."""
@@ -221,15 +226,34 @@ class GpuPipeline:
                 for h, d in zip(self.out[side + "_host"], bufs):
                     h[:first].copy_(d[:first], non_blocking=True)
                 d2h += 12 * first
-        if e2e:
-            ctx.synchronize()
         _, windows, capacity = table.info(distinct=False)
+        # normalization to max_cov 200 (insilico_read_normalization.pl --pairs_together):
+        # both mates' statistics sorted by name, pair merge, seeded selection,
+        # and the selected FASTQ records of both mates extracted
+        nm = kmer.Normalization(ctx, left_sets, tuple(b.data_ptr() for b in self.out["l_dev"]), right_sets,
+                                tuple(b.data_ptr() for b in self.out["r_dev"]), *NORM_ARGS, device=True)
+        selected = nm.counts["selected"]
+        ext = 0
+        for group in (left_sets, right_sets):
+            if e2e:
+                if self.out["ext_host"] is None:
+                    self.out["ext_host"] = t.empty(int(1.2 * (self.h_left.numel() + self.h_right.numel())) + 16,
+                                                   dtype=t.uint8).pin_memory()
+                h = self.out["ext_host"]   # a mate's records never exceed the mate's text
+                n = nm.extract_into(group, h.data_ptr() + ext, h.numel() - ext)
+            else:
+                n = nm.extract_into(group)
+            ext += n
+        nm.free()
+        table.free()   # after the dump text's download, which overlapped the coverage and selection
+        if e2e:
+            d2h += ext
+            ctx.synchronize()
         reads = n_left + n_right
         packed = sum(r.n_bases + r.n_reads for r in left_sets + right_sets)
-        table.free()
         for r in left_sets + right_sets:
             r.free()
-        return windows, reads, h2d, d2h, packed, capacity
+        return windows, reads, h2d, d2h, packed, capacity, selected, ext
 
 
 def timed(pipe, stream, steps, e2e, dist):
@@ -272,7 +296,8 @@ def run_gpu(args, dist, world, rank, local):
     ms, res = timed(pipe, stream, args.steps, False, dist)
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
-    prof = {k: ctx.profile(k) for k in ("parse", "hll", "scatter", "count", "compact", "sort", "dump", "coverage")}
+    prof = {k: ctx.profile(k) for k in ("parse", "hll", "scatter", "count", "compact", "sort", "dump", "coverage",
+                                         "norm", "extract")}
     ctx.set_profiling(False)
     # end-to-end timed region (host FASTQ in, dump text + stats out)
     ms_e2e, res_e2e = timed(pipe, stream, args.steps, True, dist)
@@ -332,15 +357,21 @@ def run_gpu(args, dist, world, rank, local):
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded; no public dataset for this path)",
             "config": {"workload": f"plain path at scale: {N_GENES} genes, {args.pairs} pairs 2x100 FASTQ, "
-                                   "1% substitutions, 0.01% N; count + histo + dump -L 2 + coverage stats",
+                                   "1% substitutions, 0.01% N; count + histo + dump -L 2 + coverage stats + "
+                                   "normalization to max_cov 200 (name sort, pair merge, seeded selection, "
+                                   "extraction of both mates' records)",
                        "pairs_per_gpu": args.pairs, "reads_per_gpu": reads, "k": K, "canonical": True,
                        "dump_min_count": MIN_COUNT, "input_bytes_per_gpu": input_bytes,
                        "l2": "inputs larger than L2 (%.1f GB FASTQ vs 129 MB)" % (input_bytes / 1e9),
                        "parallelism": f"replicas x{world}"},
             "reads_per_s": tot_reads / t_step,
+            "normalization": {"pairs_selected": res[0][6], "extracted_bytes": res[0][7],
+                              "max_cov": NORM_ARGS[0], "min_cov": NORM_ARGS[1], "max_cv": NORM_ARGS[2]},
             "kmer_occurrences_per_step": tot_windows,
+            "ms_steps": [round(x, 2) for x in ms],
             "e2e": {"value": tot_windows / t_e2e, "unit": UNIT, "reads_per_s": tot_reads / t_e2e,
-                    "ms_per_step": t_e2e * 1e3, "h2d_bytes_per_step": res_e2e[0][2],
+                    "ms_per_step": t_e2e * 1e3, "ms_steps": [round(x, 2) for x in ms_e2e],
+                    "h2d_bytes_per_step": res_e2e[0][2],
                     "d2h_bytes_per_step": res_e2e[0][3]},
             "roofline": kernels[top],
             "roofline_kernels": kernels,
@@ -428,7 +459,6 @@ def prep_bench(ctx, fastq, args):
 
 # ---------------------------------------------------------------- normalization tail
 
-NORM_ARGS = (200, 1, 10000)   # Trinity's defaults: --max_cov 200 --min_cov 1 --max_CV 10000
 
 
 def norm_bench(ctx, left, right, args):
@@ -821,14 +851,19 @@ def served_bench(ctx, args):
 
 def cpu_pipeline(left: bytes, right: bytes, threads: int):
     """The plain pipeline with the oracle on the host cores: count (hash order,
-    as jellyfish dumps), histo, dump -L 2, catalogue parse, stats per mate."""
+    as jellyfish dumps), histo, dump -L 2, catalogue parse, stats per mate,
+    then the normalization (sort, pair merge, selection, extraction of both
+    mates' records; single-threaded, as the reference's sort + Perl are)."""
     from oracle import oracle as O
     keys, counts = O.count(left + right, K, True, threads, sorted_=False)
     O.histo(counts, 1, 10000)
     dump = O.dump(keys, counts, K, MIN_COUNT)
     k2, c2 = O.load_dump(dump, K, True)
-    O.cov_stats(left, k2, c2, K, True, False, threads)
-    O.cov_stats(right, k2, c2, K, True, False, threads)
+    ls = O.cov_stats(left, k2, c2, K, True, False, threads)
+    rs = O.cov_stats(right, k2, c2, K, True, False, threads)
+    _, accs, _ = O.norm(ls, rs, *NORM_ARGS)
+    O.norm_extract(left, accs)
+    O.norm_extract(right, accs)
     return int(counts.sum(dtype="uint64"))
 
 
@@ -850,7 +885,8 @@ def cpu_baseline(args):
     return {"value": windows / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "reads_per_s": 2 * args.cpu_pairs / dt, "seconds": dt,
             "sample": f"first {args.cpu_pairs} pairs of the same seeded workload; the CPU oracle (C, OpenMP) "
-                      "count + histo + dump -L 2 + catalogue load + coverage stats of both mates"}
+                      "count + histo + dump -L 2 + catalogue load + coverage stats of both mates + normalization "
+                      "(sort, merge, selection, extraction)"}
 
 
 def run_reference(args, world, rank):
@@ -873,7 +909,8 @@ def run_reference(args, world, rank):
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
             "config": {"workload": f"plain path at scale (bounded sample: {args.cpu_pairs} pairs of the 20M-pair "
-                                   "workload)", "k": K, "canonical": True, "dump_min_count": MIN_COUNT},
+                                   "workload) incl. normalization to max_cov 200", "k": K, "canonical": True,
+                       "dump_min_count": MIN_COUNT},
             "reads_per_s": 2 * args.cpu_pairs / dt,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{args.cpu_pairs} pairs per step; the reference's jellyfish, Inchworm and "

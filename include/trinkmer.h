@@ -283,6 +283,14 @@ int tk_norm_select(tk_ctx *ctx, const tk_reads *left, const uint32_t *left_media
                    const float *left_stdev, const tk_reads *right, const uint32_t *right_median,
                    const float *right_mean, const float *right_stdev, int where, int max_cov, int min_cov,
                    int max_cv, tk_norm **out);
+/* tk_norm_select over a side whose reads are split across several read sets
+ * (e.g. record-aligned pieces of one file, tk_split_records): the side's
+ * reads are the sets' reads in order, and its statistics arrays hold them in
+ * that order.  No counterpart in the reference (its scripts read whole files). */
+int tk_norm_select_multi(tk_ctx *ctx, const tk_reads *const *left, uint32_t n_left, const uint32_t *left_median,
+                         const float *left_mean, const float *left_stdev, const tk_reads *const *right,
+                         uint32_t n_right, const uint32_t *right_median, const float *right_mean,
+                         const float *right_stdev, int where, int max_cov, int min_cov, int max_cv, tk_norm **out);
 /* counts and the byte length of the accs text */
 int tk_norm_info(const tk_norm *norm, tk_norm_counts *counts, uint64_t *accs_len);
 /* nbkc_normalize.pl's output: one selected acc per line (without "/1" or "/2") */
@@ -300,6 +308,11 @@ int tk_norm_table(tk_norm *norm, int where, char *out, uint64_t cap, uint64_t *l
  * TK_E_PARSE (the script dies with "not all specified records have been
  * retrieved"); a FASTA accession longer than 256 bytes is TK_E_RANGE. */
 int tk_norm_extract(tk_norm *norm, const tk_reads *fastq, uint64_t *len);
+/* The same over one side's reads split across several read sets (files or
+ * record-aligned pieces, in order): their records back to back, and a
+ * selected name counts as found when any of them carries it
+ * (make_normalized_reads_file reads all files of a side, insilico:502-545). */
+int tk_norm_extract_multi(tk_norm *norm, const tk_reads *const *sets, uint32_t n_sets, uint64_t *len);
 int tk_norm_extract_copy(const tk_norm *norm, int where, char *out, uint64_t cap);
 void tk_norm_free(tk_norm *norm);
 

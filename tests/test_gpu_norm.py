@@ -200,3 +200,29 @@ def test_out_of_range_statistics_are_rejected(ctx):
     zero = (np.array([0, 1], np.uint32), np.array([1.0, 1.0], np.float32), np.array([0, 0], np.float32))
     with pytest.raises(native.TrinkmerError):
         Normalization(ctx, rs, zero, min_cov=0)
+
+
+def test_sides_in_pieces_select_like_whole_sides(ctx, oracle):
+    """tk_norm_select_multi: a side split into record-aligned pieces (each its
+    own read set, statistics concatenated in order) selects what the whole
+    side selects, and the pieces' extractions concatenate to the whole one."""
+    from trinityrnaseq_gb300.kmer import split_records
+    left, right = synth.gene_pairs(seed=64, n_genes=300, n_pairs=60000, fastq=True)
+    lfq, rfq = shuffled_fastq(left.tobytes(), 5, 0.01), shuffled_fastq(right.tobytes(), 6, 0.01)
+    whole = [ReadSet(ctx, lfq), ReadSet(ctx, rfq)]
+    t = KmerTable(ctx, 25, True)
+    t.add_many(whole)
+    stats = [coverage_stats(t, r) for r in whole]
+    nm = Normalization(ctx, whole[0], stats[0], whole[1], stats[1], 20, 1, 10000)
+    pieces = []
+    for text in (lfq, rfq):
+        cuts = split_records(text, 3)
+        pieces.append([ReadSet(ctx, text[cuts[i]:cuts[i + 1]]) for i in range(3)])
+    nm2 = Normalization(ctx, pieces[0], stats[0], pieces[1], stats[1], 20, 1, 10000)
+    assert nm2.accs() == nm.accs()
+    assert nm2.table() == nm.table()
+    for side in range(2):
+        assert nm2.extract(pieces[side]) == nm.extract(whole[side])
+    # one piece alone lacks records of selected names: an error, as for a short file
+    with pytest.raises(native.TrinkmerError):
+        nm2.extract(pieces[0][0])

@@ -1025,21 +1025,30 @@ void tk_r2t_free(tk_r2t *z) {
 
 // ------------------------------------------------------------------ normalization
 
-int tk_norm_select(tk_ctx *c, const tk_reads *left, const uint32_t *left_median, const float *left_mean,
-                   const float *left_stdev, const tk_reads *right, const uint32_t *right_median,
-                   const float *right_mean, const float *right_stdev, int where, int max_cov, int min_cov,
-                   int max_cv, tk_norm **out) {
+int tk_norm_select_multi(tk_ctx *c, const tk_reads *const *left, uint32_t n_left, const uint32_t *left_median,
+                         const float *left_mean, const float *left_stdev, const tk_reads *const *right,
+                         uint32_t n_right, const uint32_t *right_median, const float *right_mean,
+                         const float *right_stdev, int where, int max_cov, int min_cov, int max_cv, tk_norm **out) {
     if (!out) return TK_E_INVAL;
     *out = nullptr;
     CHECK_CTX(c);
-    if (!left || left->ctx != c || (right && right->ctx != c))
-        return set_err(c, TK_E_INVAL, "tk_norm_select: read sets of another context");
+    if (!left || n_left == 0 || (right && n_right == 0))
+        return set_err(c, TK_E_INVAL, "tk_norm_select: no read set on a side");
     if (where != TK_HOST && where != TK_DEVICE) return set_err(c, TK_E_INVAL, "tk_norm_select: where");
-    if (left->n_reads && (!left_median || !left_mean || !left_stdev))
+    uint64_t nl = 0, nr = 0;
+    for (uint32_t i = 0; i < n_left; i++) {
+        if (!left[i] || left[i]->ctx != c) return set_err(c, TK_E_INVAL, "tk_norm_select: read sets of another context");
+        nl += left[i]->n_reads;
+    }
+    for (uint32_t i = 0; right && i < n_right; i++) {
+        if (!right[i] || right[i]->ctx != c) return set_err(c, TK_E_INVAL, "tk_norm_select: read sets of another context");
+        nr += right[i]->n_reads;
+    }
+    if (nl && (!left_median || !left_mean || !left_stdev))
         return set_err(c, TK_E_INVAL, "tk_norm_select: left statistics missing");
-    if (right && right->n_reads && (!right_median || !right_mean || !right_stdev))
+    if (right && nr && (!right_median || !right_mean || !right_stdev))
         return set_err(c, TK_E_INVAL, "tk_norm_select: right statistics missing");
-    if (left->n_reads > 0xFFFFFFFFull || (right && right->n_reads > 0xFFFFFFFFull))
+    if (nl > 0xFFFFFFFFull || nr > 0xFFFFFFFFull)
         return set_err(c, TK_E_INVAL, "tk_norm_select: more than 2^32 reads on a side");
     tk_norm *nm = new (std::nothrow) tk_norm();
     if (!nm) return TK_E_OOM;
@@ -1049,17 +1058,31 @@ int tk_norm_select(tk_ctx *c, const tk_reads *left, const uint32_t *left_median,
     nm->min_cov = min_cov;
     nm->max_cv = max_cv;
     ctx_acquire(c);
-    const tk_reads *reads[2] = {left, right};
+    const tk_reads *const *sets[2] = {left, right};
+    const uint32_t nsets[2] = {n_left, right ? n_right : 0u};
     const uint32_t *med[2] = {left_median, right_median};
     const float *mean[2] = {left_mean, right_mean};
     const float *sd[2] = {left_stdev, right_stdev};
-    int e = norm_select(nm, reads, med, mean, sd, where);
+    int e = norm_select(nm, sets, nsets, med, mean, sd, where);
     if (e) {
         tk_norm_free(nm);
         return e;
     }
     *out = nm;
     return TK_OK;
+}
+
+int tk_norm_select(tk_ctx *c, const tk_reads *left, const uint32_t *left_median, const float *left_mean,
+                   const float *left_stdev, const tk_reads *right, const uint32_t *right_median,
+                   const float *right_mean, const float *right_stdev, int where, int max_cov, int min_cov,
+                   int max_cv, tk_norm **out) {
+    if (!left) {
+        if (out) *out = nullptr;
+        return c ? set_err(c, TK_E_INVAL, "tk_norm_select: no left read set") : TK_E_INVAL;
+    }
+    return tk_norm_select_multi(c, &left, 1, left_median, left_mean, left_stdev, right ? &right : nullptr,
+                                right ? 1u : 0u, right_median, right_mean, right_stdev, where, max_cov, min_cov,
+                                max_cv, out);
 }
 
 int tk_norm_info(const tk_norm *nm, tk_norm_counts *counts, uint64_t *accs_len) {
@@ -1096,14 +1119,20 @@ int tk_norm_table(tk_norm *nm, int where, char *out, uint64_t cap, uint64_t *len
     return norm_copy_out(c, nm->d_table, nm->table_len, where, out, cap, "tk_norm_table");
 }
 
-int tk_norm_extract(tk_norm *nm, const tk_reads *fastq, uint64_t *len) {
-    if (!nm || !fastq) return TK_E_INVAL;
+int tk_norm_extract_multi(tk_norm *nm, const tk_reads *const *sets, uint32_t n_sets, uint64_t *len) {
+    if (!nm || !sets || n_sets == 0) return TK_E_INVAL;
     tk_ctx *c = nm->ctx;
     CHECK_CTX(c);
-    if (fastq->ctx != c) return set_err(c, TK_E_INVAL, "tk_norm_extract: read set of another context");
-    TK_TRY(norm_extract(nm, fastq));
+    for (uint32_t i = 0; i < n_sets; i++)
+        if (!sets[i] || sets[i]->ctx != c) return set_err(c, TK_E_INVAL, "tk_norm_extract: read set of another context");
+    TK_TRY(norm_extract(nm, sets, n_sets));
     if (len) *len = nm->ext_len;
     return TK_OK;
+}
+
+int tk_norm_extract(tk_norm *nm, const tk_reads *fastq, uint64_t *len) {
+    if (!nm || !fastq) return TK_E_INVAL;
+    return tk_norm_extract_multi(nm, &fastq, 1, len);
 }
 
 int tk_norm_extract_copy(const tk_norm *nm, int where, char *out, uint64_t cap) {

@@ -296,10 +296,12 @@ struct NormVal {
     uint8_t pad;
 };
 
-// One side's reads in the order of its sorted stats table.
+// One side's reads (from one or more read sets) in the order of its sorted
+// stats table.
 struct NormSide {
     uint64_t n = 0;
-    const char *text = nullptr;     // device text the names point into
+    uint64_t *addr = nullptr;       // read order: device address of each name
+    uint32_t *nlen = nullptr;       // read order: name length
     NormVal *val = nullptr;         // read order
     uint32_t *perm = nullptr;       // sorted position -> read
     uint64_t *h0 = nullptr, *h1 = nullptr, *off = nullptr;   // sorted: first 16 name bytes, name offset
@@ -349,10 +351,10 @@ int table_rehash(tk_table *t, uint64_t new_capacity);
 int table_count_seq(tk_table *t, const tk_reads *r);
 int reads_fasta(tk_reads *r, int append, int flags, char **d_text, uint64_t *text_len);
 int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets);
-int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *const med[2],
-                const float *const mean[2], const float *const sd[2], int where);
+int norm_select(tk_norm *nm, const tk_reads *const *const sets[2], const uint32_t nsets[2],
+                const uint32_t *const med[2], const float *const mean[2], const float *const sd[2], int where);
 int norm_table(tk_norm *nm);
-int norm_extract(tk_norm *nm, const tk_reads *fq);
+int norm_extract(tk_norm *nm, const tk_reads *const *sets, uint32_t nsets);
 void norm_release(tk_norm *nm);
 }  // namespace tk
 

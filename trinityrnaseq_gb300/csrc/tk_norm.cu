@@ -265,16 +265,30 @@ __global__ void k_norm_vals(uint64_t n, const uint32_t *__restrict__ med, const 
 
 // ---------------------------------------------------------------- name sort
 
+// A name is addressed by its device address (reads of one side may come
+// from several read sets, each with its own text).
+__device__ __forceinline__ const char *at(uint64_t a) { return reinterpret_cast<const char *>(a); }
+
 // 8 name bytes from byte 8*ch, big-endian, zero past the name's end
-__device__ __forceinline__ uint64_t name_chunk(const char *__restrict__ text, uint64_t off, uint32_t len, uint32_t ch) {
+__device__ __forceinline__ uint64_t name_chunk(const char *__restrict__ name, uint32_t len, uint32_t ch) {
     uint64_t k = 0;
     const uint32_t b0 = ch * 8;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const uint32_t p = b0 + i;
-        k = (k << 8) | (p < len ? (uint64_t)(uint8_t)text[off + p] : 0ull);
+        k = (k << 8) | (p < len ? (uint64_t)(uint8_t)name[p] : 0ull);
     }
     return k;
+}
+
+// read set -> the side's name addresses and lengths (from index first on)
+__global__ void k_name_addr(const char *__restrict__ text, const uint64_t *__restrict__ name_off,
+                            const uint32_t *__restrict__ name_len, uint64_t n, uint64_t *__restrict__ addr,
+                            uint32_t *__restrict__ len) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    addr[i] = reinterpret_cast<uint64_t>(text + name_off[i]);
+    len[i] = name_len[i];
 }
 
 __device__ __forceinline__ uint64_t slot_chunk(const uint8_t *__restrict__ slots, uint64_t r, uint32_t ch) {
@@ -306,8 +320,8 @@ __global__ void k_iota(uint32_t *__restrict__ p, uint64_t n) {
 
 // keys[i] = the sort key of read perm[i] (mode 0: name chunk ch, 1: suffix
 // chunk ch, 2: name length); orand[0] |= keys, orand[1] &= keys
-__global__ void k_sort_keys(const char *__restrict__ text, const uint64_t *__restrict__ name_off,
-                            const uint32_t *__restrict__ name_len, const uint8_t *__restrict__ slots,
+__global__ void k_sort_keys(const uint64_t *__restrict__ name_addr, const uint32_t *__restrict__ name_len,
+                            const uint8_t *__restrict__ slots,
                             const uint32_t *__restrict__ perm, uint64_t n, int mode, uint32_t ch,
                             uint64_t *__restrict__ keys, unsigned long long *__restrict__ orand) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -315,7 +329,7 @@ __global__ void k_sort_keys(const char *__restrict__ text, const uint64_t *__res
     if (i < n) {
         const uint32_t r = perm[i];
         uint64_t k;
-        if (mode == 0) k = name_chunk(text, name_off[r], name_len[r], ch);
+        if (mode == 0) k = name_chunk(at(name_addr[r]), name_len[r], ch);
         else if (mode == 1) k = slot_chunk(slots, r, ch);
         else k = name_len[r];
         keys[i] = k;
@@ -355,26 +369,27 @@ __global__ void k_sfx_slots(const NormVal *__restrict__ val, uint64_t n, uint8_t
 
 // sorted-order name arrays; core = length without a final "/<digit>" (names
 // are first header tokens, so they hold no whitespace)
-__global__ void k_sorted_names(const char *__restrict__ text, const uint64_t *__restrict__ name_off,
-                               const uint32_t *__restrict__ name_len, const uint32_t *__restrict__ perm, uint64_t n,
+__global__ void k_sorted_names(const uint64_t *__restrict__ name_addr, const uint32_t *__restrict__ name_len,
+                               const uint32_t *__restrict__ perm, uint64_t n,
                                uint64_t *__restrict__ h0, uint64_t *__restrict__ h1, uint64_t *__restrict__ off,
                                uint32_t *__restrict__ len, uint32_t *__restrict__ core) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t r = perm[i];
-    const uint64_t o = name_off[r];
+    const uint64_t o = name_addr[r];
     const uint32_t l = name_len[r];
-    h0[i] = name_chunk(text, o, l, 0);
-    h1[i] = name_chunk(text, o, l, 1);
+    const char *nm = at(o);
+    h0[i] = name_chunk(nm, l, 0);
+    h1[i] = name_chunk(nm, l, 1);
     off[i] = o;
     len[i] = l;
     uint32_t c = l;
-    if (l >= 3 && text[o + l - 2] == '/' && (uint32_t)((uint8_t)text[o + l - 1] - '0') < 10u) c = l - 2;
+    if (l >= 3 && nm[l - 2] == '/' && (uint32_t)((uint8_t)nm[l - 1] - '0') < 10u) c = l - 2;
     core[i] = c;
 }
 
 // set when a sorted neighbour has the same zero-padded name
-__global__ void k_sort_ties(const char *__restrict__ text, const uint64_t *__restrict__ h0,
+__global__ void k_sort_ties(const uint64_t *__restrict__ h0,
                             const uint64_t *__restrict__ h1, const uint64_t *__restrict__ off,
                             const uint32_t *__restrict__ len, uint64_t n, uint32_t *__restrict__ flag) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -382,7 +397,7 @@ __global__ void k_sort_ties(const char *__restrict__ text, const uint64_t *__res
     if (h0[i] != h0[i - 1] || h1[i] != h1[i - 1]) return;
     const uint32_t la = len[i - 1], lb = len[i], m = la > lb ? la : lb;
     for (uint32_t p = 16; p < m; p++) {
-        const uint8_t x = p < la ? (uint8_t)text[off[i - 1] + p] : 0, y = p < lb ? (uint8_t)text[off[i] + p] : 0;
+        const uint8_t x = p < la ? (uint8_t)at(off[i - 1])[p] : 0, y = p < lb ? (uint8_t)at(off[i])[p] : 0;
         if (x != y) return;
     }
     atomicExch(flag, 1u);
@@ -391,8 +406,7 @@ __global__ void k_sort_ties(const char *__restrict__ text, const uint64_t *__res
 // ---------------------------------------------------------------- pair merge
 
 struct SNames {
-    const char *text;
-    const uint64_t *h0, *h1, *off;
+    const uint64_t *h0, *h1, *off;   // off: the name's device address
     const uint32_t *len, *core;
 };
 
@@ -404,7 +418,7 @@ __device__ int sn_cmp(const SNames &A, uint64_t i, const SNames &B, uint64_t j) 
     if (a1 != b1) return a1 < b1 ? -1 : 1;
     const uint32_t la = A.len[i], lb = B.len[j], m = la < lb ? la : lb;
     if (m > 16) {
-        const char *pa = A.text + A.off[i], *pb = B.text + B.off[j];
+        const char *pa = at(A.off[i]), *pb = at(B.off[j]);
         for (uint32_t p = 16; p < m; p++) {
             const uint8_t x = (uint8_t)pa[p], y = (uint8_t)pb[p];
             if (x != y) return x < y ? -1 : 1;
@@ -426,7 +440,7 @@ __device__ bool sn_core_eq(const SNames &A, uint64_t i, const SNames &B, uint64_
         return ((A.h1[i] ^ B.h1[j]) & mask) == 0;
     }
     if (A.h1[i] != B.h1[j]) return false;
-    const char *pa = A.text + A.off[i], *pb = B.text + B.off[j];
+    const char *pa = at(A.off[i]), *pb = at(B.off[j]);
     for (uint32_t p = 16; p < c; p++)
         if (pa[p] != pb[p]) return false;
     return true;
@@ -601,7 +615,7 @@ __device__ __forceinline__ void row_acc(const RowArgs &a, const SNames &L, uint6
     const uint64_t i = a.pairs ? a.row_l[p] : p;
     uint32_t n = a.pairs ? L.core[i] : L.len[i];
     const uint64_t o = L.off[i];
-    if (n >= 2 && L.text[o + n - 2] == '/' && (L.text[o + n - 1] == '1' || L.text[o + n - 1] == '2')) n -= 2;
+    if (n >= 2 && at(o)[n - 2] == '/' && (at(o)[n - 1] == '1' || at(o)[n - 1] == '2')) n -= 2;
     *off = o;
     *len = n;
 }
@@ -637,7 +651,7 @@ __global__ void k_norm_accs(RowArgs a, SNames L, const uint64_t *__restrict__ ac
     uint32_t n;
     row_acc(a, L, p, &o, &n);
     char *w = out + acc_off[p];
-    for (uint32_t q = 0; q < n; q++) w[q] = L.text[o + q];
+    for (uint32_t q = 0; q < n; q++) w[q] = at(o)[q];
     w[n] = '\n';
 }
 
@@ -673,7 +687,7 @@ __global__ void k_table_write(RowArgs a, SNames L, SNames R, const uint64_t *__r
     char *o = out + offs[p];
     if (!a.pairs) {
         const uint64_t so = L.off[p];
-        for (uint32_t q = 0; q < L.len[p]; q++) *o++ = L.text[so + q];
+        for (uint32_t q = 0; q < L.len[p]; q++) *o++ = at(so)[q];
         *o++ = '\t';
         o = put_stats_fields(o, a.vl[a.perm_l[p]]);
         *o = '\n';
@@ -682,7 +696,7 @@ __global__ void k_table_write(RowArgs a, SNames L, SNames R, const uint64_t *__r
     const uint64_t i = a.row_l[p], j = a.row_r[p];
     const NormVal l = a.vl[a.perm_l[i]], r = a.vr[a.perm_r[j]];
     const uint64_t *N = a.row_n + 3 * p;
-    const char *ln = L.text + L.off[i], *rn = R.text + R.off[j];
+    const char *ln = at(L.off[i]), *rn = at(R.off[j]);
     for (uint32_t q = 0; q < L.core[i]; q++) *o++ = ln[q];
     *o++ = '\t';
     for (uint32_t q = 0; q < L.len[i]; q++) *o++ = ln[q];
@@ -938,12 +952,12 @@ __global__ void k_extract_find_fa(const char *__restrict__ text, uint64_t text_l
 
 __global__ void k_extract_write_fa(const char *__restrict__ text, uint64_t text_len,
                                    const uint64_t *__restrict__ name_off, uint64_t n,
-                                   const uint64_t *__restrict__ out_off, char *__restrict__ out) {
+                                   const uint64_t *__restrict__ out_off, uint64_t out_base, char *__restrict__ out) {
     const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n || out_off[r + 1] == out_off[r]) return;
     uint64_t a, hl, e;
     fa_extent(text, text_len, name_off, n, r, &a, &hl, &e);
-    char *o = out + out_off[r];
+    char *o = out + out_base + out_off[r];
     *o++ = '>';
     for (uint64_t p = a + 1; p < hl; p++)
         if (fa_hdr_keep((uint8_t)text[p])) *o++ = text[p];
@@ -984,11 +998,11 @@ __device__ __forceinline__ uint32_t rec_word(const char *__restrict__ text, uint
 // stores only for the words a record shares with its neighbours)
 __global__ void k_extract_copy(const char *__restrict__ text, uint64_t text_len, bool vec,
                                const uint64_t *__restrict__ name_off, uint64_t n, const uint64_t *__restrict__ out_off,
-                               char *__restrict__ out) {
+                               uint64_t out_base, char *__restrict__ out) {
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = lane_id();
     if (warp >= n) return;
-    const uint64_t o = out_off[warp], len = out_off[warp + 1] - o;
+    const uint64_t len = out_off[warp + 1] - out_off[warp], o = out_base + out_off[warp];   // out is 4-byte aligned
     if (!len) return;
     const uint64_t a0 = name_off[warp] - 1;
     const uint64_t nw = ((o + len + 3) >> 2) - (o >> 2);
@@ -1021,7 +1035,7 @@ static void lcg_tables(uint64_t a[48], uint64_t c[48]) {
 }
 
 static void side_free(tk_ctx *c, NormSide &s) {
-    void *p[] = {s.val, s.perm, s.h0, s.h1, s.off, s.len, s.core};
+    void *p[] = {s.addr, s.nlen, s.val, s.perm, s.h0, s.h1, s.off, s.len, s.core};
     for (void *q : p)
         if (q) dfree(c, q);
     s = NormSide();
@@ -1049,9 +1063,8 @@ static int read_err(tk_ctx *c, uint32_t *d_err, uint32_t h[NE_WORDS]) {
 
 // One side's names into sorted order: the LSD radix passes of the name (and,
 // when padded names tie, the full key).
-static int sort_side(tk_ctx *c, const tk_reads *r, NormSide &s) {
+static int sort_side(tk_ctx *c, NormSide &s) {
     const uint64_t n = s.n;
-    const char *text = r->d_text;
     TK_TRY(dmalloc(c, (void **)&s.perm, n * 4, "norm order"));
     TK_TRY(dmalloc(c, (void **)&s.h0, n * 8, "norm names"));
     TK_TRY(dmalloc(c, (void **)&s.h1, n * 8, "norm names"));
@@ -1070,7 +1083,7 @@ static int sort_side(tk_ctx *c, const tk_reads *r, NormSide &s) {
     TK_TRY(sc.get((void **)&orand, 16, "sort key bits"));
     TK_CUDA(c, cudaMemsetAsync(d_u32, 0, 16, c->stream));
     k_name_maxlen<<<(unsigned)std::min<uint64_t>(nm_grid(n), (uint64_t)c->sm_count * 8), NM_THREADS, 0, c->stream>>>(
-        r->d_name_len, n, d_u32);
+        s.nlen, n, d_u32);
     c->launches++;
     uint32_t maxlen = 0;
     TK_CUDA(c, cudaMemcpyAsync(&maxlen, d_u32, 4, cudaMemcpyDeviceToHost, c->stream));
@@ -1080,8 +1093,7 @@ static int sort_side(tk_ctx *c, const tk_reads *r, NormSide &s) {
     auto pass = [&](int mode, uint32_t ch) -> int {
         TK_CUDA(c, cudaMemsetAsync(orand, 0, 8, c->stream));
         TK_CUDA(c, cudaMemsetAsync(orand + 1, 0xFF, 8, c->stream));
-        k_sort_keys<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(text, r->d_name_off, r->d_name_len, slots, perm, n, mode,
-                                                               ch, keys, orand);
+        k_sort_keys<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(s.addr, s.nlen, slots, perm, n, mode, ch, keys, orand);
         c->launches++;
         TK_TRY(check_launch(c, "sort keys"));
         unsigned long long h[2];
@@ -1105,15 +1117,15 @@ static int sort_side(tk_ctx *c, const tk_reads *r, NormSide &s) {
     iota();
     for (int ch = (int)nch - 1; ch >= 0; ch--) TK_TRY(pass(0, (uint32_t)ch));
     auto gather = [&]() -> int {
-        k_sorted_names<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(text, r->d_name_off, r->d_name_len, perm, n, s.h0, s.h1,
-                                                                  s.off, s.len, s.core);
+        k_sorted_names<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(s.addr, s.nlen, perm, n, s.h0, s.h1, s.off, s.len,
+                                                                  s.core);
         c->launches++;
         return check_launch(c, "sorted names");
     };
     TK_TRY(gather());
     TK_CUDA(c, cudaMemsetAsync(d_u32, 0, 4, c->stream));
     if (n > 1) {
-        k_sort_ties<<<nm_grid(n - 1), NM_THREADS, 0, c->stream>>>(text, s.h0, s.h1, s.off, s.len, n, d_u32);
+        k_sort_ties<<<nm_grid(n - 1), NM_THREADS, 0, c->stream>>>(s.h0, s.h1, s.off, s.len, n, d_u32);
         c->launches++;
     }
     uint32_t ties = 0;
@@ -1138,7 +1150,6 @@ static int sort_side(tk_ctx *c, const tk_reads *r, NormSide &s) {
 
 static SNames snames(const NormSide &s) {
     SNames v;
-    v.text = s.text;
     v.h0 = s.h0;
     v.h1 = s.h1;
     v.off = s.off;
@@ -1234,8 +1245,8 @@ static RowArgs row_args(const tk_norm *nm) {
     return a;
 }
 
-int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *const med[2],
-                const float *const mean[2], const float *const sd[2], int where) {
+int norm_select(tk_norm *nm, const tk_reads *const *const sets[2], const uint32_t nsets[2],
+                const uint32_t *const med[2], const float *const mean[2], const float *const sd[2], int where) {
     tk_ctx *c = nm->ctx;
     cudaEvent_t ev = nullptr;
     prof_begin(c, TK_KID_NORM, &ev);
@@ -1253,12 +1264,23 @@ int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *con
     uint64_t units = 0;
     for (int sd_i = 0; sd_i < sides; sd_i++) {
         NormSide &s = nm->side[sd_i];
-        const tk_reads *r = reads[sd_i];
-        s.n = r->n_reads;
-        s.text = r->d_text;
+        s.n = 0;
+        for (uint32_t q = 0; q < nsets[sd_i]; q++) s.n += sets[sd_i][q]->n_reads;
         units += s.n;
         TK_TRY(dmalloc(c, (void **)&s.val, (s.n ? s.n : 1) * sizeof(NormVal), "norm values"));
         if (!s.n) continue;
+        TK_TRY(dmalloc(c, (void **)&s.addr, s.n * 8, "norm name addresses"));
+        TK_TRY(dmalloc(c, (void **)&s.nlen, s.n * 4, "norm name lengths"));
+        uint64_t first = 0;
+        for (uint32_t q = 0; q < nsets[sd_i]; q++) {
+            const tk_reads *r = sets[sd_i][q];
+            if (r->n_reads) {
+                k_name_addr<<<nm_grid(r->n_reads), NM_THREADS, 0, c->stream>>>(r->d_text, r->d_name_off, r->d_name_len,
+                                                                               r->n_reads, s.addr + first, s.nlen + first);
+                c->launches++;
+            }
+            first += r->n_reads;
+        }
         const uint32_t *dm = med[sd_i];
         const float *dmean = mean[sd_i], *dsd = sd[sd_i];
         if (where == TK_HOST) {
@@ -1277,7 +1299,7 @@ int norm_select(tk_norm *nm, const tk_reads *const reads[2], const uint32_t *con
         k_norm_vals<<<nm_grid(s.n), NM_THREADS, 0, c->stream>>>(s.n, dm, dmean, dsd, s.val, d_err);
         c->launches++;
         TK_TRY(check_launch(c, "norm values"));
-        TK_TRY(sort_side(c, r, s));
+        TK_TRY(sort_side(c, s));
     }
     uint32_t herr[NE_WORDS];
     TK_TRY(read_err(c, d_err, herr));
@@ -1375,17 +1397,20 @@ int norm_table(tk_norm *nm) {
     return TK_OK;
 }
 
-int norm_extract(tk_norm *nm, const tk_reads *fq) {
+// The records of sets[0..nsets) (one side's files or pieces, in order) that
+// the selection holds; every selected name must be found in one of them.
+int norm_extract(tk_norm *nm, const tk_reads *const *sets, uint32_t nsets) {
     tk_ctx *c = nm->ctx;
     if (nm->d_ext) {
         dfree(c, nm->d_ext);
         nm->d_ext = nullptr;
         nm->ext_len = 0;
     }
-    const bool fasta = fq->format == TK_FMT_FASTA;
     cudaEvent_t ev = nullptr;
     prof_begin(c, TK_KID_EXTRACT, &ev);
-    const uint64_t P = nm->n_rows, n = fq->n_reads;
+    const uint64_t P = nm->n_rows;
+    uint64_t n_all = 0;
+    for (uint32_t q = 0; q < nsets; q++) n_all += sets[q]->n_reads;
     Scratch sc(c);
     uint32_t *d_err = nullptr, *rec_len = nullptr;
     uint8_t *found = nullptr;
@@ -1415,21 +1440,31 @@ int norm_extract(tk_norm *nm, const tk_reads *fq) {
         }
     }
     const uint8_t *dup = nm->d_keydup;
-    TK_TRY(sc.get((void **)&rec_len, n * 4, "extract lengths"));
-    TK_TRY(sc.get((void **)&offs, (n + 1) * 8, "extract offsets"));
-    uint64_t total = 0;
-    if (n) {
-        if (fasta)
-            k_extract_find_fa<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off, n,
-                                                                         nm->d_accs, nm->acc_off, nm->d_hash,
-                                                                         nm->hash_mask, found, rec_len, d_err);
-        else
-            k_extract_find<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off,
-                                                                      fq->d_name_len, n, nm->d_accs, nm->acc_off,
-                                                                      nm->d_hash, nm->hash_mask, found, rec_len);
-        c->launches++;
-        TK_TRY(check_launch(c, "extract find"));
-        TK_TRY(scan_excl_u32_to_u64(c, rec_len, offs, n, &total));
+    // per set: look its records up (marking the names found), then size them
+    TK_TRY(sc.get((void **)&rec_len, n_all * 4, "extract lengths"));
+    TK_TRY(sc.get((void **)&offs, (n_all + nsets) * 8, "extract offsets"));
+    std::vector<uint64_t> base(nsets + 1, 0);
+    uint64_t first = 0;
+    for (uint32_t q = 0; q < nsets; q++) {
+        const tk_reads *fq = sets[q];
+        const uint64_t n = fq->n_reads;
+        uint64_t total = 0;
+        if (n) {
+            uint32_t *rl = rec_len + first;
+            if (fq->format == TK_FMT_FASTA)
+                k_extract_find_fa<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off,
+                                                                             n, nm->d_accs, nm->acc_off, nm->d_hash,
+                                                                             nm->hash_mask, found, rl, d_err);
+            else
+                k_extract_find<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off,
+                                                                          fq->d_name_len, n, nm->d_accs, nm->acc_off,
+                                                                          nm->d_hash, nm->hash_mask, found, rl);
+            c->launches++;
+            TK_TRY(check_launch(c, "extract find"));
+            TK_TRY(scan_excl_u32_to_u64(c, rl, offs + first + q, n, &total));
+        }
+        base[q + 1] = base[q] + total;
+        first += n;
     }
     if (P) {
         k_extract_missing<<<nm_grid(P), NM_THREADS, 0, c->stream>>>(nm->acc_off, P, dup, found, d_missing);
@@ -1445,23 +1480,35 @@ int norm_extract(tk_norm *nm, const tk_reads *fq) {
     if (missing)
         return set_err(c, TK_E_PARSE, "extract: not all selected records were found (missing " +
                                           std::to_string(missing) + ")");
+    const uint64_t total = base[nsets];
     TK_TRY(dmalloc(c, (void **)&nm->d_ext, total ? total : 1, "extracted reads"));
-    if (n && total) {
-        TK_CUDA(c, cudaMemcpyAsync(offs + n, &total, 8, cudaMemcpyHostToDevice, c->stream));
-        if (fasta) {
-            k_extract_write_fa<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, fq->d_name_off, n,
-                                                                          offs, nm->d_ext);
-        } else {
-            const bool vec = ((uintptr_t)fq->d_text & 3) == 0;
-            k_extract_copy<<<nm_grid(n * 32), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, vec,
-                                                                           fq->d_name_off, n, offs, nm->d_ext);
+    first = 0;
+    for (uint32_t q = 0; q < nsets; q++) {
+        const tk_reads *fq = sets[q];
+        const uint64_t n = fq->n_reads;
+        const uint64_t len = base[q + 1] - base[q];
+        if (n && len) {
+            uint64_t *o = offs + first + q;   // n + 1 offsets of this set
+            const uint64_t tail = len;
+            TK_CUDA(c, cudaMemcpyAsync(o + n, &tail, 8, cudaMemcpyHostToDevice, c->stream));
+            // offsets relative to this set's part, which starts at base[q] of d_ext
+            if (fq->format == TK_FMT_FASTA) {
+                k_extract_write_fa<<<nm_grid(n), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len,
+                                                                              fq->d_name_off, n, o, base[q], nm->d_ext);
+            } else {
+                const bool vec = ((uintptr_t)fq->d_text & 3) == 0;
+                k_extract_copy<<<nm_grid(n * 32), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, vec,
+                                                                               fq->d_name_off, n, o, base[q],
+                                                                               nm->d_ext);
+            }
+            c->launches++;
+            TK_TRY(check_launch(c, "extract copy"));
         }
-        c->launches++;
-        TK_TRY(check_launch(c, "extract copy"));
+        first += n;
     }
     TK_CUDA(c, cudaStreamSynchronize(c->stream));
     nm->ext_len = total;
-    prof_end(c, TK_KID_EXTRACT, ev, n);
+    prof_end(c, TK_KID_EXTRACT, ev, n_all);
     return TK_OK;
 }
 

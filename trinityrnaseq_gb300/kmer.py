@@ -64,7 +64,10 @@ def split_records(text: Buffer, n_chunks: int) -> list:
 
 
 class Context:
-    """A CUDA device context with its own stream (tk_ctx)."""
+    """A CUDA device context with its own stream (tk_ctx).  close() destroys
+    the stream: objects of other libraries that used it (e.g. PyTorch tensors
+    allocated or copied under a torch.cuda.ExternalStream of `stream`) must be
+    released first."""
 
     def __init__(self, device: int = 0):
         self.lib = N.load()
@@ -422,8 +425,10 @@ class Normalization:
 
     left_stats / right_stats are (median, mean, stdev) per read as
     coverage_stats returns them (host numpy arrays), or device addresses
-    (median_ptr, mean_ptr, stdev_ptr) with device=True.  right=None selects on
-    one side alone.  The read sets must outlive this object."""
+    (median_ptr, mean_ptr, stdev_ptr) with device=True.  A side may be a list
+    of read sets (pieces of one file; statistics in the same order).
+    right=None selects on one side alone.  The read sets must outlive this
+    object."""
 
     def __init__(self, ctx: Context, left: ReadSet, left_stats, right: Optional[ReadSet] = None, right_stats=None,
                  max_cov: int = 200, min_cov: int = 1, max_cv: int = 10000, device: bool = False):
@@ -444,12 +449,16 @@ class Normalization:
             keep.extend((med, mean, sd))
             return tuple(C.c_void_p(a.ctypes.data) for a in (med, mean, sd))
 
-        lp = ptrs(left_stats, left.n_reads)
-        rp = ptrs(right_stats, right.n_reads) if right is not None else (None, None, None)
+        lsets = list(left) if isinstance(left, (list, tuple)) else [left]
+        rsets = (list(right) if isinstance(right, (list, tuple)) else [right]) if right is not None else []
+        lp = ptrs(left_stats, sum(r.n_reads for r in lsets))
+        rp = ptrs(right_stats, sum(r.n_reads for r in rsets)) if rsets else (None, None, None)
+        lh = (C.c_void_p * len(lsets))(*[r.h for r in lsets])
+        rh = (C.c_void_p * max(len(rsets), 1))(*[r.h for r in rsets]) if rsets else None
         h = C.c_void_p()
-        ctx.check(self.lib.tk_norm_select(ctx.h, left.h, *lp, right.h if right is not None else None, *rp,
-                                          N.TK_DEVICE if device else N.TK_HOST, max_cov, min_cov, max_cv,
-                                          C.byref(h)), "tk_norm_select")
+        ctx.check(self.lib.tk_norm_select_multi(ctx.h, lh, len(lsets), *lp, rh, len(rsets), *rp,
+                                                N.TK_DEVICE if device else N.TK_HOST, max_cov, min_cov, max_cv,
+                                                C.byref(h)), "tk_norm_select")
         self.h = h
         cnt = (C.c_uint64 * 4)()
         alen = C.c_uint64()
@@ -482,17 +491,20 @@ class Normalization:
         self.ctx.check(self.lib.tk_norm_table(self.h, N.TK_HOST, buf, n.value, C.byref(n)), "tk_norm_table")
         return buf.raw[:n.value]
 
-    def extract_into(self, fastq: ReadSet, ptr: Optional[int] = None, cap: int = 0, device: bool = False) -> int:
+    def extract_into(self, fastq, ptr: Optional[int] = None, cap: int = 0, device: bool = False) -> int:
         """Runs the extraction (the text stays on the device) and returns its
-        length; with ptr, also copies it there (host, or device address)."""
+        length; with ptr, also copies it there (host, or device address).
+        fastq may be a list of read sets (one side's files or pieces)."""
         n = C.c_uint64()
-        self.ctx.check(self.lib.tk_norm_extract(self.h, fastq.h, C.byref(n)), "tk_norm_extract")
+        sets = list(fastq) if isinstance(fastq, (list, tuple)) else [fastq]
+        hs = (C.c_void_p * len(sets))(*[r.h for r in sets])
+        self.ctx.check(self.lib.tk_norm_extract_multi(self.h, hs, len(sets), C.byref(n)), "tk_norm_extract")
         if ptr is not None:
             self.ctx.check(self.lib.tk_norm_extract_copy(self.h, N.TK_DEVICE if device else N.TK_HOST,
                                                          C.c_void_p(ptr), cap), "tk_norm_extract_copy")
         return n.value
 
-    def extract(self, fastq: ReadSet) -> bytes:
+    def extract(self, fastq) -> bytes:
         """The selected records of a FASTQ read set, verbatim, in input order."""
         n = self.extract_into(fastq)
         buf = C.create_string_buffer(max(n, 1))

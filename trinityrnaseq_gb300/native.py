@@ -83,10 +83,13 @@ SIGNATURES = {
     "tk_r2t_assign": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
     "tk_r2t_free": (None, [vp]),
     "tk_norm_select": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, P(vp)]),
+    "tk_norm_select_multi": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, u32, vp, vp, vp, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, P(vp)]),
     "tk_norm_info": (C.c_int, [vp, vp, P(u64)]),
     "tk_norm_accs": (C.c_int, [vp, C.c_int, vp, u64]),
     "tk_norm_table": (C.c_int, [vp, C.c_int, vp, u64, P(u64)]),
     "tk_norm_extract": (C.c_int, [vp, vp, P(u64)]),
+    "tk_norm_extract_multi": (C.c_int, [vp, vp, u32, P(u64)]),
     "tk_norm_extract_copy": (C.c_int, [vp, C.c_int, vp, u64]),
     "tk_norm_free": (None, [vp]),
     "tk_count_bins": (C.c_int, [vp, vp, u64, C.c_int, vp, u32, C.c_int, C.c_int, u32, P(vp)]),
