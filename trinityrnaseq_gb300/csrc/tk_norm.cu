@@ -976,45 +976,61 @@ __global__ void k_extract_missing(const uint64_t *__restrict__ acc_off, uint64_t
     if (lane_id() == 0 && m) atomicAdd(missing, (unsigned long long)m);
 }
 
-// The 4 bytes of a record at record offset so (record = text[a0, a0 + n));
-// bytes outside the record read as 0.  Two aligned 4-byte loads and a funnel
-// shift when the text is 4-byte aligned and both words lie inside it.
-__device__ __forceinline__ uint32_t rec_word(const char *__restrict__ text, uint64_t text_len, bool vec, uint64_t a0,
-                                             int64_t so, uint64_t n) {
-    const int64_t a = (int64_t)a0 + so;
-    if (vec && a >= 0 && (uint64_t)((a & ~3LL) + 8) <= text_len && so >= 0 && so + 4 <= (int64_t)n) {
-        const uint32_t *p = reinterpret_cast<const uint32_t *>(text + (a & ~3LL));
-        return __funnelshift_r(__ldg(p), __ldg(p + 1), 8u * (uint32_t)(a & 3));
-    }
-    uint32_t x = 0;
-    for (int i = 0; i < 4; i++) {
-        const int64_t q = so + i;
-        if (q >= 0 && q < (int64_t)n) x |= (uint32_t)(uint8_t)text[a0 + q] << (8 * i);
-    }
-    return x;
-}
+// A block per EX_RECS consecutive records: the block's output is one
+// contiguous byte range, written as aligned 4-byte words by consecutive
+// threads (coalesced); the record holding a word is found by a binary search
+// over the block's record offsets in shared memory.  A word inside one record
+// takes two aligned source loads and a funnel shift; a word across a record
+// boundary, or shared with a neighbouring block, is written byte by byte
+// (only the block's own bytes).
+constexpr int EX_RECS = 256;
 
-// a warp per record; each lane writes aligned 4-byte output words (byte
-// stores only for the words a record shares with its neighbours)
-__global__ void k_extract_copy(const char *__restrict__ text, uint64_t text_len, bool vec,
-                               const uint64_t *__restrict__ name_off, uint64_t n, const uint64_t *__restrict__ out_off,
-                               uint64_t out_base, char *__restrict__ out) {
-    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned lane = lane_id();
-    if (warp >= n) return;
-    const uint64_t len = out_off[warp + 1] - out_off[warp], o = out_base + out_off[warp];   // out is 4-byte aligned
-    if (!len) return;
-    const uint64_t a0 = name_off[warp] - 1;
-    const uint64_t nw = ((o + len + 3) >> 2) - (o >> 2);
-    for (uint64_t w = lane; w < nw; w += 32) {
-        const int64_t so = (int64_t)(4 * w) - (int64_t)(o & 3);
-        const uint32_t x = rec_word(text, text_len, vec, a0, so, len);
-        char *d = out + (o & ~3ULL) + 4 * w;
-        if (so >= 0 && so + 4 <= (int64_t)len) {
+__global__ void __launch_bounds__(NM_THREADS) k_extract_copy(const char *__restrict__ text, uint64_t text_len, bool vec,
+                                                             const uint64_t *__restrict__ name_off, uint64_t n,
+                                                             const uint64_t *__restrict__ out_off, uint64_t out_base,
+                                                             char *__restrict__ out) {
+    __shared__ uint64_t s_off[EX_RECS + 1], s_src[EX_RECS];
+    const uint64_t r0 = (uint64_t)blockIdx.x * EX_RECS;
+    if (r0 >= n) return;
+    const uint32_t m = (uint32_t)(n - r0 < EX_RECS ? n - r0 : EX_RECS);
+    for (uint32_t i = threadIdx.x; i <= m; i += blockDim.x) {
+        s_off[i] = out_base + out_off[r0 + i];            // out_off has n + 1 entries
+        if (i < m) s_src[i] = name_off[r0 + i] - 1;       // the record's '@'
+    }
+    __syncthreads();
+    const uint64_t O0 = s_off[0], O1 = s_off[m];
+    if (O1 == O0) return;
+    const uint64_t w0 = O0 >> 2, w1 = (O1 + 3) >> 2;
+    for (uint64_t w = w0 + threadIdx.x; w < w1; w += blockDim.x) {
+        const uint64_t b = 4 * w;   // the word's first output byte
+        // the last record whose output starts at or before max(b, O0)
+        const uint64_t key = b < O0 ? O0 : b;
+        uint32_t lo = 0, hi = m;    // s_off[lo] <= key < s_off[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_off[mid] <= key) lo = mid;
+            else hi = mid;
+        }
+        char *d = out + b;
+        if (b >= O0 && b + 4 <= s_off[lo + 1]) {
+            const uint64_t a = s_src[lo] + (b - s_off[lo]);
+            uint32_t x;
+            if (vec && (a & ~3ULL) + 8 <= text_len) {
+                const uint32_t *p = reinterpret_cast<const uint32_t *>(text + (a & ~3ULL));
+                x = __funnelshift_r(__ldg(p), __ldg(p + 1), 8u * (uint32_t)(a & 3));
+            } else {
+                x = 0;
+                for (int i = 0; i < 4; i++) x |= (uint32_t)(uint8_t)text[a + i] << (8 * i);
+            }
             *reinterpret_cast<uint32_t *>(d) = x;
         } else {
-            for (int i = 0; i < 4; i++)
-                if (so + i >= 0 && so + i < (int64_t)len) d[i] = (char)(x >> (8 * i));
+            uint32_t r = lo;
+            for (int i = 0; i < 4; i++) {
+                const uint64_t q = b + i;
+                if (q < O0 || q >= O1) continue;
+                while (q >= s_off[r + 1]) r++;
+                d[i] = text[s_src[r] + (q - s_off[r])];
+            }
         }
     }
 }
@@ -1497,9 +1513,8 @@ int norm_extract(tk_norm *nm, const tk_reads *const *sets, uint32_t nsets) {
                                                                               fq->d_name_off, n, o, base[q], nm->d_ext);
             } else {
                 const bool vec = ((uintptr_t)fq->d_text & 3) == 0;
-                k_extract_copy<<<nm_grid(n * 32), NM_THREADS, 0, c->stream>>>(fq->d_text, fq->text_len, vec,
-                                                                               fq->d_name_off, n, o, base[q],
-                                                                               nm->d_ext);
+                k_extract_copy<<<(unsigned)((n + EX_RECS - 1) / EX_RECS), NM_THREADS, 0, c->stream>>>(
+                    fq->d_text, fq->text_len, vec, fq->d_name_off, n, o, base[q], nm->d_ext);
             }
             c->launches++;
             TK_TRY(check_launch(c, "extract copy"));
