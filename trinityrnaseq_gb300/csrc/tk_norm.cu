@@ -977,12 +977,13 @@ __global__ void k_extract_missing(const uint64_t *__restrict__ acc_off, uint64_t
 }
 
 // A block per EX_RECS consecutive records: the block's output is one
-// contiguous byte range, written as aligned 4-byte words by consecutive
-// threads (coalesced); the record holding a word is found by a binary search
-// over the block's record offsets in shared memory.  A word inside one record
-// takes two aligned source loads and a funnel shift; a word across a record
-// boundary, or shared with a neighbouring block, is written byte by byte
-// (only the block's own bytes).
+// contiguous byte range, written in aligned 16-byte chunks by consecutive
+// threads (coalesced); the record holding a chunk is found by a binary search
+// over the block's record offsets in shared memory.  A chunk inside one
+// record takes five aligned 4-byte source loads and four funnel shifts and
+// leaves as one 16-byte store; a chunk across a record boundary, or shared
+// with a neighbouring block, is written byte by byte (only the block's own
+// bytes).
 constexpr int EX_RECS = 256;
 
 __global__ void __launch_bounds__(NM_THREADS) k_extract_copy(const char *__restrict__ text, uint64_t text_len, bool vec,
@@ -1000,32 +1001,32 @@ __global__ void __launch_bounds__(NM_THREADS) k_extract_copy(const char *__restr
     __syncthreads();
     const uint64_t O0 = s_off[0], O1 = s_off[m];
     if (O1 == O0) return;
-    const uint64_t w0 = O0 >> 2, w1 = (O1 + 3) >> 2;
-    for (uint64_t w = w0 + threadIdx.x; w < w1; w += blockDim.x) {
-        const uint64_t b = 4 * w;   // the word's first output byte
+    const uint64_t c0 = O0 >> 4, c1 = (O1 + 15) >> 4;
+    for (uint64_t cidx = c0 + threadIdx.x; cidx < c1; cidx += blockDim.x) {
+        const uint64_t b = 16 * cidx;   // the chunk's first output byte
         // the last record whose output starts at or before max(b, O0)
         const uint64_t key = b < O0 ? O0 : b;
-        uint32_t lo = 0, hi = m;    // s_off[lo] <= key < s_off[hi]
+        uint32_t lo = 0, hi = m;        // s_off[lo] <= key < s_off[hi]
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
             if (s_off[mid] <= key) lo = mid;
             else hi = mid;
         }
         char *d = out + b;
-        if (b >= O0 && b + 4 <= s_off[lo + 1]) {
-            const uint64_t a = s_src[lo] + (b - s_off[lo]);
-            uint32_t x;
-            if (vec && (a & ~3ULL) + 8 <= text_len) {
-                const uint32_t *p = reinterpret_cast<const uint32_t *>(text + (a & ~3ULL));
-                x = __funnelshift_r(__ldg(p), __ldg(p + 1), 8u * (uint32_t)(a & 3));
-            } else {
-                x = 0;
-                for (int i = 0; i < 4; i++) x |= (uint32_t)(uint8_t)text[a + i] << (8 * i);
-            }
-            *reinterpret_cast<uint32_t *>(d) = x;
+        const uint64_t a = s_src[lo] + (b - s_off[lo]);   // source of byte b when b lies in record lo
+        if (b >= O0 && b + 16 <= s_off[lo + 1] && vec && (a & ~3ULL) + 20 <= text_len) {
+            const uint32_t *p = reinterpret_cast<const uint32_t *>(text + (a & ~3ULL));
+            const uint32_t sh = 8u * (uint32_t)(a & 3);
+            const uint32_t x0 = __ldg(p), x1 = __ldg(p + 1), x2 = __ldg(p + 2), x3 = __ldg(p + 3), x4 = __ldg(p + 4);
+            uint4 v;
+            v.x = __funnelshift_r(x0, x1, sh);
+            v.y = __funnelshift_r(x1, x2, sh);
+            v.z = __funnelshift_r(x2, x3, sh);
+            v.w = __funnelshift_r(x3, x4, sh);
+            *reinterpret_cast<uint4 *>(d) = v;
         } else {
             uint32_t r = lo;
-            for (int i = 0; i < 4; i++) {
+            for (int i = 0; i < 16; i++) {
                 const uint64_t q = b + i;
                 if (q < O0 || q >= O1) continue;
                 while (q >= s_off[r + 1]) r++;
