@@ -657,8 +657,6 @@ __global__ void k_norm_accs(RowArgs a, SNames L, const uint64_t *__restrict__ ac
 
 // ---------------------------------------------------------------- table text
 
-__device__ __forceinline__ uint32_t stats_sfx_len(const NormVal &v) { return v.sfx_len; }
-
 __device__ char *put_stats_fields(char *o, const NormVal &v) {
     o = put_dec(o, v.med);
     *o++ = '\t';
