@@ -228,6 +228,59 @@ __device__ __forceinline__ uint32_t line_word(const ParseGeom &g, uint64_t S, in
     return x;
 }
 
+// The warp copies the lines its lanes hold (lane l: text[src, src + len) to
+// seq + dst; len 0 = none), four lines at a time, one aligned 4-byte output
+// word per lane and line, all loads in flight before any store; upper-cases
+// and notes whether a line held whitespace.
+__device__ __forceinline__ void copy_group(const ParseGeom &g, uint64_t src, uint64_t dst, uint32_t len,
+                                           uint8_t *__restrict__ seq, bool &ws) {
+    const unsigned lane = lane_id();
+    unsigned todo = __ballot_sync(0xffffffffu, len > 0);
+    while (todo) {
+        uint64_t s0[4], d0[4];
+        uint32_t n[4], nw[4], wmax = 0;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int l = todo ? __ffs(todo) - 1 : 0;
+            const bool have = todo != 0;
+            todo &= todo - 1;
+            s0[b] = __shfl_sync(0xffffffffu, src, l);
+            d0[b] = __shfl_sync(0xffffffffu, dst, l);
+            n[b] = have ? __shfl_sync(0xffffffffu, len, l) : 0u;
+            nw[b] = n[b] ? (uint32_t)(((d0[b] + n[b] + 3) >> 2) - (d0[b] >> 2)) : 0u;
+            wmax = max(wmax, nw[b]);
+        }
+        for (uint32_t w0 = 0; w0 < wmax; w0 += 32) {
+            const uint32_t w = w0 + lane;
+            uint32_t x[4];
+#pragma unroll
+            for (int b = 0; b < 4; b++)
+                x[b] = w < nw[b] ? line_word(g, s0[b], (int64_t)4 * w - (int64_t)(d0[b] & 3), n[b]) : 0x41414141u;
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                if (w >= nw[b]) continue;
+                const int64_t so = (int64_t)4 * w - (int64_t)(d0[b] & 3);   // line offset of the word's first byte
+                const uint32_t t = x[b] & 0x7F7F7F7Fu;
+                // bit 7 of each byte that is a-z, then of each byte that is ' ' or 9..13
+                const uint32_t lower = (t + 0x1F1F1F1Fu) & ~(t + 0x05050505u) & ~x[b] & 0x80808080u;
+                const uint32_t sp = x[b] ^ 0x20202020u;
+                const uint32_t zsp = ~(((sp & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | sp) & 0x80808080u;
+                const uint32_t rng = (t + 0x77777777u) & ~(t + 0x72727272u) & ~x[b] & 0x80808080u;
+                ws |= (zsp | rng) != 0u;
+                const uint32_t up = x[b] ^ (lower >> 2);
+                uint8_t *o = seq + (d0[b] & ~3ULL) + 4ull * w;
+                if (so >= 0 && so + 4 <= (int64_t)n[b]) {
+                    *reinterpret_cast<uint32_t *>(o) = up;
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        if (so + i >= 0 && so + i < (int64_t)n[b]) o[i] = (uint8_t)(up >> (8 * i));
+                }
+            }
+        }
+    }
+}
+
 __global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end, const uint8_t *__restrict__ kind,
                              const uint64_t *__restrict__ line_rec, const uint64_t *__restrict__ line_out,
                              uint64_t n_lines, uint8_t *__restrict__ seq, uint64_t *__restrict__ rd_off,
@@ -252,52 +305,47 @@ __global__ void k_copy_lines(ParseGeom g, const uint64_t *__restrict__ line_end,
                 }
             }
         }
-        unsigned todo = __ballot_sync(0xffffffffu, len > 0);
-        while (todo) {
-            // four lines at a time, one aligned 4-byte output word per lane and
-            // line: all loads are in flight before any store
-            uint64_t s0[4], d0[4];
-            uint32_t n[4], nw[4], wmax = 0;
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                const int l = todo ? __ffs(todo) - 1 : 0;
-                const bool have = todo != 0;
-                todo &= todo - 1;
-                s0[b] = __shfl_sync(0xffffffffu, src, l);
-                d0[b] = __shfl_sync(0xffffffffu, dst, l);
-                n[b] = have ? __shfl_sync(0xffffffffu, len, l) : 0u;
-                nw[b] = n[b] ? (uint32_t)(((d0[b] + n[b] + 3) >> 2) - (d0[b] >> 2)) : 0u;
-                wmax = max(wmax, nw[b]);
-            }
-            for (uint32_t w0 = 0; w0 < wmax; w0 += 32) {
-                const uint32_t w = w0 + lane;
-                uint32_t x[4];
-#pragma unroll
-                for (int b = 0; b < 4; b++)
-                    x[b] = w < nw[b] ? line_word(g, s0[b], (int64_t)4 * w - (int64_t)(d0[b] & 3), n[b]) : 0x41414141u;
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    if (w >= nw[b]) continue;
-                    const int64_t so = (int64_t)4 * w - (int64_t)(d0[b] & 3);   // line offset of the word's first byte
-                    const uint32_t t = x[b] & 0x7F7F7F7Fu;
-                    // bit 7 of each byte that is a-z, then of each byte that is ' ' or 9..13
-                    const uint32_t lower = (t + 0x1F1F1F1Fu) & ~(t + 0x05050505u) & ~x[b] & 0x80808080u;
-                    const uint32_t sp = x[b] ^ 0x20202020u;
-                    const uint32_t zsp = ~(((sp & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | sp) & 0x80808080u;
-                    const uint32_t rng = (t + 0x77777777u) & ~(t + 0x72727272u) & ~x[b] & 0x80808080u;
-                    ws |= (zsp | rng) != 0u;
-                    const uint32_t up = x[b] ^ (lower >> 2);
-                    uint8_t *o = seq + (d0[b] & ~3ULL) + 4ull * w;
-                    if (so >= 0 && so + 4 <= (int64_t)n[b]) {
-                        *reinterpret_cast<uint32_t *>(o) = up;
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < 4; i++)
-                            if (so + i >= 0 && so + i < (int64_t)n[b]) o[i] = (uint8_t)(up >> (8 * i));
-                    }
-                }
-            }
+        copy_group(g, src, dst, len, seq, ws);
+    }
+    if (__any_sync(0xffffffffu, ws) && lane == 0) atomicExch(ws_seen, 1u);
+}
+
+// ---- FASTQ: records of four lines, handled per record (no per-line arrays).
+// Check: the header line starts with '@' and the third with '+' (the first
+// offending line is recorded, as k_line_kinds does); seq_len = the sequence
+// line's length.
+__global__ void k_fq_check(ParseGeom g, const uint64_t *__restrict__ line_end, uint64_t n_reads,
+                           uint32_t *__restrict__ seq_len, uint32_t *__restrict__ err) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_reads) return;
+    const uint64_t j = 4 * r;
+    const uint64_t h0 = j == 0 ? g.S : line_end[j - 1] + 1, h1 = line_end[j];
+    const uint64_t p0 = line_end[j + 1] + 1, p1 = line_end[j + 2];
+    const uint32_t fh = h1 > h0 ? (uint8_t)g.text[h0] : 0u, fp = p1 > p0 ? (uint8_t)g.text[p0] : 0u;
+    if (fh != '@') { atomicExch(&err[DE_PARSE], 1u); atomicMin(&err[DE_PARSE + 1], (uint32_t)(j + 1)); }
+    if (fp != '+') { atomicExch(&err[DE_PARSE], 1u); atomicMin(&err[DE_PARSE + 1], (uint32_t)(j + 3)); }
+    seq_len[r] = (uint32_t)(line_end[j + 1] - (h1 + 1));
+}
+
+// A warp takes 32 consecutive records: lane l records read r0 + l's start and
+// holds its sequence line, then the warp copies them as k_copy_lines does.
+__global__ void k_fq_copy(ParseGeom g, const uint64_t *__restrict__ line_end, const uint64_t *__restrict__ seq_off,
+                          uint64_t n_reads, uint8_t *__restrict__ seq, uint64_t *__restrict__ rd_off,
+                          uint32_t *__restrict__ ws_seen) {
+    const unsigned lane = lane_id();
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    bool ws = false;
+    for (uint64_t r0 = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; r0 < n_reads; r0 += warps * 32) {
+        const uint64_t r = r0 + lane;
+        uint64_t src = 0, dst = 0;
+        uint32_t len = 0;
+        if (r < n_reads) {
+            src = line_end[4 * r] + 1;
+            len = (uint32_t)(line_end[4 * r + 1] - src);
+            dst = seq_off[r] + r;
+            rd_off[r] = dst;
         }
+        copy_group(g, src, dst, len, seq, ws);
     }
     if (__any_sync(0xffffffffu, ws) && lane == 0) atomicExch(ws_seen, 1u);
 }
@@ -400,20 +448,25 @@ __global__ void k_emit(ParseGeom g, const uint64_t *__restrict__ tile_line0, con
 }
 
 // ---- N: accession and read length per record
-__global__ void k_names(ParseGeom g, const uint64_t *__restrict__ hdr_line, const uint64_t *__restrict__ line_end,
-                        uint64_t n_reads, const uint64_t *__restrict__ rd_off, uint64_t *__restrict__ name_off,
-                        uint32_t *__restrict__ name_len, uint32_t *__restrict__ max_len) {
-    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n_reads) return;
-    uint64_t j = hdr_line[r];
-    uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
-    uint64_t le = line_end[j];
-    uint64_t s = ls + 1, q = s;
-    while (q < le && !is_ws((uint8_t)g.text[q])) q++;
-    name_off[r] = s;
-    name_len[r] = (uint32_t)(q - s);
-    uint64_t L = rd_off[r + 1] - rd_off[r] - 1;
-    atomicMax(max_len, (uint32_t)(L > 0xFFFFFFFFull ? 0xFFFFFFFFull : L));
+__global__ void k_names(ParseGeom g, const uint64_t *__restrict__ hdr_line, int fastq,
+                        const uint64_t *__restrict__ line_end, uint64_t n_reads, const uint64_t *__restrict__ rd_off,
+                        uint64_t *__restrict__ name_off, uint32_t *__restrict__ name_len, uint32_t *__restrict__ max_len) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t L32 = 0;
+    if (r < n_reads) {
+        const uint64_t j = fastq ? 4 * r : hdr_line[r];   // FASTQ: the header is line 4r
+        const uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
+        const uint64_t le = line_end[j];
+        uint64_t s = ls + 1, q = s;
+        while (q < le && !is_ws((uint8_t)g.text[q])) q++;
+        name_off[r] = s;
+        name_len[r] = (uint32_t)(q - s);
+        const uint64_t L = rd_off[r + 1] - rd_off[r] - 1;
+        L32 = (uint32_t)(L > 0xFFFFFFFFull ? 0xFFFFFFFFull : L);
+    }
+    // one atomic per warp (the longest read of its 32)
+    L32 = __reduce_max_sync(0xffffffffu, L32);
+    if (lane_id() == 0 && L32) atomicMax(max_len, L32);
 }
 
 // The packed read array as 2-bit codes and invalid-position bits: thread j
@@ -519,25 +572,35 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
             e = set_err(c, TK_E_PARSE, "FASTQ input: " + std::to_string(n_lines) + " lines is not a multiple of 4");
             break;
         }
+        if ((e = cuda_check(c, cudaMemsetAsync(c->d_err, 0, DE_COUNT * 4, c->stream), "err reset"))) break;
+        uint32_t big = 0xFFFFFFFFu;
+        cudaMemcpyAsync(c->d_err + DE_PARSE + 1, &big, 4, cudaMemcpyHostToDevice, c->stream);
+        uint32_t herr[2] = {0, 0};
+        if (fastq) {
+            // 4-line records, handled per record: checks and sequence lengths,
+            // their scan gives every read's place in seq
+            n_reads = n_lines / 4;
+            if ((e = alloc((void **)&line_len, n_reads * 4, "sequence lengths"))) break;
+            k_fq_check<<<grid_for(n_reads, 256), 256, 0, c->stream>>>(g, line_end, n_reads, line_len, c->d_err);
+            c->launches++;
+            if ((e = cuda_check(c, cudaMemcpyAsync(herr, c->d_err + DE_PARSE, 8, cudaMemcpyDeviceToHost, c->stream), "err d2h"))) break;
+            if ((e = alloc((void **)&line_out, (n_reads + 1) * 8, "sequence offsets"))) break;
+            if ((e = scan_excl_u32_to_u64(c, line_len, line_out, n_reads, &n_emit))) break;   // syncs
+            if (herr[0]) {
+                e = set_err(c, TK_E_PARSE, "FASTQ input: malformed record at line " + std::to_string(herr[1]));
+                break;
+            }
+            break;
+        }
         if ((e = alloc((void **)&kind, n_lines, "line kinds"))) break;
         if ((e = alloc((void **)&is_hdr, n_lines * 4, "header flags"))) break;
         if ((e = alloc((void **)&line_rec, n_lines * 8, "line records"))) break;
         if ((e = alloc((void **)&line_len, n_lines * 4, "line lengths"))) break;
-        if ((e = cuda_check(c, cudaMemsetAsync(c->d_err, 0, DE_COUNT * 4, c->stream), "err reset"))) break;
-        uint32_t big = 0xFFFFFFFFu;
-        cudaMemcpyAsync(c->d_err + DE_PARSE + 1, &big, 4, cudaMemcpyHostToDevice, c->stream);
         k_line_kinds<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(g, line_end, n_lines, fastq, kind, is_hdr, line_len,
                                                                      c->d_err);
         c->launches++;
-        uint32_t herr[2] = {0, 0};
         if ((e = cuda_check(c, cudaMemcpyAsync(herr, c->d_err + DE_PARSE, 8, cudaMemcpyDeviceToHost, c->stream), "err d2h"))) break;
-        if (fastq) {
-            // 4-line records: record j >> 2, header line 4r, no scan needed
-            n_reads = n_lines / 4;
-            if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
-            k_fastq_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(line_rec, n_lines, hdr_line);
-            c->launches++;
-        } else {
+        {
             if ((e = scan_excl_u32_to_u64(c, is_hdr, line_rec, n_lines, &n_reads))) break;  // syncs
             if ((e = alloc((void **)&hdr_line, (n_reads + 1) * 8, "header lines"))) break;
             k_line_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(is_hdr, line_rec, n_lines, hdr_line, line_len);
@@ -572,9 +635,17 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
         uint32_t ws_seen = 0;
         if (n_tiles && n_reads) {
             cudaMemsetAsync(c->d_err + DE_WS, 0, 4, c->stream);
-            const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n_lines + 7) / 8, (uint64_t)c->sm_count * 32));
-            k_copy_lines<<<grid, 256, 0, c->stream>>>(g, line_end, kind, line_rec, line_out, n_lines, r->d_seq, r->d_rd_off,
-                                                      c->d_err + DE_WS);
+            if (fastq) {
+                const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n_reads + 255) / 256,
+                                                                                       (uint64_t)c->sm_count * 32));
+                k_fq_copy<<<grid, 256, 0, c->stream>>>(g, line_end, line_out, n_reads, r->d_seq, r->d_rd_off,
+                                                       c->d_err + DE_WS);
+            } else {
+                const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n_lines + 7) / 8,
+                                                                                       (uint64_t)c->sm_count * 32));
+                k_copy_lines<<<grid, 256, 0, c->stream>>>(g, line_end, kind, line_rec, line_out, n_lines, r->d_seq,
+                                                          r->d_rd_off, c->d_err + DE_WS);
+            }
             c->launches++;
             e = cuda_check(c, cudaMemcpyAsync(&ws_seen, c->d_err + DE_WS, 4, cudaMemcpyDeviceToHost, c->stream), "ws flag");
             if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "copy sync");
@@ -582,6 +653,20 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
         if (!e && ws_seen) {
             // some sequence line holds spaces, tabs or CRs: redo the emit byte by byte
             do {
+                if (fastq) {
+                    // the byte-wise emit works from the per-line arrays
+                    if ((e = alloc((void **)&kind, n_lines, "line kinds"))) break;
+                    if ((e = alloc((void **)&is_hdr, n_lines * 4, "header flags"))) break;
+                    if ((e = alloc((void **)&line_rec, n_lines * 8, "line records"))) break;
+                    uint32_t *ll = nullptr;
+                    uint64_t *hl = nullptr;
+                    if ((e = alloc((void **)&ll, n_lines * 4, "line lengths"))) break;
+                    if ((e = alloc((void **)&hl, (n_reads + 1) * 8, "header lines"))) break;
+                    k_line_kinds<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(g, line_end, n_lines, fastq, kind, is_hdr,
+                                                                                 ll, c->d_err);
+                    k_fastq_records<<<grid_for(n_lines, 256), 256, 0, c->stream>>>(line_rec, n_lines, hl);
+                    c->launches += 2;
+                }
                 if ((e = alloc((void **)&tile_em, n_tiles * 4, "tile emits"))) break;
                 if ((e = alloc((void **)&tile_emit0, (n_tiles + 1) * 8, "tile emit offsets"))) break;
                 k_tile_emits<<<(unsigned)n_tiles, PT_THREADS, 0, c->stream>>>(g, tile_line0, kind, line_rec, n_lines, tile_em);
@@ -598,7 +683,7 @@ int parse_reads(tk_ctx *c, tk_reads *r) {
             } while (0);
         }
         if (!e && n_tiles && n_reads) {
-            k_names<<<grid_for(n_reads, 256), 256, 0, c->stream>>>(g, hdr_line, line_end, n_reads, r->d_rd_off,
+            k_names<<<grid_for(n_reads, 256), 256, 0, c->stream>>>(g, hdr_line, fastq, line_end, n_reads, r->d_rd_off,
                                                                    r->d_name_off, r->d_name_len, d_maxlen);
             c->launches++;
         }
