@@ -13,8 +13,14 @@
 //           srand(12345); rows with median < min_cov, mean <= 0 or
 //           stdev/mean > max_CV are dropped, every other row draws rand(1)
 //           and is kept when the draw is <= max_cov / median;
-//   extract make_normalized_reads_file (insilico:470-584): the FASTQ records
-//           whose core names were kept, verbatim, in input order.
+//   extract make_normalized_reads_file (insilico:470-584): the records whose
+//           core names were kept, in input order -- FASTQ records verbatim,
+//           FASTA records as PerlLib/Fasta_reader.pm prints them; a side may
+//           be several read sets (files or pieces), and every kept name must
+//           be found in one of them.
+//
+// A side's reads may come from several read sets; names are addressed by
+// their device address throughout the selection.
 //
 // No text table exists on the device.  Each read's "%g" fields are carried as
 // (6 significant digits, decimal exponent), computed exactly from the float
