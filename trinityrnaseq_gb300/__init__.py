@@ -2,7 +2,9 @@
 
 Drop-in replacements for the three native tools Trinity drives on this path
 -- ``jellyfish count/histo/dump`` (canonical k=25 counting), Inchworm's
-``fastaToKmerCoverageStats`` and Chrysalis' ``ReadsToTranscripts`` -- built on
+``fastaToKmerCoverageStats`` and Chrysalis' ``ReadsToTranscripts`` -- and for
+the steps around them (``seqtk-trinity`` read prep, the in-silico
+normalization's sort / pair merge / selection / extraction), built on
 hand-written sm_103a CUDA kernels behind the C ABI in ``include/trinkmer.h``.
 """
 from .kmer import (Context, KmerTable, Normalization, ReadSet, ReadsToTranscripts, coverage_stats, format_histo,
