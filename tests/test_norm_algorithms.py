@@ -1,10 +1,12 @@
-"""The integer algorithms of csrc/tk_norm.cu, restated in Python and checked on
-the CPU against what they stand in for: printf's "%g" and "%.1f" (the
-decimal digits of a float, rounded half to even on its binary value, and the
-double Perl reads back from that text), the speculative chunked two-cursor
-merge of nbkc_merge_left_right_stats.pl against the plain sequential walk,
-and drand48's jump-ahead against stepping it draw by draw.  The GPU parity
-tests (tests/test_gpu_norm.py) check the CUDA code itself."""
+"""The integer algorithms of csrc/tk_norm.cu and csrc/tk_parse.cu, restated in
+Python and checked on the CPU against what they stand in for: printf's "%g"
+and "%.1f" (the decimal digits of a float, rounded half to even on its binary
+value, and the double Perl reads back from that text), the speculative
+chunked two-cursor merge of nbkc_merge_left_right_stats.pl against the plain
+sequential walk, drand48's jump-ahead against stepping it draw by draw, and
+the word-wise byte movement of the parse and the extraction against plain
+copies.  The GPU parity tests (tests/test_gpu_norm.py, test_gpu_count.py,
+test_gpu_prep.py) check the CUDA code itself."""
 import bisect
 import math
 import random
@@ -223,3 +225,112 @@ def test_drand48_jump_ahead():
         x = (a * x + c) & mask
         assert jump(x0, k) == x
     assert math.isclose(jump(x0, 1) / 2 ** 48, 0.22532851279629895, rel_tol=0, abs_tol=0)
+
+
+# ---- byte-movement algorithms of the parse and the extraction
+
+M32 = 0xFFFFFFFF
+
+
+def _fold_and_ws(x):
+    """tk_parse.cu copy_group: 4 bytes upper-cased, and whether any is
+    whitespace (' ' or 9..13), with SIMD bit tricks on one 32-bit word."""
+    t = x & 0x7F7F7F7F
+    lower = ((t + 0x1F1F1F1F) & M32) & (~((t + 0x05050505) & M32) & M32) & (~x & M32) & 0x80808080
+    sp = x ^ 0x20202020
+    zsp = (~((((sp & 0x7F7F7F7F) + 0x7F7F7F7F) & M32) | sp) & M32) & 0x80808080
+    rng = ((t + 0x77777777) & M32) & (~((t + 0x72727272) & M32) & M32) & (~x & M32) & 0x80808080
+    return x ^ (lower >> 2), (zsp | rng) != 0
+
+
+def test_simd_case_fold_and_whitespace():
+    rnd = random.Random(11)
+    cases = [[c, f, f, f] for c in range(256) for f in (0x41, 0x00, 0xFF, 0x20, 0x61)]
+    cases += [[rnd.randrange(256) for _ in range(4)] for _ in range(50000)]
+    for bs in cases:
+        x = sum(b << (8 * i) for i, b in enumerate(bs))
+        up, ws = _fold_and_ws(x)
+        assert up == sum((b - 32 if 97 <= b <= 122 else b) << (8 * i) for i, b in enumerate(bs))
+        assert ws == any(b == 32 or 9 <= b <= 13 for b in bs)
+
+
+def test_word_copy_of_lines():
+    """Aligned 4-byte output words per line, source words by funnel shift,
+    partial words at the line's ends byte by byte (line_word / copy_group)."""
+    rnd = random.Random(3)
+    for _ in range(2000):
+        L = rnd.randint(1, 400)
+        text = bytes(rnd.choice(b"acgtACGTN") for _ in range(L))
+        S = rnd.randrange(0, L)
+        n = rnd.randint(1, L - S)
+        d0 = rnd.randrange(0, 50)
+        out = bytearray(d0 + n + 8)
+        want = bytearray(out)
+        want[d0:d0 + n] = text[S:S + n].upper()
+        for w in range(((d0 + n + 3) >> 2) - (d0 >> 2)):
+            so = 4 * w - (d0 & 3)
+            a = S + so
+            if a >= 0 and (a & ~3) + 8 <= L:
+                bs = list(text[a & ~3:(a & ~3) + 8][a & 3:(a & 3) + 4])
+            else:
+                bs = [text[S + so + i] if 0 <= so + i < n else 0x41 for i in range(4)]
+            bs = [bs[i] if 0 <= so + i < n else 0x41 for i in range(4)]
+            up, _ = _fold_and_ws(sum(b << (8 * i) for i, b in enumerate(bs)))
+            o = (d0 & ~3) + 4 * w
+            for i in range(4):
+                if 0 <= so + i < n:
+                    out[o + i] = (up >> (8 * i)) & 0xFF
+        assert out == want
+
+
+def test_chunked_record_copy():
+    """tk_norm.cu k_extract_copy: a block's records as aligned 16-byte
+    chunks, the holding record by binary search, boundary chunks byte by byte."""
+    rnd = random.Random(9)
+    EX = 256
+    for _ in range(150):
+        n = rnd.randint(1, 900)
+        lens = [rnd.randint(1, 60) for _ in range(n)]
+        pos = rnd.randint(0, 7)
+        text = bytearray(rnd.getrandbits(8) for _ in range(pos))
+        name_off = []
+        for ln in lens:
+            name_off.append(pos + 1)
+            text += bytes(rnd.getrandbits(8) for _ in range(ln))
+            pos += ln
+        text += bytes(rnd.getrandbits(8) for _ in range(rnd.randint(0, 30)))
+        rec = [ln if rnd.random() < 0.6 else 0 for ln in lens]
+        off = [0]
+        for ln in rec:
+            off.append(off[-1] + ln)
+        base = rnd.randint(0, 40)
+        out = bytearray(b"\xee" * (base + off[-1] + 64))
+        want = bytearray(out)
+        for i in range(n):
+            want[base + off[i]:base + off[i] + rec[i]] = text[name_off[i] - 1:name_off[i] - 1 + rec[i]]
+        for blk in range((n + EX - 1) // EX):
+            r0 = blk * EX
+            m = min(n - r0, EX)
+            s_off = [base + off[r0 + i] for i in range(m + 1)]
+            s_src = [name_off[r0 + i] - 1 for i in range(m)]
+            O0, O1 = s_off[0], s_off[m]
+            for cidx in range(O0 >> 4, (O1 + 15) >> 4) if O1 > O0 else ():
+                b = 16 * cidx
+                key = max(b, O0)
+                lo, hi = 0, m
+                while hi - lo > 1:
+                    mid = (lo + hi) >> 1
+                    lo, hi = (mid, hi) if s_off[mid] <= key else (lo, mid)
+                a = s_src[lo] + (b - s_off[lo])
+                if b >= O0 and b + 16 <= s_off[lo + 1] and (a & ~3) + 20 <= len(text):
+                    out[b:b + 16] = text[a:a + 16]
+                else:
+                    r = lo
+                    for i in range(16):
+                        q = b + i
+                        if q < O0 or q >= O1:
+                            continue
+                        while q >= s_off[r + 1]:
+                            r += 1
+                        out[q] = text[s_src[r] + (q - s_off[r])]
+        assert out == want
