@@ -46,6 +46,7 @@ MIN_COUNT = 2           # the catalogue fastaToKmerCoverageStats reads (util/ins
 L2_BYTES = 129 * 2**20
 E2E_PIECES = 2          # record-aligned pieces per mate file on the end-to-end path
 NORM_ARGS = (200, 1, 10000)   # normalization: Trinity's --max_cov 200 --min_cov 1 --max_CV 10000
+COV_DRAM_BYTES_PER_LOOKUP = (4.189716e9 + 0.044003e9) / 38.0e6   # ncu, k_coverage at 500K pairs
 
 
 def log(*a):
@@ -351,6 +352,14 @@ def run_gpu(args, dist, world, rank, local):
                                        packed + 8.0 * windows, 0, None, None),
         }
         kernels["insert"]["random_access"]["l2_slice_ceiling_per_s"] = ceil_slice
+        # DRAM traffic of the coverage kernel: bytes per lookup from one ncu
+        # capture of the same kernel on 500K pairs (38.0M lookups into a 512 MB
+        # table: 4.190 GB read + 0.044 GB written), times this run's lookups
+        # per launch (random 16-byte loads fetch whole DRAM bursts)
+        cov_launches = max(per_step["coverage"][1], 1)
+        kernels["coverage"]["traffic"] = COV_DRAM_BYTES_PER_LOOKUP * windows / cov_launches
+        kernels["coverage"]["traffic_source"] = ("scaled from an ncu capture of k_coverage at 500K pairs: "
+                                                 f"{COV_DRAM_BYTES_PER_LOOKUP:.0f} DRAM bytes per lookup")
         top = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
         out = {
             "metric": METRIC, "value": tot_windows / t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
