@@ -181,8 +181,10 @@ class GpuPipeline:
             self.out["dump_host"] = None
             self.out["ext_host"] = None
 
-    def step(self, e2e: bool):
-        """One plain pipeline pass; returns (windows, reads, h2d_bytes, d2h_bytes)."""
+    def step(self, e2e: bool, capture: dict = None):
+        """One plain pipeline pass; returns (windows, reads, h2d_bytes, d2h_bytes).
+        With `capture` (end to end only) the pass's outputs are copied into it:
+        histo, dump text, both mates' statistics, accs text, extracted records."""
         kmer, t = self.kmer, self.torch
         ctx = self.ctx
         if e2e:
@@ -204,6 +206,9 @@ class GpuPipeline:
         table.add_many(left_sets + right_sets)
         hist = table.histo(1, 10000)
         dump_len = table.dump_fasta_len(MIN_COUNT)
+        if capture is not None:
+            capture["histo"] = hist.copy()
+            capture["distinct"] = table.info(distinct=True)[0]
         n_left = sum(r.n_reads for r in left_sets)
         n_right = sum(r.n_reads for r in right_sets)
         self._alloc_out(n_left, n_right)
@@ -234,6 +239,8 @@ class GpuPipeline:
         nm = kmer.Normalization(ctx, left_sets, tuple(b.data_ptr() for b in self.out["l_dev"]), right_sets,
                                 tuple(b.data_ptr() for b in self.out["r_dev"]), *NORM_ARGS, device=True)
         selected = nm.counts["selected"]
+        if capture is not None:
+            capture["accs"] = nm.accs()
         ext = 0
         for group in (left_sets, right_sets):
             if e2e:
@@ -241,7 +248,8 @@ class GpuPipeline:
                     self.out["ext_host"] = t.empty(int(1.2 * (self.h_left.numel() + self.h_right.numel())) + 16,
                                                    dtype=t.uint8).pin_memory()
                 h = self.out["ext_host"]   # a mate's records never exceed the mate's text
-                n = nm.extract_into(group, h.data_ptr() + ext, h.numel() - ext)
+                # the left mate's records go down while the right mate's are extracted
+                n = nm.extract_into(group, h.data_ptr() + ext, h.numel() - ext, overlap=True)
             else:
                 n = nm.extract_into(group)
             ext += n
@@ -250,6 +258,11 @@ class GpuPipeline:
         if e2e:
             d2h += ext
             ctx.synchronize()
+            if capture is not None:
+                capture["dump"] = self.out["dump_host"].numpy()[:dump_len].copy()
+                for side, n in (("l", n_left), ("r", n_right)):
+                    capture[side + "_stats"] = [h.numpy()[:n].copy() for h in self.out[side + "_host"]]
+                capture["records"] = self.out["ext_host"].numpy()[:ext].copy()
         reads = n_left + n_right
         packed = sum(r.n_bases + r.n_reads for r in left_sets + right_sets)
         for r in left_sets + right_sets:
@@ -297,8 +310,8 @@ def run_gpu(args, dist, world, rank, local):
     ms, res = timed(pipe, stream, args.steps, False, dist)
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
-    prof = {k: ctx.profile(k) for k in ("parse", "hll", "scatter", "count", "compact", "sort", "dump", "coverage",
-                                         "norm", "extract")}
+    prof = {k: ctx.profile(k) for k in ("parse", "hll", "scatter", "count", "compact", "sort", "dump", "cov_cache",
+                                         "coverage", "norm", "extract")}
     ctx.set_profiling(False)
     # end-to-end timed region (host FASTQ in, dump text + stats out)
     ms_e2e, res_e2e = timed(pipe, stream, args.steps, True, dist)
@@ -390,6 +403,8 @@ def run_gpu(args, dist, world, rank, local):
         }
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args)
+        if args.parity and world == 1:
+            out["parity_full"] = parity_full(pipe, left, right)
         del pipe
         if args.prep and world == 1:
             out["prep"] = prep_bench(ctx, left, args)
@@ -397,6 +412,8 @@ def run_gpu(args, dist, world, rank, local):
             out["normalize"] = norm_bench(ctx, left, right, args)
         if args.r2t and world == 1:
             out["r2t"] = r2t_bench(ctx, args)
+        if args.dbg and world == 1:
+            out["debruijn"] = dbg_bench(ctx, args)
         if args.bins and world == 1:
             out["batched"] = batched_bench(ctx, args)
         if args.jobs and world == 1:
@@ -694,6 +711,68 @@ def r2t_bench(ctx, args):
             "bit_exact_vs_oracle_sample": same}
 
 
+# ---------------------------------------------------------------- de Bruijn graphs
+
+def dbg_bench(ctx, args):
+    """Per-record de Bruijn graphs of the Inchworm bundle (FastaToDeBruijn
+    --graph_per_record -K 24, Trinity:2298-2302) on the read-to-component
+    bundle (100,000 contigs in 30,000 components): device = bundle resident in
+    HBM, graph text left there; e2e = host bundle in, host text out.  The oracle
+    runs the same over the whole bundle with all host threads, and its text is
+    compared with the GPU's byte for byte."""
+    import hashlib
+    import torch
+    from trinityrnaseq_gb300 import synth
+    from trinityrnaseq_gb300.kmer import DeBruijnGraphs
+    from oracle import oracle as O
+    bundle, _ = synth.bundle_reads(seed=SEED + 11, n_contigs=R2T_CONTIGS, contig_median=400.0,
+                                   n_components=R2T_COMPONENTS, max_per_component=40, n_pairs=1)
+    dev = torch.device(f"cuda:{ctx.device}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    h_b = torch.from_numpy(bundle).pin_memory()
+    d_b = h_b.to(dev)
+    torch.cuda.synchronize()
+    g = DeBruijnGraphs(ctx, d_b.data_ptr(), 24, False, length=d_b.numel(), device=True)
+    n_nodes, n_comp, n_text = g.n_nodes, g.n_components, g.text_len
+    g.free()
+    d_out = torch.empty(n_text + 16, dtype=torch.uint8, device=dev)
+    h_out = torch.empty(n_text + 16, dtype=torch.uint8).pin_memory()
+    windows = 0
+    res = {}
+    for mode in ("device", "e2e"):
+        def step():
+            if mode == "device":
+                z = DeBruijnGraphs(ctx, d_b.data_ptr(), 24, False, length=d_b.numel(), device=True)
+                z.text_into(d_out.data_ptr(), d_out.numel(), device=True)
+            else:
+                z = DeBruijnGraphs(ctx, h_b.numpy(), 24, False)
+                z.text_into(h_out.data_ptr(), h_out.numel())
+            z.free()
+        for _ in range(args.warmup):
+            step()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for _ in range(args.steps):
+                step()
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        s = ev[0].elapsed_time(ev[1]) / 1e3 / args.steps
+        res[mode] = {"ms": s * 1e3, "bundle_mb_per_s": bundle.nbytes / s / 1e6}
+    got = h_out.numpy()[:n_text].tobytes()
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    want = O.debruijn(bundle, 24, False, threads)
+    cpu_s = time.time() - t0
+    return {"workload": f"{R2T_CONTIGS} contigs in {R2T_COMPONENTS} components ({bundle.nbytes / 1e6:.0f} MB bundle): "
+                        f"{n_comp} graphs, {n_nodes} node lines, {n_text / 1e6:.0f} MB text; -K 24, both strands",
+            "nodes": n_nodes, "components": n_comp, **res,
+            "cpu": {"ms": cpu_s * 1e3, "cores": threads, "kind": "port",
+                    "sample": "the whole bundle; the oracle's restatement (C, OpenMP over records)"},
+            "bit_exact_vs_oracle": got == want, "text_sha256": hashlib.sha256(got).hexdigest()}
+
+
 # ---------------------------------------------------------------- batched and served
 
 def batched_bench(ctx, args):
@@ -898,6 +977,65 @@ def cpu_baseline(args):
                       "(sort, merge, selection, extraction)"}
 
 
+def parity_full(pipe, left, right):
+    """Bit-exact check of one whole plain-path step at its full size, outside
+    every timed region: the GPU step's outputs (end to end, host buffers)
+    against the oracle run over all the pairs on the host cores -- the sorted
+    -L 2 dump text, the histogram, both mates' median/mean/stdev, the accs
+    text of the selection and the extracted records of both mates
+    (util/insilico_read_normalization.pl:588-985 with Trinity's --max_cov 200
+    --min_cov 1 --max_CV 10000, Trinity:3426-3449).  The catalogue the
+    statistics look up is the oracle's own -L 2 pairs (what the dump text
+    loads to)."""
+    import hashlib
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    got = {}
+    pipe.step(True, capture=got)
+    sha = lambda b: hashlib.sha256(memoryview(b)).hexdigest()
+    t0 = time.time()
+    both = np.concatenate([left, right])
+    keys, counts = O.count(both, K, True, threads, sorted_=False, distinct_hint=int(got["distinct"]))
+    del both
+    t_count = time.time() - t0
+    ok = {}
+    ok["histo"] = bool(np.array_equal(O.histo(counts, 1, 10000), got["histo"]))
+    keep = counts >= MIN_COUNT
+    k2, c2 = keys[keep], counts[keep]
+    del keys, counts, keep
+    order = np.argsort(k2, kind="stable")
+    k2, c2 = k2[order], c2[order]
+    del order
+    dump = O.dump(k2, c2, K, MIN_COUNT)
+    ok["dump"] = sha(dump) == sha(got["dump"])
+    n_dump = int(k2.size)
+    del dump
+    stats_ok, tables = True, []
+    for side, text in (("l", left), ("r", right)):
+        m, a, sd = O.cov_values(text, k2, c2, K, True, threads)
+        g = got[side + "_stats"]
+        stats_ok &= bool(np.array_equal(m, g[0].view(np.uint32)) and
+                         np.array_equal(a.view(np.uint32), g[1].view(np.uint32)) and
+                         np.array_equal(sd.view(np.uint32), g[2].view(np.uint32)))
+        tables.append(O.cov_stats(text, k2, c2, K, True, False, threads))
+    ok["stats"] = stats_ok
+    del k2, c2
+    _, accs, cnt = O.norm(tables[0], tables[1], *NORM_ARGS)
+    del tables
+    ok["accs"] = accs == got["accs"]
+    h = hashlib.sha256()
+    for text in (left, right):
+        h.update(O.norm_extract(text, accs))
+    ok["records"] = h.hexdigest() == sha(got["records"])
+    return {**ok, "pairs": int(got["l_stats"][0].size), "dump_kmers": n_dump, "selected": int(cnt[1]),
+            "records_sha256": h.hexdigest(), "oracle_s": round(time.time() - t0, 1),
+            "oracle_count_s": round(t_count, 1), "oracle_threads": threads,
+            "what": "one end-to-end step's host outputs vs the oracle over all pairs: sorted -L 2 dump text, "
+                    "histo 1..10001, median/mean/stdev of both mates (float bits), accs text, extracted records"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -936,10 +1074,13 @@ def main():
     ap.add_argument("--pairs", type=int, default=FULL_PAIRS)
     ap.add_argument("--cpu-pairs", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--parity", type=int, default=1,
+                    help="full-size bit-exact check of one step against the oracle, untimed (0 = skip)")
     ap.add_argument("--prep", type=int, default=1, help="FASTQ->FASTA read prep leg (0 = skip)")
     ap.add_argument("--norm", type=int, default=1, help="normalization-tail leg (0 = skip)")
     ap.add_argument("--r2t", type=int, default=1, help="read -> component leg (0 = skip)")
     ap.add_argument("--r2t_pairs", type=int, default=50_000_000, help="read pairs of the read -> component leg")
+    ap.add_argument("--dbg", type=int, default=1, help="per-component de Bruijn graph leg (0 = skip)")
     ap.add_argument("--bins", type=int, default=5000, help="batched-bins comparison (0 = skip)")
     ap.add_argument("--jobs", type=int, default=200, help="served-stream comparison (0 = skip)")
     ap.add_argument("--job-max-reads", type=int, default=2_000_000)

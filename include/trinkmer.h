@@ -62,7 +62,9 @@ extern "C" {
 #define TK_KID_SCATTER 11     /* k-mers into hash-partition buckets (count pass 1) */
 #define TK_KID_NORM 12        /* normalization: name sort, pair merge, selection */
 #define TK_KID_EXTRACT 13     /* normalization: selected FASTQ records */
-#define TK_KID_NUM 14         /* number of kernel classes */
+#define TK_KID_COV_CACHE 14   /* coverage: the L2-resident cache of the most frequent k-mers */
+#define TK_KID_DBG 15         /* per-record de Bruijn graphs of a bundle */
+#define TK_KID_NUM 16         /* number of kernel classes */
 
 typedef struct tk_ctx tk_ctx;
 typedef struct tk_reads tk_reads;
@@ -250,6 +252,30 @@ int tk_r2t_assign(tk_r2t *r2t, const tk_reads *reads, int where, int32_t *rec,
                   uint32_t *hits, uint32_t *nwin);
 void tk_r2t_free(tk_r2t *r2t);
 
+/* ------------------------------------------------------------- de Bruijn graphs
+ * Replaces Inchworm's `FastaToDeBruijn --fasta bundled_iworm_contigs.fasta
+ * -K (k-1) --graph_per_record [--SS]` (Trinity:2298-2302), whose output
+ * util/support_scripts/partition_chrysalis_graphs_n_reads.pl cuts into one
+ * graph file per component.  Per bundle record (format as for
+ * tk_r2t_create) that has at least one window of K+1 A/C/G/T bases:
+ * "Component <id>\n" (id as tk_r2t_component_ids), then one line per
+ * distinct (K+1)-mer of the record in order of first occurrence,
+ * "<node>\t<prev>\t<count>\t<kmer>\n": node = 0, 1, ... in that order;
+ * prev = the node of the window just before the first occurrence, -1 when
+ * that is not a window of K+1 A/C/G/T (contig start, 'X' join); count =
+ * occurrences in the record, a (K+1)-mer and its reverse complement counted
+ * as one node unless `strand`; kmer = the first occurrence, upper case.
+ * The header line and one line per k-mer are what the partition script reads
+ * (partition_chrysalis_graphs_n_reads.pl:166-208); the node line's columns
+ * are this library's (the tool's source is not in the reference).  K is
+ * 1..30. */
+typedef struct tk_dbg tk_dbg;
+int tk_dbg_create(tk_ctx *ctx, const char *bundle, uint64_t len, int where, int K, int strand, tk_dbg **out);
+/* components written (records with a window), nodes (= node lines), text bytes */
+int tk_dbg_info(const tk_dbg *dbg, uint64_t *n_components, uint64_t *n_nodes, uint64_t *text_len);
+int tk_dbg_text(const tk_dbg *dbg, int where, char *out, uint64_t cap);
+void tk_dbg_free(tk_dbg *dbg);
+
 /* ------------------------------------------------------------- normalization
  * Replaces what util/insilico_read_normalization.pl does with the coverage
  * statistics of the reads (Trinity:3421-3479 runs it with --pairs_together for
@@ -314,6 +340,14 @@ int tk_norm_extract(tk_norm *norm, const tk_reads *fastq, uint64_t *len);
  * (make_normalized_reads_file reads all files of a side, insilico:502-545). */
 int tk_norm_extract_multi(tk_norm *norm, const tk_reads *const *sets, uint32_t n_sets, uint64_t *len);
 int tk_norm_extract_copy(const tk_norm *norm, int where, char *out, uint64_t cap);
+/* tk_norm_extract_copy into host memory without waiting: the extracted text
+ * is copied to `out` on the context's copy stream while later work on the
+ * context runs (e.g. the other side's tk_norm_extract).  `out` (page-locked
+ * for the copy to overlap) holds the text once tk_ctx_synchronize returns; a
+ * later extraction or tk_norm_free waits for the copy before it reuses the
+ * device text.  No counterpart in the reference (make_normalized_reads_file
+ * writes each side's file in turn, insilico:470-584). */
+int tk_norm_extract_copy_async(tk_norm *norm, char *out, uint64_t cap);
 void tk_norm_free(tk_norm *norm);
 
 /* ------------------------------------------------------------- batched bins

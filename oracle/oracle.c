@@ -47,6 +47,22 @@
  *     with no vote, shorter than k, or pct < -p is not written.
  *  D5 the component id is the integer after "s_" in the bundle header; a header
  *     without it takes its record ordinal.
+ *  D8 FastaToDeBruijn --graph_per_record -K K (Trinity:2298-2302): per bundle
+ *     record with at least one window of K+1 A/C/G/T bases, a line
+ *     "Component <id>" (id as D5) and then one line per distinct (K+1)-mer of
+ *     the record (canonical unless --SS), in order of first occurrence:
+ *     "<node>\t<prev>\t<count>\t<kmer>" -- node = 0, 1, ... in that order,
+ *     prev = the node of the window just before the first occurrence (-1 when
+ *     that window is not a valid (K+1)-mer: a record or contig start, an 'X'
+ *     join or another non-ACGT byte), count = occurrences in the record (both
+ *     strands unless --SS), kmer = the first occurrence as written, upper case.
+ *     Pinned: the "Component <id>" line starting each record and one line per
+ *     k-mer (partition_chrysalis_graphs_n_reads.pl:166-208 counts the lines
+ *     after each header as the component's k-mers, num_kmers + 24 vs the
+ *     minimum contig length at :73); a component without k-mers is left out
+ *     because that reader stops at the first empty one.  The node line's
+ *     columns are this restatement's choice (the consumers QuantifyGraph and
+ *     Butterfly are not in the reference checkout).
  */
 #include "oracle.h"
 
@@ -61,6 +77,7 @@
 #define ORC_E_INVAL (-1)
 #define ORC_E_OOM (-3)
 #define ORC_E_PARSE (-4)
+#define ORC_E_FULL (-5)
 
 static const uint64_t EMPTY = ~0ULL;
 
@@ -246,9 +263,11 @@ static int ctab_init(ctab_t *t, uint64_t want, uint32_t init_val) {
 
 static void ctab_free(ctab_t *t) { free(t->keys); free(t->vals); t->keys = NULL; t->vals = NULL; }
 
+/* The key's slot, claimed if new; CTAB_FULL when every slot holds another key. */
+#define CTAB_FULL (~0ULL)
 static uint64_t ctab_slot(ctab_t *t, uint64_t key) {
     uint64_t s = mix64(key) & t->mask;
-    for (;;) {
+    for (uint64_t probe = 0; probe <= t->mask; probe++) {
         uint64_t cur = __atomic_load_n(&t->keys[s], __ATOMIC_ACQUIRE);
         if (cur == key) return s;
         if (cur == EMPTY) {
@@ -260,6 +279,7 @@ static uint64_t ctab_slot(ctab_t *t, uint64_t key) {
         }
         s = (s + 1) & t->mask;
     }
+    return CTAB_FULL;
 }
 
 static int ctab_find(const ctab_t *t, uint64_t key, uint32_t *val) {
@@ -308,6 +328,11 @@ static int extract_table(ctab_t *t, int sorted, uint64_t **keys, uint32_t **coun
 
 int orc_count(const char *text, size_t len, int k, int canonical, int threads,
               int sorted, uint64_t **keys, uint32_t **counts, uint64_t *n) {
+    return orc_count_sized(text, len, k, canonical, threads, sorted, 0, keys, counts, n);
+}
+
+int orc_count_sized(const char *text, size_t len, int k, int canonical, int threads, int sorted,
+                    uint64_t distinct_hint, uint64_t **keys, uint32_t **counts, uint64_t *n) {
     if (k < 1 || k > 31 || !keys || !counts || !n) return ORC_E_INVAL;
     set_threads(threads);
     recs_t r;
@@ -317,17 +342,20 @@ int orc_count(const char *text, size_t len, int k, int canonical, int threads,
     for (size_t i = 0; i < r.n; i++)
         if (r.seq_len[i] >= (uint32_t)k) windows += r.seq_len[i] - k + 1;
     ctab_t t;
-    e = ctab_init(&t, windows + windows / 2 + 16, 0);
+    e = ctab_init(&t, distinct_hint ? 2 * distinct_hint + 16 : windows + windows / 2 + 16, 0);
     if (e) { recs_free(&r); return e; }
+    int full = 0;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < (int64_t)r.n; i++) {
         const char *s = r.seqbuf + r.seq_off[i];
         FOR_EACH_KMER(s, r.seq_len[i], k, canonical, key, w, {
             uint64_t slot = ctab_slot(&t, key);
-            __atomic_fetch_add(&t.vals[slot], 1u, __ATOMIC_RELAXED);
+            if (slot == CTAB_FULL) __atomic_store_n(&full, 1, __ATOMIC_RELAXED);
+            else __atomic_fetch_add(&t.vals[slot], 1u, __ATOMIC_RELAXED);
         });
     }
     recs_free(&r);
+    if (full) { ctab_free(&t); return ORC_E_FULL; }
     e = extract_table(&t, sorted, keys, counts, n);
     ctab_free(&t);
     return e;
@@ -718,6 +746,95 @@ int orc_r2t(const char *reads, size_t rlen, const char *bundle, size_t blen,
     if (!err) err = concat_chunks(chunks, nchunks, "", out, out_len);
     for (int c = 0; c < nchunks; c++) free(chunks[c].b);
     free(chunks);
+    return err;
+}
+
+/* ---------------------------------------------------------------- de Bruijn (D8) */
+
+typedef struct { uint64_t *key; uint32_t *node; uint64_t mask; } dmap_t;
+
+static uint32_t dmap_get(dmap_t *m, uint64_t key, uint32_t fresh, int *is_new) {
+    uint64_t s = mix64(key) & m->mask;
+    for (;;) {
+        if (m->key[s] == EMPTY) { m->key[s] = key; m->node[s] = fresh; *is_new = 1; return fresh; }
+        if (m->key[s] == key) { *is_new = 0; return m->node[s]; }
+        s = (s + 1) & m->mask;
+    }
+}
+
+/* one record's graph text appended to sb */
+static int dbg_record(const char *seq, uint32_t L, int K1, int ss, uint64_t comp, sbuf_t *sb) {
+    if (L < (uint32_t)K1) return 0;
+    uint64_t nw = L - K1 + 1, cap = 1024;
+    while (cap < 2 * nw) cap <<= 1;
+    dmap_t m = {malloc(cap * 8), malloc(cap * 4), cap - 1};
+    uint32_t *cnt = malloc(nw * 4), *first = malloc(nw * 4);
+    int32_t *prev = malloc(nw * 4);
+    if (!m.key || !m.node || !cnt || !first || !prev) {
+        free(m.key); free(m.node); free(cnt); free(first); free(prev);
+        return ORC_E_OOM;
+    }
+    for (uint64_t i = 0; i < cap; i++) m.key[i] = EMPTY;
+    uint32_t n = 0;
+    int64_t last_w = -2;
+    uint32_t last_node = 0;
+    FOR_EACH_KMER(seq, L, K1, !ss, key, w, {
+        int is_new;
+        uint32_t v = dmap_get(&m, key, n, &is_new);
+        if (is_new) {
+            cnt[n] = 0;
+            first[n] = (uint32_t)w;
+            prev[n] = last_w == (int64_t)w - 1 ? (int32_t)last_node : -1;
+            n++;
+        }
+        cnt[v]++;
+        last_w = (int64_t)w;
+        last_node = v;
+    });
+    int e = 0;
+    if (n) {
+        if (sb_reserve(sb, 32 + (size_t)n * (K1 + 40))) e = ORC_E_OOM;
+        else {
+            sb->n += (size_t)sprintf(sb->b + sb->n, "Component %llu\n", (unsigned long long)comp);
+            for (uint32_t i = 0; i < n; i++) {
+                sb->n += (size_t)sprintf(sb->b + sb->n, "%u\t%d\t%u\t", i, prev[i], cnt[i]);
+                for (int j = 0; j < K1; j++) {
+                    char ch = seq[first[i] + j];
+                    sb->b[sb->n++] = (ch >= 'a' && ch <= 'z') ? (char)(ch - 32) : ch;
+                }
+                sb->b[sb->n++] = '\n';
+            }
+        }
+    }
+    free(m.key); free(m.node); free(cnt); free(first); free(prev);
+    return e;
+}
+
+int orc_debruijn(const char *bundle, size_t blen, int K, int ss, int threads, char **out, size_t *out_len) {
+    if (K < 1 || K > 30) return ORC_E_INVAL;
+    set_threads(threads);
+    recs_t b;
+    int e = parse_records(bundle, blen, &b);
+    if (e) return e;
+    sbuf_t *chunks = calloc(b.n ? b.n : 1, sizeof(sbuf_t));
+    if (!chunks) { recs_free(&b); return ORC_E_OOM; }
+    int err = 0;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < (int64_t)b.n; i++) {
+        const char *h = bundle + b.acc_off[i];
+        uint32_t hl = b.acc_len[i];
+        uint64_t id = (uint64_t)i;
+        if (hl > 2 && h[0] == 's' && h[1] == '_' && h[2] >= '0' && h[2] <= '9') {
+            id = 0;
+            for (uint32_t j = 2; j < hl && h[j] >= '0' && h[j] <= '9'; j++) id = id * 10 + (uint64_t)(h[j] - '0');
+        }
+        int ee = dbg_record(b.seqbuf + b.seq_off[i], b.seq_len[i], K + 1, ss, id, &chunks[i]);
+        if (ee) err = ee;
+    }
+    if (!err) err = concat_chunks(chunks, (int)b.n, "", out, out_len);
+    for (size_t i = 0; i < b.n; i++) free(chunks[i].b);
+    free(chunks);
+    recs_free(&b);
     return err;
 }
 

@@ -37,6 +37,10 @@ extern "C" {
  * sorted != 0, else in hash-table order.  Returns 0 or a negative error. */
 int orc_count(const char *text, size_t len, int k, int canonical, int threads,
               int sorted, uint64_t **keys, uint32_t **counts, uint64_t *n);
+/* orc_count with its table sized for about distinct_hint distinct k-mers
+ * (0: for as many as there are windows); -5 when the hint was too small. */
+int orc_count_sized(const char *text, size_t len, int k, int canonical, int threads, int sorted,
+                    uint64_t distinct_hint, uint64_t **keys, uint32_t **counts, uint64_t *n);
 
 /* jellyfish histo --low low --high high: hist[0] = counts < low,
  * hist[1 + c - low] for low <= c <= high, hist[high - low + 2] = counts > high. */
@@ -105,6 +109,11 @@ int orc_norm_extract(const char *fq, size_t len, const char *accs, size_t alen, 
                      uint64_t *missing);
 
 void orc_free(void *p);
+
+/* FastaToDeBruijn --graph_per_record -K K [--SS] text (decision D8 in
+ * oracle.c): per bundle record "Component <id>" and one line per distinct
+ * (K+1)-mer in order of first occurrence. */
+int orc_debruijn(const char *bundle, size_t blen, int K, int ss, int threads, char **out, size_t *out_len);
 
 #ifdef __cplusplus
 }

@@ -33,6 +33,7 @@ def load() -> C.CDLL:
     lib = C.CDLL(str(LIB))
     vp, u64, P = C.c_void_p, C.c_uint64, C.POINTER
     lib.orc_count.argtypes = [vp, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int, P(vp), P(vp), P(u64)]
+    lib.orc_count_sized.argtypes = [vp, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int, u64, P(vp), P(vp), P(u64)]
     lib.orc_fastq_to_fasta.argtypes = [vp, C.c_size_t, C.c_int, C.c_int, P(vp), P(C.c_size_t), P(u64)]
     lib.orc_histo.argtypes = [vp, u64, u64, u64, vp]
     lib.orc_histo.restype = None
@@ -47,6 +48,7 @@ def load() -> C.CDLL:
     lib.orc_r2t_values.argtypes = [vp, C.c_size_t, vp, C.c_size_t, C.c_int, C.c_int, C.c_int, P(u64), P(vp),
                                    P(vp), P(vp)]
     lib.orc_records.argtypes = [vp, C.c_size_t, P(vp), P(C.c_size_t)]
+    lib.orc_debruijn.argtypes = [vp, C.c_size_t, C.c_int, C.c_int, C.c_int, P(vp), P(C.c_size_t)]
     lib.orc_norm.argtypes = [vp, C.c_size_t, vp, C.c_size_t, C.c_int, C.c_int, C.c_int, P(vp), P(C.c_size_t), P(vp),
                              P(C.c_size_t), P(u64)]
     lib.orc_norm_extract.argtypes = [vp, C.c_size_t, vp, C.c_size_t, P(vp), P(C.c_size_t), P(u64)]
@@ -54,6 +56,15 @@ def load() -> C.CDLL:
     lib.orc_free.restype = None
     _lib = lib
     return lib
+
+
+def _buf(text):
+    """(pointer, length) of a bytes object or a contiguous uint8 numpy array,
+    so that large texts reach the library without a copy."""
+    if isinstance(text, np.ndarray):
+        a = np.ascontiguousarray(text).view(np.uint8)
+        return C.c_void_p(a.ctypes.data if a.size else None), a.size
+    return text, len(text)
 
 
 def _chk(st: int, what: str) -> None:
@@ -67,7 +78,7 @@ def _take(ptr: C.c_void_p, n: int, dtype) -> np.ndarray:
         lib.orc_free(ptr)
         return np.zeros(0, dtype=dtype)
     nbytes = n * np.dtype(dtype).itemsize
-    a = np.frombuffer(C.string_at(ptr, nbytes), dtype=dtype).copy()
+    a = np.ctypeslib.as_array((C.c_uint8 * nbytes).from_address(ptr.value)).view(dtype).copy()
     lib.orc_free(ptr)
     return a
 
@@ -116,7 +127,8 @@ def norm_extract(fastq: bytes, accs: bytes) -> bytes:
     malformed record (ValueError(0))."""
     lib = load()
     p, n, miss = C.c_void_p(), C.c_size_t(), C.c_uint64()
-    st = lib.orc_norm_extract(fastq, len(fastq), accs, len(accs), C.byref(p), C.byref(n), C.byref(miss))
+    fp, fl = _buf(fastq)
+    st = lib.orc_norm_extract(fp, fl, accs, len(accs), C.byref(p), C.byref(n), C.byref(miss))
     if st == -4:
         raise ValueError(miss.value)
     _chk(st, "norm_extract")
@@ -131,12 +143,20 @@ def records(text: bytes) -> bytes:
     return _take_bytes(p, n.value)
 
 
-def count(text: bytes, k: int = 25, canonical: bool = True, threads: int = 0, sorted_: bool = True):
-    """(keys, counts) of every k-mer, sorted by key (jellyfish count)."""
+def count(text, k: int = 25, canonical: bool = True, threads: int = 0, sorted_: bool = True,
+          distinct_hint: int = 0):
+    """(keys, counts) of every k-mer, sorted by key (jellyfish count).  With
+    distinct_hint the table is sized for about that many distinct k-mers
+    (retried at full size when it was too small)."""
     lib = load()
     kp, cp, n = C.c_void_p(), C.c_void_p(), C.c_uint64()
-    _chk(lib.orc_count(text, len(text), k, int(canonical), threads, int(sorted_), C.byref(kp), C.byref(cp),
-                       C.byref(n)), "count")
+    p, ln = _buf(text)
+    st = lib.orc_count_sized(p, ln, k, int(canonical), threads, int(sorted_), distinct_hint, C.byref(kp),
+                             C.byref(cp), C.byref(n))
+    if st == -5 and distinct_hint:
+        st = lib.orc_count_sized(p, ln, k, int(canonical), threads, int(sorted_), 0, C.byref(kp), C.byref(cp),
+                                 C.byref(n))
+    _chk(st, "count")
     return _take(kp, n.value, np.uint64), _take(cp, n.value, np.uint32)
 
 
@@ -170,7 +190,8 @@ def cov_stats(reads: bytes, keys, counts, k: int = 25, ds: bool = True, capture:
     kk = np.ascontiguousarray(keys, dtype=np.uint64)
     cc = np.ascontiguousarray(counts, dtype=np.uint32)
     p, n = C.c_void_p(), C.c_size_t()
-    _chk(lib.orc_cov_stats(reads, len(reads), kk.ctypes.data, cc.ctypes.data, kk.size, k, int(ds), int(capture),
+    rp, rl = _buf(reads)
+    _chk(lib.orc_cov_stats(rp, rl, kk.ctypes.data, cc.ctypes.data, kk.size, k, int(ds), int(capture),
                            threads, C.byref(p), C.byref(n)), "cov_stats")
     return _take_bytes(p, n.value)
 
@@ -180,7 +201,8 @@ def cov_values(reads: bytes, keys, counts, k: int = 25, ds: bool = True, threads
     kk = np.ascontiguousarray(keys, dtype=np.uint64)
     cc = np.ascontiguousarray(counts, dtype=np.uint32)
     nr, mp, ap, sp = C.c_uint64(), C.c_void_p(), C.c_void_p(), C.c_void_p()
-    _chk(lib.orc_cov_values(reads, len(reads), kk.ctypes.data, cc.ctypes.data, kk.size, k, int(ds), threads,
+    rp, rl = _buf(reads)
+    _chk(lib.orc_cov_values(rp, rl, kk.ctypes.data, cc.ctypes.data, kk.size, k, int(ds), threads,
                             C.byref(nr), C.byref(mp), C.byref(ap), C.byref(sp)), "cov_values")
     n = nr.value
     return _take(mp, n, np.uint32), _take(ap, n, np.float32), _take(sp, n, np.float32)
@@ -201,3 +223,12 @@ def r2t_values(reads: bytes, bundle: bytes, k: int = 25, strand: bool = False, t
                             C.byref(rp), C.byref(hp), C.byref(wp)), "r2t_values")
     n = nr.value
     return _take(rp, n, np.int32), _take(hp, n, np.uint32), _take(wp, n, np.uint32)
+
+
+def debruijn(bundle, K: int = 24, ss: bool = False, threads: int = 0) -> bytes:
+    """FastaToDeBruijn --graph_per_record -K K [--SS] output (decision D8)."""
+    lib = load()
+    p, n = C.c_void_p(), C.c_size_t()
+    bp, bl = _buf(bundle)
+    _chk(lib.orc_debruijn(bp, bl, K, int(ss), threads, C.byref(p), C.byref(n)), "debruijn")
+    return _take_bytes(p, n.value)

@@ -46,6 +46,13 @@ What each fixture pins:
   r2t.bundle.fa r2t.reads.fa small bundle and reads
   r2t.out.sort               the oracle's readsToComponents rows through
                              `sort -k1,1n -k3,3nr -k2,2` under LC_ALL=C (Trinity:2258)
+  r2t.bundle.deBruijn.gz     the oracle's FastaToDeBruijn --graph_per_record -K 24
+                             text of r2t.bundle.fa (decision D8)
+  r2t.bundle.deBruijn.partitions
+                             what util/support_scripts/partition_chrysalis_graphs_n_reads.pl
+                             (-N 1000 -L 100) makes of that text and r2t.out.sort:
+                             per listed component, its id and the line counts of
+                             the graph and reads files it wrote
 """
 import gzip
 import os
@@ -349,9 +356,36 @@ def make_norm(ref: Path) -> None:
     rs.unlink()
 
 
+def make_debruijn(ref: Path) -> None:
+    """The de Bruijn text of the small bundle, and the reference's partition
+    script run on it (Trinity:2319-2323)."""
+    import shutil
+    import tempfile
+    text = O.debruijn((HERE / "r2t.bundle.fa").read_bytes(), 24, False)
+    (HERE / "r2t.bundle.deBruijn.gz").write_bytes(gzip.compress(text, mtime=0))
+    with tempfile.TemporaryDirectory() as tmp:
+        t = Path(tmp)
+        (t / "bundle.deBruijn").write_bytes(text)
+        shutil.copy(HERE / "r2t.out.sort", t / "readsToComponents.out.sort")
+        perl(ref, "util/support_scripts/partition_chrysalis_graphs_n_reads.pl", "--deBruijns",
+             t / "bundle.deBruijn", "--componentReads", t / "readsToComponents.out.sort", "-N", 1000, "-L", 100)
+        rows = []
+        for line in (t / "component_base_listing.txt").read_text().splitlines():
+            comp, base = line.split("\t")
+            g = Path(base + ".graph.tmp").read_bytes().count(b"\n")
+            r = Path(base + ".reads.tmp").read_bytes().count(b"\n")
+            rows.append(f"{comp}\t{g}\t{r}\n")
+        (HERE / "r2t.bundle.deBruijn.partitions").write_text("".join(rows))
+
+
 def main() -> None:
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit(__doc__)
+    ref = Path(sys.argv[1])
     HERE.mkdir(exist_ok=True)
+    if len(sys.argv) > 2 and sys.argv[2] == "--debruijn-only":
+        make_debruijn(ref)
+        return
     if len(sys.argv) > 2 and sys.argv[2] == "--prep-only":
         make_prep(ref)
         return
@@ -400,6 +434,7 @@ def main() -> None:
     srt = subprocess.run(["sort", "-k1,1n", "-k3,3nr", "-k2,2"], input=rows, stdout=subprocess.PIPE, check=True,
                          env=dict(os.environ, LC_ALL="C")).stdout
     (HERE / "r2t.out.sort").write_bytes(srt)
+    make_debruijn(ref)
     print("fixtures written to", HERE)
 
 

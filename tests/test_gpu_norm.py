@@ -226,3 +226,24 @@ def test_sides_in_pieces_select_like_whole_sides(ctx, oracle):
     # one piece alone lacks records of selected names: an error, as for a short file
     with pytest.raises(native.TrinkmerError):
         nm2.extract(pieces[0][0])
+
+
+def test_extract_copy_async_overlaps_the_next_extraction(ctx):
+    """tk_norm_extract_copy_async: one side's records go down on the copy
+    stream while the other side's are extracted; both land intact."""
+    torch = pytest.importorskip("torch")
+    left, right = synth.gene_pairs(seed=33, n_genes=300, n_pairs=30000, fastq=True)
+    sides = [ReadSet(ctx, x.tobytes()) for x in (left, right)]
+    fas = [ReadSet(ctx, r.to_fasta(a, if_missing=True)) for r, a in zip(sides, (1, 2))]
+    t = KmerTable(ctx, 25, True)
+    t.add_many(fas)
+    st = [coverage_stats(t, r) for r in fas]
+    nm = Normalization(ctx, fas[0], st[0], fas[1], st[1], 20, 1, 10000)
+    want = [nm.extract(r) for r in sides]
+    assert all(len(w) > 0 for w in want)
+    bufs = [torch.zeros(len(w) + 16, dtype=torch.uint8).pin_memory() for w in want]
+    lens = [nm.extract_into(r, b.data_ptr(), b.numel(), overlap=True) for r, b in zip(sides, bufs)]
+    ctx.synchronize()
+    for b, n, w in zip(bufs, lens, want):
+        assert b.numpy()[:n].tobytes() == w
+    nm.free()

@@ -177,3 +177,35 @@ def test_norm_extract_fasta_matches_reference(oracle, golden):
     with pytest.raises(ValueError) as e:
         oracle.norm_extract(fa, (golden / "norm.pairs.c5.accs").read_bytes())
     assert str(e.value) == "1"
+
+
+def test_debruijn_text_is_what_the_partition_script_read(oracle, golden):
+    """The oracle's FastaToDeBruijn text of the small bundle is the one the
+    reference's partition_chrysalis_graphs_n_reads.pl was run on: per
+    component it wrote, a graph file of the header plus one line per k-mer."""
+    import gzip
+    text = oracle.debruijn((golden / "r2t.bundle.fa").read_bytes(), 24, False)
+    assert text == gzip.decompress((golden / "r2t.bundle.deBruijn.gz").read_bytes())
+    lines = {}
+    comp = None
+    for line in text.split(b"\n")[:-1]:
+        if line.startswith(b"Component"):
+            comp = int(line.split()[1])
+            lines[comp] = 0
+        else:
+            assert len(line.split(b"\t")) == 4
+            lines[comp] += 1
+    for row in (golden / "r2t.bundle.deBruijn.partitions").read_text().splitlines():
+        c, g, _ = map(int, row.split("\t"))
+        assert g == 1 + lines[c]
+
+
+def test_debruijn_small_cases(oracle):
+    # 'X' joins and non-ACGT bytes break windows; a record with no window is
+    # left out; canonical nodes count both strands
+    text = oracle.debruijn(b">s_5\nACGTACGTAAXCCC\n>s_6\nAC\n>x\nacgtNacgta\n", 4, False)
+    assert text == (b"Component 5\n0\t-1\t3\tACGTA\n1\t0\t2\tCGTAC\n2\t0\t1\tCGTAA\n"
+                    b"Component 2\n0\t-1\t1\tACGTA\n")
+    ss = oracle.debruijn(b">s_5\nACGTACGTAAXCCC\n", 4, True)
+    assert ss == b"Component 5\n0\t-1\t2\tACGTA\n1\t0\t1\tCGTAC\n2\t1\t1\tGTACG\n3\t2\t1\tTACGT\n4\t0\t1\tCGTAA\n"
+    assert oracle.debruijn(b"", 24, False) == b""

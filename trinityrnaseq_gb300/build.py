@@ -28,7 +28,7 @@ BIN = PKG / "bin"
 INCLUDE = ROOT / "include"
 
 CUDA_SOURCES = ["tk_api.cu", "tk_scan.cu", "tk_parse.cu", "tk_table.cu", "tk_cov.cu", "tk_r2t.cu", "tk_bins.cu", "tk_server.cu",
-                "tk_fasta.cu", "tk_norm.cu"]
+                "tk_fasta.cu", "tk_norm.cu", "tk_dbg.cu"]
 TOOL_SOURCES = {
     "jellyfish": ["jellyfish.cpp"],
     "fastaToKmerCoverageStats": ["fastaToKmerCoverageStats.cpp"],
@@ -36,6 +36,7 @@ TOOL_SOURCES = {
     "trinkmerd": ["trinkmerd.cpp"],
     "seqtk-trinity": ["seqtk_trinity.cpp"],
     "insilico_read_normalization": ["insilico_read_normalization.cpp"],
+    "FastaToDeBruijn": ["FastaToDeBruijn.cpp"],
 }
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -265,6 +265,12 @@ static void dump_invalidate(tk_table *t) {
     t->dump_valid = false;
 }
 
+// the table's contents change: its dump text and coverage cache are stale
+static void table_changed(tk_table *t) {
+    dump_invalidate(t);
+    t->hot_valid = false;
+}
+
 }  // namespace tk
 
 using namespace tk;
@@ -725,7 +731,7 @@ int tk_table_add_reads(tk_table *t, const tk_reads *r) {
     tk_ctx *c = t->ctx;
     CHECK_CTX(c);
     if (r->ctx != c) return set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
-    dump_invalidate(t);
+    table_changed(t);
     return table_count_seq(t, r);
 }
 
@@ -737,7 +743,7 @@ int tk_table_add_reads_multi(tk_table *t, const tk_reads *const *sets, uint32_t 
         if (!sets[i]) return set_err(c, TK_E_INVAL, "tk_table_add_reads_multi: null read set");
         if (sets[i]->ctx != c) return set_err(c, TK_E_INVAL, "read set and table belong to different contexts");
     }
-    dump_invalidate(t);
+    table_changed(t);
     return table_count_many(t, sets, (int)n_sets);
 }
 
@@ -852,7 +858,7 @@ int tk_table_load_pairs(tk_table *t, const uint64_t *keys, const uint32_t *count
     tk_ctx *c = t->ctx;
     CHECK_CTX(c);
     if (n == 0) return TK_OK;
-    dump_invalidate(t);
+    table_changed(t);
     void *dk = nullptr, *dc = nullptr;
     bool ok_k = false, ok_c = false;
     int e = stage_in(c, keys, n * 8, where, &dk, &ok_k);
@@ -871,7 +877,7 @@ int tk_table_load_dump_fasta(tk_table *t, const char *text, uint64_t len, int wh
     TK_TRY(tk_reads_parse(c, text, len, where, &r));
     int e = TK_OK;
     if (r->format == TK_FMT_FASTQ) e = set_err(c, TK_E_PARSE, "k-mer catalogue must be FASTA ('>COUNT' headers)");
-    dump_invalidate(t);
+    table_changed(t);
     if (!e) e = table_load_dump_reads(t, r);
     tk_reads_free(r);
     return e;
@@ -885,6 +891,7 @@ void tk_table_free(tk_table *t) {
     dfree(c, t->d_ovf);
     dfree(c, t->d_counters);
     dfree(c, t->d_hll);
+    dfree(c, t->d_hot);
     dump_invalidate(t);
     delete t;
     ctx_release(c);
@@ -921,6 +928,34 @@ int tk_coverage_stats(tk_table *t, const tk_reads *r, int where, uint32_t *media
 
 // ------------------------------------------------------------------ R2T
 
+// Component id of every bundle record: the integer after "s_" in its
+// accession, else the record ordinal.
+static int bundle_component_ids(tk_ctx *c, const tk_reads *b, const char *bundle, uint64_t len, int where,
+                                std::vector<uint64_t> *ids) {
+    ids->assign(b->n_reads, 0);
+    std::vector<uint64_t> off(b->n_reads);
+    std::vector<uint32_t> nl(b->n_reads);
+    TK_TRY(tk_reads_names(b, off.data(), nl.data()));
+    std::vector<char> host_text;
+    const char *ht = bundle;
+    if (where == TK_DEVICE) {
+        host_text.resize(len);
+        TK_CUDA(c, cudaMemcpy(host_text.data(), bundle, len, cudaMemcpyDeviceToHost));
+        ht = host_text.data();
+    }
+    for (uint64_t i = 0; i < b->n_reads; i++) {
+        const char *h = ht + off[i];
+        const uint32_t L = nl[i];
+        uint64_t id = i;
+        if (L > 2 && h[0] == 's' && h[1] == '_' && h[2] >= '0' && h[2] <= '9') {
+            id = 0;
+            for (uint32_t j = 2; j < L && h[j] >= '0' && h[j] <= '9'; j++) id = id * 10 + (uint64_t)(h[j] - '0');
+        }
+        (*ids)[i] = id;
+    }
+    return TK_OK;
+}
+
 int tk_r2t_create(tk_ctx *c, const char *bundle, uint64_t len, int where, int k, int strand, tk_r2t **out) {
     CHECK_CTX(c);
     if (!out) return TK_E_INVAL;
@@ -938,29 +973,8 @@ int tk_r2t_create(tk_ctx *c, const char *bundle, uint64_t len, int where, int k,
     if (!e && b->format == TK_FMT_FASTQ) e = set_err(c, TK_E_PARSE, "bundle must be FASTA");
     if (!e) e = r2t_build(z, b);
     if (!e) {
-        // component ids from the headers: integer after "s_", else the record ordinal
         z->n_records = b->n_reads;
-        z->comp_id.resize(b->n_reads);
-        std::vector<uint64_t> off(b->n_reads);
-        std::vector<uint32_t> nl(b->n_reads);
-        e = tk_reads_names(b, off.data(), nl.data());
-        std::vector<char> host_text;
-        const char *ht = bundle;
-        if (!e && where == TK_DEVICE) {
-            host_text.resize(len);
-            e = cuda_check(c, cudaMemcpy(host_text.data(), bundle, len, cudaMemcpyDeviceToHost), "bundle d2h");
-            ht = host_text.data();
-        }
-        for (uint64_t i = 0; !e && i < b->n_reads; i++) {
-            const char *h = ht + off[i];
-            uint32_t L = nl[i];
-            uint64_t id = i;
-            if (L > 2 && h[0] == 's' && h[1] == '_' && h[2] >= '0' && h[2] <= '9') {
-                id = 0;
-                for (uint32_t j = 2; j < L && h[j] >= '0' && h[j] <= '9'; j++) id = id * 10 + (uint64_t)(h[j] - '0');
-            }
-            z->comp_id[i] = id;
-        }
+        e = bundle_component_ids(c, b, bundle, len, where, &z->comp_id);
     }
     if (b) tk_reads_free(b);
     if (e) {
@@ -1020,6 +1034,64 @@ void tk_r2t_free(tk_r2t *z) {
     tk_ctx *c = z->ctx;
     if (z->table) tk_table_free(z->table);
     delete z;
+    ctx_release(c);
+}
+
+// ------------------------------------------------------------------ de Bruijn graphs
+
+static int norm_copy_out(tk_ctx *c, const char *src, uint64_t len, int where, char *out, uint64_t cap,
+                         const char *what);
+
+int tk_dbg_create(tk_ctx *c, const char *bundle, uint64_t len, int where, int K, int strand, tk_dbg **out) {
+    CHECK_CTX(c);
+    if (!out) return TK_E_INVAL;
+    *out = nullptr;
+    if (K < 1 || K > MAX_K - 1) return set_err(c, TK_E_INVAL, "FastaToDeBruijn: K must be in 1..30");
+    tk_dbg *g = new (std::nothrow) tk_dbg();
+    if (!g) return TK_E_OOM;
+    g->ctx = c;
+    ctx_acquire(c);
+    g->k = K;
+    g->strand = strand ? 1 : 0;
+    tk_reads *b = nullptr;
+    int e = tk_reads_parse(c, bundle, len, where, &b);
+    if (!e && b->format == TK_FMT_FASTQ) e = set_err(c, TK_E_PARSE, "bundle must be FASTA");
+    std::vector<uint64_t> ids;
+    if (!e) {
+        g->n_records = b->n_reads;
+        e = bundle_component_ids(c, b, bundle, len, where, &ids);
+    }
+    if (!e) e = dbg_build(g, b, ids);
+    if (b) tk_reads_free(b);
+    if (e) {
+        tk_dbg_free(g);
+        return e;
+    }
+    *out = g;
+    return TK_OK;
+}
+
+int tk_dbg_info(const tk_dbg *g, uint64_t *n_components, uint64_t *n_nodes, uint64_t *text_len) {
+    if (!g) return TK_E_INVAL;
+    if (n_components) *n_components = g->n_components;
+    if (n_nodes) *n_nodes = g->n_nodes;
+    if (text_len) *text_len = g->text_len;
+    return TK_OK;
+}
+
+int tk_dbg_text(const tk_dbg *g, int where, char *out, uint64_t cap) {
+    if (!g) return TK_E_INVAL;
+    tk_ctx *c = g->ctx;
+    CHECK_CTX(c);
+    return norm_copy_out(c, g->d_text, g->text_len, where, out, cap, "tk_dbg_text");
+}
+
+void tk_dbg_free(tk_dbg *g) {
+    if (!g) return;
+    tk_ctx *c = g->ctx;
+    cudaSetDevice(c->device);
+    dfree(c, g->d_text);
+    delete g;
     ctx_release(c);
 }
 
@@ -1140,6 +1212,27 @@ int tk_norm_extract_copy(const tk_norm *nm, int where, char *out, uint64_t cap) 
     tk_ctx *c = nm->ctx;
     CHECK_CTX(c);
     return norm_copy_out(c, nm->d_ext, nm->ext_len, where, out, cap, "tk_norm_extract_copy");
+}
+
+int tk_norm_extract_copy_async(tk_norm *nm, char *out, uint64_t cap) {
+    if (!nm) return TK_E_INVAL;
+    tk_ctx *c = nm->ctx;
+    CHECK_CTX(c);
+    if (!out && nm->ext_len) return set_err(c, TK_E_INVAL, "tk_norm_extract_copy_async: no buffer");
+    if (cap < nm->ext_len) return set_err(c, TK_E_RANGE, "tk_norm_extract_copy_async: buffer smaller than the text");
+    if (!nm->ext_len) return TK_OK;
+    cudaStream_t cs = copy_stream(c);
+    if (!cs) return norm_copy_out(c, nm->d_ext, nm->ext_len, TK_HOST, out, cap, "tk_norm_extract_copy_async");
+    cudaEvent_t built = nullptr;
+    TK_CUDA(c, cudaEventCreateWithFlags(&built, cudaEventDisableTiming));
+    int e = cuda_check(c, cudaEventRecord(built, c->stream), "event record");
+    if (!e) e = cuda_check(c, cudaStreamWaitEvent(cs, built, 0), "copy stream wait");
+    cudaEventDestroy(built);
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(out, nm->d_ext, nm->ext_len, cudaMemcpyDeviceToHost, cs), "records d2h");
+    if (!e && !nm->ext_copy_done)
+        e = cuda_check(c, cudaEventCreateWithFlags(&nm->ext_copy_done, cudaEventDisableTiming), "event");
+    if (!e) e = cuda_check(c, cudaEventRecord(nm->ext_copy_done, cs), "event record");
+    return e;
 }
 
 void tk_norm_free(tk_norm *nm) {

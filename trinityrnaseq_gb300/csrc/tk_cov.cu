@@ -11,9 +11,26 @@
 // Reads with at most 256 windows: one warp per read, values in registers,
 // warp bitonic sort (tk_warp.cuh).  Longer reads: one block per read, values
 // in a global scratch slab, block bitonic sort.
+//
+// Coverage cache.  The reads whose coverage is asked for are, in Trinity's
+// use, the reads that were counted (insilico_read_normalization.pl counts
+// both mate files and then looks every window of each up again), so a k-mer
+// is looked up about as often as its count.  Before the first pass over a
+// large table, the k-mers with the highest counts are copied into a small
+// table sized to stay in L2 (64 MB, TRINKMER_COV_CACHE_MB): 32-byte buckets of
+// four 8-byte entries; bucket = the top bits of a bijective hash of the key
+// on its 2k bits, entry = (the rest of the hash << cbits) | count, so one
+// sector answers a lookup.  Each bucket keeps the four highest counts that
+// hash to it (a key displaces the smallest entry when its count is larger).
+// A lookup that misses the cache reads the table itself, so the statistics
+// do not depend on what the cache holds.  Random lookups into HBM run at
+// ~40 G/s on GB300 whatever the table size above 1 GB, and into an
+// L2-resident table at ~300 G/s; at the plain path's scale the 6-7M k-mers
+// the cache holds answer ~70% of the lookups.
 #include "tk_warp.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 
@@ -21,6 +38,134 @@ namespace tk {
 
 constexpr int CV_THREADS = 256;
 constexpr uint32_t CV_WARP_MAX = 256;   // windows handled by the warp path
+
+// ------------------------------------------------------------------ coverage cache
+
+struct CovCache {
+    uint64_t *ent;     // 4 entries per bucket; nullptr = no cache
+    int n;             // key bits (2k)
+    int rbits;         // hash bits an entry keeps; the other 64 - rbits hold the count
+};
+
+// A bijection of [0, 2^n): xor-shifts and multiplications by odd constants,
+// each invertible modulo 2^n, so (bucket, remainder) identifies the key.
+__host__ __device__ __forceinline__ uint64_t kmix_n(uint64_t x, int n) {
+    const uint64_t m = (1ULL << n) - 1;   // n <= 62
+    const int s = (n + 1) >> 1;
+    x ^= x >> s;
+    x = (x * 0x9E3779B97F4A7C15ULL) & m;
+    x ^= x >> s;
+    x = (x * 0xD6E8FEB86659FD93ULL) & m;
+    x ^= x >> s;
+    return x;
+}
+
+__device__ __forceinline__ bool cache_get(const CovCache &cc, uint64_t key, uint32_t *val) {
+    const uint64_t h = kmix_n(key, cc.n);
+    const uint64_t *b = cc.ent + ((h >> cc.rbits) << 2);
+    const uint64_t r = h & ((1ULL << cc.rbits) - 1);
+    const int cbits = 64 - cc.rbits;
+    uint64_t e0, e1, e2, e3, pol;
+    // L2 evict-last: the cache's lines outlive the table lines streamed past them
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    asm("ld.global.L2::cache_hint.v4.u64 {%0,%1,%2,%3}, [%4], %5;"
+        : "=l"(e0), "=l"(e1), "=l"(e2), "=l"(e3)
+        : "l"(b), "l"(pol));
+    // an entry is never 0 (its count is >= 2), so an empty entry matches nothing
+    uint64_t hit = 0;
+    hit = (e0 && (e0 >> cbits) == r) ? e0 : hit;
+    hit = (e1 && (e1 >> cbits) == r) ? e1 : hit;
+    hit = (e2 && (e2 >> cbits) == r) ? e2 : hit;
+    hit = (e3 && (e3 >> cbits) == r) ? e3 : hit;
+    *val = (uint32_t)(hit & (~0ULL >> cc.rbits));
+    return hit != 0;
+}
+
+// the count of `key` for the statistics: the cache, else the table (1 when absent)
+__device__ __forceinline__ uint32_t cov_lookup(const CovCache &cc, DevTable t, uint64_t key) {
+    uint32_t v;
+    if (cc.ent && cache_get(cc, key, &v)) return v;
+    return tbl_get(t, key, 1u);
+}
+
+// Offers one (key, count) to its bucket: into an empty entry, else in place
+// of the smallest count when larger.  A CAS lost to another thread re-reads
+// the bucket; after 32 rounds the key is left out (the cache stays valid).
+__device__ __forceinline__ void cache_offer(const CovCache &cc, uint64_t key, uint64_t count) {
+    const uint64_t h = kmix_n(key, cc.n);
+    unsigned long long *b = reinterpret_cast<unsigned long long *>(cc.ent + ((h >> cc.rbits) << 2));
+    const uint64_t cmask = ~0ULL >> cc.rbits;
+    const unsigned long long mine = ((h & ((1ULL << cc.rbits) - 1)) << (64 - cc.rbits)) | count;
+    for (int round = 0; round < 32; round++) {
+        int at = 0;
+        unsigned long long old = 0, least = ~0ULL;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const unsigned long long e = *reinterpret_cast<volatile unsigned long long *>(b + j);
+            const unsigned long long c = e ? (e & cmask) : 0ULL;
+            if (c < least) {
+                least = c;
+                at = j;
+                old = e;
+            }
+        }
+        if (count <= least) return;
+        if (atomicCAS(b + at, old, mine) == old) return;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cache_build(const Slot *__restrict__ slots, uint64_t cap, CovCache cc) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t cmask = ~0ULL >> cc.rbits;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
+        const ulonglong2 s = __ldcs(reinterpret_cast<const ulonglong2 *>(slots + i));
+        const uint64_t c = (uint32_t)s.y;
+        if (s.x == EMPTY_KEY || c < 2 || c > cmask) continue;
+        cache_offer(cc, s.x, c);
+    }
+}
+
+static uint64_t cache_bytes_wanted() {
+    uint64_t mb = 64;
+    if (const char *v = getenv("TRINKMER_COV_CACHE_MB")) mb = strtoull(v, nullptr, 10);
+    return mb << 20;
+}
+
+// The cache of table t (built when missing or stale); cc->ent == nullptr when
+// the table is small enough for L2 to hold it whole, or k is too small.
+static int cache_get_or_build(tk_table *t, CovCache *cc) {
+    cc->ent = nullptr;
+    tk_ctx *c = t->ctx;
+    const uint64_t want = cache_bytes_wanted();
+    if (want < 32 || t->capacity * sizeof(Slot) < 4 * want) return TK_OK;
+    int hbits = 0;
+    while ((32ULL << (hbits + 1)) <= want) hbits++;
+    const int n = 2 * t->k;
+    if (n - hbits < 1 || 64 - (n - hbits) < 2) return TK_OK;
+    const uint64_t bytes = 32ULL << hbits;
+    cc->n = n;
+    cc->rbits = n - hbits;
+    if (!t->hot_valid || t->hot_bytes != bytes) {
+        if (t->d_hot && t->hot_bytes != bytes) {
+            dfree(c, t->d_hot);
+            t->d_hot = nullptr;
+        }
+        if (!t->d_hot) TK_TRY(dmalloc(c, (void **)&t->d_hot, bytes, "coverage cache"));
+        t->hot_bytes = bytes;
+        TK_CUDA(c, cudaMemsetAsync(t->d_hot, 0, bytes, c->stream));
+        cc->ent = t->d_hot;
+        cudaEvent_t ev;
+        prof_begin(c, TK_KID_COV_CACHE, &ev);
+        const uint64_t blocks = std::min<uint64_t>((t->capacity + 255) / 256, (uint64_t)c->sm_count * 16);
+        k_cache_build<<<(unsigned)std::max<uint64_t>(blocks, 1), 256, 0, c->stream>>>(t->t.slots, t->capacity, *cc);
+        c->launches++;
+        prof_end(c, TK_KID_COV_CACHE, ev, t->capacity);
+        TK_TRY(check_launch(c, "coverage cache"));
+        t->hot_valid = true;
+    }
+    cc->ent = t->d_hot;
+    return TK_OK;
+}
 
 // Integer statistics of one read, uniform over the warp.
 struct ReadSums {
@@ -30,16 +175,19 @@ struct ReadSums {
 constexpr uint32_t LONG_READ = 0xFFFFFFFFu;   // cnt of a read left to the long-read pass
 
 template <int S, bool CANON>
-__device__ __forceinline__ ReadSums cov_warp_read(DevTable t, const uint8_t *__restrict__ seq, uint64_t start,
-                                                  uint32_t nwin, int k, uint64_t *words) {
+__device__ __forceinline__ ReadSums cov_warp_read(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
+                                                  const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin,
+                                                  int k) {
     const uint32_t span = (nwin + 31) / 32;
     uint32_t v[S];
+    uint32_t vm = 0;
     uint32_t cnt = 0;
     uint64_t sum = 0, hi = 0, lo = 0;
-    auto body = [&](int j, bool valid, uint64_t key) {
-        uint32_t c = PAD_VAL;
+    lane_windows_codes<S, CANON>(codes, inv, start, nwin, span, k, [&](int j, bool valid, uint64_t key) {
+        uint32_t c = 0;
         if (valid) {
-            c = tbl_get(t, key, 1u);
+            c = cov_lookup(cc, t, key);
+            vm |= 1u << j;
             cnt++;
             sum += c;
             uint64_t sq = (uint64_t)c * c;   // < 2^64
@@ -48,17 +196,14 @@ __device__ __forceinline__ ReadSums cov_warp_read(DevTable t, const uint8_t *__r
             lo = nlo;
         }
         v[j] = c;
-    };
-    if (!lane_windows_packed<S, CANON>(seq, start, nwin, span, k, words, body))
-        lane_windows<S, CANON>(seq, start, nwin, span, k, body);
+    });
     ReadSums rs;
     rs.cnt = warp_sum(cnt);
     rs.sum = warp_sum(sum);
     warp_sum_u128(hi, lo);
     rs.hi = hi;
     rs.lo = lo;
-    warp_bitonic_sort<S>(v);
-    rs.med = rs.cnt ? warp_elem<S>(v, rs.cnt / 2) : 0u;
+    rs.med = rs.cnt ? warp_select<S>(v, vm, rs.cnt / 2) : 0u;
     return rs;
 }
 
@@ -70,25 +215,30 @@ __device__ __forceinline__ ReadSums cov_warp_read(DevTable t, const uint8_t *__r
 // CV_WARP_MAX windows are appended to long_list (or, with no list, left to a
 // separate pass) and not written here.
 template <bool CANON>
-__device__ __forceinline__ void cov_warp_chunk(DevTable t, const uint8_t *__restrict__ seq,
+__device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
+                                               const uint32_t *__restrict__ inv,
                                                const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k, uint64_t r0,
                                                uint32_t *__restrict__ median, float *__restrict__ mean,
                                                float *__restrict__ stdev, uint32_t *__restrict__ long_list,
-                                               unsigned long long *__restrict__ long_n, ReadSums *__restrict__ held,
-                                               uint64_t *words) {
+                                               unsigned long long *__restrict__ long_n, ReadSums *__restrict__ held) {
     const unsigned lane = lane_id();
     const uint32_t nr = n_reads - r0 < 32 ? (uint32_t)(n_reads - r0) : 32u;
+    // lane i holds the start of read r0 + i; the end of the last is one more load
+    const uint64_t my_start = rd_off[r0 + (lane < nr ? lane : nr)];
+    const uint64_t last_end = __shfl_sync(0xffffffffu, my_start, (int)(nr < 32 ? nr : 31));
+    const uint64_t end_nr = nr < 32 ? last_end : rd_off[r0 + 32];
     for (uint32_t i = 0; i < nr; i++) {
         const uint64_t r = r0 + i;
-        const uint64_t start = rd_off[r];
-        const uint64_t L = rd_off[r + 1] - start - 1;
+        const uint64_t start = __shfl_sync(0xffffffffu, my_start, (int)i);
+        const uint64_t next = i + 1 < 32 ? __shfl_sync(0xffffffffu, my_start, (int)(i + 1) & 31) : end_nr;
+        const uint64_t L = (i + 1 < nr ? next : end_nr) - start - 1;
         const uint32_t nwin = L >= (uint64_t)k ? (uint32_t)(L - k + 1) : 0u;
         ReadSums rs;
         bool is_long = false;
-        if (nwin <= 32) rs = cov_warp_read<1, CANON>(t, seq, start, nwin, k, words);
-        else if (nwin <= 64) rs = cov_warp_read<2, CANON>(t, seq, start, nwin, k, words);
-        else if (nwin <= 128) rs = cov_warp_read<4, CANON>(t, seq, start, nwin, k, words);
-        else if (nwin <= CV_WARP_MAX) rs = cov_warp_read<8, CANON>(t, seq, start, nwin, k, words);
+        if (nwin <= 32) rs = cov_warp_read<1, CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (nwin <= 64) rs = cov_warp_read<2, CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (nwin <= 128) rs = cov_warp_read<4, CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (nwin <= CV_WARP_MAX) rs = cov_warp_read<8, CANON>(cc, t, codes, inv, start, nwin, k);
         else {
             is_long = true;
             if (long_list && lane == 0) long_list[atomicAdd(long_n, 1ULL)] = (uint32_t)r;
@@ -111,23 +261,23 @@ __device__ __forceinline__ void cov_warp_chunk(DevTable t, const uint8_t *__rest
 }
 
 template <bool CANON>
-__global__ void __launch_bounds__(CV_THREADS, 6) k_coverage(DevTable t, const uint8_t *__restrict__ seq,
+__global__ void __launch_bounds__(CV_THREADS, 6) k_coverage(CovCache cc, DevTable t, const uint64_t *__restrict__ codes,
+                                                        const uint32_t *__restrict__ inv,
                                                         const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
                                                         uint32_t *__restrict__ median, float *__restrict__ mean,
                                                         float *__restrict__ stdev, uint32_t *__restrict__ long_list,
                                                         unsigned long long *__restrict__ long_n) {
     __shared__ ReadSums held[CV_THREADS];
-    __shared__ uint64_t words[CV_THREADS / 32][12];
     const uint64_t warps = (uint64_t)gridDim.x * (CV_THREADS / 32);
     const uint64_t chunks = (n_reads + 31) / 32;
     for (uint64_t ch = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); ch < chunks; ch += warps)
-        cov_warp_chunk<CANON>(t, seq, rd_off, n_reads, k, ch * 32, median, mean, stdev, long_list, long_n,
-                              held + (threadIdx.x & ~31u), words[threadIdx.x >> 5]);
+        cov_warp_chunk<CANON>(cc, t, codes, inv, rd_off, n_reads, k, ch * 32, median, mean, stdev, long_list, long_n,
+                              held + (threadIdx.x & ~31u));
 }
 
 // long reads: one block per read, `slab` = this block's scratch (n2max values)
 template <bool CANON>
-__global__ void __launch_bounds__(CV_THREADS) k_coverage_long(DevTable t, const uint8_t *__restrict__ seq,
+__global__ void __launch_bounds__(CV_THREADS) k_coverage_long(CovCache cc, DevTable t, const uint8_t *__restrict__ seq,
                                                              const uint64_t *__restrict__ rd_off,
                                                              const uint32_t *__restrict__ list, uint64_t n_long, int k,
                                                              uint32_t *__restrict__ scratch, uint64_t n2max,
@@ -142,7 +292,8 @@ __global__ void __launch_bounds__(CV_THREADS) k_coverage_long(DevTable t, const 
         const uint32_t nwin = (uint32_t)(rd_off[r + 1] - start - 1 - (k - 1));
         uint32_t n2 = 1;
         while (n2 < nwin) n2 <<= 1;
-        block_window_values<CANON>(seq, start, nwin, n2, k, slab, [&](uint64_t key) { return tbl_get(t, key, 1u); });
+        block_window_values<CANON>(seq, start, nwin, n2, k, slab,
+                                   [&](uint64_t key) { return cov_lookup(cc, t, key); });
         uint32_t cnt = 0;
         uint64_t sum = 0, hi = 0, lo = 0;
         for (uint32_t w = threadIdx.x; w < nwin; w += blockDim.x) {
@@ -206,6 +357,8 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
             dt = tbl_empty(empty);
         }
     }
+    CovCache cc{};
+    if (!e && t->capacity) e = cache_get_or_build(t, &cc);
     if (!e) {
         const uint64_t chunks = (n + 31) / 32;
         const unsigned grid = (unsigned)std::max<uint64_t>(
@@ -213,11 +366,11 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COVERAGE, &ev);
         if (t->canonical)
-            k_coverage<true><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
-                                                                 d_stdev, long_list, long_n);
+            k_coverage<true><<<grid, CV_THREADS, 0, c->stream>>>(cc, dt, rd->d_codes, rd->d_inv, rd->d_rd_off, n, k,
+                                                                 d_median, d_mean, d_stdev, long_list, long_n);
         else
-            k_coverage<false><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
-                                                                  d_stdev, long_list, long_n);
+            k_coverage<false><<<grid, CV_THREADS, 0, c->stream>>>(cc, dt, rd->d_codes, rd->d_inv, rd->d_rd_off, n, k,
+                                                                  d_median, d_mean, d_stdev, long_list, long_n);
         c->launches++;
         prof_end(c, TK_KID_COVERAGE, ev, rd->n_bases);
         e = check_launch(c, "coverage");
@@ -236,10 +389,10 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
         if (!e) {
             if (t->canonical)
                 k_coverage_long<true><<<(unsigned)grid, CV_THREADS, 0, c->stream>>>(
-                    dt, rd->d_seq, rd->d_rd_off, long_list, hl, k, scratch, n2max, d_median, d_mean, d_stdev);
+                    cc, dt, rd->d_seq, rd->d_rd_off, long_list, hl, k, scratch, n2max, d_median, d_mean, d_stdev);
             else
                 k_coverage_long<false><<<(unsigned)grid, CV_THREADS, 0, c->stream>>>(
-                    dt, rd->d_seq, rd->d_rd_off, long_list, hl, k, scratch, n2max, d_median, d_mean, d_stdev);
+                    cc, dt, rd->d_seq, rd->d_rd_off, long_list, hl, k, scratch, n2max, d_median, d_mean, d_stdev);
             c->launches++;
             e = check_launch(c, "coverage long");
             dfree(c, scratch);
@@ -275,17 +428,18 @@ static __device__ __align__(16) Slot g_noalloc_empty[2] = {{EMPTY_KEY, 0u, 0u}, 
 
 // short reads only (<= 256 windows); longer reads are left to k_coverage_long_slab
 template <bool CANON>
-__global__ void __launch_bounds__(CV_THREADS, 4) k_coverage_short(DevTable t, const uint8_t *__restrict__ seq,
+__global__ void __launch_bounds__(CV_THREADS, 4) k_coverage_short(DevTable t, const uint64_t *__restrict__ codes,
+                                                              const uint32_t *__restrict__ inv,
                                                               const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
                                                               uint32_t *__restrict__ median, float *__restrict__ mean,
                                                               float *__restrict__ stdev) {
     __shared__ ReadSums held[CV_THREADS];
-    __shared__ uint64_t words[CV_THREADS / 32][12];
     const uint64_t warps = (uint64_t)gridDim.x * (CV_THREADS / 32);
     const uint64_t chunks = (n_reads + 31) / 32;
+    const CovCache none{};
     for (uint64_t ch = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); ch < chunks; ch += warps)
-        cov_warp_chunk<CANON>(t, seq, rd_off, n_reads, k, ch * 32, median, mean, stdev, nullptr, nullptr,
-                              held + (threadIdx.x & ~31u), words[threadIdx.x >> 5]);
+        cov_warp_chunk<CANON>(none, t, codes, inv, rd_off, n_reads, k, ch * 32, median, mean, stdev, nullptr, nullptr,
+                              held + (threadIdx.x & ~31u));
 }
 
 // reads with more than 256 windows, one block per read, found by a strided scan
@@ -390,11 +544,11 @@ int coverage_stats_noalloc(tk_table *t, const tk_reads *rd, uint32_t *d_median, 
     const unsigned grid = (unsigned)std::max<uint64_t>(
         1, std::min<uint64_t>((chunks + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
     if (t->canonical)
-        k_coverage_short<true><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
-                                                                   d_stdev);
+        k_coverage_short<true><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_codes, rd->d_inv, rd->d_rd_off, n, k,
+                                                                   d_median, d_mean, d_stdev);
     else
-        k_coverage_short<false><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_seq, rd->d_rd_off, n, k, d_median, d_mean,
-                                                                    d_stdev);
+        k_coverage_short<false><<<grid, CV_THREADS, 0, c->stream>>>(dt, rd->d_codes, rd->d_inv, rd->d_rd_off, n, k,
+                                                                    d_median, d_mean, d_stdev);
     c->launches++;
     TK_TRY(check_launch(c, "coverage (no allocation)"));
     if (rd->max_len >= (uint32_t)k && rd->max_len - k + 1 > CV_WARP_MAX) {

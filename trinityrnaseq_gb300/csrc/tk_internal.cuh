@@ -273,6 +273,11 @@ struct tk_table {
     uint64_t dump_len = 0;
     uint32_t dump_min = 0;
     bool dump_valid = false;
+    // coverage cache (tk_cov.cu): the k-mers with the highest counts in an
+    // L2-sized table, built on the first coverage pass after a change
+    uint64_t *d_hot = nullptr;
+    uint64_t hot_bytes = 0;
+    bool hot_valid = false;
 };
 
 struct tk_r2t {
@@ -282,6 +287,16 @@ struct tk_r2t {
     tk_table *table = nullptr;              // key -> bundle record index
     uint64_t n_records = 0;
     std::vector<uint64_t> comp_id;          // per bundle record
+};
+
+// per-record de Bruijn k-mer graphs of a bundle (tk_dbg.cu)
+struct tk_dbg {
+    tk_ctx *ctx = nullptr;
+    int k = 24;                             // -K: node lines are (k+1)-mers
+    int strand = 0;
+    char *d_text = nullptr;
+    uint64_t text_len = 0;
+    uint64_t n_records = 0, n_components = 0, n_nodes = 0, n_windows = 0;
 };
 
 namespace tk {
@@ -325,6 +340,7 @@ struct tk_norm {
     uint64_t table_len = 0;
     char *d_ext = nullptr;                         // last extraction
     uint64_t ext_len = 0;
+    cudaEvent_t ext_copy_done = nullptr;           // an asynchronous host copy of d_ext in flight
     uint32_t *d_hash = nullptr;                    // selected names: row index per slot, ~0 empty
     uint8_t *d_keydup = nullptr;                   // per row: its name is another row's, or empty
     uint64_t hash_mask = 0;
@@ -356,6 +372,7 @@ int norm_select(tk_norm *nm, const tk_reads *const *const sets[2], const uint32_
 int norm_table(tk_norm *nm);
 int norm_extract(tk_norm *nm, const tk_reads *const *sets, uint32_t nsets);
 void norm_release(tk_norm *nm);
+int dbg_build(tk_dbg *g, const tk_reads *b, const std::vector<uint64_t> &comp_id);
 }  // namespace tk
 
 #define TK_TRY(x) do { int _e = (x); if (_e) return _e; } while (0)

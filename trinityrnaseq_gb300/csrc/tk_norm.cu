@@ -1422,6 +1422,8 @@ int norm_table(tk_norm *nm) {
 // the selection holds; every selected name must be found in one of them.
 int norm_extract(tk_norm *nm, const tk_reads *const *sets, uint32_t nsets) {
     tk_ctx *c = nm->ctx;
+    // the device text is released in stream order after its host copy ends
+    if (nm->ext_copy_done) cudaStreamWaitEvent(c->stream, nm->ext_copy_done, 0);
     if (nm->d_ext) {
         dfree(c, nm->d_ext);
         nm->d_ext = nullptr;
@@ -1534,6 +1536,11 @@ int norm_extract(tk_norm *nm, const tk_reads *const *sets, uint32_t nsets) {
 
 void norm_release(tk_norm *nm) {
     tk_ctx *c = nm->ctx;
+    if (nm->ext_copy_done) {
+        cudaStreamWaitEvent(c->stream, nm->ext_copy_done, 0);
+        cudaEventDestroy(nm->ext_copy_done);
+        nm->ext_copy_done = nullptr;
+    }
     side_free(c, nm->side[0]);
     side_free(c, nm->side[1]);
     void *p[] = {nm->row_l, nm->row_r, nm->row_n, nm->acc_off, nm->d_accs, nm->d_table, nm->d_ext, nm->d_hash,

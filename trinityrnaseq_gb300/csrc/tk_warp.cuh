@@ -125,6 +125,87 @@ __device__ __forceinline__ bool lane_windows_packed(const uint8_t *__restrict__ 
     return true;
 }
 
+// Windows of one read cut from the read set's 2-bit codes (codes[j] holds
+// positions 32j .. 32j+31, first position in the top bits; bit 31-i of inv[j]
+// is set when position 32j+i is not A/C/G/T; word -1 exists).  Lane l owns
+// windows [l*span, l*span + span) of the read starting at position `start`;
+// with span <= 8 their end positions fall in two consecutive code words, so
+// the lane loads three words (and their invalid bits) once and cuts each
+// window out of a pair with one funnel shift.  f(j, valid, key) for
+// j = 0..S-1 (window lane*span + j).
+template <int S, bool CANON, typename F>
+__device__ __forceinline__ void lane_windows_codes(const uint64_t *__restrict__ codes,
+                                                   const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin,
+                                                   uint32_t span, int k, F &&f) {
+    static_assert(S <= 8, "a lane's windows end in at most two code words");
+    const uint32_t w0 = lane_id() * span;
+    const uint64_t e0 = start + w0 + (uint64_t)k - 1;   // end position of the lane's first window
+    const int64_t q0 = (int64_t)(e0 >> 5);
+    uint64_t c0 = 0, c1 = 0, c2 = 0;
+    uint32_t i0 = ~0u, i1 = ~0u, i2 = ~0u;
+    if (w0 < nwin) {
+        c0 = __ldg(codes + q0 - 1);
+        c1 = __ldg(codes + q0);
+        c2 = __ldg(codes + q0 + 1);
+        i0 = __ldg(inv + q0 - 1);
+        i1 = __ldg(inv + q0);
+        i2 = __ldg(inv + q0 + 1);
+    }
+    const uint64_t kmask = (1ULL << (2 * k)) - 1;
+    const uint64_t vmask = (1ULL << k) - 1;
+    const uint32_t e_off = (uint32_t)(e0 & 31);
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+        const bool in = (uint32_t)j < span && w0 + j < nwin;
+        bool valid = false;
+        uint64_t key = 0;
+        if (in) {
+            // the window ends at position 32 + i of the pair (words q-1, q)
+            const uint32_t e = e_off + (uint32_t)j;
+            const bool second = e >= 32;
+            const int i = (int)(e & 31);
+            const uint64_t hi = second ? c1 : c0, lo = second ? c2 : c1;
+            const uint64_t m = second ? (((uint64_t)i1 << 32) | i2) : (((uint64_t)i0 << 32) | i1);
+            valid = ((m >> (31 - i)) & vmask) == 0;
+            const int s = 62 - 2 * i;
+            const uint64_t fw = (s ? ((lo >> s) | (hi << (64 - s))) : lo) & kmask;
+            key = fw;
+            if (CANON) {
+                const uint64_t rc = kmer_revcomp(fw, k);
+                key = rc < fw ? rc : fw;
+            }
+        }
+        f(j, valid, key);
+    }
+}
+
+// Element m (0-based, ascending) of the warp's valid values -- value v[j] of a
+// lane counts when bit j of its vm is set -- by a bit-serial radix select from
+// the top bit of the largest value: per bit, the values that agree with the
+// prefix chosen so far and have a 0 there are counted with one warp-wide add;
+// the target has a 0 there when m is below that count.  Costs one pass per
+// significant bit of the largest count instead of a full sort.
+template <int S>
+__device__ __forceinline__ uint32_t warp_select(const uint32_t (&v)[S], uint32_t vm, uint32_t m) {
+    uint32_t lmax = 0;
+#pragma unroll
+    for (int j = 0; j < S; j++)
+        if ((vm >> j) & 1u) lmax = max(lmax, v[j]);
+    const uint32_t mx = __reduce_max_sync(0xffffffffu, lmax);
+    uint32_t prefix = 0;
+    for (int b = 31 - __clz(mx); b >= 0; b--) {   // no pass when every value is 0
+        uint32_t c = 0;
+#pragma unroll
+        for (int j = 0; j < S; j++) c += (((vm >> j) & 1u) && ((v[j] ^ prefix) >> b) == 0) ? 1u : 0u;
+        c = __reduce_add_sync(0xffffffffu, c);
+        if (m >= c) {
+            m -= c;
+            prefix |= 1u << b;
+        }
+    }
+    return prefix;
+}
+
 template <int S>
 __device__ __forceinline__ void warp_bitonic_sort(uint32_t (&v)[S]) {
     const unsigned lane = lane_id();

@@ -417,6 +417,49 @@ class ReadsToTranscripts:
         return rec[:n], hits[:n], nwin[:n]
 
 
+class DeBruijnGraphs:
+    """Per-record de Bruijn graphs of a bundle (tk_dbg; Inchworm's
+    FastaToDeBruijn --graph_per_record, Trinity:2298-2302).  `bundle` is a host
+    buffer, or a device address with `length` and device=True."""
+
+    def __init__(self, ctx: Context, bundle, K: int = 24, strand: bool = False, length: Optional[int] = None,
+                 device: bool = False):
+        self.ctx, self.lib, self.K, self.strand = ctx, ctx.lib, K, strand
+        if device:
+            ptr, n, where = int(bundle), int(length), N.TK_DEVICE
+        else:
+            ptr, n, _ = _host_ptr(bundle)
+            where = N.TK_HOST
+        h = C.c_void_p()
+        ctx.check(self.lib.tk_dbg_create(ctx.h, C.c_void_p(ptr), n, where, K, int(strand), C.byref(h)),
+                  "tk_dbg_create")
+        self.h = h
+        nc, nn, nt = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        ctx.check(self.lib.tk_dbg_info(h, C.byref(nc), C.byref(nn), C.byref(nt)), "tk_dbg_info")
+        self.n_components, self.n_nodes, self.text_len = nc.value, nn.value, nt.value
+
+    def text_into(self, ptr: int, cap: int, device: bool = False) -> int:
+        self.ctx.check(self.lib.tk_dbg_text(self.h, N.TK_DEVICE if device else N.TK_HOST, C.c_void_p(ptr), cap),
+                       "tk_dbg_text")
+        return self.text_len
+
+    def text(self) -> bytes:
+        buf = np.zeros(max(self.text_len, 1), dtype=np.uint8)
+        self.text_into(buf.ctypes.data, buf.size)
+        return buf[:self.text_len].tobytes()
+
+    def free(self) -> None:
+        if getattr(self, "h", None) and _live():
+            self.lib.tk_dbg_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 class Normalization:
     """In-silico normalization over coverage statistics (tk_norm): the sort,
     pair merge and selection util/insilico_read_normalization.pl runs through
@@ -491,15 +534,22 @@ class Normalization:
         self.ctx.check(self.lib.tk_norm_table(self.h, N.TK_HOST, buf, n.value, C.byref(n)), "tk_norm_table")
         return buf.raw[:n.value]
 
-    def extract_into(self, fastq, ptr: Optional[int] = None, cap: int = 0, device: bool = False) -> int:
+    def extract_into(self, fastq, ptr: Optional[int] = None, cap: int = 0, device: bool = False,
+                     overlap: bool = False) -> int:
         """Runs the extraction (the text stays on the device) and returns its
         length; with ptr, also copies it there (host, or device address).
-        fastq may be a list of read sets (one side's files or pieces)."""
+        fastq may be a list of read sets (one side's files or pieces).  With
+        overlap (host ptr, page-locked) the copy runs on the context's copy
+        stream behind later work and has landed once ctx.synchronize()
+        returns (tk_norm_extract_copy_async)."""
         n = C.c_uint64()
         sets = list(fastq) if isinstance(fastq, (list, tuple)) else [fastq]
         hs = (C.c_void_p * len(sets))(*[r.h for r in sets])
         self.ctx.check(self.lib.tk_norm_extract_multi(self.h, hs, len(sets), C.byref(n)), "tk_norm_extract")
-        if ptr is not None:
+        if ptr is not None and overlap and not device:
+            self.ctx.check(self.lib.tk_norm_extract_copy_async(self.h, C.c_void_p(ptr), cap),
+                           "tk_norm_extract_copy_async")
+        elif ptr is not None:
             self.ctx.check(self.lib.tk_norm_extract_copy(self.h, N.TK_DEVICE if device else N.TK_HOST,
                                                          C.c_void_p(ptr), cap), "tk_norm_extract_copy")
         return n.value

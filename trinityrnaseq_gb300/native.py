@@ -32,6 +32,7 @@ TK_FA_REVCOMP, TK_FA_IGNORE_DIRTY, TK_FA_IF_MISSING = 1, 2, 4
 KID = {
     "parse": 0, "hll": 1, "count": 2, "compact": 3, "sort": 4, "dump": 5, "load": 6,
     "coverage": 7, "r2t_build": 8, "r2t_assign": 9, "bins": 10, "scatter": 11, "norm": 12, "extract": 13,
+    "cov_cache": 14, "dbg": 15,
 }
 
 u64, u32, i32, vp = C.c_uint64, C.c_uint32, C.c_int32, C.c_void_p
@@ -91,6 +92,11 @@ SIGNATURES = {
     "tk_norm_extract": (C.c_int, [vp, vp, P(u64)]),
     "tk_norm_extract_multi": (C.c_int, [vp, vp, u32, P(u64)]),
     "tk_norm_extract_copy": (C.c_int, [vp, C.c_int, vp, u64]),
+    "tk_norm_extract_copy_async": (C.c_int, [vp, vp, u64]),
+    "tk_dbg_create": (C.c_int, [vp, vp, u64, C.c_int, C.c_int, C.c_int, P(vp)]),
+    "tk_dbg_info": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
+    "tk_dbg_text": (C.c_int, [vp, C.c_int, vp, u64]),
+    "tk_dbg_free": (None, [vp]),
     "tk_norm_free": (None, [vp]),
     "tk_count_bins": (C.c_int, [vp, vp, u64, C.c_int, vp, u32, C.c_int, C.c_int, u32, P(vp)]),
     "tk_count_bins_ex": (C.c_int, [vp, vp, u64, C.c_int, vp, u32, C.c_int, C.c_int, vp, vp, P(vp)]),
