@@ -226,11 +226,15 @@ int tk_coverage_stats(tk_table *table, const tk_reads *reads, int where, uint32_
  * mid-run.  The table and read set are created beforehand (that is where
  * their memory is allocated); median/mean/stdev are DEVICE arrays of n_reads
  * entries owned by the caller.  Reads longer than 256 windows use a fixed
- * 16 MiB slab of static device memory (held by every GPU that loads the
- * library until exit), which limits a read to 131,072 windows (TK_E_RANGE
- * beyond that).  The first call on a device looks up that slab's address.
- * All calls share the slab: calls that overlap on the GPU race.  Returns after
- * synchronising the context's stream. */
+ * 16 MiB slab of static device memory, which limits a read to 131,072
+ * windows (TK_E_RANGE beyond that).  The slab is part of the library's
+ * device code for the coverage kernels: a GPU commits it when that code is
+ * loaded there and holds it until the process exits.  Under CUDA's lazy
+ * module loading (the default) that can be the first call of this entry
+ * point on the device, which also looks up the slab's address -- so make a
+ * first call (an empty read set will do) before dividing the GPU's memory
+ * among jobs.  All calls share the slab: calls that overlap on the GPU race.
+ * Returns after synchronising the context's stream. */
 int tk_coverage_stats_noalloc(tk_table *table, const tk_reads *reads, uint32_t *median,
                               float *mean, float *stdev);
 
@@ -380,9 +384,14 @@ void tk_bins_free(tk_bins *bins);
 /* ------------------------------------------------------------- serving
  * A resident job server: `slots` worker slots, each with its own context and
  * stream, and an HBM admission budget (0 = 80% of the free memory).  A queued
- * job starts as soon as a slot is free and its memory estimate fits what the
- * running jobs leave of the budget, so jobs arriving while others run are
- * admitted as slots and memory free up and their work overlaps on the GPU.
+ * job starts as soon as a slot is free, its memory estimate (an upper bound
+ * of what it allocates) fits what the running jobs leave of the budget, and
+ * the GPU reports that much memory free (cudaMemGetInfo, plus the blocks the
+ * slot keeps cached for reuse, less 1/64 of the GPU as a margin), so jobs
+ * arriving while others run are admitted as slots and memory free up and
+ * their work overlaps on the GPU.  A job that fits the budget but not the
+ * free memory waits until no job runs.  A slot keeps at most budget / slots
+ * of freed blocks cached between jobs.
  * Each job computes what the plain calls compute (a result does not depend on
  * the other jobs).  The reference's nearest equivalent is ParaFly's process
  * fan-out (Trinity:3652) and the two concurrent stats processes of
@@ -437,6 +446,9 @@ int tk_server_stats(tk_server *server, uint64_t *budget, uint64_t *in_use, int *
  * with the same k, strandedness and input format (up to 64 jobs / 256 MB)
  * as the bins of one tk_count_bins_ex pass. */
 int tk_server_batched_jobs(tk_server *server, uint64_t *jobs);
+/* Admission passes that found a queued job within the budget but above the
+ * GPU's free memory (and so left it queued). */
+int tk_server_held_by_free_memory(tk_server *server, uint64_t *admissions);
 /* Waits for queued and running jobs, then stops the workers. */
 void tk_server_destroy(tk_server *server);
 

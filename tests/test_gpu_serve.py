@@ -109,3 +109,33 @@ def test_served_normalization_selects_like_plain_calls(ctx):
             srv.release(jid)
         assert srv.wait(extra)[0] == 0
         srv.release(extra)
+
+
+def test_admission_waits_for_free_device_memory(ctx):
+    """With most of the GPU's memory held outside the server (here by
+    PyTorch), jobs that fit the budget but not the free memory are held back
+    and run one at a time; every result still equals the job run alone."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device(f"cuda:{ctx.device}")
+    jobs = [(N.TK_JOB_COUNT, synth.transcriptome_reads(seed=500 + i, n_reads=400000).tobytes(), b"", 1)
+            for i in range(3)]
+    alone = [plain_run(ctx, k, t1, t2, min_count=mc) for k, t1, t2, mc in jobs]
+    ctx.trim()
+    torch.cuda.synchronize(dev)
+    free, total = torch.cuda.mem_get_info(dev)
+    # leave about 3 GB free: less than the 1/64 margin plus a job's estimate
+    # (32 x its ~31 MB text), more than a job of this size really allocates
+    hog = torch.empty(max(0, free - (3 << 30)), dtype=torch.uint8, device=dev)
+    try:
+        with Server(ctx.device, slots=3, hbm_budget=1 << 40) as srv:
+            ids = [submit(srv, *j) for j in jobs]
+            for jid, (kind, *_), want in zip(ids, jobs, alone):
+                st, _, _ = srv.wait(jid)
+                assert st == 0, srv.error(jid)
+                assert same(srv.result(jid, kind), want)
+                srv.release(jid)
+            assert srv.held_by_free_memory() > 0
+            assert srv.stats()[2] == 1       # never two at once
+    finally:
+        del hog
+        torch.cuda.empty_cache()

@@ -204,3 +204,28 @@ def test_insilico_read_normalization_fasta(native_built, oracle, tmp_path, pairs
     for (tag, _), w in zip(sides, want):
         assert (out / f"{tag}.norm.fa").read_bytes() == w, tag
     assert (out / "l.fa.normalized_K25_maxC30_minC1_maxCV10000.fa").exists()
+
+
+def test_trinkmer_bins_writes_each_bins_catalogue(native_built, oracle, tmp_path):
+    """Phase 2's per-bin k-mer catalogues (what `inchworm --reads ...
+    --minKmerCount 2 --DS` builds in each bin's Trinity run) from one batched
+    pass over the reads list file that write_partitioned_trinity_cmds.pl reads
+    (the last field of each line is a bin's reads file)."""
+    from trinityrnaseq_gb300 import synth
+    text, off, _ = synth.power_law_bins(seed=9, n_bins=25, alpha=1.8, min_reads=50, max_reads=3000)
+    t = text.tobytes()
+    paths = []
+    for b in range(25):
+        p = tmp_path / f"c{b}.trinity.reads.fa"
+        p.write_bytes(t[int(off[b]):int(off[b + 1])])
+        paths.append(p)
+    (tmp_path / "partitioned_reads.files.list").write_text(
+        "".join(f"bin{b}\t{p}\n" if b % 2 else f"{p}\n" for b, p in enumerate(paths)))
+    run([BIN / "trinkmer_bins", "--reads_list_file", tmp_path / "partitioned_reads.files.list", "-K", 25,
+         "--min_kmer_cov", 2, "--histo", "--max_batch_gb", 0.0001], cwd=tmp_path)
+    for p in paths:
+        keys, counts = oracle.count(p.read_bytes(), 25, True)
+        assert (tmp_path / (p.name + ".K25.kmers.fa")).read_bytes() == oracle.dump(keys, counts, 25, 2)
+        h = oracle.histo(counts, 1, 10000)
+        want = "".join(f"{c} {h[c]}\n" for c in range(1, 10002) if h[c])
+        assert (tmp_path / (p.name + ".K25.histo")).read_text() == want

@@ -2,7 +2,8 @@
 allocate device memory while computing (their HBM is already divided among
 jobs, or an allocation failure or cudaMalloc's implicit synchronisation is not
 acceptable mid-run).  Checked through the C ABI against the allocating entry
-point, bit for bit, on two calls in a row that share the static scratch slab.
+point and the oracle, bit for bit, on two calls in a row that share the static
+scratch slab.
 
 This file is collected last on purpose, so a failure here leaves every other
 test already run."""
@@ -20,8 +21,11 @@ def _reads() -> bytes:
     short = synth.transcriptome_reads(seed=31, n_reads=20000).tobytes()
     rnd = np.random.default_rng(7)
     longs = []
-    for i in range(12):  # reads above 256 windows go through the static slab
-        L = int(rnd.integers(300, 5000))
+    # reads above 256 windows go through the static slab: a dozen of 300 to
+    # 5000 bases, one of exactly 257 windows and one at the slab's limit of
+    # 131,072 windows (k = 25)
+    lens = [int(x) for x in rnd.integers(300, 5000, 12)] + [257 + 24, 131072 + 24]
+    for i, L in enumerate(lens):
         s = rnd.choice(np.frombuffer(b"ACGT", dtype=np.uint8), L)
         s[rnd.integers(0, L, 2)] = ord("N")
         longs.append(b">long%d\n" % i + s.tobytes() + b"\n")
@@ -40,21 +44,28 @@ def _call(lib, table, rs, torch, dev):
     return (med.cpu().numpy().view(np.uint32), mean.cpu().numpy(), sd.cpu().numpy())
 
 
-def test_noalloc_matches_allocating_path_twice(ctx):
+def test_noalloc_matches_allocating_path_twice(ctx, oracle):
+    """Two calls in a row against the allocating entry point and against the
+    oracle's statistics of the same text (the long-read path of both entry
+    points shares its helpers, so the oracle is the independent check)."""
     torch = pytest.importorskip("torch")
     dev = torch.device(f"cuda:{ctx.device}")
     lib = native.load()
     text = _reads()
+    catalogue = text + text[:200000]
     table = KmerTable(ctx, 25, True)
-    table.count_text(text + text[:200000])
+    table.count_text(catalogue)
     rs = ReadSet(ctx, text)
-    assert rs.max_len > 280
+    assert rs.max_len == 131072 + 24
     want = coverage_stats(table, rs)
+    keys, counts = oracle.count(catalogue, 25, True)
+    om, oa, osd = oracle.cov_values(text, keys, counts, 25, True)
+    np.testing.assert_array_equal(want[0], om)
     for _ in range(2):
         got = _call(lib, table, rs, torch, dev)
-        np.testing.assert_array_equal(got[0], want[0])
-        np.testing.assert_array_equal(got[1].view(np.uint32), want[1].view(np.uint32))
-        np.testing.assert_array_equal(got[2].view(np.uint32), want[2].view(np.uint32))
+        for g, w, o in zip(got, want, (om, oa, osd)):
+            np.testing.assert_array_equal(g.view(np.uint32), w.view(np.uint32))
+            np.testing.assert_array_equal(g.view(np.uint32), o.view(np.uint32))
 
 
 def test_noalloc_rejects_reads_beyond_its_limit(ctx):

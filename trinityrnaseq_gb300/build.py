@@ -37,6 +37,7 @@ TOOL_SOURCES = {
     "seqtk-trinity": ["seqtk_trinity.cpp"],
     "insilico_read_normalization": ["insilico_read_normalization.cpp"],
     "FastaToDeBruijn": ["FastaToDeBruijn.cpp"],
+    "trinkmer_bins": ["trinkmer_bins.cpp"],
 }
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -63,6 +63,12 @@ static size_t big_cache_max() {
 }
 #define BIG_CACHE_MAX big_cache_max()
 
+uint64_t ctx_cached_bytes(const tk_ctx *c) {
+    uint64_t n = 0;
+    for (auto &b : c->big_free) n += b.second;
+    return n;
+}
+
 static void big_release(tk_ctx *c) {
     if (c->big_free.empty()) return;
     cudaStreamSynchronize(c->stream);

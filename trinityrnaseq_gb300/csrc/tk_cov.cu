@@ -412,9 +412,11 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
 // admission budget, or a pipeline that must not risk an allocation failure or
 // the implicit device synchronisation cudaMalloc/cudaFree can bring in the
 // middle of its work.  For them the long-read statistics use a fixed slab in
-// this file-scope device array instead of cudaMalloc'd scratch.  Every GPU
-// that loads the library holds the array (16 MiB) until the process exits.
-// Host code must not pass `g_noalloc_scratch` itself to a kernel: in host code
+// this file-scope device array instead of cudaMalloc'd scratch.  A GPU holds
+// the array (16 MiB) from the moment this file's device code is loaded on it
+// until the process exits; under lazy module loading that is the first launch
+// of one of its kernels or the first address lookup below, whichever comes
+// first.  Host code must not pass `g_noalloc_scratch` itself to a kernel: in host code
 // that name is a host-side stand-in, so its device address is fetched once per
 // device with cudaGetSymbolAddress (see noalloc_scratch_ptr).
 
@@ -442,8 +444,10 @@ __global__ void __launch_bounds__(CV_THREADS, 4) k_coverage_short(DevTable t, co
                               held + (threadIdx.x & ~31u));
 }
 
-// reads with more than 256 windows, one block per read, found by a strided scan
-// of all reads; block b works in slab b of the static array
+// Reads with more than 256 windows, one block per read; block b works in
+// slab b of the static array.  A block takes 256 reads at a time, one per
+// thread, lists the long ones in shared memory and then works through the
+// list, so finding the long reads costs one parallel pass over the reads.
 template <bool CANON>
 __global__ void __launch_bounds__(CV_THREADS) k_coverage_long_slab(DevTable t, const uint8_t *__restrict__ seq,
                                                                   const uint64_t *__restrict__ rd_off, uint64_t n_reads,
@@ -452,52 +456,68 @@ __global__ void __launch_bounds__(CV_THREADS) k_coverage_long_slab(DevTable t, c
                                                                   float *__restrict__ stdev) {
     __shared__ uint32_t s_cnt[CV_THREADS / 32];
     __shared__ uint64_t s_sum[CV_THREADS / 32], s_hi[CV_THREADS / 32], s_lo[CV_THREADS / 32];
+    __shared__ uint32_t s_list[CV_THREADS];
+    __shared__ uint32_t s_nlong;
     uint32_t *slab = scratch + (uint64_t)blockIdx.x * NOALLOC_SLAB;
-    for (uint64_t r = blockIdx.x; r < n_reads; r += gridDim.x) {
-        const uint64_t start = rd_off[r];
-        const uint64_t L = rd_off[r + 1] - start - 1;
-        if (L < (uint64_t)k || L - k + 1 <= CV_WARP_MAX) continue;   // uniform over the block
-        const uint32_t nwin = (uint32_t)(L - k + 1);
-        uint32_t n2 = 1;
-        while (n2 < nwin) n2 <<= 1;
-        // every slab entry read below is written first: nothing carries over between reads or calls
-        block_window_values<CANON>(seq, start, nwin, n2, k, slab, [&](uint64_t key) { return tbl_get(t, key, 1u); });
-        uint32_t cnt = 0;
-        uint64_t sum = 0, hi = 0, lo = 0;
-        for (uint32_t w = threadIdx.x; w < nwin; w += blockDim.x) {
-            uint32_t c = slab[w];
-            if (c == PAD_VAL) continue;
-            cnt++;
-            sum += c;
-            uint64_t sq = (uint64_t)c * c, nlo = lo + sq;
-            hi += nlo < lo;
-            lo = nlo;
-        }
-        cnt = warp_sum(cnt);
-        sum = warp_sum(sum);
-        warp_sum_u128(hi, lo);
-        if (lane_id() == 0) {
-            s_cnt[threadIdx.x >> 5] = cnt;
-            s_sum[threadIdx.x >> 5] = sum;
-            s_hi[threadIdx.x >> 5] = hi;
-            s_lo[threadIdx.x >> 5] = lo;
-        }
-        block_bitonic_sort(slab, n2);
-        if (threadIdx.x == 0) {
-            uint32_t tc = 0;
-            uint64_t ts = 0, th = 0, tl = 0;
-            for (int w = 0; w < CV_THREADS / 32; w++) {
-                tc += s_cnt[w];
-                ts += s_sum[w];
-                uint64_t nl = tl + s_lo[w];
-                th += s_hi[w] + (nl < tl);
-                tl = nl;
+    for (uint64_t base = (uint64_t)blockIdx.x * CV_THREADS; base < n_reads; base += (uint64_t)gridDim.x * CV_THREADS) {
+        if (threadIdx.x == 0) s_nlong = 0;
+        __syncthreads();
+        {
+            const uint64_t r = base + threadIdx.x;
+            if (r < n_reads) {
+                const uint64_t L = rd_off[r + 1] - rd_off[r] - 1;
+                if (L >= (uint64_t)k && L - k + 1 > CV_WARP_MAX) s_list[atomicAdd(&s_nlong, 1u)] = threadIdx.x;
             }
-            float m, s;
-            finish_stats(tc, ts, th, tl, &m, &s);
-            median[r] = tc ? slab[tc / 2] : 0u;
-            mean[r] = m;
-            stdev[r] = s;
+        }
+        __syncthreads();
+        const uint32_t n_long = s_nlong;
+        for (uint32_t li = 0; li < n_long; li++) {
+            const uint64_t r = base + s_list[li];
+            const uint64_t start = rd_off[r];
+            const uint64_t L = rd_off[r + 1] - start - 1;
+            const uint32_t nwin = (uint32_t)(L - k + 1);
+            uint32_t n2 = 1;
+            while (n2 < nwin) n2 <<= 1;
+            // every slab entry read below is written first: nothing carries over between reads or calls
+            block_window_values<CANON>(seq, start, nwin, n2, k, slab, [&](uint64_t key) { return tbl_get(t, key, 1u); });
+            uint32_t cnt = 0;
+            uint64_t sum = 0, hi = 0, lo = 0;
+            for (uint32_t w = threadIdx.x; w < nwin; w += blockDim.x) {
+                uint32_t c = slab[w];
+                if (c == PAD_VAL) continue;
+                cnt++;
+                sum += c;
+                uint64_t sq = (uint64_t)c * c, nlo = lo + sq;
+                hi += nlo < lo;
+                lo = nlo;
+            }
+            cnt = warp_sum(cnt);
+            sum = warp_sum(sum);
+            warp_sum_u128(hi, lo);
+            if (lane_id() == 0) {
+                s_cnt[threadIdx.x >> 5] = cnt;
+                s_sum[threadIdx.x >> 5] = sum;
+                s_hi[threadIdx.x >> 5] = hi;
+                s_lo[threadIdx.x >> 5] = lo;
+            }
+            block_bitonic_sort(slab, n2);
+            if (threadIdx.x == 0) {
+                uint32_t tc = 0;
+                uint64_t ts = 0, th = 0, tl = 0;
+                for (int w = 0; w < CV_THREADS / 32; w++) {
+                    tc += s_cnt[w];
+                    ts += s_sum[w];
+                    uint64_t nl = tl + s_lo[w];
+                    th += s_hi[w] + (nl < tl);
+                    tl = nl;
+                }
+                float m, s;
+                finish_stats(tc, ts, th, tl, &m, &s);
+                median[r] = tc ? slab[tc / 2] : 0u;
+                mean[r] = m;
+                stdev[r] = s;
+            }
+            __syncthreads();
         }
         __syncthreads();
     }

@@ -352,6 +352,7 @@ namespace tk {
 int set_err(tk_ctx *c, int code, const std::string &msg);
 int cuda_check(tk_ctx *c, cudaError_t e, const char *what);
 int dmalloc(tk_ctx *c, void **p, size_t bytes, const char *what);
+uint64_t ctx_cached_bytes(const tk_ctx *c);   // freed blocks the context keeps for reuse
 void dfree(tk_ctx *c, void *p);
 void prof_begin(tk_ctx *c, int kid, cudaEvent_t *ev);
 void prof_end(tk_ctx *c, int kid, cudaEvent_t ev, uint64_t units);

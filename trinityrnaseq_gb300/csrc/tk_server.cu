@@ -4,9 +4,10 @@
 // processes (trinity-plugins/ParaFly, Trinity:3652) and Perl threads running
 // two fastaToKmerCoverageStats at once (util/insilico_read_normalization.pl:
 // 853-854).  Here one resident process keeps a set of worker slots, each with
-// its own CUDA context stream, and admits queued jobs whenever a slot is free
-// and the job's HBM estimate fits the remaining budget (first queued job that
-// fits, so small jobs flow around a large one that waits for memory).  Jobs in
+// its own CUDA context stream, and admits queued jobs whenever a slot is free,
+// the job's HBM estimate fits the remaining budget and the GPU has that much
+// memory free (first queued job that fits, so small jobs flow around a large
+// one that waits for memory).  Jobs in
 // different slots run concurrently on the GPU.  Every job computes exactly
 // what the plain single-job calls compute, so a result does not depend on
 // what else was running.
@@ -54,6 +55,7 @@ struct tk_server {
     int running = 0;
     int max_running = 0;
     uint64_t batched_jobs = 0;               // jobs that ran inside a batched pass
+    uint64_t held_by_free = 0;               // admissions put off because the GPU had too little free memory
 };
 
 namespace {
@@ -260,6 +262,21 @@ int run_r2t(tk_ctx *c, Job &j) {
 constexpr size_t BATCH_JOBS = 64;
 constexpr uint64_t BATCH_BYTES = 256ULL << 20;
 
+// Device memory a job starting on slot context c can get now: what the GPU
+// reports free plus the blocks c keeps cached for reuse, less a margin for
+// the CUDA runtime's own needs.  Memory the other slots' running jobs have not
+// allocated yet is covered by the budget check; this check catches memory
+// held outside the budget (other processes, other slots' caches).
+uint64_t free_for(tk_ctx *c) {
+    size_t f = 0, t = 0;
+    if (!c || cudaMemGetInfo(&f, &t) != cudaSuccess) {
+        cudaGetLastError();
+        return ~0ULL;   // unknown: leave admission to the budget
+    }
+    const uint64_t avail = (uint64_t)f + tk::ctx_cached_bytes(c), margin = (uint64_t)t / 64;
+    return avail > margin ? avail - margin : 0;
+}
+
 void worker_loop(tk_server *s) {
     tk_ctx *c = nullptr;
     int ce = tk_ctx_create(s->device, &c);
@@ -272,11 +289,18 @@ void worker_loop(tk_server *s) {
                     if (c) tk_ctx_destroy(c);
                     return;
                 }
-                // first queued job that fits the remaining budget; a job
-                // larger than the whole budget runs when nothing else holds memory
+                // first queued job that fits both the remaining budget and the
+                // memory the GPU has free for this slot (its estimate is an
+                // upper bound of what it allocates); a job larger than either
+                // runs when nothing else is running
+                const uint64_t avail = s->queue.empty() ? 0 : free_for(c);
+                bool held = false;
                 for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
                     uint64_t need = std::min((*it)->est, s->budget);
-                    if (s->in_use + need <= s->budget) {
+                    const bool fits_budget = s->in_use + need <= s->budget;
+                    const bool fits_free = need <= avail || s->running == 0;
+                    if (fits_budget && !fits_free) held = true;
+                    if (fits_budget && fits_free) {
                         Job *j = *it;
                         s->queue.erase(it);
                         s->in_use += need;
@@ -285,12 +309,15 @@ void worker_loop(tk_server *s) {
                         break;
                     }
                 }
+                if (held) s->held_by_free++;
                 if (!batch.empty()) break;
                 s->cv_work.wait(lk);
             }
             // continuous batching: later count jobs of the same kind of input
             // join this one in a single batched pass while memory allows
             Job *head = batch[0];
+            const uint64_t fb = free_for(c);
+            const uint64_t avail_batch = fb == ~0ULL ? ~0ULL : s->in_use - head->est + fb;
             if (head->spec.kind == TK_JOB_COUNT && head->spec.len < BATCH_BYTES) {
                 uint64_t bytes = head->spec.len;
                 const char fmt = text_format(head->spec);
@@ -299,7 +326,8 @@ void worker_loop(tk_server *s) {
                     const tk_job_spec &q = j->spec;
                     uint64_t need = std::min(j->est, s->budget);
                     if (q.kind == TK_JOB_COUNT && q.k == head->spec.k && q.canonical == head->spec.canonical &&
-                        bytes + q.len <= BATCH_BYTES && text_format(q) == fmt && s->in_use + need <= s->budget) {
+                        bytes + q.len <= BATCH_BYTES && text_format(q) == fmt && s->in_use + need <= s->budget &&
+                        s->in_use + need <= avail_batch) {
                         it = s->queue.erase(it);
                         s->in_use += need;
                         j->est = need;
@@ -331,6 +359,8 @@ void worker_loop(tk_server *s) {
                 if (st[i]) j.error = tk_ctx_last_error(c);
             }
         }
+        // keep this slot's cache of freed blocks within its share of the budget
+        if (c && tk::ctx_cached_bytes(c) > s->budget / (uint64_t)s->slots) tk_ctx_trim(c);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             const auto t_done = clk::now();
@@ -444,6 +474,13 @@ int tk_server_stats(tk_server *s, uint64_t *budget, uint64_t *in_use, int *max_c
     if (budget) *budget = s->budget;
     if (in_use) *in_use = s->in_use;
     if (max_concurrent) *max_concurrent = s->max_running;
+    return TK_OK;
+}
+
+int tk_server_held_by_free_memory(tk_server *s, uint64_t *admissions) {
+    if (!s || !admissions) return TK_E_INVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *admissions = s->held_by_free;
     return TK_OK;
 }
 

@@ -126,6 +126,7 @@ SIGNATURES.update({
     "tk_server_stats": (C.c_int, [vp, P(u64), P(u64), P(C.c_int)]),
     "tk_server_destroy": (None, [vp]),
     "tk_server_batched_jobs": (C.c_int, [vp, P(u64)]),
+    "tk_server_held_by_free_memory": (C.c_int, [vp, P(u64)]),
 })
 
 

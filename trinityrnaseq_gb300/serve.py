@@ -91,6 +91,12 @@ class Server:
         N.check(self.lib.tk_server_batched_jobs(self.h, C.byref(n)), "tk_server_batched_jobs")
         return n.value
 
+    def held_by_free_memory(self) -> int:
+        """Admission passes that left a job queued for lack of free GPU memory."""
+        n = C.c_uint64()
+        N.check(self.lib.tk_server_held_by_free_memory(self.h, C.byref(n)), "tk_server_held_by_free_memory")
+        return n.value
+
     def stats(self) -> Tuple[int, int, int]:
         b, u, m = C.c_uint64(), C.c_uint64(), C.c_int()
         N.check(self.lib.tk_server_stats(self.h, C.byref(b), C.byref(u), C.byref(m)), "tk_server_stats")
