@@ -270,6 +270,52 @@ class GpuPipeline:
         return windows, reads, h2d, d2h, packed, capacity, selected, ext
 
 
+def numa_nodes_of(addr: int) -> dict:
+    """Pages per NUMA node of the host mapping holding `addr` (/proc/self/numa_maps)."""
+    try:
+        best = None
+        for line in open("/proc/self/numa_maps"):
+            f = line.split()
+            if int(f[0], 16) <= addr and (best is None or int(f[0], 16) > int(best[0], 16)):
+                best = f
+        if best is None:
+            return {}
+        return {kv.split("=")[0]: int(kv.split("=")[1]) for kv in best if kv.startswith("N") and "=" in kv}
+    except Exception:
+        return {}
+
+
+def gpu_numa_node(device: int):
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(device), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=20).stdout.strip().lower()
+        dom, rest = bus.split(":", 1)
+        return int(open(f"/sys/bus/pci/devices/{dom[-4:]}:{rest}/numa_node").read())
+    except Exception:
+        return None
+
+
+def link_rates(pipe):
+    """H2D and D2H GB/s of the end-to-end step's own page-locked buffers (one
+    copy of a mate file each way, CUDA events), and their NUMA placement."""
+    import torch
+    h = pipe.h_left
+    d = torch.empty(h.numel(), dtype=torch.uint8, device=pipe.dev)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    d.copy_(h, non_blocking=True)
+    e[1].record()
+    h.copy_(d, non_blocking=True)
+    e[2].record()
+    torch.cuda.synchronize()
+    n = h.numel()
+    out = {"h2d_gbs": n / (e[0].elapsed_time(e[1]) / 1e3) / 1e9, "d2h_gbs": n / (e[1].elapsed_time(e[2]) / 1e3) / 1e9,
+           "host_buffer_numa_pages": numa_nodes_of(h.data_ptr()), "gpu_numa_node": gpu_numa_node(pipe.dev.index)}
+    del d
+    return out
+
+
 def timed(pipe, stream, steps, e2e, dist):
     import torch
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -316,6 +362,7 @@ def run_gpu(args, dist, world, rank, local):
     # end-to-end timed region (host FASTQ in, dump text + stats out)
     ms_e2e, res_e2e = timed(pipe, stream, args.steps, True, dist)
     windows, reads = res[0][0], res[0][1]
+    link = link_rates(pipe)
     t_step = dist.max(statistics.mean(ms)) / 1e3
     t_e2e = dist.max(statistics.mean(ms_e2e)) / 1e3
     tot_windows = dist.sum(windows)
@@ -394,7 +441,9 @@ def run_gpu(args, dist, world, rank, local):
             "e2e": {"value": tot_windows / t_e2e, "unit": UNIT, "reads_per_s": tot_reads / t_e2e,
                     "ms_per_step": t_e2e * 1e3, "ms_steps": [round(x, 2) for x in ms_e2e],
                     "h2d_bytes_per_step": res_e2e[0][2],
-                    "d2h_bytes_per_step": res_e2e[0][3]},
+                    "d2h_bytes_per_step": res_e2e[0][3],
+                    "h2d_gbs_per_step": res_e2e[0][2] / t_e2e / 1e9, "d2h_gbs_per_step": res_e2e[0][3] / t_e2e / 1e9,
+                    "link": link, "ratio_to_device": t_e2e / t_step},
             "roofline": kernels[top],
             "roofline_kernels": kernels,
             "kernels_ms_per_step": {k: v[0] for k, v in per_step.items()},
@@ -415,7 +464,11 @@ def run_gpu(args, dist, world, rank, local):
         if args.dbg and world == 1:
             out["debruijn"] = dbg_bench(ctx, args)
         if args.bins and world == 1:
-            out["batched"] = batched_bench(ctx, args)
+            out["batched"] = batched_bench(ctx, args, args.bins)
+        if args.bins_total and world == 1:
+            # the configuration's other reading: the same distribution with as
+            # many bins as its stated ~60M-read total takes
+            out["batched_60M_reads"] = batched_bench(ctx, args, args.bins_total, sample_every=997)
         if args.jobs and world == 1:
             out["served"] = served_bench(ctx, args)
     ctx.close()
@@ -775,44 +828,62 @@ def dbg_bench(ctx, args):
 
 # ---------------------------------------------------------------- batched and served
 
-def batched_bench(ctx, args):
+def batched_bench(ctx, args, n_bins, sample_every=97):
     """Per-bin counting + dump of power-law read bins (alpha 1.8, 50..200,000
     reads, 100 nt, 1% error, each from its own 1-20-transcript locus): one
-    batched call (tk_count_bins; median of three after a warm-up call)
-    against one plain count + dump per bin, both from host FASTA to host dump
-    text."""
+    batched call (tk_count_bins; median of three after a warm-up call) from a
+    page-locked host FASTA to a page-locked host dump text, against one plain
+    count + dump per bin (the way ParaFly runs one Trinity per bin).  Every
+    `sample_every`-th bin's dump is compared byte for byte."""
+    import torch
     from trinityrnaseq_gb300 import KmerTable, synth
     from trinityrnaseq_gb300.kmer import count_bins
     t0 = time.time()
-    text, off, nreads = synth.power_law_bins(seed=SEED + 7, n_bins=args.bins, alpha=1.8, min_reads=50,
+    text, off, nreads = synth.power_law_bins(seed=SEED + 7, n_bins=n_bins, alpha=1.8, min_reads=50,
                                              max_reads=200_000, read_len=100, err=0.01)
-    log(f"batched: {args.bins} bins, {int(nreads.sum())} reads ({text.nbytes / 1e9:.2f} GB) in {time.time() - t0:.1f}s")
-    t = text.tobytes()
-    count_bins(ctx, t, off, K, True, 1)   # warm-up: block-shape autotune and the batch's device buffers
+    log(f"batched: {n_bins} bins, {int(nreads.sum())} reads ({text.nbytes / 1e9:.2f} GB) in {time.time() - t0:.1f}s")
+    t_text = torch.from_numpy(text).pin_memory()   # the tensors own the page-locked memory
+    h_text = t_text.numpy()
+    del text
+    dump, toff, kmers = count_bins(ctx, h_text, off, K, True, 1)   # warm-up: autotune, device buffers
+    t_out = torch.empty(len(dump) + 16, dtype=torch.uint8).pin_memory()
+    h_out = t_out.numpy()
     ts = []
     for _ in range(3):
         tb = time.time()
-        dump, toff, kmers = count_bins(ctx, t, off, K, True, 1)
+        dump, toff, kmers = count_bins(ctx, h_text, off, K, True, 1, out=h_out)
         ts.append(time.time() - tb)
     t_batched = statistics.median(ts)
-    # plain: one count + dump per bin, the way ParaFly runs one Trinity per bin
+    # per-phase device times of one more call (CUDA events around each phase)
+    ctx.set_profiling(True)
+    ctx.reset_profile()
+    tb = time.time()
+    count_bins(ctx, h_text, off, K, True, 1, out=h_out)
+    wall = time.time() - tb
+    phases = {name: ctx.profile(kid)[0] for name, kid in (("parse", "parse"), ("sketch", "hll"), ("count", "bins"),
+                                                          ("compact", "compact"), ("sort", "sort"), ("format", "dump"))}
+    ctx.set_profiling(False)
+    phases["host_and_copies"] = wall * 1e3 - sum(phases.values())
+    # plain: one count + dump per bin
     tp = time.time()
     same = True
-    for b in range(args.bins):
-        bt = t[int(off[b]):int(off[b + 1])]
+    for b in range(n_bins):
+        bt = h_text[int(off[b]):int(off[b + 1])]
         tab = KmerTable(ctx, K, True)
         tab.count_text(bt)
         d = tab.dump_fasta(1)
         tab.free()
-        if b % 97 == 0:
-            same &= d == dump[int(toff[b]):int(toff[b + 1])]
+        if b % sample_every == 0:
+            same &= d == bytes(dump[int(toff[b]):int(toff[b + 1])])
     t_plain = time.time() - tp
-    return {"workload": f"{args.bins} power-law bins (alpha 1.8, 50..200000 reads), 100 nt, 1% error; "
-                        "count + dump -L 1 per bin, host FASTA in, host dump text out",
-            "reads": int(nreads.sum()), "kmers": int(kmers), "batched_s": t_batched, "plain_s": t_plain,
+    return {"workload": f"{n_bins} power-law bins (alpha 1.8, 50..200000 reads), 100 nt, 1% error; "
+                        "count + dump -L 1 per bin, page-locked host FASTA in, host dump text out",
+            "bins": n_bins, "reads": int(nreads.sum()), "kmers": int(kmers), "batched_s": t_batched, "plain_s": t_plain,
             "batched_kmers_per_s": kmers / t_batched, "plain_kmers_per_s": kmers / t_plain,
             "batched_reads_per_s": float(nreads.sum()) / t_batched, "plain_reads_per_s": float(nreads.sum()) / t_plain,
-            "speedup_vs_plain": t_plain / t_batched, "sampled_bins_identical": bool(same)}
+            "speedup_vs_plain": t_plain / t_batched, "sampled_bins_identical": bool(same),
+            "bins_compared": (n_bins + sample_every - 1) // sample_every,
+            "phases_ms": {k: round(v, 2) for k, v in phases.items()}}
 
 
 def served_bench(ctx, args):
@@ -890,7 +961,9 @@ def served_bench(ctx, args):
         return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
 
     levels = {}
-    for load in (0.5, 1.0, 1.5, float("inf")):
+    # 0.5x, 1x and 1.5x the plain capacity (the configuration's loads); 3x is
+    # above what the server itself sustains, so jobs queue and batch
+    for load in (0.5, 1.0, 1.5, 3.0, float("inf")):
         # inf: every job submitted at once (the server's saturated throughput)
         gaps = rng.exponential(1.0 / (capacity * load), size=len(jobs)) if load != float("inf") else [0.0] * len(jobs)
         with Server(ctx.device, slots=args.slots, hbm_budget=int(args.budget_gb * 1e9)) as srv:
@@ -921,13 +994,14 @@ def served_bench(ctx, args):
                 srv.release(jid)
             maxc = srv.stats()[2]
             nbatched = srv.batched_jobs()
+            held = srv.held_by_free_memory()
         lat.sort()
         name = "burst" if load == float("inf") else f"{load}x"
         levels[name] = {"offered_jobs_per_s": capacity * load if load != float("inf") else None,
                         "jobs_per_s": len(jobs) / wall,
                               "reads_per_s": total_reads / wall, "p50_ms": lat[len(lat) // 2],
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_concurrent": maxc,
-                              "jobs_in_batched_passes": nbatched,
+                              "jobs_in_batched_passes": nbatched, "admissions_held_by_free_hbm": held,
                               "bit_exact_vs_plain": bool(ok)}
     return {"workload": f"{len(jobs)} jobs (60% count, 30% normalize with selection and extraction, "
                         f"10% read-to-component), reads log-uniform "
@@ -1082,7 +1156,9 @@ def main():
     ap.add_argument("--r2t_pairs", type=int, default=50_000_000, help="read pairs of the read -> component leg")
     ap.add_argument("--dbg", type=int, default=1, help="per-component de Bruijn graph leg (0 = skip)")
     ap.add_argument("--bins", type=int, default=5000, help="batched-bins comparison (0 = skip)")
-    ap.add_argument("--jobs", type=int, default=200, help="served-stream comparison (0 = skip)")
+    ap.add_argument("--bins-total", type=int, default=70000,
+                    help="batched bins at the configuration's ~60M-read total (0 = skip)")
+    ap.add_argument("--jobs", type=int, default=400, help="served-stream comparison (0 = skip)")
     ap.add_argument("--job-max-reads", type=int, default=2_000_000)
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--budget-gb", type=float, default=150.0)

@@ -363,6 +363,7 @@ static void ctx_release_now(tk_ctx *c) {
     }
     for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : c->free_events) cudaEventDestroy(e);
+    if (c->bins_exec) cudaGraphExecDestroy(c->bins_exec);
     cudaFree(c->d_err);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     cudaMemPool_t pool;

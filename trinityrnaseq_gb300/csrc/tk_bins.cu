@@ -14,7 +14,8 @@
 //     block size is picked by timing candidates on the first batch;
 //  4. one persistent counting launch over all bins, captured in a CUDA graph
 //     together with the slice fill (re-launched when a slice overflows, with
-//     that slice doubled);
+//     that slice doubled); the context keeps the executable graph and each
+//     later batch updates it in place rather than instantiating it again;
 //  5. one compaction of every slice into (bin << 2k | key, count), one radix
 //     sort, one K4 formatting pass; bin b's dump is a contiguous byte range.
 //
@@ -340,9 +341,12 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
         if (n) {
             const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 256 * BC_SPAN - 1) / (256 * BC_SPAN),
                                                                                      (uint64_t)c->sm_count * 8));
+            cudaEvent_t ev;
+            prof_begin(c, TK_KID_HLL, &ev);
             if (canonical) k_bin_sketch<true><<<grid, 256, 0, c->stream>>>(r.d_seq, n, k, d_seq0, n_bins, d_regs, d_win);
             else k_bin_sketch<false><<<grid, 256, 0, c->stream>>>(r.d_seq, n, k, d_seq0, n_bins, d_regs, d_win);
             c->launches++;
+            prof_end(c, TK_KID_HLL, ev, n);
         }
         e = cuda_check(c, cudaMemcpyAsync(regs.data(), d_regs, regs.size() * 4, cudaMemcpyDeviceToHost, c->stream), "sketch d2h");
         if (!e) e = cuda_check(c, cudaMemcpyAsync(win.data(), d_win, n_bins * 8, cudaMemcpyDeviceToHost, c->stream), "windows d2h");
@@ -417,10 +421,21 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
             else launch_count<false>(c, block, r.d_seq, n, k, g, slots, d_ovf);
         }
         e = cuda_check(c, cudaStreamEndCapture(c->stream, &graph), "capture end");
-        if (!e) e = cuda_check(c, cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+        // the context's executable graph takes this batch's parameters in
+        // place (same two nodes, new pointers and sizes); a refused update
+        // means a new instantiation
+        if (!e && c->bins_exec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(c->bins_exec, graph, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(c->bins_exec);
+                c->bins_exec = nullptr;
+            }
+        }
+        if (!e && !c->bins_exec) e = cuda_check(c, cudaGraphInstantiate(&c->bins_exec, graph, 0), "graph instantiate");
+        if (!e) exec = c->bins_exec;
         if (!e) e = cuda_check(c, cudaGraphLaunch(exec, c->stream), "graph launch");
         prof_end(c, TK_KID_BINS, ev, kmers);
-        if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (!e) e = cuda_check(c, cudaMemcpyAsync(ovf.data(), d_ovf, n_bins * 4, cudaMemcpyDeviceToHost, c->stream), "ovf d2h");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "bins count sync");

@@ -44,65 +44,80 @@ constexpr uint32_t CV_WARP_MAX = 256;   // windows handled by the warp path
 struct CovCache {
     uint64_t *ent;     // 4 entries per bucket; nullptr = no cache
     int n;             // key bits (2k)
-    int rbits;         // hash bits an entry keeps; the other 64 - rbits hold the count
+    int rbits;         // hash bits below the bucket index (<= 32): an entry is (those bits << 32) | count
 };
 
-// A bijection of [0, 2^n): xor-shifts and multiplications by odd constants,
-// each invertible modulo 2^n, so (bucket, remainder) identifies the key.
-__host__ __device__ __forceinline__ uint64_t kmix_n(uint64_t x, int n) {
-    const uint64_t m = (1ULL << n) - 1;   // n <= 62
-    const int s = (n + 1) >> 1;
-    x ^= x >> s;
-    x = (x * 0x9E3779B97F4A7C15ULL) & m;
-    x ^= x >> s;
-    x = (x * 0xD6E8FEB86659FD93ULL) & m;
-    x ^= x >> s;
-    return x;
+// A bijection of [0, 2^n) (n <= 62): a three-round Feistel network over the
+// key's two halves with 32-bit multiply-xorshift round functions, so every
+// step (xor of one half with a function of the other) is invertible and the
+// (bucket, remainder) pair identifies the key.  32-bit arithmetic keeps it to
+// a dozen instructions.
+__host__ __device__ __forceinline__ uint32_t feistel_f(uint32_t x, uint32_t m) {
+    x *= m;
+    return x ^ (x >> 15);
 }
 
-__device__ __forceinline__ bool cache_get(const CovCache &cc, uint64_t key, uint32_t *val) {
+__host__ __device__ __forceinline__ uint64_t kmix_n(uint64_t key, int n) {
+    const int hl = n >> 1, hh = n - hl;   // 1 <= hl <= hh <= 31
+    const uint32_t ml = (uint32_t)((1ULL << hl) - 1), mh = (uint32_t)((1ULL << hh) - 1);
+    uint32_t lo = (uint32_t)key & ml, hi = (uint32_t)(key >> hl) & mh;
+    lo ^= feistel_f(hi, 0x9E3779B1u) & ml;
+    hi ^= feistel_f(lo, 0x85EBCA77u) & mh;
+    lo ^= feistel_f(hi, 0xC2B2AE3Du) & ml;
+    return ((uint64_t)hi << hl) | lo;
+}
+
+// The cache's bucket of `key` and the 32-bit tag its entry carries.
+__device__ __forceinline__ const uint64_t *cache_bucket(const CovCache &cc, uint64_t key, uint32_t *tag) {
     const uint64_t h = kmix_n(key, cc.n);
-    const uint64_t *b = cc.ent + ((h >> cc.rbits) << 2);
-    const uint64_t r = h & ((1ULL << cc.rbits) - 1);
-    const int cbits = 64 - cc.rbits;
+    *tag = (uint32_t)(h & ((1ULL << cc.rbits) - 1));
+    return cc.ent + ((h >> cc.rbits) << 2);
+}
+
+// the count of the bucket entry tagged `tag`, or 0 (an entry's count is >= 2,
+// so an empty entry matches nothing)
+__device__ __forceinline__ uint32_t cache_match(const uint64_t *b, uint32_t tag) {
     uint64_t e0, e1, e2, e3, pol;
     // L2 evict-last: the cache's lines outlive the table lines streamed past them
     asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
     asm("ld.global.L2::cache_hint.v4.u64 {%0,%1,%2,%3}, [%4], %5;"
         : "=l"(e0), "=l"(e1), "=l"(e2), "=l"(e3)
         : "l"(b), "l"(pol));
-    // an entry is never 0 (its count is >= 2), so an empty entry matches nothing
-    uint64_t hit = 0;
-    hit = (e0 && (e0 >> cbits) == r) ? e0 : hit;
-    hit = (e1 && (e1 >> cbits) == r) ? e1 : hit;
-    hit = (e2 && (e2 >> cbits) == r) ? e2 : hit;
-    hit = (e3 && (e3 >> cbits) == r) ? e3 : hit;
-    *val = (uint32_t)(hit & (~0ULL >> cc.rbits));
-    return hit != 0;
+    uint32_t c = 0;
+    c = (uint32_t)(e0 >> 32) == tag ? (uint32_t)e0 : c;
+    c = (uint32_t)(e1 >> 32) == tag ? (uint32_t)e1 : c;
+    c = (uint32_t)(e2 >> 32) == tag ? (uint32_t)e2 : c;
+    c = (uint32_t)(e3 >> 32) == tag ? (uint32_t)e3 : c;
+    return c;
 }
 
 // the count of `key` for the statistics: the cache, else the table (1 when absent)
 __device__ __forceinline__ uint32_t cov_lookup(const CovCache &cc, DevTable t, uint64_t key) {
-    uint32_t v;
-    if (cc.ent && cache_get(cc, key, &v)) return v;
+    if (cc.ent) {
+        uint32_t tag;
+        const uint64_t *b = cache_bucket(cc, key, &tag);
+        const uint32_t v = cache_match(b, tag);
+        if (v) return v;
+    }
     return tbl_get(t, key, 1u);
 }
 
 // Offers one (key, count) to its bucket: into an empty entry, else in place
 // of the smallest count when larger.  A CAS lost to another thread re-reads
 // the bucket; after 32 rounds the key is left out (the cache stays valid).
-__device__ __forceinline__ void cache_offer(const CovCache &cc, uint64_t key, uint64_t count) {
-    const uint64_t h = kmix_n(key, cc.n);
-    unsigned long long *b = reinterpret_cast<unsigned long long *>(cc.ent + ((h >> cc.rbits) << 2));
-    const uint64_t cmask = ~0ULL >> cc.rbits;
-    const unsigned long long mine = ((h & ((1ULL << cc.rbits) - 1)) << (64 - cc.rbits)) | count;
+__device__ __forceinline__ void cache_offer(const CovCache &cc, uint64_t key, uint32_t count) {
+    uint32_t tag;
+    unsigned long long *b =
+        reinterpret_cast<unsigned long long *>(const_cast<uint64_t *>(cache_bucket(cc, key, &tag)));
+    const unsigned long long mine = ((unsigned long long)tag << 32) | count;
     for (int round = 0; round < 32; round++) {
         int at = 0;
-        unsigned long long old = 0, least = ~0ULL;
+        unsigned long long old = 0;
+        uint32_t least = ~0u;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const unsigned long long e = *reinterpret_cast<volatile unsigned long long *>(b + j);
-            const unsigned long long c = e ? (e & cmask) : 0ULL;
+            const uint32_t c = (uint32_t)e;   // 0 for an empty entry
             if (c < least) {
                 least = c;
                 at = j;
@@ -116,11 +131,10 @@ __device__ __forceinline__ void cache_offer(const CovCache &cc, uint64_t key, ui
 
 __global__ void __launch_bounds__(256) k_cache_build(const Slot *__restrict__ slots, uint64_t cap, CovCache cc) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t cmask = ~0ULL >> cc.rbits;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += stride) {
         const ulonglong2 s = __ldcs(reinterpret_cast<const ulonglong2 *>(slots + i));
-        const uint64_t c = (uint32_t)s.y;
-        if (s.x == EMPTY_KEY || c < 2 || c > cmask) continue;
+        const uint32_t c = (uint32_t)s.y;
+        if (s.x == EMPTY_KEY || c < 2) continue;
         cache_offer(cc, s.x, c);
     }
 }
@@ -141,7 +155,7 @@ static int cache_get_or_build(tk_table *t, CovCache *cc) {
     int hbits = 0;
     while ((32ULL << (hbits + 1)) <= want) hbits++;
     const int n = 2 * t->k;
-    if (n - hbits < 1 || 64 - (n - hbits) < 2) return TK_OK;
+    if (n - hbits < 1 || n - hbits > 32) return TK_OK;   // tiny key spaces; k > 26 at 64 MB
     const uint64_t bytes = 32ULL << hbits;
     cc->n = n;
     cc->rbits = n - hbits;
@@ -174,38 +188,160 @@ struct ReadSums {
 };
 constexpr uint32_t LONG_READ = 0xFFFFFFFFu;   // cnt of a read left to the long-read pass
 
+// A read's windows in three stages.  Stage 1: the lane's keys and their
+// validity, and the cache's count for each (0 = not in the cache).  Stage 2:
+// the table for the windows the cache did not answer.  Stage 3: the read's
+// statistics.  The lookups of a stage are independent loads issued together.
+template <int S, bool CANON>
+__device__ __forceinline__ void cov_stage1(const CovCache &cc, const uint64_t *__restrict__ codes,
+                                           const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin, int k,
+                                           uint64_t (&key)[S], uint32_t (&v)[S], uint32_t &vm) {
+    const uint32_t span = (nwin + 31) / 32;
+    vm = 0;
+    lane_windows_codes<S, CANON>(codes, inv, start, nwin, span, k, [&](int j, bool valid, uint64_t kk) {
+        key[j] = kk;
+        vm |= (valid ? 1u : 0u) << j;
+    });
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+        v[j] = 0;
+        if (cc.ent && ((vm >> j) & 1u)) {
+            uint32_t tag;
+            const uint64_t *b = cache_bucket(cc, key[j], &tag);
+            v[j] = cache_match(b, tag);
+        }
+    }
+}
+
+template <int S>
+__device__ __forceinline__ void cov_stage2(DevTable t, const uint64_t (&key)[S], uint32_t (&v)[S], uint32_t vm) {
+#pragma unroll
+    for (int j = 0; j < S; j++)
+        if (((vm >> j) & 1u) && v[j] == 0) v[j] = tbl_get(t, key[j], 1u);
+}
+
+template <int S>
+__device__ __forceinline__ ReadSums cov_stage3(const uint32_t (&v)[S], uint32_t vm) {
+    ReadSums rs;
+    rs.cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(vm));
+    uint32_t lmax = 0;
+#pragma unroll
+    for (int j = 0; j < S; j++)
+        if ((vm >> j) & 1u) lmax = max(lmax, v[j]);
+    const uint32_t mx = __reduce_max_sync(0xffffffffu, lmax);
+    if (mx < (1u << 23)) {
+        // every count below 2^23: a lane's sum fits 32 bits and its sum of
+        // squares 64 bits, and the warp totals (< 2^31 and < 2^54) are exact
+        // through warp-wide adds of 16-bit pieces
+        uint32_t sum = 0;
+        uint64_t sq = 0;
+#pragma unroll
+        for (int j = 0; j < S; j++)
+            if ((vm >> j) & 1u) {
+                sum += v[j];
+                sq += (uint64_t)v[j] * v[j];
+            }
+        rs.sum = __reduce_add_sync(0xffffffffu, sum);
+        const uint64_t q0 = __reduce_add_sync(0xffffffffu, (uint32_t)(sq & 0xFFFF));
+        const uint64_t q1 = __reduce_add_sync(0xffffffffu, (uint32_t)((sq >> 16) & 0xFFFF));
+        const uint64_t q2 = __reduce_add_sync(0xffffffffu, (uint32_t)((sq >> 32) & 0xFFFF));
+        const uint64_t q3 = __reduce_add_sync(0xffffffffu, (uint32_t)(sq >> 48));
+        rs.lo = q0 + (q1 << 16) + (q2 << 32) + (q3 << 48);
+        rs.hi = 0;
+    } else {
+        uint64_t sum = 0, hi = 0, lo = 0;
+#pragma unroll
+        for (int j = 0; j < S; j++)
+            if ((vm >> j) & 1u) {
+                sum += v[j];
+                const uint64_t sq = (uint64_t)v[j] * v[j], nlo = lo + sq;
+                hi += nlo < lo;
+                lo = nlo;
+            }
+        rs.sum = warp_sum(sum);
+        warp_sum_u128(hi, lo);
+        rs.hi = hi;
+        rs.lo = lo;
+    }
+    rs.med = rs.cnt ? warp_select<S>(v, vm, rs.cnt / 2, mx) : 0u;
+    return rs;
+}
+
 template <int S, bool CANON>
 __device__ __forceinline__ ReadSums cov_warp_read(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
                                                   const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin,
                                                   int k) {
-    const uint32_t span = (nwin + 31) / 32;
-    uint32_t v[S];
-    uint32_t vm = 0;
-    uint32_t cnt = 0;
-    uint64_t sum = 0, hi = 0, lo = 0;
-    lane_windows_codes<S, CANON>(codes, inv, start, nwin, span, k, [&](int j, bool valid, uint64_t key) {
-        uint32_t c = 0;
-        if (valid) {
-            c = cov_lookup(cc, t, key);
-            vm |= 1u << j;
-            cnt++;
-            sum += c;
-            uint64_t sq = (uint64_t)c * c;   // < 2^64
-            uint64_t nlo = lo + sq;
-            hi += nlo < lo;
-            lo = nlo;
-        }
-        v[j] = c;
-    });
-    ReadSums rs;
-    rs.cnt = warp_sum(cnt);
-    rs.sum = warp_sum(sum);
-    warp_sum_u128(hi, lo);
-    rs.hi = hi;
-    rs.lo = lo;
-    rs.med = rs.cnt ? warp_select<S>(v, vm, rs.cnt / 2) : 0u;
-    return rs;
+    uint64_t key[S];
+    uint32_t v[S], vm;
+    cov_stage1<S, CANON>(cc, codes, inv, start, nwin, k, key, v, vm);
+    cov_stage2<S>(t, key, v, vm);
+    return cov_stage3<S>(v, vm);
 }
+
+// Pipelined form of the stages for a chunk of one window class S (S <= 4:
+// reads of up to 128 windows).  Stage 1 of read i+1 (keys, cache answers)
+// also issues an L2 prefetch of the table slot of every window the cache did
+// not answer; the table lookups of read i+1 run only after the statistics of
+// read i, by which time those slots have arrived.  Nothing of a read but its
+// counts and masks stays in registers between its stages: the table stage
+// cuts its keys from the codes again.
+template <int S, bool CANON>
+__device__ __forceinline__ void cov_pstage1(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
+                                            const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin, int k,
+                                            uint32_t (&v)[S], uint32_t &vm, uint32_t &miss) {
+    uint64_t key[S];
+    cov_stage1<S, CANON>(cc, codes, inv, start, nwin, k, key, v, vm);
+    miss = 0;
+#pragma unroll
+    for (int j = 0; j < S; j++)
+        if (((vm >> j) & 1u) && v[j] == 0) {
+            miss |= 1u << j;
+            const Slot *p = &t.slots[tbl_home(t, mix64(key[j]))];
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+        }
+}
+
+template <int S, bool CANON>
+__device__ __forceinline__ void cov_pstage2(DevTable t, const uint64_t *__restrict__ codes,
+                                            const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin, int k,
+                                            uint32_t (&v)[S], uint32_t miss) {
+    if (!__any_sync(0xffffffffu, miss != 0)) return;
+    const uint32_t span = (nwin + 31) / 32;
+    lane_windows_codes<S, CANON>(codes, inv, start, nwin, span, k, [&](int j, bool, uint64_t key) {
+        if ((miss >> j) & 1u) v[j] = tbl_get(t, key, 1u);
+    });
+}
+
+template <int S, bool CANON, typename ST, typename NW>
+__device__ __forceinline__ void cov_chunk_pipelined(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
+                                                    const uint32_t *__restrict__ inv, uint32_t nr, int k, ST &&starts,
+                                                    NW &&nwins, ReadSums *__restrict__ held) {
+    const unsigned lane = lane_id();
+    uint32_t vA[S], vB[S], mA, mB, xA, xB;
+    cov_pstage1<S, CANON>(cc, t, codes, inv, starts(0), nwins(0), k, vA, mA, xA);
+    for (uint32_t i = 0; i < nr; i += 2) {
+        if (i + 1 < nr) cov_pstage1<S, CANON>(cc, t, codes, inv, starts(i + 1), nwins(i + 1), k, vB, mB, xB);
+        cov_pstage2<S, CANON>(t, codes, inv, starts(i), nwins(i), k, vA, xA);
+        const ReadSums ra = cov_stage3<S>(vA, mA);
+        if (lane == 0) held[i] = ra;
+        if (i + 1 < nr) {
+            if (i + 2 < nr) cov_pstage1<S, CANON>(cc, t, codes, inv, starts(i + 2), nwins(i + 2), k, vA, mA, xA);
+            cov_pstage2<S, CANON>(t, codes, inv, starts(i + 1), nwins(i + 1), k, vB, xB);
+            const ReadSums rb = cov_stage3<S>(vB, mB);
+            if (lane == 0) held[i + 1] = rb;
+        }
+    }
+}
+
+// window class of a read: the registers per lane its windows need (9 = long)
+__device__ __forceinline__ uint32_t cov_class(uint32_t nwin) {
+    return nwin <= 32 ? 1u : nwin <= 64 ? 2u : nwin <= 96 ? 3u : nwin <= 128 ? 4u : nwin <= 192 ? 6u
+           : nwin <= CV_WARP_MAX ? 8u : 9u;
+}
+
+// chunks whose reads share a class of at most this many registers per lane
+// take the pipelined path
+constexpr uint32_t CV_PIPE_MAX_CLASS = 4;
 
 // One warp, 32 consecutive reads [r0, r0 + 32): the warp computes each read's
 // sums in turn and lane i keeps read r0 + i's; then every lane finishes its own
@@ -227,7 +363,25 @@ __device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, c
     const uint64_t my_start = rd_off[r0 + (lane < nr ? lane : nr)];
     const uint64_t last_end = __shfl_sync(0xffffffffu, my_start, (int)(nr < 32 ? nr : 31));
     const uint64_t end_nr = nr < 32 ? last_end : rd_off[r0 + 32];
-    for (uint32_t i = 0; i < nr; i++) {
+    // lane i's read: its window count and class; a chunk of one class takes
+    // the pipelined path
+    const uint64_t my_next = lane + 1 < nr ? __shfl_down_sync(0xffffffffu, my_start, 1) : end_nr;
+    const uint64_t my_len = lane < nr ? my_next - my_start - 1 : 0;
+    const uint32_t my_nwin = my_len >= (uint64_t)k ? (uint32_t)(my_len - k + 1) : 0u;
+    const uint32_t cls0 = __shfl_sync(0xffffffffu, cov_class(my_nwin), 0);
+    const bool one_class =
+        __all_sync(0xffffffffu, lane >= nr || cov_class(my_nwin) == cls0) && cls0 <= CV_PIPE_MAX_CLASS;
+    if (one_class) {
+        auto starts = [&](uint32_t i) { return __shfl_sync(0xffffffffu, my_start, (int)i); };
+        auto nwins = [&](uint32_t i) { return __shfl_sync(0xffffffffu, my_nwin, (int)i); };
+        switch (cls0) {
+        case 1: cov_chunk_pipelined<1, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
+        case 2: cov_chunk_pipelined<2, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
+        case 3: cov_chunk_pipelined<3, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
+        default: cov_chunk_pipelined<4, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
+        }
+    }
+    for (uint32_t i = 0; !one_class && i < nr; i++) {
         const uint64_t r = r0 + i;
         const uint64_t start = __shfl_sync(0xffffffffu, my_start, (int)i);
         const uint64_t next = i + 1 < 32 ? __shfl_sync(0xffffffffu, my_start, (int)(i + 1) & 31) : end_nr;
@@ -237,7 +391,9 @@ __device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, c
         bool is_long = false;
         if (nwin <= 32) rs = cov_warp_read<1, CANON>(cc, t, codes, inv, start, nwin, k);
         else if (nwin <= 64) rs = cov_warp_read<2, CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (nwin <= 96) rs = cov_warp_read<3, CANON>(cc, t, codes, inv, start, nwin, k);
         else if (nwin <= 128) rs = cov_warp_read<4, CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (nwin <= 192) rs = cov_warp_read<6, CANON>(cc, t, codes, inv, start, nwin, k);
         else if (nwin <= CV_WARP_MAX) rs = cov_warp_read<8, CANON>(cc, t, codes, inv, start, nwin, k);
         else {
             is_long = true;
@@ -360,9 +516,20 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
     CovCache cc{};
     if (!e && t->capacity) e = cache_get_or_build(t, &cc);
     if (!e) {
+        // one wave of resident blocks, each warp striding over the 32-read
+        // chunks (a grid of several partial waves leaves SMs idle at its end)
+        static int per_sm[2] = {0, 0};
+        const int ci = t->canonical ? 1 : 0;
+        if (!per_sm[ci]) {
+            int b = 0;
+            if (t->canonical) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<true>, CV_THREADS, 0);
+            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<false>, CV_THREADS, 0);
+            per_sm[ci] = std::max(1, b);
+        }
         const uint64_t chunks = (n + 31) / 32;
         const unsigned grid = (unsigned)std::max<uint64_t>(
-            1, std::min<uint64_t>((chunks + CV_THREADS / 32 - 1) / (CV_THREADS / 32), (uint64_t)c->sm_count * 16));
+            1, std::min<uint64_t>((chunks + CV_THREADS / 32 - 1) / (CV_THREADS / 32),
+                                  (uint64_t)c->sm_count * (uint64_t)per_sm[ci]));
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COVERAGE, &ev);
         if (t->canonical)

@@ -223,6 +223,9 @@ struct tk_ctx {
     std::unordered_map<void *, size_t> big_used;
     int max_probes = 4096;
     int sm_count = 152;
+    // the batched-bins fill + count graph, updated in place for each batch
+    // (tk_bins.cu) and instantiated again only when an update is refused
+    cudaGraphExec_t bins_exec = nullptr;
     // read sets, tables and bundles alive on this context; tk_ctx_destroy
     // defers the release until the last of them is freed
     std::atomic<int> live{0};

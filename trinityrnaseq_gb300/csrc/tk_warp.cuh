@@ -186,12 +186,8 @@ __device__ __forceinline__ void lane_windows_codes(const uint64_t *__restrict__ 
 // the target has a 0 there when m is below that count.  Costs one pass per
 // significant bit of the largest count instead of a full sort.
 template <int S>
-__device__ __forceinline__ uint32_t warp_select(const uint32_t (&v)[S], uint32_t vm, uint32_t m) {
-    uint32_t lmax = 0;
-#pragma unroll
-    for (int j = 0; j < S; j++)
-        if ((vm >> j) & 1u) lmax = max(lmax, v[j]);
-    const uint32_t mx = __reduce_max_sync(0xffffffffu, lmax);
+__device__ __forceinline__ uint32_t warp_select(const uint32_t (&v)[S], uint32_t vm, uint32_t m, uint32_t mx) {
+    // mx: the largest valid value of the warp
     uint32_t prefix = 0;
     for (int b = 31 - __clz(mx); b >= 0; b--) {   // no pass when every value is 0
         uint32_t c = 0;

@@ -563,9 +563,11 @@ class Normalization:
 
 
 def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool = True,
-               min_count: int = 1) -> Tuple[bytes, np.ndarray, int]:
+               min_count: int = 1, out: Optional[np.ndarray] = None) -> Tuple[bytes, np.ndarray, int]:
     """Per-bin k-mer dumps of back-to-back FASTA bins in one batched GPU pass
-    (tk_count_bins).  Returns (dump text, n_bins + 1 byte offsets, k-mers counted)."""
+    (tk_count_bins).  Returns (dump text, n_bins + 1 byte offsets, k-mers counted);
+    with `out` (a uint8 array, e.g. page-locked, large enough) the text is
+    copied there and a view of it is returned instead of bytes."""
     ptr, n, keep = _host_ptr(text)
     off = np.ascontiguousarray(bin_off, dtype=np.uint64)
     nb = off.size - 1
@@ -577,6 +579,9 @@ def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool
         ctx.check(ctx.lib.tk_bins_info(h, C.byref(tl), C.byref(km)), "tk_bins_info")
         offs = np.zeros(nb + 1, dtype=np.uint64)
         ctx.check(ctx.lib.tk_bins_dump_offsets(h, offs.ctypes.data), "tk_bins_dump_offsets")
+        if out is not None and out.size >= tl.value:
+            ctx.check(ctx.lib.tk_bins_dump_text(h, out.ctypes.data, out.size), "tk_bins_dump_text")
+            return out[:tl.value], offs, km.value
         buf = np.zeros(max(tl.value, 1), dtype=np.uint8)
         ctx.check(ctx.lib.tk_bins_dump_text(h, buf.ctypes.data, buf.size), "tk_bins_dump_text")
         return buf[:tl.value].tobytes(), offs, km.value
