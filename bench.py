@@ -677,7 +677,7 @@ def r2t_bench(ctx, args):
     = build the bundle k-mer table, parse the reads, vote per read; device =
     reads FASTA resident in HBM and the per-read results left there; e2e =
     pinned host FASTA in, per-read (record, hits, windows) copied back.  The
-    CPU leg runs the oracle with all host threads on the first 1M reads."""
+    CPU leg runs the oracle with all host threads on the first 10M reads."""
     import numpy as np
     import torch
     from trinityrnaseq_gb300 import kmer, synth
@@ -736,11 +736,12 @@ def r2t_bench(ctx, args):
     cap = 1 << max(10, int(np.ceil(np.log2(info["kmers"] / 0.6 + 1))))
     ceil_lookup = ctx.random_access_rate(cap * 16, atomics=False)
     rate = lookups / (ms_assign / 1e3)
-    # CPU: the oracle with all host threads on the first 1M reads; and the
+    # CPU: the oracle with all host threads on the first 10M reads; and the
     # GPU's votes for the same reads compared with it
-    m = min(1_000_000, n)
-    head = reads[:min(reads.nbytes, 2 * m * 256)].tobytes()
-    sample = b"\n".join(head.split(b"\n", 2 * m)[:2 * m]) + b"\n"
+    m = min(args.r2t_check_reads, n)
+    lim = min(reads.nbytes, 2 * m * 256)            # 2-line records of < 256 bytes
+    nl = np.flatnonzero(reads[:lim] == 10)
+    sample = reads[:int(nl[2 * m - 1]) + 1]          # the first m records, no copy
     threads = os.cpu_count() or 1
     t0 = time.time()
     want = O.r2t_values(sample, b, K, False, threads)
@@ -967,13 +968,16 @@ def served_bench(ctx, args):
         # inf: every job submitted at once (the server's saturated throughput)
         gaps = rng.exponential(1.0 / (capacity * load), size=len(jobs)) if load != float("inf") else [0.0] * len(jobs)
         with Server(ctx.device, slots=args.slots, hbm_budget=int(args.budget_gb * 1e9)) as srv:
-            # a resident server is warm: one untimed job of each kind per slot first
-            warm = [j for kind in (N.TK_JOB_COUNT, N.TK_JOB_NORMALIZE, N.TK_JOB_R2T)
-                    for j in [x for x in jobs if x[0] == kind][:args.slots]]
-            for kind, a, b, _ in warm:
-                wid = submit(srv, kind, a, b)
-                srv.wait(wid)
-                srv.release(wid)
+            # a resident server is warm: per kind, one untimed job per slot
+            # submitted together (so that every slot, not just the first to
+            # wake, has run each kind once), twice over
+            for _ in range(2):
+                for kind in (N.TK_JOB_COUNT, N.TK_JOB_NORMALIZE, N.TK_JOB_R2T):
+                    warm = [x for x in jobs if x[0] == kind][:args.slots]
+                    wids = [submit(srv, k, a, b) for k, a, b, _ in warm]
+                    for wid in wids:
+                        srv.wait(wid)
+                        srv.release(wid)
             start = time.time()
             ids = []
             t_next = start
@@ -1155,6 +1159,8 @@ def main():
     ap.add_argument("--r2t", type=int, default=1, help="read -> component leg (0 = skip)")
     ap.add_argument("--r2t_pairs", type=int, default=50_000_000, help="read pairs of the read -> component leg")
     ap.add_argument("--dbg", type=int, default=1, help="per-component de Bruijn graph leg (0 = skip)")
+    ap.add_argument("--r2t-check-reads", type=int, default=10_000_000,
+                    help="reads of the read -> component leg checked against (and timed on) the oracle")
     ap.add_argument("--bins", type=int, default=5000, help="batched-bins comparison (0 = skip)")
     ap.add_argument("--bins-total", type=int, default=70000,
                     help="batched bins at the configuration's ~60M-read total (0 = skip)")

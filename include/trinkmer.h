@@ -270,7 +270,7 @@ void tk_r2t_free(tk_r2t *r2t);
  * occurrences in the record, a (K+1)-mer and its reverse complement counted
  * as one node unless `strand`; kmer = the first occurrence, upper case.
  * The header line and one line per k-mer are what the partition script reads
- * (partition_chrysalis_graphs_n_reads.pl:166-208); the node line's columns
+ * (partition_chrysalis_graphs_n_reads.pl:197-223); the node line's columns
  * are this library's (the tool's source is not in the reference).  K is
  * 1..30. */
 typedef struct tk_dbg tk_dbg;

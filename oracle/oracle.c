@@ -57,9 +57,9 @@
  *     join or another non-ACGT byte), count = occurrences in the record (both
  *     strands unless --SS), kmer = the first occurrence as written, upper case.
  *     Pinned: the "Component <id>" line starting each record and one line per
- *     k-mer (partition_chrysalis_graphs_n_reads.pl:166-208 counts the lines
+ *     k-mer (partition_chrysalis_graphs_n_reads.pl:197-223 counts the lines
  *     after each header as the component's k-mers, num_kmers + 24 vs the
- *     minimum contig length at :73); a component without k-mers is left out
+ *     minimum contig length at :76); a component without k-mers is left out
  *     because that reader stops at the first empty one.  The node line's
  *     columns are this restatement's choice (the consumers QuantifyGraph and
  *     Butterfly are not in the reference checkout).

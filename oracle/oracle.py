@@ -219,7 +219,9 @@ def r2t(reads: bytes, bundle: bytes, k: int = 25, strand: bool = False, min_pct:
 def r2t_values(reads: bytes, bundle: bytes, k: int = 25, strand: bool = False, threads: int = 0):
     lib = load()
     nr, rp, hp, wp = C.c_uint64(), C.c_void_p(), C.c_void_p(), C.c_void_p()
-    _chk(lib.orc_r2t_values(reads, len(reads), bundle, len(bundle), k, int(strand), threads, C.byref(nr),
+    ip, il = _buf(reads)
+    bp, bl = _buf(bundle)
+    _chk(lib.orc_r2t_values(ip, il, bp, bl, k, int(strand), threads, C.byref(nr),
                             C.byref(rp), C.byref(hp), C.byref(wp)), "r2t_values")
     n = nr.value
     return _take(rp, n, np.int32), _take(hp, n, np.uint32), _take(wp, n, np.uint32)

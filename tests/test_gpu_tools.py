@@ -229,3 +229,44 @@ def test_trinkmer_bins_writes_each_bins_catalogue(native_built, oracle, tmp_path
         h = oracle.histo(counts, 1, 10000)
         want = "".join(f"{c} {h[c]}\n" for c in range(1, 10002) if h[c])
         assert (tmp_path / (p.name + ".K25.histo")).read_text() == want
+
+
+def test_unchanged_perl_normalization_over_the_drop_ins(native_built, tmp_path):
+    """util/insilico_read_normalization.pl as shipped, with bin/jellyfish and
+    bin/seqtk-trinity found first on PATH and bin/fastaToKmerCoverageStats as
+    $TRINITY_HOME/Inchworm/bin/fastaToKmerCoverageStats, selects the same
+    reads as bin/insilico_read_normalization.  Needs a reference checkout
+    (TRINITY_REFERENCE_HOME) and Perl with DB_File; skipped otherwise.  The
+    script is copied into a scratch tree under tmp_path whose PerlLib and
+    util/support_scripts point at the reference's, so that its
+    $FindBin::RealBin/.. is the scratch tree holding the drop-ins."""
+    import shutil
+    from pathlib import Path
+    from trinityrnaseq_gb300 import synth
+    ref = os.environ.get("TRINITY_REFERENCE_HOME")
+    if not ref or not Path(ref, "util", "insilico_read_normalization.pl").exists():
+        pytest.skip("no reference checkout named by TRINITY_REFERENCE_HOME")
+    if not shutil.which("perl") or subprocess.run(["perl", "-MDB_File", "-Mthreads", "-e", "1"]).returncode:
+        pytest.skip("perl with DB_File and threads is required")
+    home = tmp_path / "trinity"
+    (home / "util").mkdir(parents=True)
+    (home / "Inchworm" / "bin").mkdir(parents=True)
+    (home / "trinity-plugins" / "BIN").mkdir(parents=True)
+    shutil.copy(Path(ref, "util", "insilico_read_normalization.pl"), home / "util")
+    os.symlink(Path(ref, "util", "support_scripts"), home / "util" / "support_scripts")
+    os.symlink(Path(ref, "PerlLib"), home / "PerlLib")
+    os.symlink(BIN / "fastaToKmerCoverageStats", home / "Inchworm" / "bin" / "fastaToKmerCoverageStats")
+    os.symlink(BIN / "seqtk-trinity", home / "trinity-plugins" / "BIN" / "seqtk-trinity")
+    left, right = synth.gene_pairs(seed=73, n_genes=80, n_pairs=8000, fastq=True)
+    (tmp_path / "l.fq").write_bytes(left.tobytes())
+    (tmp_path / "r.fq").write_bytes(right.tobytes())
+    common = ["--seqType", "fq", "--JM", "2G", "--max_cov", 30, "--min_cov", 1, "--max_CV", 10000, "--CPU", 4,
+              "--left", "l.fq", "--right", "r.fq", "--pairs_together", "--PARALLEL_STATS"]
+    env = dict(os.environ, PATH=f"{BIN}:{os.environ.get('PATH', '')}")
+    r = subprocess.run(["perl", str(home / "util" / "insilico_read_normalization.pl"), *map(str, common),
+                        "--output", "perl_out"], cwd=tmp_path, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    assert r.returncode == 0, r.stderr.decode()[-2000:]
+    run([BIN / "insilico_read_normalization", *common, "--output", "gpu_out"], cwd=tmp_path)
+    for tag in ("left", "right"):
+        assert (tmp_path / "perl_out" / f"{tag}.norm.fq").read_bytes() == \
+            (tmp_path / "gpu_out" / f"{tag}.norm.fq").read_bytes(), tag
