@@ -365,7 +365,9 @@ __device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, c
     const uint64_t end_nr = nr < 32 ? last_end : rd_off[r0 + 32];
     // lane i's read: its window count and class; a chunk of one class takes
     // the pipelined path
-    const uint64_t my_next = lane + 1 < nr ? __shfl_down_sync(0xffffffffu, my_start, 1) : end_nr;
+    // (every lane takes part in the shuffle; only its use depends on the lane)
+    const uint64_t from_next_lane = __shfl_down_sync(0xffffffffu, my_start, 1);
+    const uint64_t my_next = lane + 1 < nr ? from_next_lane : end_nr;
     const uint64_t my_len = lane < nr ? my_next - my_start - 1 : 0;
     const uint32_t my_nwin = my_len >= (uint64_t)k ? (uint32_t)(my_len - k + 1) : 0u;
     const uint32_t cls0 = __shfl_sync(0xffffffffu, cov_class(my_nwin), 0);
