@@ -359,10 +359,13 @@ def run_gpu(args, dist, world, rank, local):
     prof = {k: ctx.profile(k) for k in ("parse", "hll", "scatter", "count", "compact", "sort", "dump", "cov_cache",
                                          "coverage", "norm", "extract")}
     ctx.set_profiling(False)
-    # end-to-end timed region (host FASTQ in, dump text + stats out)
+    # end-to-end timed region (host FASTQ in, dump text + stats out), with
+    # the host link's rates measured just before and just after it (they
+    # vary with the host's other load)
+    link = {"before": link_rates(pipe)}
     ms_e2e, res_e2e = timed(pipe, stream, args.steps, True, dist)
+    link["after"] = link_rates(pipe)
     windows, reads = res[0][0], res[0][1]
-    link = link_rates(pipe)
     t_step = dist.max(statistics.mean(ms)) / 1e3
     t_e2e = dist.max(statistics.mean(ms_e2e)) / 1e3
     tot_windows = dist.sum(windows)

@@ -192,6 +192,9 @@ constexpr uint32_t LONG_READ = 0xFFFFFFFFu;   // cnt of a read left to the long-
 // validity, and the cache's count for each (0 = not in the cache).  Stage 2:
 // the table for the windows the cache did not answer.  Stage 3: the read's
 // statistics.  The lookups of a stage are independent loads issued together.
+// (Pipelining two reads -- the next read's cache answers and table prefetches
+// before the current read's statistics -- was 2.4x slower on GB300: the
+// registers it holds across stages spill.)
 template <int S, bool CANON>
 __device__ __forceinline__ void cov_stage1(const CovCache &cc, const uint64_t *__restrict__ codes,
                                            const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin, int k,
@@ -278,71 +281,6 @@ __device__ __forceinline__ ReadSums cov_warp_read(const CovCache &cc, DevTable t
     return cov_stage3<S>(v, vm);
 }
 
-// Pipelined form of the stages for a chunk of one window class S (S <= 4:
-// reads of up to 128 windows).  Stage 1 of read i+1 (keys, cache answers)
-// also issues an L2 prefetch of the table slot of every window the cache did
-// not answer; the table lookups of read i+1 run only after the statistics of
-// read i, by which time those slots have arrived.  Nothing of a read but its
-// counts and masks stays in registers between its stages: the table stage
-// cuts its keys from the codes again.
-template <int S, bool CANON>
-__device__ __forceinline__ void cov_pstage1(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
-                                            const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin, int k,
-                                            uint32_t (&v)[S], uint32_t &vm, uint32_t &miss) {
-    uint64_t key[S];
-    cov_stage1<S, CANON>(cc, codes, inv, start, nwin, k, key, v, vm);
-    miss = 0;
-#pragma unroll
-    for (int j = 0; j < S; j++)
-        if (((vm >> j) & 1u) && v[j] == 0) {
-            miss |= 1u << j;
-            const Slot *p = &t.slots[tbl_home(t, mix64(key[j]))];
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-        }
-}
-
-template <int S, bool CANON>
-__device__ __forceinline__ void cov_pstage2(DevTable t, const uint64_t *__restrict__ codes,
-                                            const uint32_t *__restrict__ inv, uint64_t start, uint32_t nwin, int k,
-                                            uint32_t (&v)[S], uint32_t miss) {
-    if (!__any_sync(0xffffffffu, miss != 0)) return;
-    const uint32_t span = (nwin + 31) / 32;
-    lane_windows_codes<S, CANON>(codes, inv, start, nwin, span, k, [&](int j, bool, uint64_t key) {
-        if ((miss >> j) & 1u) v[j] = tbl_get(t, key, 1u);
-    });
-}
-
-template <int S, bool CANON, typename ST, typename NW>
-__device__ __forceinline__ void cov_chunk_pipelined(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
-                                                    const uint32_t *__restrict__ inv, uint32_t nr, int k, ST &&starts,
-                                                    NW &&nwins, ReadSums *__restrict__ held) {
-    const unsigned lane = lane_id();
-    uint32_t vA[S], vB[S], mA, mB, xA, xB;
-    cov_pstage1<S, CANON>(cc, t, codes, inv, starts(0), nwins(0), k, vA, mA, xA);
-    for (uint32_t i = 0; i < nr; i += 2) {
-        if (i + 1 < nr) cov_pstage1<S, CANON>(cc, t, codes, inv, starts(i + 1), nwins(i + 1), k, vB, mB, xB);
-        cov_pstage2<S, CANON>(t, codes, inv, starts(i), nwins(i), k, vA, xA);
-        const ReadSums ra = cov_stage3<S>(vA, mA);
-        if (lane == 0) held[i] = ra;
-        if (i + 1 < nr) {
-            if (i + 2 < nr) cov_pstage1<S, CANON>(cc, t, codes, inv, starts(i + 2), nwins(i + 2), k, vA, mA, xA);
-            cov_pstage2<S, CANON>(t, codes, inv, starts(i + 1), nwins(i + 1), k, vB, xB);
-            const ReadSums rb = cov_stage3<S>(vB, mB);
-            if (lane == 0) held[i + 1] = rb;
-        }
-    }
-}
-
-// window class of a read: the registers per lane its windows need (9 = long)
-__device__ __forceinline__ uint32_t cov_class(uint32_t nwin) {
-    return nwin <= 32 ? 1u : nwin <= 64 ? 2u : nwin <= 96 ? 3u : nwin <= 128 ? 4u : nwin <= 192 ? 6u
-           : nwin <= CV_WARP_MAX ? 8u : 9u;
-}
-
-// chunks whose reads share a class of at most this many registers per lane
-// take the pipelined path
-constexpr uint32_t CV_PIPE_MAX_CLASS = 4;
-
 // One warp, 32 consecutive reads [r0, r0 + 32): the warp computes each read's
 // sums in turn and lane i keeps read r0 + i's; then every lane finishes its own
 // read.  The floating-point finish runs on the FP64 pipe, whose cost is per
@@ -363,27 +301,7 @@ __device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, c
     const uint64_t my_start = rd_off[r0 + (lane < nr ? lane : nr)];
     const uint64_t last_end = __shfl_sync(0xffffffffu, my_start, (int)(nr < 32 ? nr : 31));
     const uint64_t end_nr = nr < 32 ? last_end : rd_off[r0 + 32];
-    // lane i's read: its window count and class; a chunk of one class takes
-    // the pipelined path
-    // (every lane takes part in the shuffle; only its use depends on the lane)
-    const uint64_t from_next_lane = __shfl_down_sync(0xffffffffu, my_start, 1);
-    const uint64_t my_next = lane + 1 < nr ? from_next_lane : end_nr;
-    const uint64_t my_len = lane < nr ? my_next - my_start - 1 : 0;
-    const uint32_t my_nwin = my_len >= (uint64_t)k ? (uint32_t)(my_len - k + 1) : 0u;
-    const uint32_t cls0 = __shfl_sync(0xffffffffu, cov_class(my_nwin), 0);
-    const bool one_class =
-        __all_sync(0xffffffffu, lane >= nr || cov_class(my_nwin) == cls0) && cls0 <= CV_PIPE_MAX_CLASS;
-    if (one_class) {
-        auto starts = [&](uint32_t i) { return __shfl_sync(0xffffffffu, my_start, (int)i); };
-        auto nwins = [&](uint32_t i) { return __shfl_sync(0xffffffffu, my_nwin, (int)i); };
-        switch (cls0) {
-        case 1: cov_chunk_pipelined<1, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
-        case 2: cov_chunk_pipelined<2, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
-        case 3: cov_chunk_pipelined<3, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
-        default: cov_chunk_pipelined<4, CANON>(cc, t, codes, inv, nr, k, starts, nwins, held); break;
-        }
-    }
-    for (uint32_t i = 0; !one_class && i < nr; i++) {
+    for (uint32_t i = 0; i < nr; i++) {
         const uint64_t r = r0 + i;
         const uint64_t start = __shfl_sync(0xffffffffu, my_start, (int)i);
         const uint64_t next = i + 1 < 32 ? __shfl_sync(0xffffffffu, my_start, (int)(i + 1) & 31) : end_nr;
