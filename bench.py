@@ -981,6 +981,7 @@ def served_bench(ctx, args):
                     for wid in wids:
                         srv.wait(wid)
                         srv.release(wid)
+            batched0 = srv.batched_jobs()   # the warm-up's own batched passes are not counted
             start = time.time()
             ids = []
             t_next = start
@@ -1000,7 +1001,7 @@ def served_bench(ctx, args):
                 ok = ok and same(srv.result(jid, "normalize_select" if kind == N.TK_JOB_NORMALIZE else kind), want)
                 srv.release(jid)
             maxc = srv.stats()[2]
-            nbatched = srv.batched_jobs()
+            nbatched = srv.batched_jobs() - batched0
             held = srv.held_by_free_memory()
         lat.sort()
         name = "burst" if load == float("inf") else f"{load}x"
