@@ -85,7 +85,8 @@ def _take(ptr: C.c_void_p, n: int, dtype) -> np.ndarray:
 
 def _take_bytes(ptr: C.c_void_p, n: int) -> bytes:
     lib = load()
-    b = C.string_at(ptr, n) if n else b""
+    # (string_at takes a C int size: texts of 2 GB and more go through an array)
+    b = (C.c_char * n).from_address(ptr.value).raw if n else b""
     lib.orc_free(ptr)
     return b
 
