@@ -333,6 +333,19 @@ def timed(pipe, stream, steps, e2e, dist):
     return ms, res
 
 
+def leg_done(name, out):
+    """After a leg: its result on stderr (kept if a later leg fails), and the
+    page-locked host memory PyTorch caches for reuse given back, so that the
+    legs' large host buffers do not add up."""
+    import gc
+    import torch
+    log(f"{name}: " + json.dumps(out.get(name))[:4000])
+    gc.collect()
+    empty = getattr(torch._C, "_host_emptyCache", None)
+    if empty is not None:
+        empty()
+
+
 def run_gpu(args, dist, world, rank, local):
     import torch
     from trinityrnaseq_gb300 import Context, native
@@ -457,23 +470,22 @@ def run_gpu(args, dist, world, rank, local):
             out["cpu_baseline"] = cpu_baseline(args)
         if args.parity and world == 1:
             out["parity_full"] = parity_full(pipe, left, right)
+            leg_done("parity_full", out)
         del pipe
-        if args.prep and world == 1:
-            out["prep"] = prep_bench(ctx, left, args)
-        if args.norm and world == 1:
-            out["normalize"] = norm_bench(ctx, left, right, args)
-        if args.r2t and world == 1:
-            out["r2t"] = r2t_bench(ctx, args)
-        if args.dbg and world == 1:
-            out["debruijn"] = dbg_bench(ctx, args)
-        if args.bins and world == 1:
-            out["batched"] = batched_bench(ctx, args, args.bins)
-        if args.bins_total and world == 1:
-            # the configuration's other reading: the same distribution with as
-            # many bins as its stated ~60M-read total takes
-            out["batched_60M_reads"] = batched_bench(ctx, args, args.bins_total, sample_every=997)
-        if args.jobs and world == 1:
-            out["served"] = served_bench(ctx, args)
+        legs = [("prep", args.prep, lambda: prep_bench(ctx, left, args)),
+                ("normalize", args.norm, lambda: norm_bench(ctx, left, right, args)),
+                ("r2t", args.r2t, lambda: r2t_bench(ctx, args)),
+                ("debruijn", args.dbg, lambda: dbg_bench(ctx, args)),
+                ("batched", args.bins, lambda: batched_bench(ctx, args, args.bins)),
+                # the configuration's other reading: the same distribution with
+                # as many bins as its stated ~60M-read total takes
+                ("batched_60M_reads", args.bins_total,
+                 lambda: batched_bench(ctx, args, args.bins_total, sample_every=997)),
+                ("served", args.jobs, lambda: served_bench(ctx, args))]
+        for name, on, fn in legs:
+            if on and world == 1:
+                out[name] = fn()
+                leg_done(name, out)
     ctx.close()
     return out
 
