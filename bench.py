@@ -46,7 +46,9 @@ MIN_COUNT = 2           # the catalogue fastaToKmerCoverageStats reads (util/ins
 L2_BYTES = 129 * 2**20
 E2E_PIECES = 2          # record-aligned pieces per mate file on the end-to-end path
 NORM_ARGS = (200, 1, 10000)   # normalization: Trinity's --max_cov 200 --min_cov 1 --max_CV 10000
-COV_DRAM_BYTES_PER_LOOKUP = (4.189716e9 + 0.044003e9) / 38.0e6   # ncu, k_coverage at 500K pairs
+# ncu, one k_coverage launch at 20M pairs (one mate: 1,516,211,092 lookups):
+# dram__bytes_read.sum 115.28 GB + dram__bytes_write.sum 1.51 GB
+COV_DRAM_BYTES_PER_LOOKUP = (115.28e9 + 1.51e9) / (3_032_422_183 / 2)
 
 
 def log(*a):
@@ -298,9 +300,14 @@ def gpu_numa_node(device: int):
 def link_rates(pipe):
     """H2D and D2H GB/s of the end-to-end step's own page-locked buffers (one
     copy of a mate file each way, CUDA events), and their NUMA placement."""
+    return copy_rates(pipe.h_left, pipe.dev)
+
+
+def copy_rates(h, dev):
+    """H2D and D2H GB/s of one page-locked host tensor (one copy each way,
+    CUDA events; the tensor's contents are kept) and its NUMA placement."""
     import torch
-    h = pipe.h_left
-    d = torch.empty(h.numel(), dtype=torch.uint8, device=pipe.dev)
+    d = torch.empty(h.numel(), dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
     e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     e[0].record()
@@ -311,7 +318,7 @@ def link_rates(pipe):
     torch.cuda.synchronize()
     n = h.numel()
     out = {"h2d_gbs": n / (e[0].elapsed_time(e[1]) / 1e3) / 1e9, "d2h_gbs": n / (e[1].elapsed_time(e[2]) / 1e3) / 1e9,
-           "host_buffer_numa_pages": numa_nodes_of(h.data_ptr()), "gpu_numa_node": gpu_numa_node(pipe.dev.index)}
+           "host_buffer_numa_pages": numa_nodes_of(h.data_ptr()), "gpu_numa_node": gpu_numa_node(dev.index)}
     del d
     return out
 
@@ -428,14 +435,15 @@ def run_gpu(args, dist, world, rank, local):
                                        packed + 8.0 * windows, 0, None, None),
         }
         kernels["insert"]["random_access"]["l2_slice_ceiling_per_s"] = ceil_slice
-        # DRAM traffic of the coverage kernel: bytes per lookup from one ncu
-        # capture of the same kernel on 500K pairs (38.0M lookups into a 512 MB
-        # table: 4.190 GB read + 0.044 GB written), times this run's lookups
-        # per launch (random 16-byte loads fetch whole DRAM bursts)
+        # DRAM traffic of the coverage kernel: one ncu capture (1 pass) of the
+        # same kernel on the 20M-pair workload, per lookup, times this run's
+        # lookups per launch (random 16-byte loads fetch whole DRAM bursts)
         cov_launches = max(per_step["coverage"][1], 1)
         kernels["coverage"]["traffic"] = COV_DRAM_BYTES_PER_LOOKUP * windows / cov_launches
-        kernels["coverage"]["traffic_source"] = ("scaled from an ncu capture of k_coverage at 500K pairs: "
-                                                 f"{COV_DRAM_BYTES_PER_LOOKUP:.0f} DRAM bytes per lookup")
+        kernels["coverage"]["traffic_source"] = (
+            "ncu capture of one k_coverage launch at 20M pairs (115.28 GB read + 1.51 GB written), "
+            + ("this workload" if args.pairs == FULL_PAIRS else
+               f"scaled by lookups: {COV_DRAM_BYTES_PER_LOOKUP:.0f} DRAM bytes per lookup"))
         top = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
         out = {
             "metric": METRIC, "value": tot_windows / t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -521,6 +529,7 @@ def prep_bench(ctx, fastq, args):
     d_out = torch.empty(n_out + 16, dtype=torch.uint8, device=dev)
     h_out = torch.empty(n_out + 16, dtype=torch.uint8).pin_memory()
     res = {}
+    link = copy_rates(h_in, dev)
     for mode, out in (("device", d_out), ("e2e", h_out)):
         for _ in range(args.warmup):
             run(mode == "e2e", out)
@@ -534,6 +543,7 @@ def prep_bench(ctx, fastq, args):
         torch.cuda.synchronize()
         s = ev[0].elapsed_time(ev[1]) / 1e3 / args.steps
         res[mode] = {"reads_per_s": reads / s, "input_gb_per_s": n_bytes / s / 1e9, "ms": s * 1e3}
+    res["e2e"]["link_before"] = link
     # bit-exact check and CPU time on a 1M-record sample
     cut = kmer.split_records(fastq, max(1, reads // 1_000_000))[1]
     sample = fastq[:cut].tobytes()
@@ -634,6 +644,7 @@ def norm_bench(ctx, left, right, args):
         for r in fas + fqs:
             r.free()
 
+    link = copy_rates(h_fq[0], dev)
     s_e2e = timed_region(whole)
     for r in fa + fq:
         r.free()
@@ -673,7 +684,7 @@ def norm_bench(ctx, left, right, args):
             "e2e": {"pairs_per_s": pairs / s_e2e, "ms": s_e2e * 1e3,
                     "what": "pinned host FASTQ of both sides -> parse, prep, count, stats, tail, extraction -> "
                             "pinned host normalized FASTQ",
-                    "h2d_bytes": sum(h.numel() for h in h_fq), "d2h_bytes": sum(ext)},
+                    "h2d_bytes": sum(h.numel() for h in h_fq), "d2h_bytes": sum(ext), "link_before": link},
             "cpu": {"pairs_per_s": m / cpu_s, "cores": 1, "kind": "port",
                     "sample": f"first {m} pairs; the oracle's sort + merge + selection + extraction from stats tables"},
             "bit_exact_vs_oracle_sample": same}
@@ -726,6 +737,7 @@ def r2t_bench(ctx, args):
         z.free()
 
     res = {}
+    link = copy_rates(h_reads, dev)
     for mode in ("device", "e2e"):
         for _ in range(args.warmup):
             step(mode == "e2e")
@@ -745,6 +757,7 @@ def r2t_bench(ctx, args):
             prof = {k: ctx.profile(k) for k in ("parse", "r2t_build", "r2t_assign")}
             ctx.set_profiling(False)
         res[mode] = {"reads_per_s": n / s, "ms": s * 1e3}
+    res["e2e"]["link_before"] = link
     lookups = int(h_out[2].numpy().astype(np.int64).sum())
     assigned = int((h_out[0].numpy() >= 0).sum())
     ms_assign = prof["r2t_assign"][0] / args.steps

@@ -37,3 +37,19 @@ def test_bins_with_empty_and_tiny_bins(ctx, oracle):
     for b, p in enumerate(parts):
         k, c = oracle.count(p, 25, False)
         assert dump[int(toff[b]):int(toff[b + 1])] == oracle.dump(k, c, 25, 1)
+
+
+@pytest.mark.parametrize("k,n_bins,max_reads", [(25, 20000, 12), (31, 40, 400)])
+def test_bins_whose_bin_and_kmer_exceed_one_word(ctx, oracle, k, n_bins, max_reads):
+    # 2k + bits(bin) > 64: 20,000 bins at k = 25 (50 + 15 bits), 40 bins at
+    # k = 31 (62 + 6 bits) take the two-sort (k-mer, then bin) order
+    text, off, _ = synth.power_law_bins(seed=5, n_bins=n_bins, alpha=1.8, min_reads=1, max_reads=max_reads)
+    t = text.tobytes()
+    dump, toff, kmers = count_bins(ctx, t, off, k, True, 1)
+    assert toff[0] == 0 and toff[-1] == len(dump)
+    total = 0
+    for b in range(n_bins):
+        keys, counts = oracle.count(t[int(off[b]):int(off[b + 1])], k, True)
+        total += int(counts.sum())
+        assert dump[int(toff[b]):int(toff[b + 1])] == oracle.dump(keys, counts, k, 1), f"bin {b}"
+    assert kmers == total

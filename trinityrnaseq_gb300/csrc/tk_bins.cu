@@ -17,7 +17,9 @@
 //     that slice doubled); the context keeps the executable graph and each
 //     later batch updates it in place rather than instantiating it again;
 //  5. one compaction of every slice into (bin << 2k | key, count), one radix
-//     sort, one K4 formatting pass; bin b's dump is a contiguous byte range.
+//     sort (past 2^(64 - 2k) bins: a sort by k-mer, then a stable sort of the
+//     record order by bin), one K4 formatting pass; bin b's dump is a
+//     contiguous byte range.
 //
 // Each bin's dump equals a separate plain `jellyfish count` + `dump -L m` of
 // that bin (sorted by key).
@@ -147,12 +149,15 @@ __global__ void k_bin_count(const uint8_t *__restrict__ seq, uint64_t n, int k, 
 
 constexpr uint64_t BIN_HISTO = 10002;   // jellyfish histo bins for low 1, high 10000
 
-// every occupied slot with count >= its bin's minimum, keyed (bin << 2k) | key;
-// with `histo`, also every occupied slot's count into its bin's histogram
+// every occupied slot with count >= its bin's minimum, keyed (bin << 2k) | key
+// or, with `obins` (bin and key do not fit 64 bits together), keyed by the
+// k-mer with its bin in `obins`; with `histo`, also every occupied slot's count
+// into its bin's histogram
 __global__ void k_bin_compact(const Slot *__restrict__ slots, uint64_t cap, const uint64_t *__restrict__ base,
                               uint32_t n_bins, int k, const uint32_t *__restrict__ min_count,
                               uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals,
-                              unsigned long long *__restrict__ n_out, unsigned long long *__restrict__ histo) {
+                              uint32_t *__restrict__ obins, unsigned long long *__restrict__ n_out,
+                              unsigned long long *__restrict__ histo) {
     const unsigned lane = lane_id();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x; b0 < cap; b0 += stride) {
@@ -181,24 +186,56 @@ __global__ void k_bin_compact(const Slot *__restrict__ slots, uint64_t cap, cons
         wb = __shfl_sync(0xffffffffu, wb, 0);
         if (sel) {
             uint64_t o = wb + __popc(m & ((1u << lane) - 1u));
-            okeys[o] = (bin << (2 * k)) | v.x;
+            if (obins) {
+                okeys[o] = v.x;
+                obins[o] = (uint32_t)bin;
+            } else {
+                okeys[o] = (bin << (2 * k)) | v.x;
+            }
             ovals[o] = c;
         }
     }
 }
 
-// first sorted record of every bin (and n at the end)
-__global__ void k_bin_bounds(const uint64_t *__restrict__ keys, uint64_t n, int k, uint32_t n_bins,
+// first sorted record of every bin (and n at the end); the bin of a record is
+// its key >> shift
+__global__ void k_bin_bounds(const uint64_t *__restrict__ keys, uint64_t n, int shift, uint32_t n_bins,
                              uint64_t *__restrict__ first) {
     uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b > n_bins) return;
-    const uint64_t target = (uint64_t)b << (2 * k);
+    const uint64_t target = (uint64_t)b << shift;
     uint64_t lo = 0, hi = n;
     while (lo < hi) {
         uint64_t mid = (lo + hi) >> 1;
         if (keys[mid] < target) lo = mid + 1; else hi = mid;
     }
     first[b] = lo;
+}
+
+// Wide (bin, k-mer) order, for batches whose bin index and 2k key bits do not
+// fit one 64-bit word: a stable sort by k-mer carrying record indices, then a
+// stable sort of those indices by bin, then one gather.
+__global__ void k_bin_iota(uint32_t *__restrict__ v, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        v[i] = (uint32_t)i;
+}
+
+__global__ void k_bin_gather_bins(const uint32_t *__restrict__ bins, const uint32_t *__restrict__ by_kmer, uint64_t n,
+                                  uint64_t *__restrict__ bkey, uint32_t *__restrict__ pos) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        bkey[i] = bins[by_kmer[i]];
+        pos[i] = (uint32_t)i;
+    }
+}
+
+__global__ void k_bin_gather_final(const uint64_t *__restrict__ kmer_sorted, const uint32_t *__restrict__ by_kmer,
+                                   const uint32_t *__restrict__ by_bin, const uint32_t *__restrict__ cnt, uint64_t n,
+                                   uint64_t *__restrict__ okeys, uint32_t *__restrict__ ocnt) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = by_bin[i];
+        okeys[i] = kmer_sorted[j];
+        ocnt[i] = cnt[by_kmer[j]];
+    }
 }
 
 __device__ __forceinline__ uint32_t dec_digits10(uint32_t v) {
@@ -473,18 +510,25 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
         e = alloc((void **)&d_histo, (uint64_t)n_bins * BIN_HISTO * 8, "bin histograms");
         if (!e) cudaMemsetAsync(d_histo, 0, (uint64_t)n_bins * BIN_HISTO * 8, c->stream);
     }
+    // (bin << 2k) | key is one 64-bit sort key while it fits: up to 2^(64 - 2k)
+    // bins (16384 at k = 25); past that the wide order below
+    int bin_bits = 1;
+    while ((1ULL << bin_bits) < n_bins) bin_bits++;
+    const bool wide = 2 * k + bin_bits > 64;
     // occupied slots <= min(windows, slots)
     const uint64_t upper = std::max<uint64_t>(1, std::min<uint64_t>(kmers, total));
+    uint32_t *obins = nullptr;
     if (!e) e = alloc((void **)&k0, upper * 8, "bin keys");
     if (!e) e = alloc((void **)&v0, upper * 4, "bin counts");
     if (!e) e = alloc((void **)&k1, upper * 8, "bin keys tmp");
     if (!e) e = alloc((void **)&v1, upper * 4, "bin counts tmp");
+    if (!e && wide) e = alloc((void **)&obins, upper * 4, "bin of each record");
     if (!e) {
         cudaMemsetAsync(d_n, 0, 8, c->stream);
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COMPACT, &ev);
         k_bin_compact<<<(unsigned)c->sm_count * 8, 256, 0, c->stream>>>(slots, total, d_base, n_bins, k, d_minc, k0, v0,
-                                                                        d_n, d_histo);
+                                                                        obins, d_n, d_histo);
         c->launches++;
         prof_end(c, TK_KID_COMPACT, ev, total);
         e = cuda_check(c, cudaMemcpyAsync(&hn, d_n, 8, cudaMemcpyDeviceToHost, c->stream), "bins n d2h");
@@ -493,17 +537,54 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
                                               c->stream), "bin histograms d2h");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "bins compact sync");
     }
-    bool in_tmp = false;
-    int bin_bits = 1;
-    while ((1u << bin_bits) < n_bins) bin_bits++;
-    if (!e && hn > 1) {
+    uint64_t *keys = k0, *bin_keys = k0;   // sorted records; what the bin bounds search
+    uint32_t *cnts = v0;
+    int bin_shift = 2 * k;
+    if (!e && wide && hn > 0xFFFFFFFFull)
+        e = set_err(c, TK_E_RANGE, "a batch of bins holds more than 2^32 distinct k-mers: split it");
+    if (!e && (wide ? hn >= 1 : hn > 1)) {
         cudaEvent_t ev;
         prof_begin(c, TK_KID_SORT, &ev);
-        e = radix_sort_pairs(c, k0, v0, hn, 2 * k + bin_bits, k1, v1, &in_tmp);
+        if (!wide) {
+            bool in_tmp = false;
+            e = radix_sort_pairs(c, k0, v0, hn, 2 * k + bin_bits, k1, v1, &in_tmp);
+            keys = bin_keys = in_tmp ? k1 : k0;
+            cnts = in_tmp ? v1 : v0;
+        } else {
+            uint32_t *ia0 = nullptr, *ia1 = nullptr, *jb0 = nullptr, *jb1 = nullptr;
+            uint64_t *bk0 = nullptr, *bk1 = nullptr;
+            e = alloc((void **)&ia0, hn * 4, "record order by k-mer");
+            if (!e) e = alloc((void **)&ia1, hn * 4, "record order by k-mer tmp");
+            if (!e) e = alloc((void **)&jb0, hn * 4, "record order by bin");
+            if (!e) e = alloc((void **)&jb1, hn * 4, "record order by bin tmp");
+            if (!e) e = alloc((void **)&bk0, hn * 8, "record bins");
+            if (!e) e = alloc((void **)&bk1, hn * 8, "record bins tmp");
+            const unsigned grid = (unsigned)c->sm_count * 8;
+            bool ta = false, tb = false;
+            if (!e) {
+                k_bin_iota<<<grid, 256, 0, c->stream>>>(ia0, hn);
+                c->launches++;
+                e = radix_sort_pairs(c, k0, ia0, hn, 2 * k, k1, ia1, &ta);
+            }
+            uint64_t *by_kmer_key = ta ? k1 : k0;
+            uint32_t *by_kmer = ta ? ia1 : ia0;
+            if (!e) {
+                k_bin_gather_bins<<<grid, 256, 0, c->stream>>>(obins, by_kmer, hn, bk0, jb0);
+                c->launches++;
+                e = radix_sort_pairs(c, bk0, jb0, hn, bin_bits, bk1, jb1, &tb);
+            }
+            if (!e) {
+                keys = ta ? k0 : k1;
+                k_bin_gather_final<<<grid, 256, 0, c->stream>>>(by_kmer_key, by_kmer, tb ? jb1 : jb0, v0, hn, keys, v1);
+                c->launches++;
+                cnts = v1;
+                bin_keys = tb ? bk1 : bk0;
+                bin_shift = 0;
+                e = check_launch(c, "bin wide order");
+            }
+        }
         prof_end(c, TK_KID_SORT, ev, hn);
     }
-    uint64_t *keys = in_tmp ? k1 : k0;
-    uint32_t *cnts = in_tmp ? v1 : v0;
     uint64_t *first = nullptr, *d_text0 = nullptr, *offs = nullptr;
     uint32_t *lens = nullptr;
     uint64_t text_len = 0;
@@ -515,7 +596,7 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
     if (!e) {
         cudaEvent_t ev;
         prof_begin(c, TK_KID_DUMP, &ev);
-        k_bin_bounds<<<(n_bins + 256) / 256, 256, 0, c->stream>>>(keys, hn, k, n_bins, first);
+        k_bin_bounds<<<(n_bins + 256) / 256, 256, 0, c->stream>>>(bin_keys, hn, bin_shift, n_bins, first);
         c->launches++;
         if (hn) {
             k_bin_dump_len<<<(unsigned)((hn + 255) / 256), 256, 0, c->stream>>>(cnts, hn, k, lens);
