@@ -17,7 +17,6 @@ int parse_reads(tk_ctx *c, tk_reads *r);
 int table_info(tk_table *t, uint64_t *distinct, uint64_t *total, uint64_t *capacity);
 int table_histo(tk_table *t, uint64_t low, uint64_t high, uint64_t *hist);
 int table_sorted_pairs(tk_table *t, uint32_t min_count, uint64_t **keys, uint32_t **cnt, uint64_t *n);
-int format_dump(tk_ctx *c, const uint64_t *keys, const uint32_t *cnt, uint64_t n, int k, char **text, uint64_t *len);
 int table_insert_pairs(tk_table *t, const uint64_t *d_keys, const uint32_t *d_cnt, uint64_t n);
 int table_load_dump_reads(tk_table *t, const tk_reads *r);
 int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d_mean, float *d_stdev);

@@ -148,121 +148,123 @@ __global__ void k_bin_count(const uint8_t *__restrict__ seq, uint64_t n, int k, 
 }
 
 constexpr uint64_t BIN_HISTO = 10002;   // jellyfish histo bins for low 1, high 10000
+constexpr int BCP_ITEMS = 8;            // slots per thread per compaction tile (2048-slot tiles)
 
-// every occupied slot with count >= its bin's minimum, keyed (bin << 2k) | key
-// or, with `obins` (bin and key do not fit 64 bits together), keyed by the
-// k-mer with its bin in `obins`; with `histo`, also every occupied slot's count
-// into its bin's histogram
-__global__ void k_bin_compact(const Slot *__restrict__ slots, uint64_t cap, const uint64_t *__restrict__ base,
-                              uint32_t n_bins, int k, const uint32_t *__restrict__ min_count,
-                              uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals,
-                              uint32_t *__restrict__ obins, unsigned long long *__restrict__ n_out,
-                              unsigned long long *__restrict__ histo) {
-    const unsigned lane = lane_id();
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x; b0 < cap; b0 += stride) {
-        uint64_t i = b0 + threadIdx.x;
-        ulonglong2 v;
-        v.x = EMPTY_KEY;
-        v.y = 0;
-        if (i < cap) v = __ldcs(reinterpret_cast<const ulonglong2 *>(&slots[i]));
-        const bool occ = v.x != EMPTY_KEY;
-        const uint64_t bin = occ ? bin_of(base, n_bins, i) : 0;
-        const uint32_t c = (uint32_t)v.y;
-        bool sel = occ && c >= min_count[bin];
-        if (histo) {
-            // warp-merged increments: equal (bin, bucket) lanes add once
-            const uint64_t cell = occ ? bin * BIN_HISTO + (c > 10000u ? 10001u : c) : ~0ULL;
-            const unsigned act = __ballot_sync(0xffffffffu, occ);
-            if (occ) {
-                const unsigned peers = __match_any_sync(act, cell);
-                if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&histo[cell], (unsigned long long)__popc(peers));
+// largest b in [lo, hi) with base[b] <= p (base[lo] <= p)
+__device__ __forceinline__ uint32_t bin_in(const uint64_t *__restrict__ base, uint32_t lo, uint32_t hi, uint64_t p) {
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= p) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Every occupied slot with count >= its bin's minimum, as (local bin << 2k) |
+// key with its count, into its bin group's output range.  Bins are grouped
+// 2^gshift at a time so that the local bin and the key fit one 64-bit sort
+// key; group g's records go to [group_cur[g] at launch, ...).  Slices are
+// powers of two of at least 32 slots laid out back to back, so every 32-slot
+// aligned run (one warp's load) lies in one bin.  A 2048-slot tile inside one
+// group reserves its output with one atomic; a tile that crosses a group
+// boundary reserves per warp load.  WRITE false: only the per-group counts
+// (group_cur zeroed at launch).  With `histo` (WRITE only), every occupied
+// slot's count also goes into its bin's histogram.
+template <bool WRITE>
+__global__ void __launch_bounds__(256) k_bin_compact(const Slot *__restrict__ slots, uint64_t cap,
+                                                     const uint64_t *__restrict__ base, uint32_t n_bins, int k,
+                                                     int gshift, const uint32_t *__restrict__ min_count,
+                                                     unsigned long long *__restrict__ group_cur,
+                                                     uint64_t *__restrict__ okeys, uint32_t *__restrict__ ovals,
+                                                     unsigned long long *__restrict__ histo) {
+    __shared__ uint32_t sm[256 / 32 + 1];
+    __shared__ unsigned long long s_base;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint64_t chunk = 256ull * BCP_ITEMS;
+    const uint32_t lmask = (uint32_t)((1ull << gshift) - 1ull);
+    for (uint64_t t0 = (uint64_t)blockIdx.x * chunk; t0 < cap; t0 += (uint64_t)gridDim.x * chunk) {
+        const uint64_t tl = min(t0 + chunk, cap) - 1;
+        const uint32_t b0 = bin_of(base, n_bins, t0), b1 = bin_of(base, n_bins, tl);
+        const uint32_t g0 = (uint32_t)((uint64_t)b0 >> gshift), g1 = (uint32_t)((uint64_t)b1 >> gshift);
+        ulonglong2 v[BCP_ITEMS];
+        uint32_t bin[BCP_ITEMS];
+        uint32_t selm = 0, nsel = 0;
+#pragma unroll
+        for (int j = 0; j < BCP_ITEMS; j++) {
+            const uint64_t run = t0 + (uint64_t)j * 256 + warp * 32;   // this warp's 32-slot run
+            const uint64_t i = run + lane;
+            v[j].x = EMPTY_KEY;
+            v[j].y = 0;
+            bin[j] = run <= tl ? bin_in(base, b0, b1 + 1, run) : b1;
+            if (i < cap) v[j] = __ldcs(reinterpret_cast<const ulonglong2 *>(&slots[i]));
+            const bool occ = v[j].x != EMPTY_KEY;
+            const uint32_t c = (uint32_t)v[j].y;
+            const bool sel = occ && c >= min_count[bin[j]];
+            selm |= (sel ? 1u : 0u) << j;
+            nsel += sel;
+            if (WRITE && histo) {
+                // warp-merged increments: equal buckets (one bin per run) add once
+                const uint64_t cell = (uint64_t)bin[j] * BIN_HISTO + (c > 10000u ? 10001u : c);
+                const unsigned act = __ballot_sync(0xffffffffu, occ);
+                if (occ) {
+                    const unsigned peers = __match_any_sync(act, cell);
+                    if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&histo[cell], (unsigned long long)__popc(peers));
+                }
             }
         }
-        unsigned m = __ballot_sync(0xffffffffu, sel);
-        if (!m) continue;
-        unsigned long long wb = 0;
-        if (lane == 0) wb = atomicAdd(n_out, (unsigned long long)__popc(m));
-        wb = __shfl_sync(0xffffffffu, wb, 0);
-        if (sel) {
-            uint64_t o = wb + __popc(m & ((1u << lane) - 1u));
-            if (obins) {
-                okeys[o] = v.x;
-                obins[o] = (uint32_t)bin;
-            } else {
-                okeys[o] = (bin << (2 * k)) | v.x;
+        if (g0 == g1) {
+            uint32_t tot;
+            const uint32_t pre = block_excl_scan<uint32_t>(nsel, sm, &tot);
+            if (tot == 0) continue;                   // uniform over the block
+            if (threadIdx.x == 0) s_base = atomicAdd(&group_cur[g0], (unsigned long long)tot);
+            __syncthreads();
+            if (WRITE) {
+                uint64_t o = s_base + pre;
+#pragma unroll
+                for (int j = 0; j < BCP_ITEMS; j++)
+                    if ((selm >> j) & 1u) {
+                        okeys[o] = ((uint64_t)(bin[j] & lmask) << (2 * k)) | v[j].x;
+                        ovals[o] = (uint32_t)v[j].y;
+                        o++;
+                    }
             }
-            ovals[o] = c;
+            __syncthreads();
+        } else {
+#pragma unroll
+            for (int j = 0; j < BCP_ITEMS; j++) {
+                const unsigned m = __ballot_sync(0xffffffffu, (selm >> j) & 1u);
+                if (!m) continue;
+                unsigned long long wb = 0;
+                if (lane == 0) wb = atomicAdd(&group_cur[(uint64_t)bin[j] >> gshift], (unsigned long long)__popc(m));
+                wb = __shfl_sync(0xffffffffu, wb, 0);
+                if (WRITE && ((selm >> j) & 1u)) {
+                    const uint64_t o = wb + __popc(m & ((1u << lane) - 1u));
+                    okeys[o] = ((uint64_t)(bin[j] & lmask) << (2 * k)) | v[j].x;
+                    ovals[o] = (uint32_t)v[j].y;
+                }
+            }
         }
     }
 }
 
-// first sorted record of every bin (and n at the end); the bin of a record is
-// its key >> shift
-__global__ void k_bin_bounds(const uint64_t *__restrict__ keys, uint64_t n, int shift, uint32_t n_bins,
-                             uint64_t *__restrict__ first) {
+// first sorted record of every bin (and n at the end): bin b is local bin
+// b & (2^gshift - 1) of group b >> gshift, whose records are
+// [goff[g], goff[g + 1]) sorted by (local bin << 2k) | key
+__global__ void k_bin_bounds(const uint64_t *__restrict__ keys, const uint64_t *__restrict__ goff, int gshift, int k,
+                             uint32_t n_bins, uint64_t n, uint64_t *__restrict__ first) {
     uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b > n_bins) return;
-    const uint64_t target = (uint64_t)b << shift;
-    uint64_t lo = 0, hi = n;
+    if (b == n_bins) {
+        first[b] = n;
+        return;
+    }
+    const uint32_t g = (uint32_t)((uint64_t)b >> gshift);
+    const uint64_t target = (uint64_t)(b & (uint32_t)((1ull << gshift) - 1ull)) << (2 * k);
+    uint64_t lo = goff[g], hi = goff[g + 1];
     while (lo < hi) {
         uint64_t mid = (lo + hi) >> 1;
         if (keys[mid] < target) lo = mid + 1; else hi = mid;
     }
     first[b] = lo;
-}
-
-// Wide (bin, k-mer) order, for batches whose bin index and 2k key bits do not
-// fit one 64-bit word: a stable sort by k-mer carrying record indices, then a
-// stable sort of those indices by bin, then one gather.
-__global__ void k_bin_iota(uint32_t *__restrict__ v, uint64_t n) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        v[i] = (uint32_t)i;
-}
-
-__global__ void k_bin_gather_bins(const uint32_t *__restrict__ bins, const uint32_t *__restrict__ by_kmer, uint64_t n,
-                                  uint64_t *__restrict__ bkey, uint32_t *__restrict__ pos) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        bkey[i] = bins[by_kmer[i]];
-        pos[i] = (uint32_t)i;
-    }
-}
-
-__global__ void k_bin_gather_final(const uint64_t *__restrict__ kmer_sorted, const uint32_t *__restrict__ by_kmer,
-                                   const uint32_t *__restrict__ by_bin, const uint32_t *__restrict__ cnt, uint64_t n,
-                                   uint64_t *__restrict__ okeys, uint32_t *__restrict__ ocnt) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t j = by_bin[i];
-        okeys[i] = kmer_sorted[j];
-        ocnt[i] = cnt[by_kmer[j]];
-    }
-}
-
-__device__ __forceinline__ uint32_t dec_digits10(uint32_t v) {
-    uint32_t d = 1;
-    while (v >= 10) { v /= 10; d++; }
-    return d;
-}
-
-__global__ void k_bin_dump_len(const uint32_t *__restrict__ cnt, uint64_t n, int k, uint32_t *__restrict__ len) {
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) len[i] = 3u + dec_digits10(cnt[i]) + (uint32_t)k;
-}
-
-__global__ void k_bin_dump_write(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ cnt,
-                                 const uint64_t *__restrict__ off, uint64_t n, int k, char *__restrict__ out) {
-    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    char *p = out + off[i];
-    uint32_t c = cnt[i];
-    uint32_t nd = dec_digits10(c);
-    p[0] = '>';
-    for (int d = (int)nd; d >= 1; d--) { p[d] = (char)('0' + c % 10); c /= 10; }
-    p[nd + 1] = '\n';
-    const uint64_t key = keys[i];
-    char *q = p + nd + 2;
-    for (int j = 0; j < k; j++) q[j] = "ACGT"[(key >> (2 * (k - 1 - j))) & 3];
-    q[k] = '\n';
 }
 
 __global__ void k_bin_text_bounds(const uint64_t *__restrict__ first, const uint64_t *__restrict__ off, uint64_t n,
@@ -496,127 +498,122 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
         for (uint32_t b = 0; b < n_bins; b++) { base[b] = total; total += 1ULL << lbits[b]; }
         base[n_bins] = total;
     }
-    // 5. compact, sort by (bin, key), format
+    // 5. compact, sort by (bin, key), format.  (bin << 2k) | key is one
+    //    64-bit sort key while it fits: up to 2^(64 - 2k) bins (16384 at
+    //    k = 25, 4 at k = 31).  Past that, bins are taken in groups of
+    //    2^(64 - 2k): each group's records get their own output range (a
+    //    counting pass first) and are sorted by (local bin << 2k) | key.
     uint64_t *k0 = nullptr, *k1 = nullptr;
     uint32_t *v0 = nullptr, *v1 = nullptr;
-    unsigned long long *d_n = nullptr;
-    unsigned long long hn = 0;
+    unsigned long long *d_gcur = nullptr;
     uint32_t *d_minc = nullptr;
     unsigned long long *d_histo = nullptr;
-    if (!e) e = alloc((void **)&d_n, 8, "bins n");
+    int bin_bits = 0;
+    while ((1ULL << bin_bits) < n_bins) bin_bits++;
+    const int gshift = std::min(bin_bits, 64 - 2 * k);
+    const uint32_t n_groups = (uint32_t)(((uint64_t)n_bins + (1ULL << gshift) - 1) >> gshift);
+    std::vector<unsigned long long> gcount(n_groups, 0), goff(n_groups + 1, 0);
+    if (!e) e = alloc((void **)&d_gcur, (n_groups + 1) * 8, "bin group cursors");
     if (!e) e = alloc((void **)&d_minc, n_bins * 4, "bin minimum counts");
     if (!e) e = cuda_check(c, cudaMemcpyAsync(d_minc, min_counts_h, n_bins * 4, cudaMemcpyHostToDevice, c->stream), "min counts");
     if (!e && histos_h) {
         e = alloc((void **)&d_histo, (uint64_t)n_bins * BIN_HISTO * 8, "bin histograms");
         if (!e) cudaMemsetAsync(d_histo, 0, (uint64_t)n_bins * BIN_HISTO * 8, c->stream);
     }
-    // (bin << 2k) | key is one 64-bit sort key while it fits: up to 2^(64 - 2k)
-    // bins (16384 at k = 25); past that the wide order below
-    int bin_bits = 1;
-    while ((1ULL << bin_bits) < n_bins) bin_bits++;
-    const bool wide = 2 * k + bin_bits > 64;
     // occupied slots <= min(windows, slots)
     const uint64_t upper = std::max<uint64_t>(1, std::min<uint64_t>(kmers, total));
-    uint32_t *obins = nullptr;
     if (!e) e = alloc((void **)&k0, upper * 8, "bin keys");
     if (!e) e = alloc((void **)&v0, upper * 4, "bin counts");
     if (!e) e = alloc((void **)&k1, upper * 8, "bin keys tmp");
     if (!e) e = alloc((void **)&v1, upper * 4, "bin counts tmp");
-    if (!e && wide) e = alloc((void **)&obins, upper * 4, "bin of each record");
+    const unsigned cgrid = (unsigned)c->sm_count * 8;
     if (!e) {
-        cudaMemsetAsync(d_n, 0, 8, c->stream);
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COMPACT, &ev);
-        k_bin_compact<<<(unsigned)c->sm_count * 8, 256, 0, c->stream>>>(slots, total, d_base, n_bins, k, d_minc, k0, v0,
-                                                                        obins, d_n, d_histo);
-        c->launches++;
+        cudaMemsetAsync(d_gcur, 0, (n_groups + 1) * 8, c->stream);
+        if (n_groups > 1) {
+            k_bin_compact<false><<<cgrid, 256, 0, c->stream>>>(slots, total, d_base, n_bins, k, gshift, d_minc, d_gcur,
+                                                               nullptr, nullptr, nullptr);
+            c->launches++;
+            e = cuda_check(c, cudaMemcpyAsync(gcount.data(), d_gcur, n_groups * 8, cudaMemcpyDeviceToHost, c->stream),
+                           "bin group counts d2h");
+            if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "bin group counts sync");
+            for (uint32_t g = 0; !e && g < n_groups; g++) goff[g + 1] = goff[g] + gcount[g];
+            if (!e) e = cuda_check(c, cudaMemcpyAsync(d_gcur, goff.data(), n_groups * 8, cudaMemcpyHostToDevice, c->stream),
+                                   "bin group offsets h2d");
+        }
+        if (!e) {
+            k_bin_compact<true><<<cgrid, 256, 0, c->stream>>>(slots, total, d_base, n_bins, k, gshift, d_minc, d_gcur, k0,
+                                                              v0, d_histo);
+            c->launches++;
+        }
         prof_end(c, TK_KID_COMPACT, ev, total);
-        e = cuda_check(c, cudaMemcpyAsync(&hn, d_n, 8, cudaMemcpyDeviceToHost, c->stream), "bins n d2h");
+        if (!e && n_groups == 1) {
+            e = cuda_check(c, cudaMemcpyAsync(gcount.data(), d_gcur, 8, cudaMemcpyDeviceToHost, c->stream), "bins n d2h");
+            goff[1] = 0;
+        }
         if (!e && d_histo)
             e = cuda_check(c, cudaMemcpyAsync(histos_h, d_histo, (uint64_t)n_bins * BIN_HISTO * 8, cudaMemcpyDeviceToHost,
                                               c->stream), "bin histograms d2h");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "bins compact sync");
+        if (!e && n_groups == 1) goff[1] = gcount[0];
     }
-    uint64_t *keys = k0, *bin_keys = k0;   // sorted records; what the bin bounds search
+    const uint64_t hn = goff[n_groups];
+    // every group sorts the same number of bits, so the groups of more than
+    // one record end in the same buffer; a group that ended in the other one
+    // (a single record: no pass) is moved there
+    uint64_t *keys = k0;
     uint32_t *cnts = v0;
-    int bin_shift = 2 * k;
-    if (!e && wide && hn > 0xFFFFFFFFull)
-        e = set_err(c, TK_E_RANGE, "a batch of bins holds more than 2^32 distinct k-mers: split it");
-    if (!e && (wide ? hn >= 1 : hn > 1)) {
+    if (!e && hn > 1) {
         cudaEvent_t ev;
         prof_begin(c, TK_KID_SORT, &ev);
-        if (!wide) {
-            bool in_tmp = false;
-            e = radix_sort_pairs(c, k0, v0, hn, 2 * k + bin_bits, k1, v1, &in_tmp);
-            keys = bin_keys = in_tmp ? k1 : k0;
-            cnts = in_tmp ? v1 : v0;
-        } else {
-            uint32_t *ia0 = nullptr, *ia1 = nullptr, *jb0 = nullptr, *jb1 = nullptr;
-            uint64_t *bk0 = nullptr, *bk1 = nullptr;
-            e = alloc((void **)&ia0, hn * 4, "record order by k-mer");
-            if (!e) e = alloc((void **)&ia1, hn * 4, "record order by k-mer tmp");
-            if (!e) e = alloc((void **)&jb0, hn * 4, "record order by bin");
-            if (!e) e = alloc((void **)&jb1, hn * 4, "record order by bin tmp");
-            if (!e) e = alloc((void **)&bk0, hn * 8, "record bins");
-            if (!e) e = alloc((void **)&bk1, hn * 8, "record bins tmp");
-            const unsigned grid = (unsigned)c->sm_count * 8;
-            bool ta = false, tb = false;
-            if (!e) {
-                k_bin_iota<<<grid, 256, 0, c->stream>>>(ia0, hn);
-                c->launches++;
-                e = radix_sort_pairs(c, k0, ia0, hn, 2 * k, k1, ia1, &ta);
-            }
-            uint64_t *by_kmer_key = ta ? k1 : k0;
-            uint32_t *by_kmer = ta ? ia1 : ia0;
-            if (!e) {
-                k_bin_gather_bins<<<grid, 256, 0, c->stream>>>(obins, by_kmer, hn, bk0, jb0);
-                c->launches++;
-                e = radix_sort_pairs(c, bk0, jb0, hn, bin_bits, bk1, jb1, &tb);
-            }
-            if (!e) {
-                keys = ta ? k0 : k1;
-                k_bin_gather_final<<<grid, 256, 0, c->stream>>>(by_kmer_key, by_kmer, tb ? jb1 : jb0, v0, hn, keys, v1);
-                c->launches++;
-                cnts = v1;
-                bin_keys = tb ? bk1 : bk0;
-                bin_shift = 0;
-                e = check_launch(c, "bin wide order");
-            }
+        const int bits = 2 * k + gshift;
+        std::vector<char> in_tmp(n_groups, 0);
+        int final_tmp = -1;
+        for (uint32_t g = 0; !e && g < n_groups; g++) {
+            const uint64_t o = goff[g], m = goff[g + 1] - o;
+            if (m == 0) continue;
+            bool t = false;
+            e = radix_sort_pairs(c, k0 + o, v0 + o, m, bits, k1 + o, v1 + o, &t);
+            in_tmp[g] = t;
+            if (m > 1 && final_tmp < 0) final_tmp = t ? 1 : 0;
         }
+        if (final_tmp < 0) final_tmp = 0;
+        for (uint32_t g = 0; !e && g < n_groups; g++) {
+            const uint64_t o = goff[g], m = goff[g + 1] - o;
+            if (m == 0 || in_tmp[g] == final_tmp) continue;
+            uint64_t *ks = in_tmp[g] ? k1 : k0, *kd = final_tmp ? k1 : k0;
+            uint32_t *vs = in_tmp[g] ? v1 : v0, *vd = final_tmp ? v1 : v0;
+            e = cuda_check(c, cudaMemcpyAsync(kd + o, ks + o, m * 8, cudaMemcpyDeviceToDevice, c->stream), "bin key move");
+            if (!e) e = cuda_check(c, cudaMemcpyAsync(vd + o, vs + o, m * 4, cudaMemcpyDeviceToDevice, c->stream), "bin count move");
+        }
+        keys = final_tmp ? k1 : k0;
+        cnts = final_tmp ? v1 : v0;
         prof_end(c, TK_KID_SORT, ev, hn);
     }
-    uint64_t *first = nullptr, *d_text0 = nullptr, *offs = nullptr;
-    uint32_t *lens = nullptr;
+    uint64_t *first = nullptr, *d_text0 = nullptr, *d_goff = nullptr, *offs = nullptr;
     uint64_t text_len = 0;
     char *d_dump = nullptr;
     if (!e) e = alloc((void **)&first, (n_bins + 1) * 8, "bin first record");
     if (!e) e = alloc((void **)&d_text0, (n_bins + 1) * 8, "bin text offsets");
-    if (!e) e = alloc((void **)&lens, std::max<uint64_t>(hn, 1) * 4, "bin record lengths");
-    if (!e) e = alloc((void **)&offs, (std::max<uint64_t>(hn, 1) + 1) * 8, "bin record offsets");
+    if (!e) e = alloc((void **)&d_goff, (n_groups + 1) * 8, "bin group offsets");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(d_goff, goff.data(), (n_groups + 1) * 8, cudaMemcpyHostToDevice, c->stream),
+                           "bin group offsets");
     if (!e) {
-        cudaEvent_t ev;
-        prof_begin(c, TK_KID_DUMP, &ev);
-        k_bin_bounds<<<(n_bins + 256) / 256, 256, 0, c->stream>>>(bin_keys, hn, bin_shift, n_bins, first);
+        k_bin_bounds<<<(n_bins + 256) / 256, 256, 0, c->stream>>>(keys, d_goff, gshift, k, n_bins, hn, first);
         c->launches++;
-        if (hn) {
-            k_bin_dump_len<<<(unsigned)((hn + 255) / 256), 256, 0, c->stream>>>(cnts, hn, k, lens);
-            c->launches++;
-            e = scan_excl_u32_to_u64(c, lens, offs, hn, &text_len);
-        }
-        if (!e) e = dmalloc(c, (void **)&d_dump, std::max<uint64_t>(text_len, 1), "bin dump text");
-        if (!e && hn) {
-            k_bin_dump_write<<<(unsigned)((hn + 255) / 256), 256, 0, c->stream>>>(keys, cnts, offs, hn, k, d_dump);
-            c->launches++;
-        }
-        if (!e) {
-            k_bin_text_bounds<<<(n_bins + 256) / 256, 256, 0, c->stream>>>(first, offs, hn, text_len, n_bins, d_text0);
-            c->launches++;
-            out->text0.resize(n_bins + 1);
-            e = cuda_check(c, cudaMemcpyAsync(out->text0.data(), d_text0, (n_bins + 1) * 8, cudaMemcpyDeviceToHost, c->stream), "text bounds");
-        }
-        prof_end(c, TK_KID_DUMP, ev, hn);
+        // K4 formats the low 2k bits of each key
+        e = format_dump(c, keys, cnts, hn, k, &d_dump, &text_len, &offs);
+    }
+    if (!e) {
+        k_bin_text_bounds<<<(n_bins + 256) / 256, 256, 0, c->stream>>>(first, offs, hn, text_len, n_bins, d_text0);
+        c->launches++;
+        out->text0.resize(n_bins + 1);
+        e = cuda_check(c, cudaMemcpyAsync(out->text0.data(), d_text0, (n_bins + 1) * 8, cudaMemcpyDeviceToHost, c->stream),
+                       "text bounds");
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "bins dump sync");
     }
+    if (offs) dfree(c, offs);
     if (slots) dfree(c, slots);
     cleanup();
     if (e) {

@@ -363,6 +363,9 @@ void prof_add_units(tk_ctx *c, int kid, uint64_t units);
 int check_launch(tk_ctx *c, const char *what);
 int scan_excl_u64(tk_ctx *c, const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *total_host);
 int scan_excl_u32_to_u64(tk_ctx *c, const uint32_t *in, uint64_t *out, uint64_t n, uint64_t *total_host);
+// K4 formatting of sorted (key, count) pairs (tk_table.cu)
+int format_dump(tk_ctx *c, const uint64_t *keys, const uint32_t *cnt, uint64_t n, int k, char **text, uint64_t *len,
+                uint64_t **offs_out = nullptr);
 int radix_sort_pairs(tk_ctx *c, uint64_t *keys, uint32_t *vals, uint64_t n, int bits,
                      uint64_t *tmp_keys, uint32_t *tmp_vals, bool *result_in_tmp, int first_bit = 0);
 int table_alloc(tk_table *t, uint64_t capacity);

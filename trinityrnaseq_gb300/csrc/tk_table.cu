@@ -1213,11 +1213,14 @@ int table_sorted_pairs(tk_table *t, uint32_t min_count, uint64_t **keys_out, uin
     return TK_OK;
 }
 
-// K4: format sorted pairs as ">COUNT\nKMER\n" into a device buffer.
+// K4: format sorted pairs as ">COUNT\nKMER\n" into a device buffer (the low
+// 2k bits of each key); with offs_out, the n record start offsets are handed
+// to the caller (its device block to free) instead of freed.
 int format_dump(tk_ctx *c, const uint64_t *keys, const uint32_t *cnt, uint64_t n, int k, char **text_out,
-                uint64_t *len_out) {
+                uint64_t *len_out, uint64_t **offs_out) {
     *text_out = nullptr;
     *len_out = 0;
+    if (offs_out) *offs_out = nullptr;
     if (n == 0) return TK_OK;
     uint32_t *lens = nullptr;
     uint64_t *offs = nullptr;
@@ -1240,11 +1243,13 @@ int format_dump(tk_ctx *c, const uint64_t *keys, const uint32_t *cnt, uint64_t n
     }
     prof_end(c, TK_KID_DUMP, ev, n);
     dfree(c, lens);
-    if (offs) dfree(c, offs);
     if (e) {
+        if (offs) dfree(c, offs);
         if (text) dfree(c, text);
         return e;
     }
+    if (offs_out) *offs_out = offs;
+    else dfree(c, offs);
     *text_out = text;
     *len_out = total;
     return TK_OK;
