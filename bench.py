@@ -1015,11 +1015,12 @@ def served_bench(ctx, args):
                 while time.time() < t_next:
                     time.sleep(min(0.0005, max(0.0, t_next - time.time())))
                 ids.append(submit(srv, kind, a, b))
-            lat, sts = [], []
+            lat, sts, queued = [], [], []
             for jid in ids:
-                st, l_ms, _ = srv.wait(jid)
+                st, l_ms, q_ms = srv.wait(jid)
                 sts.append(st)
                 lat.append(l_ms)
+                queued.append(q_ms)
             wall = time.time() - start
             ok = all(s == 0 for s in sts)
             for jid, (kind, *_), want in zip(ids, jobs, alone):
@@ -1028,6 +1029,16 @@ def served_bench(ctx, args):
             maxc = srv.stats()[2]
             nbatched = srv.batched_jobs() - batched0
             held = srv.held_by_free_memory()
+        # where the tail comes from: time queued before a slot took the job,
+        # time in the slot, and the tail per job kind
+        pct = lambda xs, f: sorted(xs)[min(len(xs) - 1, int(f * len(xs)))] if xs else None
+        service = [l - q for l, q in zip(lat, queued)]
+        by_kind = {}
+        for (kind, *_), l in zip(jobs, lat):
+            by_kind.setdefault({N.TK_JOB_COUNT: "count", N.TK_JOB_NORMALIZE: "normalize"}.get(kind, "r2t"), []).append(l)
+        tail = {"p99_queued_ms": pct(queued, 0.99), "p99_in_slot_ms": pct(service, 0.99),
+                "p50_in_slot_ms": pct(service, 0.5),
+                "p99_ms_by_kind": {k: pct(v, 0.99) for k, v in by_kind.items()}}
         lat.sort()
         name = "burst" if load == float("inf") else f"{load}x"
         levels[name] = {"offered_jobs_per_s": capacity * load if load != float("inf") else None,
@@ -1035,7 +1046,7 @@ def served_bench(ctx, args):
                               "reads_per_s": total_reads / wall, "p50_ms": lat[len(lat) // 2],
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_concurrent": maxc,
                               "jobs_in_batched_passes": nbatched, "admissions_held_by_free_hbm": held,
-                              "bit_exact_vs_plain": bool(ok)}
+                              **tail, "bit_exact_vs_plain": bool(ok)}
     return {"workload": f"{len(jobs)} jobs (60% count, 30% normalize with selection and extraction, "
                         f"10% read-to-component), reads log-uniform "
                         f"10k..{args.job_max_reads}, Poisson arrivals; {args.slots} slots, {args.budget_gb} GB budget",

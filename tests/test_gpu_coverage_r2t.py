@@ -75,12 +75,13 @@ def test_stats_long_and_odd_reads(ctx, oracle, golden):
     assert_stats(got, oracle.cov_values(text, keys, counts, 25, True))
 
 
-def window_class_reads(seed, k, n_per_len=3):
+def window_class_reads(seed, k, n_per_len=3, nwins=None):
     """Reads whose window counts straddle every per-lane register class of the
     warp path (1, 2, 4, 8 values per lane) and the long-read path, a third of
     them with an N."""
     rnd = np.random.default_rng(seed)
-    nwins = [0, 1, 2, 31, 32, 33, 63, 64, 65, 76, 127, 128, 129, 200, 255, 256, 257, 300]
+    if nwins is None:
+        nwins = [0, 1, 2, 31, 32, 33, 63, 64, 65, 76, 127, 128, 129, 200, 255, 256, 257, 300]
     out = []
     for nw in nwins:
         for i in range(n_per_len):
@@ -100,6 +101,19 @@ def test_stats_every_window_class_and_k(ctx, oracle, k, ds):
     keys, counts = oracle.count(catalogue, k, ds)
     rs, got = stats_gpu(ctx, catalogue, text, k, ds)
     assert_stats(got, oracle.cov_values(text, keys, counts, k, ds))
+
+
+@pytest.mark.parametrize("longest", [96, 128])
+@pytest.mark.parametrize("ds", [True, False])
+def test_stats_narrow_read_sets(ctx, oracle, longest, ds):
+    """Read sets whose longest read has at most 96 or 128 windows go to the
+    kernels compiled only for those classes (8 blocks per SM)."""
+    nw = [w for w in (0, 1, 2, 31, 32, 33, 63, 64, 65, 76, 95, 96, 97, 127, 128) if w <= longest]
+    text = window_class_reads(7, 25, 4, nw) + synth.transcriptome_reads(seed=8, n_reads=20000).tobytes()
+    catalogue = text + window_class_reads(107, 25, 4, nw)
+    keys, counts = oracle.count(catalogue, 25, ds)
+    rs, got = stats_gpu(ctx, catalogue, text, 25, ds)
+    assert_stats(got, oracle.cov_values(text, keys, counts, 25, ds))
 
 
 def test_stats_parity_1M_reads(ctx, oracle):

@@ -9,8 +9,8 @@
 // mean and stdev come from exact integer sums (see finish_stats).
 //
 // Reads with at most 256 windows: one warp per read, values in registers,
-// warp bitonic sort (tk_warp.cuh).  Longer reads: one block per read, values
-// in a global scratch slab, block bitonic sort.
+// median by a warp radix select (tk_warp.cuh).  Longer reads: one block per
+// read, values in a global scratch slab, block bitonic sort.
 //
 // Coverage cache.  The reads whose coverage is asked for are, in Trinity's
 // use, the reads that were counted (insilico_read_normalization.pl counts
@@ -26,7 +26,11 @@
 // do not depend on what the cache holds.  Random lookups into HBM run at
 // ~40 G/s on GB300 whatever the table size above 1 GB, and into an
 // L2-resident table at ~300 G/s; at the plain path's scale the 6-7M k-mers
-// the cache holds answer ~70% of the lookups.
+// the cache holds answer ~70% of the lookups.  (Most lookups the cache
+// misses are k-mers seen once, whose answer is 1.  A 32 or 64 MB bit filter
+// of the keys whose count is not 1, consulted before the table, made the pass
+// ~8% slower on GB300: its lines share L2 with the cache's, and a lookup that
+// passes it pays two dependent loads.)
 #include "tk_warp.cuh"
 
 #include <algorithm>
@@ -287,8 +291,10 @@ __device__ __forceinline__ ReadSums cov_warp_read(const CovCache &cc, DevTable t
 // warp instruction whatever the number of active lanes, so finishing 32 reads
 // in one pass costs what one read alone would.  Reads with more than
 // CV_WARP_MAX windows are appended to long_list (or, with no list, left to a
-// separate pass) and not written here.
-template <bool CANON>
+// separate pass) and not written here.  MAXS = the largest window class
+// compiled in (windows per lane); a read set whose reads all have at most
+// 32 * MAXS windows needs no larger one.
+template <bool CANON, int MAXS = 8>
 __device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, const uint64_t *__restrict__ codes,
                                                const uint32_t *__restrict__ inv,
                                                const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k, uint64_t r0,
@@ -312,9 +318,9 @@ __device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, c
         if (nwin <= 32) rs = cov_warp_read<1, CANON>(cc, t, codes, inv, start, nwin, k);
         else if (nwin <= 64) rs = cov_warp_read<2, CANON>(cc, t, codes, inv, start, nwin, k);
         else if (nwin <= 96) rs = cov_warp_read<3, CANON>(cc, t, codes, inv, start, nwin, k);
-        else if (nwin <= 128) rs = cov_warp_read<4, CANON>(cc, t, codes, inv, start, nwin, k);
-        else if (nwin <= 192) rs = cov_warp_read<6, CANON>(cc, t, codes, inv, start, nwin, k);
-        else if (nwin <= CV_WARP_MAX) rs = cov_warp_read<8, CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (MAXS >= 4 && nwin <= 128) rs = cov_warp_read<(MAXS >= 4 ? 4 : 1), CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (MAXS >= 6 && nwin <= 192) rs = cov_warp_read<(MAXS >= 6 ? 6 : 1), CANON>(cc, t, codes, inv, start, nwin, k);
+        else if (MAXS >= 8 && nwin <= CV_WARP_MAX) rs = cov_warp_read<(MAXS >= 8 ? 8 : 1), CANON>(cc, t, codes, inv, start, nwin, k);
         else {
             is_long = true;
             if (long_list && lane == 0) long_list[atomicAdd(long_n, 1ULL)] = (uint32_t)r;
@@ -336,8 +342,10 @@ __device__ __forceinline__ void cov_warp_chunk(const CovCache &cc, DevTable t, c
     }
 }
 
-template <bool CANON>
-__global__ void __launch_bounds__(CV_THREADS, 6) k_coverage(CovCache cc, DevTable t, const uint64_t *__restrict__ codes,
+// MAXS 3 / 4: read sets whose reads have at most 96 / 128 windows (up to 120 /
+// 152 nt at k = 25), 8 blocks per SM; MAXS 8: every read, 6 blocks per SM.
+template <bool CANON, int MAXS>
+__global__ void __launch_bounds__(CV_THREADS, MAXS <= 4 ? 8 : 6) k_coverage(CovCache cc, DevTable t, const uint64_t *__restrict__ codes,
                                                         const uint32_t *__restrict__ inv,
                                                         const uint64_t *__restrict__ rd_off, uint64_t n_reads, int k,
                                                         uint32_t *__restrict__ median, float *__restrict__ mean,
@@ -347,8 +355,8 @@ __global__ void __launch_bounds__(CV_THREADS, 6) k_coverage(CovCache cc, DevTabl
     const uint64_t warps = (uint64_t)gridDim.x * (CV_THREADS / 32);
     const uint64_t chunks = (n_reads + 31) / 32;
     for (uint64_t ch = (uint64_t)blockIdx.x * (CV_THREADS / 32) + (threadIdx.x >> 5); ch < chunks; ch += warps)
-        cov_warp_chunk<CANON>(cc, t, codes, inv, rd_off, n_reads, k, ch * 32, median, mean, stdev, long_list, long_n,
-                              held + (threadIdx.x & ~31u));
+        cov_warp_chunk<CANON, MAXS>(cc, t, codes, inv, rd_off, n_reads, k, ch * 32, median, mean, stdev, long_list,
+                                    long_n, held + (threadIdx.x & ~31u));
 }
 
 // long reads: one block per read, `slab` = this block's scratch (n2max values)
@@ -438,12 +446,20 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
     if (!e) {
         // one wave of resident blocks, each warp striding over the 32-read
         // chunks (a grid of several partial waves leaves SMs idle at its end)
-        static int per_sm[2] = {0, 0};
-        const int ci = t->canonical ? 1 : 0;
+        // the narrowest kernel that holds the longest read's windows
+        static int per_sm[6] = {0, 0, 0, 0, 0, 0};
+        const uint64_t max_win = rd->max_len >= (uint32_t)k ? rd->max_len - k + 1 : 0;
+        const int ci = (t->canonical ? 1 : 0) + (max_win <= 96 ? 4 : max_win <= 128 ? 2 : 0);
         if (!per_sm[ci]) {
             int b = 0;
-            if (t->canonical) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<true>, CV_THREADS, 0);
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<false>, CV_THREADS, 0);
+            switch (ci) {
+            case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<false, 8>, CV_THREADS, 0); break;
+            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<true, 8>, CV_THREADS, 0); break;
+            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<false, 4>, CV_THREADS, 0); break;
+            case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<true, 4>, CV_THREADS, 0); break;
+            case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<false, 3>, CV_THREADS, 0); break;
+            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_coverage<true, 3>, CV_THREADS, 0); break;
+            }
             per_sm[ci] = std::max(1, b);
         }
         const uint64_t chunks = (n + 31) / 32;
@@ -452,12 +468,18 @@ int coverage_stats(tk_table *t, const tk_reads *rd, uint32_t *d_median, float *d
                                   (uint64_t)c->sm_count * (uint64_t)per_sm[ci]));
         cudaEvent_t ev;
         prof_begin(c, TK_KID_COVERAGE, &ev);
-        if (t->canonical)
-            k_coverage<true><<<grid, CV_THREADS, 0, c->stream>>>(cc, dt, rd->d_codes, rd->d_inv, rd->d_rd_off, n, k,
-                                                                 d_median, d_mean, d_stdev, long_list, long_n);
-        else
-            k_coverage<false><<<grid, CV_THREADS, 0, c->stream>>>(cc, dt, rd->d_codes, rd->d_inv, rd->d_rd_off, n, k,
-                                                                  d_median, d_mean, d_stdev, long_list, long_n);
+#define TK_COV_LAUNCH(C, M)                                                                                   \
+    k_coverage<C, M><<<grid, CV_THREADS, 0, c->stream>>>(cc, dt, rd->d_codes, rd->d_inv, rd->d_rd_off, n, k, d_median, \
+                                                         d_mean, d_stdev, long_list, long_n)
+        switch (ci) {
+        case 0: TK_COV_LAUNCH(false, 8); break;
+        case 1: TK_COV_LAUNCH(true, 8); break;
+        case 2: TK_COV_LAUNCH(false, 4); break;
+        case 3: TK_COV_LAUNCH(true, 4); break;
+        case 4: TK_COV_LAUNCH(false, 3); break;
+        default: TK_COV_LAUNCH(true, 3); break;
+        }
+#undef TK_COV_LAUNCH
         c->launches++;
         prof_end(c, TK_KID_COVERAGE, ev, rd->n_bases);
         e = check_launch(c, "coverage");
