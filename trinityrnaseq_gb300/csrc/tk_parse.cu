@@ -197,86 +197,104 @@ __global__ void k_fastq_records(uint64_t *__restrict__ line_rec, uint64_t n_line
     if ((j & 3) == 0) hdr_line[j >> 2] = j;
 }
 
-// ---- fast path, copy.  A warp takes 32 consecutive lines: lane l loads line
-// l's metadata (coalesced), header lines record their read's start, and then
-// the warp copies the group's sequence lines one after another, 32 bytes per
-// step with four steps in flight, upper-casing into seq.  A sequence line
-// holding whitespace sets *ws_seen and the byte-wise path redoes the emit.
-// The 4 bytes at offset so of a line of n bytes starting at text position S;
-// bytes outside the line read as 'A' (neither whitespace nor lower case).
-// Two aligned 4-byte loads and a funnel shift when the text is aligned and
-// both words lie inside it, byte loads otherwise.
-__device__ __forceinline__ uint32_t line_word(const ParseGeom &g, uint64_t S, int64_t so, uint32_t n) {
+// ---- fast path, copy.  A warp takes 32 consecutive lines (or records): lane l
+// loads line l's metadata (coalesced), header lines record their read's start,
+// and then the warp copies the group's sequence lines in aligned 16-byte
+// output words (copy_group), upper-casing into seq.  A sequence line holding
+// whitespace sets *ws_seen and the byte-wise path redoes the emit.
+// The 16 bytes at offset so of a line of n bytes starting at text position
+// S, as four words; bytes outside the line read as 'A'.  Five aligned 4-byte
+// loads and funnel shifts when the text is aligned and they lie inside it,
+// byte loads otherwise.
+__device__ __forceinline__ void line_word16(const ParseGeom &g, uint64_t S, int64_t so, uint32_t n, uint32_t (&x)[4]) {
     const int64_t a = (int64_t)S + so;
-    uint32_t x;
-    if (g.vec && a >= 0 && (uint64_t)((a & ~3LL) + 8) <= g.len) {
+    if (g.vec && a >= 0 && (uint64_t)((a & ~3LL) + 20) <= g.len) {
         const uint32_t *p = reinterpret_cast<const uint32_t *>(g.text + (a & ~3LL));
-        x = __funnelshift_r(__ldg(p), __ldg(p + 1), 8u * (uint32_t)(a & 3));
-    } else {
-        x = 0;
-        for (int i = 0; i < 4; i++) {
-            const int64_t q = so + i;
-            const uint32_t c = (q >= 0 && q < (int64_t)n) ? (uint8_t)g.text[S + q] : 0x41u;
-            x |= c << (8 * i);
-        }
-        return x;
-    }
-    if (so >= 0 && so + 4 <= (int64_t)n) return x;
+        const uint32_t sh = 8u * (uint32_t)(a & 3);
+        uint32_t w[5];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
-        if (so + i < 0 || so + i >= (int64_t)n) x = (x & ~(0xFFu << (8 * i))) | (0x41u << (8 * i));
-    return x;
+        for (int i = 0; i < 5; i++) w[i] = __ldg(p + i);
+#pragma unroll
+        for (int i = 0; i < 4; i++) x[i] = __funnelshift_r(w[i], w[i + 1], sh);
+        if (so >= 0 && so + 16 <= (int64_t)n) return;
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            if (so + i < 0 || so + i >= (int64_t)n) x[i >> 2] = (x[i >> 2] & ~(0xFFu << (8 * (i & 3)))) | (0x41u << (8 * (i & 3)));
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        x[j] = 0;
+        for (int i = 0; i < 4; i++) {
+            const int64_t q = so + 4 * j + i;
+            const uint32_t c = (q >= 0 && q < (int64_t)n) ? (uint8_t)g.text[S + q] : 0x41u;
+            x[j] |= c << (8 * i);
+        }
+    }
+}
+
+// Upper-cases a word of bases; notes whether it held whitespace (' ' or 9..13).
+__device__ __forceinline__ uint32_t upcase_word(uint32_t x, bool &ws) {
+    const uint32_t t = x & 0x7F7F7F7Fu;
+    // bit 7 of each byte that is a-z, then of each byte that is ' ' or 9..13
+    const uint32_t lower = (t + 0x1F1F1F1Fu) & ~(t + 0x05050505u) & ~x & 0x80808080u;
+    const uint32_t sp = x ^ 0x20202020u;
+    const uint32_t zsp = ~(((sp & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | sp) & 0x80808080u;
+    const uint32_t rng = (t + 0x77777777u) & ~(t + 0x72727272u) & ~x & 0x80808080u;
+    ws |= (zsp | rng) != 0u;
+    return x ^ (lower >> 2);
 }
 
 // The warp copies the lines its lanes hold (lane l: text[src, src + len) to
-// seq + dst; len 0 = none), four lines at a time, one aligned 4-byte output
-// word per lane and line, all loads in flight before any store; upper-cases
-// and notes whether a line held whitespace.
+// seq + dst; len 0 = none), upper-casing, and notes whether a line held
+// whitespace.  The output is cut into the aligned 16-byte words the lines
+// touch; the warp numbers the words of its 32 lines one after another (a scan
+// of each line's word count) and each lane takes every 32nd, so the lanes stay
+// busy whatever the line lengths; a lane finds its word's line by a binary
+// search over the lanes' first word numbers.  A word wholly inside its line
+// is one 16-byte store; the first and last word of a line (shared with the
+// separator and the neighbouring line) are stored byte by byte.  seq is
+// 16-byte aligned.
 __device__ __forceinline__ void copy_group(const ParseGeom &g, uint64_t src, uint64_t dst, uint32_t len,
                                            uint8_t *__restrict__ seq, bool &ws) {
     const unsigned lane = lane_id();
-    unsigned todo = __ballot_sync(0xffffffffu, len > 0);
-    while (todo) {
-        uint64_t s0[4], d0[4];
-        uint32_t n[4], nw[4], wmax = 0;
+    const uint32_t nw = len ? (uint32_t)(((dst + len + 15) >> 4) - (dst >> 4)) : 0u;
+    uint32_t incl = nw;
 #pragma unroll
-        for (int b = 0; b < 4; b++) {
-            const int l = todo ? __ffs(todo) - 1 : 0;
-            const bool have = todo != 0;
-            todo &= todo - 1;
-            s0[b] = __shfl_sync(0xffffffffu, src, l);
-            d0[b] = __shfl_sync(0xffffffffu, dst, l);
-            n[b] = have ? __shfl_sync(0xffffffffu, len, l) : 0u;
-            nw[b] = n[b] ? (uint32_t)(((d0[b] + n[b] + 3) >> 2) - (d0[b] >> 2)) : 0u;
-            wmax = max(wmax, nw[b]);
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t first = incl - nw;   // this lane's line's first word number
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t t = base + lane;
+        // the last lane whose first word number is <= t: its line holds word t
+        // (a line without words shares its first number with the next line)
+        int i = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t f = __shfl_sync(0xffffffffu, first, (i + step) & 31);
+            if (i + step < 32 && f <= t) i += step;
         }
-        for (uint32_t w0 = 0; w0 < wmax; w0 += 32) {
-            const uint32_t w = w0 + lane;
-            uint32_t x[4];
+        const uint64_t s_i = __shfl_sync(0xffffffffu, src, i);
+        const uint64_t d_i = __shfl_sync(0xffffffffu, dst, i);
+        const uint32_t n_i = __shfl_sync(0xffffffffu, len, i);
+        const uint32_t f_i = __shfl_sync(0xffffffffu, first, i);
+        if (t >= total) continue;
+        const uint64_t out = (d_i & ~15ULL) + 16ull * (t - f_i);   // the word's first output byte
+        const int64_t so = (int64_t)out - (int64_t)d_i;            // its offset in the line
+        uint32_t x[4];
+        line_word16(g, s_i, so, n_i, x);
 #pragma unroll
-            for (int b = 0; b < 4; b++)
-                x[b] = w < nw[b] ? line_word(g, s0[b], (int64_t)4 * w - (int64_t)(d0[b] & 3), n[b]) : 0x41414141u;
+        for (int q = 0; q < 4; q++) x[q] = upcase_word(x[q], ws);
+        uint8_t *o = seq + out;
+        if (so >= 0 && so + 16 <= (int64_t)n_i) {
+            *reinterpret_cast<uint4 *>(o) = make_uint4(x[0], x[1], x[2], x[3]);
+        } else {
 #pragma unroll
-            for (int b = 0; b < 4; b++) {
-                if (w >= nw[b]) continue;
-                const int64_t so = (int64_t)4 * w - (int64_t)(d0[b] & 3);   // line offset of the word's first byte
-                const uint32_t t = x[b] & 0x7F7F7F7Fu;
-                // bit 7 of each byte that is a-z, then of each byte that is ' ' or 9..13
-                const uint32_t lower = (t + 0x1F1F1F1Fu) & ~(t + 0x05050505u) & ~x[b] & 0x80808080u;
-                const uint32_t sp = x[b] ^ 0x20202020u;
-                const uint32_t zsp = ~(((sp & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | sp) & 0x80808080u;
-                const uint32_t rng = (t + 0x77777777u) & ~(t + 0x72727272u) & ~x[b] & 0x80808080u;
-                ws |= (zsp | rng) != 0u;
-                const uint32_t up = x[b] ^ (lower >> 2);
-                uint8_t *o = seq + (d0[b] & ~3ULL) + 4ull * w;
-                if (so >= 0 && so + 4 <= (int64_t)n[b]) {
-                    *reinterpret_cast<uint32_t *>(o) = up;
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-                        if (so + i >= 0 && so + i < (int64_t)n[b]) o[i] = (uint8_t)(up >> (8 * i));
-                }
-            }
+            for (int q = 0; q < 16; q++)
+                if (so + q >= 0 && so + q < (int64_t)n_i) o[q] = (uint8_t)(x[q >> 2] >> (8 * (q & 3)));
         }
     }
 }
