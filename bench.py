@@ -143,7 +143,7 @@ class Clocks:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "sm_mhz_min": min(sm) if sm else None, "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def workload(pairs: int, seed: int):
@@ -1007,6 +1007,8 @@ def served_bench(ctx, args):
                         srv.wait(wid)
                         srv.release(wid)
             batched0 = srv.batched_jobs()   # the warm-up's own batched passes are not counted
+            clocks = Clocks(ctx.device)
+            clocks.start()
             start = time.time()
             ids = []
             t_next = start
@@ -1022,6 +1024,7 @@ def served_bench(ctx, args):
                 lat.append(l_ms)
                 queued.append(q_ms)
             wall = time.time() - start
+            clk = clocks.stop()
             ok = all(s == 0 for s in sts)
             for jid, (kind, *_), want in zip(ids, jobs, alone):
                 ok = ok and same(srv.result(jid, "normalize_select" if kind == N.TK_JOB_NORMALIZE else kind), want)
@@ -1046,7 +1049,7 @@ def served_bench(ctx, args):
                               "reads_per_s": total_reads / wall, "p50_ms": lat[len(lat) // 2],
                               "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "max_concurrent": maxc,
                               "jobs_in_batched_passes": nbatched, "admissions_held_by_free_hbm": held,
-                              **tail, "bit_exact_vs_plain": bool(ok)}
+                              **tail, "clocks": clk, "bit_exact_vs_plain": bool(ok)}
     return {"workload": f"{len(jobs)} jobs (60% count, 30% normalize with selection and extraction, "
                         f"10% read-to-component), reads log-uniform "
                         f"10k..{args.job_max_reads}, Poisson arrivals; {args.slots} slots, {args.budget_gb} GB budget",

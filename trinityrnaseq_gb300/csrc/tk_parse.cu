@@ -202,11 +202,23 @@ __global__ void k_fastq_records(uint64_t *__restrict__ line_rec, uint64_t n_line
 // and then the warp copies the group's sequence lines in aligned 16-byte
 // output words (copy_group), upper-casing into seq.  A sequence line holding
 // whitespace sets *ws_seen and the byte-wise path redoes the emit.
+// Byte mask of the bytes [a, b) of a 4-byte word (0 <= a, b <= 4).
+__device__ __forceinline__ uint32_t byte_mask(int a, int b) {
+    return b > a ? (0xFFFFFFFFu >> (32 - 8 * (b - a))) << (8 * a) : 0u;
+}
+
 // The 16 bytes at offset so of a line of n bytes starting at text position
-// S, as four words; bytes outside the line read as 'A'.  Five aligned 4-byte
-// loads and funnel shifts when the text is aligned and they lie inside it,
-// byte loads otherwise.
-__device__ __forceinline__ void line_word16(const ParseGeom &g, uint64_t S, int64_t so, uint32_t n, uint32_t (&x)[4]) {
+// S, as four words, and per word the mask of its bytes inside the line
+// (bytes outside it read as 'A').  Five aligned 4-byte loads and funnel
+// shifts when the text is aligned and they lie inside it, byte loads
+// otherwise.
+__device__ __forceinline__ void line_word16(const ParseGeom &g, uint64_t S, int64_t so, uint32_t n, uint32_t (&x)[4],
+                                            uint32_t (&in)[4]) {
+    const int64_t rest = (int64_t)n - so;                    // bytes [lo, hi) are in the line
+    const int lo = so < 0 ? (so < -16 ? 16 : (int)-so) : 0;
+    const int hi = rest < 16 ? (rest < 0 ? 0 : (int)rest) : 16;
+#pragma unroll
+    for (int q = 0; q < 4; q++) in[q] = byte_mask(min(max(lo - 4 * q, 0), 4), min(max(hi - 4 * q, 0), 4));
     const int64_t a = (int64_t)S + so;
     if (g.vec && a >= 0 && (uint64_t)((a & ~3LL) + 20) <= g.len) {
         const uint32_t *p = reinterpret_cast<const uint32_t *>(g.text + (a & ~3LL));
@@ -215,20 +227,16 @@ __device__ __forceinline__ void line_word16(const ParseGeom &g, uint64_t S, int6
 #pragma unroll
         for (int i = 0; i < 5; i++) w[i] = __ldg(p + i);
 #pragma unroll
-        for (int i = 0; i < 4; i++) x[i] = __funnelshift_r(w[i], w[i + 1], sh);
-        if (so >= 0 && so + 16 <= (int64_t)n) return;
-#pragma unroll
-        for (int i = 0; i < 16; i++)
-            if (so + i < 0 || so + i >= (int64_t)n) x[i >> 2] = (x[i >> 2] & ~(0xFFu << (8 * (i & 3)))) | (0x41u << (8 * (i & 3)));
+        for (int q = 0; q < 4; q++) x[q] = (__funnelshift_r(w[q], w[q + 1], sh) & in[q]) | (0x41414141u & ~in[q]);
         return;
     }
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        x[j] = 0;
+    for (int q = 0; q < 4; q++) {
+        x[q] = 0;
         for (int i = 0; i < 4; i++) {
-            const int64_t q = so + 4 * j + i;
-            const uint32_t c = (q >= 0 && q < (int64_t)n) ? (uint8_t)g.text[S + q] : 0x41u;
-            x[j] |= c << (8 * i);
+            const int64_t o = so + 4 * q + i;
+            const uint32_t c = (o >= 0 && o < (int64_t)n) ? (uint8_t)g.text[S + o] : 0x41u;
+            x[q] |= c << (8 * i);
         }
     }
 }
@@ -284,17 +292,26 @@ __device__ __forceinline__ void copy_group(const ParseGeom &g, uint64_t src, uin
         if (t >= total) continue;
         const uint64_t out = (d_i & ~15ULL) + 16ull * (t - f_i);   // the word's first output byte
         const int64_t so = (int64_t)out - (int64_t)d_i;            // its offset in the line
-        uint32_t x[4];
-        line_word16(g, s_i, so, n_i, x);
+        uint32_t x[4], in[4];
+        line_word16(g, s_i, so, n_i, x, in);
 #pragma unroll
         for (int q = 0; q < 4; q++) x[q] = upcase_word(x[q], ws);
         uint8_t *o = seq + out;
         if (so >= 0 && so + 16 <= (int64_t)n_i) {
             *reinterpret_cast<uint4 *>(o) = make_uint4(x[0], x[1], x[2], x[3]);
         } else {
+            // a line's first or last word: whole 4-byte pieces inside the
+            // line as words, the piece cut by a line end byte by byte
 #pragma unroll
-            for (int q = 0; q < 16; q++)
-                if (so + q >= 0 && so + q < (int64_t)n_i) o[q] = (uint8_t)(x[q >> 2] >> (8 * (q & 3)));
+            for (int q = 0; q < 4; q++) {
+                if (in[q] == 0xFFFFFFFFu) {
+                    reinterpret_cast<uint32_t *>(o)[q] = x[q];
+                } else if (in[q]) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        if ((in[q] >> (8 * i)) & 0xFFu) o[4 * q + i] = (uint8_t)(x[q] >> (8 * i));
+                }
+            }
         }
     }
 }
@@ -476,6 +493,8 @@ __global__ void k_names(ParseGeom g, const uint64_t *__restrict__ hdr_line, int 
         const uint64_t ls = j == 0 ? g.S : line_end[j - 1] + 1;
         const uint64_t le = line_end[j];
         uint64_t s = ls + 1, q = s;
+        // byte by byte: a thread's header bytes share sectors, and 16-byte
+        // word loads of unrelated headers per lane were slower
         while (q < le && !is_ws((uint8_t)g.text[q])) q++;
         name_off[r] = s;
         name_len[r] = (uint32_t)(q - s);

@@ -181,22 +181,28 @@ __device__ __forceinline__ void lane_windows_codes(const uint64_t *__restrict__ 
 
 // Element m (0-based, ascending) of the warp's valid values -- value v[j] of a
 // lane counts when bit j of its vm is set -- by a bit-serial radix select from
-// the top bit of the largest value: per bit, the values that agree with the
-// prefix chosen so far and have a 0 there are counted with one warp-wide add;
-// the target has a 0 there when m is below that count.  Costs one pass per
-// significant bit of the largest count instead of a full sort.
+// the top bit of the largest value: per bit, the values still in the running
+// (valid, and equal to the prefix chosen so far above this bit: bit j of
+// `alive`) that have a 0 there are counted with one warp-wide add; the target
+// has a 0 there when m is below that count, and the running set shrinks to
+// the values on the target's side.  Costs one pass per significant bit of the
+// largest count instead of a full sort.
 template <int S>
 __device__ __forceinline__ uint32_t warp_select(const uint32_t (&v)[S], uint32_t vm, uint32_t m, uint32_t mx) {
     // mx: the largest valid value of the warp
-    uint32_t prefix = 0;
+    uint32_t prefix = 0, alive = vm;
     for (int b = 31 - __clz(mx); b >= 0; b--) {   // no pass when every value is 0
-        uint32_t c = 0;
+        uint32_t ones = 0;
 #pragma unroll
-        for (int j = 0; j < S; j++) c += (((vm >> j) & 1u) && ((v[j] ^ prefix) >> b) == 0) ? 1u : 0u;
-        c = __reduce_add_sync(0xffffffffu, c);
-        if (m >= c) {
+        for (int j = 0; j < S; j++) ones |= ((v[j] >> b) & 1u) << j;
+        const uint32_t zeros = alive & ~ones;
+        const uint32_t c = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(zeros));
+        if (m < c) {
+            alive = zeros;
+        } else {
             m -= c;
             prefix |= 1u << b;
+            alive &= ones;
         }
     }
     return prefix;
