@@ -353,6 +353,33 @@ def leg_done(name, out):
         empty()
 
 
+def parse_only(args):
+    """The parse of one mate file resident in HBM (the left mates of the
+    --pairs workload), six times, CUDA events around each: a small fixed
+    command for per-kernel captures of the parse."""
+    import torch
+    from trinityrnaseq_gb300 import Context
+    from trinityrnaseq_gb300 import kmer
+    ctx = Context(0)
+    left, _ = workload(args.pairs, SEED)
+    dev = torch.device("cuda:0")
+    d = torch.from_numpy(left).to(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            rs = kmer.ReadSet(ctx, d.data_ptr(), d.numel(), device=True)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        rs.free()
+    return {"parse_only": {"records": args.pairs, "fastq_bytes": int(left.nbytes), "ms": ms,
+                           "what": "ReadSet of the left mates from HBM; the first parse sizes the buffers"}}
+
+
 def run_gpu(args, dist, world, rank, local):
     import torch
     from trinityrnaseq_gb300 import Context, native
@@ -1211,7 +1238,12 @@ def main():
     ap.add_argument("--job-max-reads", type=int, default=2_000_000)
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--parse-only", action="store_true",
+                    help="only time the parse of the left mates, six times (for kernel captures)")
     args = ap.parse_args()
+    if args.parse_only:
+        print(json.dumps(parse_only(args)), flush=True)
+        return
     world, rank, local = dist_env()
     if args.impl == "reference":
         out = run_reference(args, world, rank)
