@@ -246,4 +246,11 @@ def test_extract_copy_async_overlaps_the_next_extraction(ctx):
     ctx.synchronize()
     for b, n, w in zip(bufs, lens, want):
         assert b.numpy()[:n].tobytes() == w
+    # several extractions in flight at once (each earlier text kept until its
+    # copy ends), then the handle freed before anything is waited for
+    more = [torch.zeros(len(want[i % 2]) + 16, dtype=torch.uint8).pin_memory() for i in range(5)]
+    lens = [nm.extract_into(sides[i % 2], b.data_ptr(), b.numel(), overlap=True) for i, b in enumerate(more)]
     nm.free()
+    ctx.synchronize()
+    for i, (b, n) in enumerate(zip(more, lens)):
+        assert b.numpy()[:n].tobytes() == want[i % 2]

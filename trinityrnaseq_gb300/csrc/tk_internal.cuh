@@ -344,6 +344,7 @@ struct tk_norm {
     char *d_ext = nullptr;                         // last extraction
     uint64_t ext_len = 0;
     cudaEvent_t ext_copy_done = nullptr;           // an asynchronous host copy of d_ext in flight
+    std::vector<std::pair<char *, cudaEvent_t>> ext_retired;   // earlier extractions whose host copy may still run
     uint32_t *d_hash = nullptr;                    // selected names: row index per slot, ~0 empty
     uint8_t *d_keydup = nullptr;                   // per row: its name is another row's, or empty
     uint64_t hash_mask = 0;

@@ -1420,15 +1420,43 @@ int norm_table(tk_norm *nm) {
 
 // The records of sets[0..nsets) (one side's files or pieces, in order) that
 // the selection holds; every selected name must be found in one of them.
+// Earlier extractions' device texts whose host copies have ended go back to
+// the allocator; with `all`, every one, the context's stream first waiting
+// for the copies still running (so a later user of a block is ordered after
+// them).
+static void ext_reap(tk_norm *nm, bool all) {
+    tk_ctx *c = nm->ctx;
+    auto &r = nm->ext_retired;
+    size_t keep = 0;
+    for (size_t i = 0; i < r.size(); i++) {
+        if (all || cudaEventQuery(r[i].second) == cudaSuccess) {
+            cudaStreamWaitEvent(c->stream, r[i].second, 0);
+            dfree(c, r[i].first);
+            cudaEventDestroy(r[i].second);
+        } else {
+            r[keep++] = r[i];
+        }
+    }
+    r.resize(keep);
+    cudaGetLastError();   // a query that reported a copy still running
+}
+
 int norm_extract(tk_norm *nm, const tk_reads *const *sets, uint32_t nsets) {
     tk_ctx *c = nm->ctx;
-    // the device text is released in stream order after its host copy ends
-    if (nm->ext_copy_done) cudaStreamWaitEvent(c->stream, nm->ext_copy_done, 0);
+    // the previous text, if its host copy may still run, is retired with that
+    // copy's event rather than waited for: this extraction runs while the
+    // previous one downloads
     if (nm->d_ext) {
-        dfree(c, nm->d_ext);
+        if (nm->ext_copy_done) {
+            nm->ext_retired.emplace_back(nm->d_ext, nm->ext_copy_done);
+            nm->ext_copy_done = nullptr;
+        } else {
+            dfree(c, nm->d_ext);
+        }
         nm->d_ext = nullptr;
         nm->ext_len = 0;
     }
+    ext_reap(nm, false);
     cudaEvent_t ev = nullptr;
     prof_begin(c, TK_KID_EXTRACT, &ev);
     const uint64_t P = nm->n_rows;
@@ -1541,6 +1569,7 @@ void norm_release(tk_norm *nm) {
         cudaEventDestroy(nm->ext_copy_done);
         nm->ext_copy_done = nullptr;
     }
+    ext_reap(nm, true);
     side_free(c, nm->side[0]);
     side_free(c, nm->side[1]);
     void *p[] = {nm->row_l, nm->row_r, nm->row_n, nm->acc_off, nm->d_accs, nm->d_table, nm->d_ext, nm->d_hash,
