@@ -46,9 +46,13 @@ MIN_COUNT = 2           # the catalogue fastaToKmerCoverageStats reads (util/ins
 L2_BYTES = 129 * 2**20
 E2E_PIECES = 2          # record-aligned pieces per mate file on the end-to-end path
 NORM_ARGS = (200, 1, 10000)   # normalization: Trinity's --max_cov 200 --min_cov 1 --max_CV 10000
-# ncu, one k_coverage launch at 20M pairs (one mate: 1,516,211,092 lookups):
-# dram__bytes_read.sum 115.28 GB + dram__bytes_write.sum 1.51 GB
-COV_DRAM_BYTES_PER_LOOKUP = (115.28e9 + 1.51e9) / (3_032_422_183 / 2)
+# ncu (--cache-control none), one k_coverage launch at 20M pairs (one mate:
+# 1,516,211,092 lookups): dram__bytes_read.sum 121.66 GB + dram__bytes_write.sum 2.11 GB
+COV_DRAM_BYTES_PER_LOOKUP = (121.66e9 + 2.11e9) / (3_032_422_183 / 2)
+# ncu (--cache-control none), the 1537 count launches of one step at 20M pairs
+# (512 x k_sr_hist, k_sr_scatter, k_sr_build + k_insert_pairs): 48.63 GB read +
+# 39.53 GB written, for 3,032,422,183 occurrences
+COUNT_DRAM_BYTES_PER_OCCURRENCE = (48.63e9 + 39.53e9) / 3_032_422_183
 
 
 def log(*a):
@@ -469,9 +473,15 @@ def run_gpu(args, dist, world, rank, local):
         cov_launches = max(per_step["coverage"][1], 1)
         kernels["coverage"]["traffic"] = COV_DRAM_BYTES_PER_LOOKUP * windows / cov_launches
         kernels["coverage"]["traffic_source"] = (
-            "ncu capture of one k_coverage launch at 20M pairs (115.28 GB read + 1.51 GB written), "
-            + ("this workload" if args.pairs == FULL_PAIRS else
-               f"scaled by lookups: {COV_DRAM_BYTES_PER_LOOKUP:.0f} DRAM bytes per lookup"))
+            "ncu capture (--cache-control none) of one k_coverage launch at 20M pairs (121.66 GB read + 2.11 GB "
+            "written), " + ("this workload" if args.pairs == FULL_PAIRS else
+                            f"scaled by lookups: {COV_DRAM_BYTES_PER_LOOKUP:.0f} DRAM bytes per lookup"))
+        ins_launches = max(per_step["count"][1], 1)
+        kernels["insert"]["traffic"] = COUNT_DRAM_BYTES_PER_OCCURRENCE * windows / ins_launches
+        kernels["insert"]["traffic_source"] = (
+            "ncu capture (--cache-control none) of one step's 1537 count launches at 20M pairs (48.63 GB read + "
+            "39.53 GB written), per launch" + ("" if args.pairs == FULL_PAIRS else
+                                               f", scaled by occurrences: {COUNT_DRAM_BYTES_PER_OCCURRENCE:.1f} B each"))
         # the dominant kernel: k_coverage, one kernel with ~29% of the step in
         # the launch list; the count's ~28% is spread over three kernels
         # (k_sr_build, the largest, ~12%), reported under roofline_kernels

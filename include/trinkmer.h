@@ -348,8 +348,9 @@ int tk_norm_extract_copy(const tk_norm *norm, int where, char *out, uint64_t cap
  * is copied to `out` on the context's copy stream while later work on the
  * context runs (e.g. the other side's tk_norm_extract).  `out` (page-locked
  * for the copy to overlap) holds the text once tk_ctx_synchronize returns; a
- * later extraction or tk_norm_free waits for the copy before it reuses the
- * device text.  No counterpart in the reference (make_normalized_reads_file
+ * later extraction does not wait for the copy (the earlier device text is
+ * kept until its copy has ended), and tk_norm_free orders the context's
+ * later work after it.  No counterpart in the reference (make_normalized_reads_file
  * writes each side's file in turn, insilico:470-584). */
 int tk_norm_extract_copy_async(tk_norm *norm, char *out, uint64_t cap);
 void tk_norm_free(tk_norm *norm);
