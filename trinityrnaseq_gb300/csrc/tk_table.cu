@@ -299,10 +299,14 @@ __global__ void __launch_bounds__(CT_THREADS) k_part_step(const uint64_t *__rest
 // linear-probing table.  Global atomics drop from two per occurrence to the
 // deferred keys alone, and a fresh slice needs no separate fill.
 constexpr int SR_MIN_LBITS = 12;        // slices below 4096 slots keep the atomic path
-constexpr int SR_BUILD_PER_SM = 4;      // build blocks resident per SM: the slice is cut into one wave of ranges
-constexpr int SR_MAX_SLOTS = 4600;      // slots of one range in shared memory (12 bytes each)
+// Two build blocks of 1024 threads per SM (32 registers, 110 KB of shared
+// memory each) with ranges of up to 9200 slots: half the ranges per slice of
+// four 512-thread blocks with 4600, so the regrouping passes' per-range work
+// (counts, cursor atomics, runs) halves; 58.1 -> 50.9 ms per step at 20M pairs.
+constexpr int SR_BUILD_PER_SM = 2;      // build blocks resident per SM: the slice is cut into one wave of ranges
+constexpr int SR_MAX_SLOTS = 9200;      // slots of one range in shared memory (12 bytes each)
 constexpr int SR_THREADS = 1024;        // regrouping passes (2 blocks per SM: few per-block range counts)
-constexpr int SR_BUILD_THREADS = 512;
+constexpr int SR_BUILD_THREADS = 1024;
 constexpr int SR_MINI = 64;
 constexpr size_t SR_SMEM = (size_t)(SR_MAX_SLOTS + SR_MINI) * 12;
 
@@ -916,7 +920,8 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     uint64_t max_part = 0;
     for (int p = 0; p < nparts; p++) max_part = std::max(max_part, pb[p + 1] - pb[p]);
     // blocks of the regrouping passes: two per SM, more if a block's chunk
-    // would not fit in the scatter's shared memory
+    // would not fit in the scatter's shared memory (rounding that up to whole
+    // waves of two blocks per SM was slower: 52.5 against 50.9 ms per step)
     const unsigned G = (unsigned)std::max<uint64_t>((uint64_t)c->sm_count * 2, (max_part + SRS_MAX - 1) / SRS_MAX);
     const uint64_t cells = (uint64_t)nsub * G;
     uint64_t defer_cap = std::max<uint64_t>(1u << 16, std::min<uint64_t>(pb[nparts] / 64, 1u << 24));
