@@ -906,7 +906,7 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     tk_ctx *c = t->ctx;
     *done = false;
     const int nparts = 1 << t->t.pbits;
-    // ranges per slice: one wave of three build blocks per SM, more if a range
+    // ranges per slice: one wave of SR_BUILD_PER_SM build blocks per SM, more if a range
     // would not fit in shared memory
     const uint64_t slice = 1ULL << t->t.lbits, wave = (uint64_t)c->sm_count * SR_BUILD_PER_SM;
     uint32_t nsub;
