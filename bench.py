@@ -50,9 +50,9 @@ NORM_ARGS = (200, 1, 10000)   # normalization: Trinity's --max_cov 200 --min_cov
 # 1,516,211,092 lookups): dram__bytes_read.sum 121.66 GB + dram__bytes_write.sum 2.11 GB
 COV_DRAM_BYTES_PER_LOOKUP = (121.66e9 + 2.11e9) / (3_032_422_183 / 2)
 # ncu (--cache-control none), the 1537 count launches of one step at 20M pairs
-# (512 x k_sr_hist, k_sr_scatter, k_sr_build + k_insert_pairs): 48.63 GB read +
-# 39.53 GB written, for 3,032,422,183 occurrences
-COUNT_DRAM_BYTES_PER_OCCURRENCE = (48.63e9 + 39.53e9) / 3_032_422_183
+# (512 x k_sr_hist, k_sr_scatter, k_sr_build + k_insert_pairs): 48.68 GB read +
+# 38.22 GB written, for 3,032,422,183 occurrences
+COUNT_DRAM_BYTES_PER_OCCURRENCE = (48.68e9 + 38.22e9) / 3_032_422_183
 
 
 def log(*a):
@@ -479,8 +479,8 @@ def run_gpu(args, dist, world, rank, local):
         ins_launches = max(per_step["count"][1], 1)
         kernels["insert"]["traffic"] = COUNT_DRAM_BYTES_PER_OCCURRENCE * windows / ins_launches
         kernels["insert"]["traffic_source"] = (
-            "ncu capture (--cache-control none) of one step's 1537 count launches at 20M pairs (48.63 GB read + "
-            "39.53 GB written), per launch" + ("" if args.pairs == FULL_PAIRS else
+            "ncu capture (--cache-control none) of one step's 1537 count launches at 20M pairs (48.68 GB read + "
+            "38.22 GB written), per launch" + ("" if args.pairs == FULL_PAIRS else
                                                f", scaled by occurrences: {COUNT_DRAM_BYTES_PER_OCCURRENCE:.1f} B each"))
         # the dominant kernel: k_coverage, one kernel with ~29% of the step in
         # the launch list; the count's ~28% is spread over three kernels
