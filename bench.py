@@ -932,6 +932,7 @@ def batched_bench(ctx, args, n_bins, sample_every=97):
     wall = time.time() - tb
     phases = {name: ctx.profile(kid)[0] for name, kid in (("parse", "parse"), ("sketch", "hll"), ("count", "bins"),
                                                           ("compact", "compact"), ("sort", "sort"), ("format", "dump"))}
+    tuning = count_bins.last_tuning   # block size, slice load factor (tuned on the warm-up call), relaunches
     ctx.set_profiling(False)
     phases["host_and_copies"] = wall * 1e3 - sum(phases.values())
     # plain: one count + dump per bin
@@ -953,7 +954,7 @@ def batched_bench(ctx, args, n_bins, sample_every=97):
             "batched_reads_per_s": float(nreads.sum()) / t_batched, "plain_reads_per_s": float(nreads.sum()) / t_plain,
             "speedup_vs_plain": t_plain / t_batched, "sampled_bins_identical": bool(same),
             "bins_compared": (n_bins + sample_every - 1) // sample_every,
-            "phases_ms": {k: round(v, 2) for k, v in phases.items()}}
+            "phases_ms": {k: round(v, 2) for k, v in phases.items()}, "tuning": tuning}
 
 
 def served_bench(ctx, args):

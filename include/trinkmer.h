@@ -380,6 +380,12 @@ int tk_bins_info(const tk_bins *bins, uint64_t *text_len, uint64_t *kmers);
 /* n_bins + 1 byte offsets of each bin's dump in the text */
 int tk_bins_dump_offsets(const tk_bins *bins, uint64_t *offsets);
 int tk_bins_dump_text(const tk_bins *bins, char *dst, uint64_t cap);
+/* How the batch was counted: the count kernel's block size and the slices'
+ * load factor (per mille), both tuned once per device (the load factor on
+ * the first batch of at least 50M k-mers, by timing 0.45, 0.6 and 0.75), and
+ * how many times overflowing slices were doubled and the count relaunched.
+ * The dumps do not depend on any of them. */
+int tk_bins_tuning(const tk_bins *bins, int *block, int *load_per_mille, int *relaunches);
 void tk_bins_free(tk_bins *bins);
 
 /* ------------------------------------------------------------- serving

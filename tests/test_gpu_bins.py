@@ -53,3 +53,23 @@ def test_bins_whose_bin_and_kmer_exceed_one_word(ctx, oracle, k, n_bins, max_rea
         total += int(counts.sum())
         assert dump[int(toff[b]):int(toff[b + 1])] == oracle.dump(keys, counts, k, 1), f"bin {b}"
     assert kmers == total
+
+
+def test_load_factor_tuning_leaves_the_dumps_unchanged(ctx, oracle):
+    """The first batch of at least 50M k-mers on a device times three slice
+    load factors before counting; the chosen block size and load factor are
+    reported, and the dumps equal those of the next (tuned) call and the
+    oracle's per-bin counts."""
+    text, off, _ = synth.power_law_bins(seed=17, n_bins=1000, alpha=1.8, min_reads=50, max_reads=200_000)
+    t = text.tobytes()
+    first, toff1, kmers = count_bins(ctx, t, off, 25, True, 1)
+    tuning = count_bins.last_tuning
+    assert tuning["block"] in (128, 256, 512)
+    if kmers >= 50 << 20:
+        assert tuning["load"] in (0.45, 0.6, 0.75)
+    second, toff2, _ = count_bins(ctx, t, off, 25, True, 1)
+    assert count_bins.last_tuning["load"] == tuning["load"]
+    assert first == second and np.array_equal(toff1, toff2)
+    for b in range(0, len(off) - 1, 97):
+        keys, counts = oracle.count(t[int(off[b]):int(off[b + 1])], 25, True)
+        assert first[int(toff1[b]):int(toff1[b + 1])] == oracle.dump(keys, counts, 25, 1), f"bin {b}"

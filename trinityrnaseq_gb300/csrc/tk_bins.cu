@@ -301,14 +301,19 @@ struct tk_bins {
     uint64_t kmers = 0;                     // windows counted
     uint64_t table_slots = 0;
     int block = 256;
+    int load_pm = 0;                        // slice load factor, per mille
     int relaunches = 0;
 };
 
 namespace tk {
 int parse_reads(tk_ctx *c, tk_reads *r);
 
-// block sizes the count kernel is tuned over, per context (0 = not tuned yet)
+// block sizes the count kernel is tuned over, per device (0 = not tuned yet)
 static int g_tuned_block[64];
+// slice load factor (per mille) chosen per device on the first batch of at
+// least BIN_TUNE_MIN windows (0 = not tuned yet: the caller's default)
+static int g_tuned_load[64];
+constexpr uint64_t BIN_TUNE_MIN = 50ull << 20;
 
 template <bool CANON>
 static void launch_count(tk_ctx *c, int block, const uint8_t *seq, uint64_t n, int k, BinGeom g, Slot *slots,
@@ -392,20 +397,24 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
         if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "sketch sync");
     }
     // 3. slice per bin, sized from its sketch (never above its window count)
+    //    for a load factor: estimated distinct k-mers / load, a power of two
     std::vector<uint64_t> base(n_bins + 1);
     std::vector<uint8_t> lbits(n_bins);
     uint64_t total = 0, kmers = 0;
-    for (uint32_t b = 0; !e && b < n_bins; b++) {
-        double est = std::min<double>(hll32(&regs[(size_t)b * BIN_HLL_M]) * 1.35, (double)win[b]);
-        uint64_t want = (uint64_t)(est / load) + 1;
-        int lb = 5;
-        while ((1ULL << lb) < want) lb++;
-        lbits[b] = (uint8_t)lb;
-        base[b] = total;
-        total += 1ULL << lb;
-        kmers += win[b];
-    }
-    base[n_bins] = total;
+    for (uint32_t b = 0; !e && b < n_bins; b++) kmers += win[b];
+    auto size_slices = [&](double L) {
+        total = 0;
+        for (uint32_t b = 0; b < n_bins; b++) {
+            double est = std::min<double>(hll32(&regs[(size_t)b * BIN_HLL_M]) * 1.35, (double)win[b]);
+            uint64_t want = (uint64_t)(est / L) + 1;
+            int lb = 5;
+            while ((1ULL << lb) < want) lb++;
+            lbits[b] = (uint8_t)lb;
+            base[b] = total;
+            total += 1ULL << lb;
+        }
+        base[n_bins] = total;
+    };
     Slot *slots = nullptr;
     uint64_t *d_base = nullptr;
     uint8_t *d_lbits = nullptr;
@@ -414,6 +423,43 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
     if (!e) e = alloc((void **)&d_lbits, n_bins, "bin slice sizes");
     if (!e) e = alloc((void **)&d_ovf, n_bins * 4, "bin overflow flags");
     std::vector<uint32_t> ovf(n_bins);
+    if (!e && !g_tuned_load[c->device & 63] && n && kmers >= BIN_TUNE_MIN) {
+        // autotune the slice load factor once per device on a batch of this
+        // size: fill + count timed for each candidate (fuller slices are
+        // smaller to fill and sweep but probe longer); the dumps do not
+        // depend on it, every bin's records being sorted by key
+        const int tb = g_tuned_block[c->device & 63] ? g_tuned_block[c->device & 63] : 256;
+        double best = 1e30;
+        int best_pm = (int)(load * 1000 + 0.5);
+        for (int pm : {450, 600, 750}) {
+            size_slices(pm / 1000.0);
+            Slot *ts = nullptr;
+            if ((e = dmalloc(c, (void **)&ts, total * sizeof(Slot), "bin tables (tuning)"))) break;
+            cudaMemcpyAsync(d_base, base.data(), (n_bins + 1) * 8, cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(d_lbits, lbits.data(), n_bins, cudaMemcpyHostToDevice, c->stream);
+            cudaMemsetAsync(d_ovf, 0, n_bins * 4, c->stream);
+            BinGeom g{d_seq0, d_base, d_lbits, n_bins};
+            cudaEvent_t a, b2;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b2);
+            cudaEventRecord(a, c->stream);
+            k_bin_fill<<<(unsigned)c->sm_count * 8, 256, 0, c->stream>>>(ts, total);
+            if (canonical) launch_count<true>(c, tb, r.d_seq, n, k, g, ts, d_ovf);
+            else launch_count<false>(c, tb, r.d_seq, n, k, g, ts, d_ovf);
+            cudaEventRecord(b2, c->stream);
+            e = cuda_check(c, cudaEventSynchronize(b2), "load tuning");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b2);
+            cudaEventDestroy(a);
+            cudaEventDestroy(b2);
+            dfree(c, ts);
+            if (e) break;
+            if (ms < best) { best = ms; best_pm = pm; }
+        }
+        if (!e) g_tuned_load[c->device & 63] = best_pm;
+    }
+    const int load_pm = g_tuned_load[c->device & 63] ? g_tuned_load[c->device & 63] : (int)(load * 1000 + 0.5);
+    if (!e) size_slices(load_pm / 1000.0);
     // 4. fill + persistent count, captured in a CUDA graph; a slice that
     //    overflowed is doubled and the graph rebuilt and relaunched
     int relaunch = 0;
@@ -625,6 +671,7 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
     out->kmers = kmers;
     out->table_slots = total;
     out->block = block;
+    out->load_pm = load_pm;
     out->relaunches = relaunch;
     return TK_OK;
 }
@@ -683,6 +730,14 @@ int tk_bins_dump_text(const tk_bins *z, char *dst, uint64_t cap) {
     if (cap < z->text_len) return tk::set_err(c, TK_E_RANGE, "tk_bins_dump_text: buffer smaller than the dumps");
     if (z->text_len) TK_CUDA(c, cudaMemcpyAsync(dst, z->d_text, z->text_len, cudaMemcpyDeviceToHost, c->stream));
     return tk::cuda_check(c, cudaStreamSynchronize(c->stream), "bins text sync");
+}
+
+int tk_bins_tuning(const tk_bins *z, int *block, int *load_per_mille, int *relaunches) {
+    if (!z) return TK_E_INVAL;
+    if (block) *block = z->block;
+    if (load_per_mille) *load_per_mille = z->load_pm;
+    if (relaunches) *relaunches = z->relaunches;
+    return TK_OK;
 }
 
 void tk_bins_free(tk_bins *z) {

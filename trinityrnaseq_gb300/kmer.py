@@ -567,7 +567,9 @@ def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool
     """Per-bin k-mer dumps of back-to-back FASTA bins in one batched GPU pass
     (tk_count_bins).  Returns (dump text, n_bins + 1 byte offsets, k-mers counted);
     with `out` (a uint8 array, e.g. page-locked, large enough) the text is
-    copied there and a view of it is returned instead of bytes."""
+    copied there and a view of it is returned instead of bytes.  The call's
+    block size, slice load factor and relaunches (tk_bins_tuning) are left in
+    count_bins.last_tuning."""
     ptr, n, keep = _host_ptr(text)
     off = np.ascontiguousarray(bin_off, dtype=np.uint64)
     nb = off.size - 1
@@ -579,6 +581,9 @@ def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool
         ctx.check(ctx.lib.tk_bins_info(h, C.byref(tl), C.byref(km)), "tk_bins_info")
         offs = np.zeros(nb + 1, dtype=np.uint64)
         ctx.check(ctx.lib.tk_bins_dump_offsets(h, offs.ctypes.data), "tk_bins_dump_offsets")
+        blk, lpm, rl = C.c_int(), C.c_int(), C.c_int()
+        ctx.check(ctx.lib.tk_bins_tuning(h, C.byref(blk), C.byref(lpm), C.byref(rl)), "tk_bins_tuning")
+        count_bins.last_tuning = {"block": blk.value, "load": lpm.value / 1000.0, "relaunches": rl.value}
         if out is not None and out.size >= tl.value:
             ctx.check(ctx.lib.tk_bins_dump_text(h, out.ctypes.data, out.size), "tk_bins_dump_text")
             return out[:tl.value], offs, km.value
@@ -587,6 +592,9 @@ def count_bins(ctx: Context, text: Buffer, bin_off, k: int = 25, canonical: bool
         return buf[:tl.value].tobytes(), offs, km.value
     finally:
         ctx.lib.tk_bins_free(h)
+
+
+count_bins.last_tuning = None
 
 
 # ---------------------------------------------------------------- text formats

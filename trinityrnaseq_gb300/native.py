@@ -103,6 +103,7 @@ SIGNATURES = {
     "tk_bins_info": (C.c_int, [vp, P(u64), P(u64)]),
     "tk_bins_dump_offsets": (C.c_int, [vp, vp]),
     "tk_bins_dump_text": (C.c_int, [vp, vp, u64]),
+    "tk_bins_tuning": (C.c_int, [vp, P(C.c_int), P(C.c_int), P(C.c_int)]),
     "tk_bins_free": (None, [vp]),
 }
 
