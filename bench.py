@@ -174,6 +174,12 @@ class GpuPipeline:
         self.d_right = self.h_right.to(dev)
         torch.cuda.synchronize(dev)
         self.dev = dev
+        # the statistics' downloads run on their own stream, ordered against
+        # the context's stream by events (coverage before the copy, the copy
+        # before the next step's coverage overwrites the device buffers)
+        self.ctx_stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+        self.copy_stream = torch.cuda.Stream(device=dev)
+        self.stats_copied = None
         self.pieces = max(1, pieces)
         self.n_reads = None
         self.out = None
@@ -226,6 +232,8 @@ class GpuPipeline:
             # the text's download overlaps the coverage pass; synchronised below
             table.dump_fasta_into_async(MIN_COUNT, self.out["dump_host"].data_ptr(), self.out["dump_host"].numel())
             d2h += dump_len
+        if self.stats_copied is not None:
+            self.ctx_stream.wait_event(self.stats_copied)   # the last step's statistics have gone down
         for side, group in (("l", left_sets), ("r", right_sets)):
             bufs = self.out[side + "_dev"]
             first = 0
@@ -234,11 +242,18 @@ class GpuPipeline:
                                          bufs[2].data_ptr() + 4 * first, device=True)
                 first += rs.n_reads
             if e2e:
-                # the statistics go down once per mate, queued on the context's
-                # stream after its coverage passes
-                for h, d in zip(self.out[side + "_host"], bufs):
-                    h[:first].copy_(d[:first], non_blocking=True)
+                # the statistics go down once per mate on the copy stream,
+                # after its coverage passes, while the next work runs
+                covered = t.cuda.Event()
+                covered.record(self.ctx_stream)
+                self.copy_stream.wait_event(covered)
+                with t.cuda.stream(self.copy_stream):
+                    for h, d in zip(self.out[side + "_host"], bufs):
+                        h[:first].copy_(d[:first], non_blocking=True)
                 d2h += 12 * first
+        if e2e:
+            self.stats_copied = t.cuda.Event()
+            self.stats_copied.record(self.copy_stream)
         _, windows, capacity = table.info(distinct=False)
         # normalization to max_cov 200 (insilico_read_normalization.pl --pairs_together):
         # both mates' statistics sorted by name, pair merge, seeded selection,
@@ -264,6 +279,7 @@ class GpuPipeline:
         table.free()   # after the dump text's download, which overlapped the coverage and selection
         if e2e:
             d2h += ext
+            self.ctx_stream.wait_event(self.stats_copied)   # the step ends after its downloads
             ctx.synchronize()
             if capture is not None:
                 capture["dump"] = self.out["dump_host"].numpy()[:dump_len].copy()
