@@ -200,23 +200,25 @@ class GpuPipeline:
         histo, dump text, both mates' statistics, accs text, extracted records."""
         kmer, t = self.kmer, self.torch
         ctx = self.ctx
+        table = kmer.KmerTable(ctx, K, True)
         if e2e:
-            # each mate's FASTQ in record-aligned pieces: a piece is parsed while
-            # the next one uploads (the split reads only bytes near each cut)
+            # each mate's FASTQ in record-aligned pieces, all uploads queued at
+            # once: a piece is parsed and its k-mers bucketed while the next
+            # ones upload, then all are counted (the split reads only bytes
+            # near each cut)
             pieces = []
             for h in (self.h_left, self.h_right):
                 a = h.numpy()
                 cuts = kmer.split_records(a, self.pieces)
                 pieces += [a[cuts[i]:cuts[i + 1]] for i in range(self.pieces)]
-            sets = kmer.ReadSet.parse_many(ctx, pieces)
+            sets = table.count_texts(pieces)
             left_sets, right_sets = sets[:self.pieces], sets[self.pieces:]
             h2d = self.h_left.numel() + self.h_right.numel()
         else:
             left_sets = [kmer.ReadSet(ctx, self.d_left.data_ptr(), self.d_left.numel(), device=True)]
             right_sets = [kmer.ReadSet(ctx, self.d_right.data_ptr(), self.d_right.numel(), device=True)]
             h2d = 0
-        table = kmer.KmerTable(ctx, K, True)
-        table.add_many(left_sets + right_sets)
+            table.add_many(left_sets + right_sets)
         hist = table.histo(1, 10000)
         dump_len = table.dump_fasta_len(MIN_COUNT)
         if capture is not None:

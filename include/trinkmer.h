@@ -174,6 +174,16 @@ int tk_table_add_reads(tk_table *table, const tk_reads *reads);
 /* Adds several read sets in one pass over the table (e.g. both mate files:
  * jellyfish counts `cat left.fa right.fa`, Trinity:1641). */
 int tk_table_add_reads_multi(tk_table *table, const tk_reads *const *sets, uint32_t n_sets);
+/* tk_reads_parse_many followed by tk_table_add_reads_multi, overlapped: with
+ * host texts every upload is queued at once, and each text's first counting
+ * pass (its windows' bucket histogram, distinct-k-mer sketch and bucketing)
+ * runs as soon as the text is parsed, while the later texts still upload;
+ * the second pass then counts all of them into the table.  The n read sets
+ * are returned in `out` (the caller frees them); on error none is.  The
+ * counts equal those of tk_table_add_reads_multi.  No counterpart in the
+ * reference (jellyfish reads its files itself). */
+int tk_table_count_texts(tk_table *table, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
+                         tk_reads **out);
 int tk_table_count_text(tk_table *table, const char *text, uint64_t len, int where);
 /* distinct k-mers (a scan of the table; pass NULL to skip it), occurrences
  * added, slots. */

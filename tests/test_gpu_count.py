@@ -214,3 +214,73 @@ def test_block_cache_trim_and_zero_cap(native_built, ctx, oracle):
     left, right = synth.gene_pairs(seed=43, n_genes=3000, n_pairs=200000, fastq=False)
     keys, counts = oracle.count(left.tobytes() + right.tobytes(), 25, True)
     assert p.stdout == oracle.dump(keys, counts, 25, 2)
+
+
+def pieces_of(texts, n):
+    from trinityrnaseq_gb300 import kmer
+    out = []
+    for a in texts:
+        cuts = kmer.split_records(a, n)
+        out += [a[int(cuts[i]):int(cuts[i + 1])] for i in range(n)]
+    return out
+
+
+def test_count_texts_equals_parse_then_add(ctx, oracle):
+    """tk_table_count_texts: each host text's first counting pass runs as soon
+    as it is parsed (per-text key buffers, the partitions read as one segment
+    of each); the counts and the read sets equal parse_many + add_many."""
+    left, right = synth.gene_pairs(seed=61, n_genes=1500, n_pairs=200000, fastq=True, n_rate=0.005)
+    pieces = pieces_of((left, right), 3)
+    pieces.insert(2, np.zeros(0, dtype=np.uint8))   # an empty text among them
+    whole = left.tobytes() + right.tobytes()
+    t = KmerTable(ctx, 25, True)
+    sets = t.count_texts(pieces)
+    assert_pairs(t.dump(1), oracle.count(whole, 25, True))
+    ref = ReadSet.parse_many(ctx, pieces)
+    assert [r.n_reads for r in sets] == [r.n_reads for r in ref]
+    for a, b in zip(sets, ref):
+        assert a.accessions() == b.accessions() and a.sequences() == b.sequences()
+    # counted again into the now filled table (the atomic path over several key buffers)
+    t.count_texts(pieces[:3])
+    assert_pairs(t.dump(1), oracle.count(whole + b"".join(p.tobytes() for p in pieces[:3]), 25, True))
+
+
+def test_count_texts_beyond_one_pass_of_sets(ctx, oracle):
+    """More texts than one counting pass takes (64): parsed, then counted in groups."""
+    text = synth.transcriptome_reads(seed=62, n_reads=70000).tobytes()
+    arr = np.frombuffer(text, dtype=np.uint8)
+    pieces = pieces_of((arr,), 70)
+    t = KmerTable(ctx, 25, True)
+    sets = t.count_texts(pieces)
+    assert len(sets) == 70 and sum(r.n_reads for r in sets) == 70000
+    assert_pairs(t.dump(1), oracle.count(text, 25, True))
+
+
+def test_multi_set_partitioned_table_and_deferred_fallback(native_built, oracle):
+    """Several read sets into a multi-partition table, by ranges and, with the
+    deferred list capped at one entry, by the atomic fallback: both exact."""
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import sys\n"
+        "from trinityrnaseq_gb300 import Context, KmerTable, ReadSet, synth\n"
+        "ctx = Context(0)\n"
+        "text = synth.transcriptome_reads(seed=63, n_transcripts=4000, n_reads=600_000, err=0.02).tobytes()\n"
+        "q = len(text) // 3\n"
+        "cut = [0, text.index(b'\\n>', q) + 1, text.index(b'\\n>', 2 * q) + 1, len(text)]\n"
+        "sets = [ReadSet(ctx, text[cut[i]:cut[i + 1]]) for i in range(3)]\n"
+        "t = KmerTable(ctx, 25, True)\n"
+        "t.add_many(sets)\n"
+        "assert t.info()[2] > (1 << 21)\n"
+        "sys.stdout.buffer.write(t.dump_fasta(1))\n")
+    text = synth.transcriptome_reads(seed=63, n_transcripts=4000, n_reads=600_000, err=0.02).tobytes()
+    keys, counts = oracle.count(text, 25, True)
+    want = oracle.dump(keys, counts, 25, 1)
+    for cap in (None, "1"):
+        env = dict(os.environ)
+        if cap:
+            env["TRINKMER_DEFER_CAP"] = cap
+        run = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, timeout=600)
+        assert run.returncode == 0, run.stderr[-2000:]
+        assert run.stdout == want, cap

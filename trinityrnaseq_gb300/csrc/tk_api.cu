@@ -492,21 +492,21 @@ int tk_reads_parse(tk_ctx *c, const char *text, uint64_t len, int where, tk_read
     return TK_OK;
 }
 
-int tk_reads_parse_many(tk_ctx *c, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
-                        tk_reads **out) {
-    CHECK_CTX(c);
-    if (!out || (!texts && n) || (!lens && n)) return set_err(c, TK_E_INVAL, "tk_reads_parse_many: null argument");
-    for (uint32_t i = 0; i < n; i++) {
-        out[i] = nullptr;
-        if (!texts[i] && lens[i]) return set_err(c, TK_E_INVAL, "tk_reads_parse_many: null text");
-    }
+}  // extern "C"
+
+// Parses n texts; `after(i, reads)` runs on each read set as soon as it is
+// parsed, while the later host texts are still uploading.
+template <typename After>
+static int parse_many_then(tk_ctx *c, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
+                           tk_reads **out, After &&after) {
     cudaStream_t cs = where == TK_HOST ? copy_stream(c) : nullptr;
     if (!cs) {
         // device texts (or no copy stream): one after another
         for (uint32_t i = 0; i < n; i++) {
             int e = tk_reads_parse(c, texts[i], lens[i], where, &out[i]);
+            if (!e) e = after(i, out[i]);
             if (e) {
-                for (uint32_t j = 0; j < i; j++) { tk_reads_free(out[j]); out[j] = nullptr; }
+                for (uint32_t j = 0; j <= i; j++) { tk_reads_free(out[j]); out[j] = nullptr; }
                 return e;
             }
         }
@@ -546,6 +546,7 @@ int tk_reads_parse_many(tk_ctx *c, const char *const *texts, const uint64_t *len
         out[i] = r;
         made = i + 1;
         e = parse_reads(c, r);
+        if (!e) e = after(i, r);
     }
     if (e) {
         cudaStreamSynchronize(cs);
@@ -559,6 +560,50 @@ int tk_reads_parse_many(tk_ctx *c, const char *const *texts, const uint64_t *len
         if (landed[i]) cudaEventDestroy(landed[i]);
     }
     if (allocated) cudaEventDestroy(allocated);
+    return e;
+}
+
+extern "C" {
+
+int tk_reads_parse_many(tk_ctx *c, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
+                        tk_reads **out) {
+    CHECK_CTX(c);
+    if (!out || (!texts && n) || (!lens && n)) return set_err(c, TK_E_INVAL, "tk_reads_parse_many: null argument");
+    for (uint32_t i = 0; i < n; i++) {
+        out[i] = nullptr;
+        if (!texts[i] && lens[i]) return set_err(c, TK_E_INVAL, "tk_reads_parse_many: null text");
+    }
+    return parse_many_then(c, texts, lens, n, where, out, [](uint32_t, tk_reads *) { return TK_OK; });
+}
+
+int tk_table_count_texts(tk_table *t, const char *const *texts, const uint64_t *lens, uint32_t n, int where,
+                         tk_reads **out) {
+    if (!t) return TK_E_INVAL;
+    tk_ctx *c = t->ctx;
+    CHECK_CTX(c);
+    if (!out || (!texts && n) || (!lens && n)) return set_err(c, TK_E_INVAL, "tk_table_count_texts: null argument");
+    for (uint32_t i = 0; i < n; i++) {
+        out[i] = nullptr;
+        if (!texts[i] && lens[i]) return set_err(c, TK_E_INVAL, "tk_table_count_texts: null text");
+    }
+    if (n > COUNT_MAX_SETS) {
+        // more texts than one counting pass takes: parse, then count in groups
+        TK_TRY(tk_reads_parse_many(c, texts, lens, n, where, out));
+        int e = tk_table_add_reads_multi(t, out, n);
+        if (e)
+            for (uint32_t i = 0; i < n; i++) { tk_reads_free(out[i]); out[i] = nullptr; }
+        return e;
+    }
+    table_changed(t);
+    TK_TRY(table_count_begin(t));
+    std::vector<BucketKeys> bk(n);
+    int e = parse_many_then(c, texts, lens, n, where, out,
+                            [&](uint32_t i, tk_reads *r) { return table_bucket_pass(t, r, &bk[i]); });
+    if (!e) e = table_count_buckets(t, bk);
+    if (e) {
+        for (BucketKeys &b : bk) table_bucket_free(t, &b);
+        for (uint32_t i = 0; i < n; i++) { tk_reads_free(out[i]); out[i] = nullptr; }
+    }
     return e;
 }
 

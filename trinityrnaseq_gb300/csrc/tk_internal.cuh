@@ -375,6 +375,22 @@ int table_rehash(tk_table *t, uint64_t new_capacity);
 int table_count_seq(tk_table *t, const tk_reads *r);
 int reads_fasta(tk_reads *r, int append, int flags, char **d_text, uint64_t *text_len);
 int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets);
+// One read set's k-mers after counting pass 1: bucket-major over the set's
+// own columns (one per block of its grid); region (bucket, column) starts at
+// offs[bucket * cols + column] and is padded to whole 32-byte sectors.
+struct BucketKeys {
+    uint64_t *keys = nullptr;   // nullptr: the set has no windows
+    uint64_t *offs = nullptr;   // NBUCKETS * cols + 1
+    uint64_t cols = 0;
+};
+// Counting in two steps (tk_table.cu): table_count_begin, then pass 1 per
+// read set as each becomes ready (at most 64 sets), then pass 2 over all of
+// them (which frees their key buffers).
+int table_count_begin(tk_table *t);
+int table_bucket_pass(tk_table *t, const tk_reads *r, BucketKeys *out);
+void table_bucket_free(tk_table *t, BucketKeys *bk);
+int table_count_buckets(tk_table *t, std::vector<BucketKeys> &bk);
+constexpr uint32_t COUNT_MAX_SETS = 64;
 int norm_select(tk_norm *nm, const tk_reads *const *const sets[2], const uint32_t nsets[2],
                 const uint32_t *const med[2], const float *const mean[2], const float *const sd[2], int where);
 int norm_table(tk_norm *nm);

@@ -323,23 +323,85 @@ __device__ __forceinline__ uint32_t key_range(const DevTable &t, uint64_t key, u
     return slot_range(t, mix64(key) & t.lmask, nsub);
 }
 
-// Keys [ps, pe) split evenly over the blocks.  Per block, keys per range
-// (counts[range * gridDim.x + block]) and, summed over blocks after rounding
-// each up to a multiple of 4, per range (totals, zeroed beforehand).
-__global__ void __launch_bounds__(SR_THREADS) k_sr_hist(const uint64_t *__restrict__ keys, uint64_t ps, uint64_t pe,
+// A partition's keys: one segment of each read set's bucket buffer, taken
+// as one sequence (index i of segment s is key cum[s] + i of the sequence).
+struct KeySeg {
+    const uint64_t *keys;
+    uint64_t len;
+};
+constexpr int MAX_KEY_SEGS = (int)COUNT_MAX_SETS;   // read sets counted in one pass (more are counted in groups)
+
+struct SegView {
+    const uint64_t *ptr[MAX_KEY_SEGS];
+    uint64_t cum[MAX_KEY_SEGS + 1];
+    uint32_t n;
+};
+
+// Loads the partition's segment table into shared memory (all threads).
+__device__ __forceinline__ void seg_view_load(SegView &v, const KeySeg *__restrict__ segs, uint32_t nseg) {
+    if (threadIdx.x == 0) {
+        uint64_t c = 0;
+        for (uint32_t s = 0; s < nseg; s++) {
+            v.ptr[s] = segs[s].keys;
+            v.cum[s] = c;
+            c += segs[s].len;
+        }
+        v.cum[nseg] = c;
+        v.n = nseg;
+    }
+    __syncthreads();
+}
+
+// A thread's walk over ascending sequence indices: the current segment's
+// pointer, first index and end in registers; shared memory is read only when
+// the walk crosses into a later segment.
+struct SegCursor {
+    const uint64_t *ptr;
+    uint64_t first, end;
+    uint32_t s;
+};
+
+__device__ __forceinline__ void seg_cursor_at(const SegView &v, SegCursor &c, uint32_t s) {
+    c.s = s;
+    c.ptr = v.ptr[s];
+    c.first = v.cum[s];
+    c.end = v.cum[s + 1];
+}
+
+// Key i of the sequence (i at or after every index the cursor gave before).
+__device__ __forceinline__ uint64_t seg_key(const SegView &v, SegCursor &c, uint64_t i) {
+    while (i >= c.end && c.s + 1 < v.n) seg_cursor_at(v, c, c.s + 1);
+    return __ldcs(c.ptr + (i - c.first));
+}
+
+// The segment holding sequence index i.
+__device__ __forceinline__ uint32_t seg_of(const SegView &v, uint64_t i) {
+    uint32_t s = 0;
+    while (s + 1 < v.n && i >= v.cum[s + 1]) s++;
+    return s;
+}
+
+// The partition's keys split evenly over the blocks.  Per block, keys per
+// range (counts[range * gridDim.x + block]) and, summed over blocks after
+// rounding each up to a multiple of 4, per range (totals, zeroed beforehand).
+__global__ void __launch_bounds__(SR_THREADS) k_sr_hist(const KeySeg *__restrict__ segs, uint32_t nseg,
                                                        DevTable t, uint32_t nsub, uint32_t *__restrict__ counts,
                                                        uint32_t *__restrict__ totals) {
     extern __shared__ uint32_t sr_h[];
+    __shared__ SegView sv;
     for (uint32_t i = threadIdx.x; i < nsub; i += SR_THREADS) sr_h[i] = 0;
-    __syncthreads();
-    const uint64_t chunk = (pe - ps + gridDim.x - 1) / gridDim.x;
-    const uint64_t lo = ps + (uint64_t)blockIdx.x * chunk, hi = min(pe, lo + chunk);
+    seg_view_load(sv, segs, nseg);   // synchronises
+    const uint64_t n = sv.cum[sv.n];
+    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t lo = (uint64_t)blockIdx.x * chunk, hi = min(n, lo + chunk);
+    SegCursor cur;
+    seg_cursor_at(sv, cur, seg_of(sv, lo));
     for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += 4 * SR_THREADS) {
         uint64_t k4[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const uint64_t i = i0 + (uint64_t)u * SR_THREADS;
-            k4[u] = i < hi ? __ldcs(keys + i) : EMPTY_KEY;
+            const uint64_t i = i0 + (uint64_t)u * SR_THREADS;   // ascending over u and over the loop
+            k4[u] = i < hi ? seg_key(sv, cur, i) : EMPTY_KEY;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++)
@@ -377,7 +439,7 @@ __device__ __forceinline__ void range_starts(const uint32_t *__restrict__ totals
 constexpr int SRS_MAX = 12288;   // keys of one block's chunk (the host sizes the grid to fit)
 static inline size_t SRS_SMEM(uint32_t nsub) { return (size_t)SRS_MAX * 8 + (size_t)nsub * 16; }
 
-__global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__restrict__ keys, uint64_t ps, uint64_t pe,
+__global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const KeySeg *__restrict__ segs, uint32_t nseg,
                                                           DevTable t, uint32_t nsub, const uint32_t *__restrict__ counts,
                                                           const uint32_t *__restrict__ totals,
                                                           unsigned long long *__restrict__ cursor,
@@ -388,6 +450,8 @@ __global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__res
     uint32_t *lstart = reinterpret_cast<uint32_t *>(gbase + nsub);                      // [nsub]
     uint32_t *lcur = lstart + nsub;                                                      // [nsub]
     __shared__ uint32_t sm[SR_THREADS / 32 + 1];
+    __shared__ SegView sv;
+    seg_view_load(sv, segs, nseg);   // synchronises
     range_starts(totals, nsub, reinterpret_cast<uint64_t *>(gbase));
     // this block's run of every range, and where its keys sit in shared memory
     const uint32_t per = (nsub + SR_THREADS - 1) / SR_THREADS;
@@ -407,14 +471,17 @@ __global__ void __launch_bounds__(SR_THREADS) k_sr_scatter(const uint64_t *__res
         lcur[r] = 0;
     }
     __syncthreads();
-    const uint64_t chunk = (pe - ps + gridDim.x - 1) / gridDim.x;
-    const uint64_t lo = ps + (uint64_t)blockIdx.x * chunk, hi = min(pe, lo + chunk);
+    const uint64_t n = sv.cum[sv.n];
+    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t lo = (uint64_t)blockIdx.x * chunk, hi = min(n, lo + chunk);
+    SegCursor cur;
+    seg_cursor_at(sv, cur, seg_of(sv, lo));
     for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += 4 * SR_THREADS) {
         uint64_t k4[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const uint64_t i = i0 + (uint64_t)u * SR_THREADS;
-            k4[u] = i < hi ? __ldcs(keys + i) : EMPTY_KEY;
+            const uint64_t i = i0 + (uint64_t)u * SR_THREADS;   // ascending over u and over the loop
+            k4[u] = i < hi ? seg_key(sv, cur, i) : EMPTY_KEY;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
@@ -880,21 +947,25 @@ static uint64_t pow2_at_least(uint64_t x) {
 // launch CAS-probes and adds partition p's keys into it.  Preparing slice p+1
 // inside the insert of p instead (the writes of one slice competing in L2 with
 // the atomics on the other) measured ~12% slower.
-static int count_by_atomics(tk_table *t, const uint64_t *keys, const uint64_t *offs, uint64_t cols) {
+static int count_by_atomics(tk_table *t, const std::vector<BucketKeys> &bk) {
     tk_ctx *c = t->ctx;
     const int nparts = 1 << t->t.pbits;
     const int mode = t->fresh ? NEXT_FILL : (t->t.pbits > 0 ? NEXT_PREFETCH : NEXT_NONE);
     const unsigned igrid = (unsigned)c->sm_count * 8;
     for (int p = 0; p < nparts; p++) {
-        if (mode != NEXT_NONE) {
-            k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(keys, offs, cols, -1, p, t->t, mode, c->max_probes,
+        if (mode != NEXT_NONE) {   // slice p filled (fresh) or prefetched once, then every set's keys of partition p
+            k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(bk[0].keys, bk[0].offs, bk[0].cols, -1, p, t->t, mode,
+                                                             c->max_probes, t->d_ovf, (uint32_t *)(t->d_ovf + t->ovf_cap),
+                                                             t->ovf_cap, t->d_counters);
+            c->launches++;
+        }
+        for (const BucketKeys &b : bk) {
+            if (!b.keys) continue;
+            k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(b.keys, b.offs, b.cols, p, -1, t->t, mode, c->max_probes,
                                                              t->d_ovf, (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap,
                                                              t->d_counters);
             c->launches++;
         }
-        k_part_step<<<igrid, CT_THREADS, 0, c->stream>>>(keys, offs, cols, p, -1, t->t, mode, c->max_probes, t->d_ovf,
-                                                         (uint32_t *)(t->d_ovf + t->ovf_cap), t->ovf_cap, t->d_counters);
-        c->launches++;
     }
     return check_launch(c, "count insert");
 }
@@ -902,7 +973,7 @@ static int count_by_atomics(tk_table *t, const uint64_t *keys, const uint64_t *o
 // Pass 2 by ranges on a fresh table (see k_sr_build).  *done is false when
 // the deferred list overran its capacity: the table is then emptied again and
 // the caller counts with count_by_atomics instead, so nothing is lost.
-static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *offs, uint64_t cols, bool *done) {
+static int count_by_ranges(tk_table *t, const std::vector<BucketKeys> &bk, bool *done) {
     tk_ctx *c = t->ctx;
     *done = false;
     const int nparts = 1 << t->t.pbits;
@@ -913,24 +984,44 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     if (slice / 1024 < wave) nsub = (uint32_t)(slice / 1024);   // a small slice: ranges of 1024 slots
     else nsub = (uint32_t)(wave * ((slice + wave * SR_MAX_SLOTS - 1) / (wave * SR_MAX_SLOTS)));   // whole waves
     const uint64_t bpp = (uint64_t)(NBUCKETS >> t->t.pbits);
-    // partition boundaries on the host: the first offset of each partition's buckets
-    std::vector<uint64_t> pb(nparts + 1);
-    TK_CUDA(c, cudaMemcpy2DAsync(pb.data(), 8, offs, bpp * cols * 8, 8, nparts + 1, cudaMemcpyDeviceToHost, c->stream));
+    // partition boundaries on the host: the first offset of each partition's
+    // buckets in each set's buffer; partition p's keys are one segment of each
+    const uint32_t nsets = (uint32_t)bk.size();
+    std::vector<std::vector<uint64_t>> pb(nsets, std::vector<uint64_t>(nparts + 1));
+    for (uint32_t q = 0; q < nsets; q++)
+        if (bk[q].keys)
+            TK_CUDA(c, cudaMemcpy2DAsync(pb[q].data(), 8, bk[q].offs, bpp * bk[q].cols * 8, 8, nparts + 1,
+                                         cudaMemcpyDeviceToHost, c->stream));
     TK_CUDA(c, cudaStreamSynchronize(c->stream));
-    uint64_t max_part = 0;
-    for (int p = 0; p < nparts; p++) max_part = std::max(max_part, pb[p + 1] - pb[p]);
+    std::vector<KeySeg> segs((size_t)nparts * nsets);
+    uint64_t max_part = 0, all_keys = 0;
+    for (int p = 0; p < nparts; p++) {
+        uint64_t part = 0;
+        for (uint32_t q = 0; q < nsets; q++) {
+            KeySeg &g = segs[(size_t)p * nsets + q];
+            g.keys = bk[q].keys ? bk[q].keys + pb[q][p] : nullptr;
+            g.len = bk[q].keys ? pb[q][p + 1] - pb[q][p] : 0;
+            part += g.len;
+        }
+        max_part = std::max(max_part, part);
+        all_keys += part;
+    }
     // blocks of the regrouping passes: two per SM, more if a block's chunk
     // would not fit in the scatter's shared memory (rounding that up to whole
     // waves of two blocks per SM was slower: 52.5 against 50.9 ms per step)
     const unsigned G = (unsigned)std::max<uint64_t>((uint64_t)c->sm_count * 2, (max_part + SRS_MAX - 1) / SRS_MAX);
     const uint64_t cells = (uint64_t)nsub * G;
-    uint64_t defer_cap = std::max<uint64_t>(1u << 16, std::min<uint64_t>(pb[nparts] / 64, 1u << 24));
+    uint64_t defer_cap = std::max<uint64_t>(1u << 16, std::min<uint64_t>(all_keys / 64, 1u << 24));
     if (const char *v = getenv("TRINKMER_DEFER_CAP")) defer_cap = std::max<uint64_t>(1, strtoull(v, nullptr, 10));   // tests: force the fallback
     uint64_t *range_keys = nullptr, *defer_keys = nullptr;
     uint32_t *counts = nullptr, *defer_cnt = nullptr, *totals = nullptr;
     unsigned long long *defer_n = nullptr, *cursor = nullptr;
+    KeySeg *d_segs = nullptr;
     // a partition's keys plus the sector rounding of every (range, block) run
     int e = dmalloc(c, (void **)&range_keys, (max_part + 3 * cells + 1) * 8, "range keys");
+    if (!e) e = dmalloc(c, (void **)&d_segs, segs.size() * sizeof(KeySeg), "partition segments");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(KeySeg), cudaMemcpyHostToDevice,
+                                              c->stream), "partition segments h2d");
     if (!e) e = dmalloc(c, (void **)&counts, cells * 4, "range counts");
     if (!e) e = dmalloc(c, (void **)&totals, 2ull * nsub * 4, "range totals");
     if (!e) e = dmalloc(c, (void **)&cursor, 2ull * nsub * 8, "range cursors");
@@ -945,12 +1036,14 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_sr_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    (int)SRS_SMEM(nsub)), "range scatter smem");
     for (int p = 0; !e && p < nparts; p++) {
-        const uint64_t ps = pb[p], pe = pb[p + 1];
+        uint64_t part = 0;
+        for (uint32_t q = 0; q < nsets; q++) part += segs[(size_t)p * nsets + q].len;
+        const KeySeg *ps = d_segs + (size_t)p * nsets;
         uint32_t *tot = totals + (uint64_t)(p & 1) * nsub, *tot_next = totals + (uint64_t)((p + 1) & 1) * nsub;
         unsigned long long *cur = cursor + (uint64_t)(p & 1) * nsub, *cur_next = cursor + (uint64_t)((p + 1) & 1) * nsub;
-        if (pe > ps) {
-            k_sr_hist<<<G, SR_THREADS, nsub * 4, c->stream>>>(keys, ps, pe, t->t, nsub, counts, tot);
-            k_sr_scatter<<<G, SR_THREADS, SRS_SMEM(nsub), c->stream>>>(keys, ps, pe, t->t, nsub, counts, tot, cur, range_keys);
+        if (part) {
+            k_sr_hist<<<G, SR_THREADS, nsub * 4, c->stream>>>(ps, nsets, t->t, nsub, counts, tot);
+            k_sr_scatter<<<G, SR_THREADS, SRS_SMEM(nsub), c->stream>>>(ps, nsets, t->t, nsub, counts, tot, cur, range_keys);
             c->launches += 2;
         }
         k_sr_build<<<nsub, SR_BUILD_THREADS, SR_SMEM, c->stream>>>(range_keys, tot, nsub, p, t->t, 1, tot_next, cur_next,
@@ -979,6 +1072,7 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
         if (!e) *done = true;
     }
     dfree(c, range_keys);
+    if (d_segs) dfree(c, d_segs);
     dfree(c, counts);
     dfree(c, totals);
     dfree(c, cursor);
@@ -988,89 +1082,103 @@ static int count_by_ranges(tk_table *t, const uint64_t *keys, const uint64_t *of
     return e;
 }
 
-// Counts every window of one or more packed read arrays into the table in a
-// single partitioned pass (the table is touched once for all of them).
-int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
+// Pass 1 for one read set: the bucket histogram of its windows with the HLL
+// sketch (a union into t->d_hll) and the window count (added to
+// t->d_counters[1]), then its windows into a key buffer of its own, bucket
+// by bucket.  The two kernels use one fixed grid, so every tile goes to the
+// same block (histogram column) in both.
+int table_bucket_pass(tk_table *t, const tk_reads *r, BucketKeys *out) {
     tk_ctx *c = t->ctx;
-    uint64_t total_len = 0;
-    std::vector<uint64_t> lens(nsets);
-    for (int s = 0; s < nsets; s++) total_len += (lens[s] = sets[s]->seq_len);
-    if (total_len == 0) return TK_OK;
-    // the two passes over each read array use one fixed grid, so every tile
-    // goes to the same block (histogram column) in both
+    *out = BucketKeys();
+    const uint64_t len = r->seq_len;
+    if (len == 0) return TK_OK;
     const uint64_t tile = (uint64_t)SC_THREADS * CT_SPAN;
-    std::vector<unsigned> grids(nsets);
-    std::vector<uint64_t> col0(nsets);
-    uint64_t cols = 0;
-    for (int s = 0; s < nsets; s++) {
-        grids[s] = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((lens[s] + tile - 1) / tile, (uint64_t)c->sm_count));
-        col0[s] = cols;
-        cols += grids[s];
-    }
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((len + tile - 1) / tile, (uint64_t)c->sm_count));
+    const uint64_t cols = grid, cells = (uint64_t)NBUCKETS * cols;
     uint32_t *hist = nullptr;
     uint64_t *offs = nullptr, *keys = nullptr;
-    const uint64_t cells = (uint64_t)NBUCKETS * cols;
     TK_TRY(dmalloc(c, (void **)&hist, cells * 4, "bucket histogram"));
     int e = dmalloc(c, (void **)&offs, (cells + 1) * 8, "bucket offsets");
-    if (!e) e = cuda_check(c, cudaMemsetAsync(t->d_counters + 1, 0, 8, c->stream), "window counter");
     cudaEvent_t ev;
-    uint64_t windows = 0;
     if (!e) {
-        // pass 1a: bucket histogram + HLL sketch (union with everything counted before)
         prof_begin(c, TK_KID_HLL, &ev);
-        for (int s = 0; s < nsets; s++) {
-            if (t->canonical)
-                k_part_hist<true><<<grids[s], HIST_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
-                                                                          hist, cols, col0[s], t->d_hll, t->d_counters + 1);
-            else
-                k_part_hist<false><<<grids[s], HIST_THREADS, 0, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s], t->k,
-                                                                           hist, cols, col0[s], t->d_hll, t->d_counters + 1);
-            c->launches++;
-        }
-        prof_end(c, TK_KID_HLL, ev, total_len);
+        if (t->canonical)
+            k_part_hist<true><<<grid, HIST_THREADS, 0, c->stream>>>(r->d_codes, r->d_inv, len, t->k, hist, cols, 0,
+                                                                  t->d_hll, t->d_counters + 1);
+        else
+            k_part_hist<false><<<grid, HIST_THREADS, 0, c->stream>>>(r->d_codes, r->d_inv, len, t->k, hist, cols, 0,
+                                                                   t->d_hll, t->d_counters + 1);
+        c->launches++;
+        prof_end(c, TK_KID_HLL, ev, len);
         e = check_launch(c, "bucket histogram");
     }
-    uint64_t padded = 0;   // key-buffer entries: the windows plus the EMPTY_KEY padding of every region
+    // key-buffer entries: the windows plus the EMPTY_KEY padding of every
+    // region (0 exactly when the set has no windows)
+    uint64_t padded = 0;
     if (!e) e = scan_excl_u32_to_u64(c, hist, offs, cells, &padded);   // synchronises
-    if (!e) {
+    if (!e && padded) {
         cudaMemcpyAsync(offs + cells, &padded, 8, cudaMemcpyHostToDevice, c->stream);
-        std::vector<uint32_t> regs(HLL_M);
-        e = cuda_check(c, cudaMemcpyAsync(regs.data(), t->d_hll, HLL_M * 4, cudaMemcpyDeviceToHost, c->stream), "hll d2h");
-        if (!e) e = cuda_check(c, cudaMemcpyAsync(&windows, t->d_counters + 1, 8, cudaMemcpyDeviceToHost, c->stream),
-                               "window count d2h");
-        if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "hll sync");
-        if (!e) {
-            double est = hll_estimate(regs.data());
-            uint64_t want = pow2_at_least((uint64_t)(est * 1.08 / t->max_load) + 1);
-            if (t->capacity == 0) e = table_alloc_geom(t, want, 0, false);   // fresh: filled slice by slice below
-            else if (want > t->capacity) e = table_rehash(t, want);
-        }
-    }
-    if (!e && windows) e = dmalloc(c, (void **)&keys, padded * 8, "bucketed k-mers");
-    if (!e && windows) {
-        // pass 1b: k-mers into their buckets
+        e = dmalloc(c, (void **)&keys, padded * 8, "bucketed k-mers");
         static_assert(SC_SMEM <= 227 * 1024, "bucket staging exceeds shared memory");
-        e = cuda_check(c, cudaFuncSetAttribute(k_part_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SC_SMEM),
-                       "scatter smem");
+        if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_part_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)SC_SMEM), "scatter smem");
         if (!e) e = cuda_check(c, cudaFuncSetAttribute(k_part_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                        (int)SC_SMEM), "scatter smem");
-        prof_begin(c, TK_KID_SCATTER, &ev);
-        for (int s = 0; !e && s < nsets; s++) {
+        if (!e) {
+            prof_begin(c, TK_KID_SCATTER, &ev);
             if (t->canonical)
-                k_part_scatter<true><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s],
-                                                                                  t->k, offs, cols, col0[s], keys);
+                k_part_scatter<true><<<grid, SC_THREADS, SC_SMEM, c->stream>>>(r->d_codes, r->d_inv, len, t->k, offs, cols,
+                                                                              0, keys);
             else
-                k_part_scatter<false><<<grids[s], SC_THREADS, SC_SMEM, c->stream>>>(sets[s]->d_codes, sets[s]->d_inv, lens[s],
-                                                                                   t->k, offs, cols, col0[s], keys);
+                k_part_scatter<false><<<grid, SC_THREADS, SC_SMEM, c->stream>>>(r->d_codes, r->d_inv, len, t->k, offs, cols,
+                                                                               0, keys);
             c->launches++;
+            prof_end(c, TK_KID_SCATTER, ev, padded);
+            e = check_launch(c, "bucket scatter");
         }
-        prof_end(c, TK_KID_SCATTER, ev, windows);
-        if (!e) e = check_launch(c, "bucket scatter");
-        if (!e) e = overflow_reset(t);
+    }
+    dfree(c, hist);
+    if (e || !padded) {
+        if (keys) dfree(c, keys);
+        if (offs) dfree(c, offs);
+        return e;
+    }
+    out->keys = keys;
+    out->offs = offs;
+    out->cols = cols;
+    return TK_OK;
+}
+
+void table_bucket_free(tk_table *t, BucketKeys *bk) {
+    if (bk->keys) dfree(t->ctx, bk->keys);
+    if (bk->offs) dfree(t->ctx, bk->offs);
+    *bk = BucketKeys();
+}
+
+// Pass 2 for the sets whose pass 1 ran since the window counter was reset:
+// the table sized from the HLL sketch (allocated fresh, or grown), then every
+// set's keys counted partition by partition; frees the key buffers.
+int table_count_buckets(tk_table *t, std::vector<BucketKeys> &bk) {
+    tk_ctx *c = t->ctx;
+    uint64_t windows = 0;
+    std::vector<uint32_t> regs(HLL_M);
+    int e = cuda_check(c, cudaMemcpyAsync(regs.data(), t->d_hll, HLL_M * 4, cudaMemcpyDeviceToHost, c->stream), "hll d2h");
+    if (!e) e = cuda_check(c, cudaMemcpyAsync(&windows, t->d_counters + 1, 8, cudaMemcpyDeviceToHost, c->stream),
+                           "window count d2h");
+    if (!e) e = cuda_check(c, cudaStreamSynchronize(c->stream), "hll sync");
+    if (!e) {
+        double est = hll_estimate(regs.data());
+        uint64_t want = pow2_at_least((uint64_t)(est * 1.08 / t->max_load) + 1);
+        if (t->capacity == 0) e = table_alloc_geom(t, want, 0, false);   // fresh: filled slice by slice below
+        else if (want > t->capacity) e = table_rehash(t, want);
+    }
+    cudaEvent_t ev;
+    if (!e && windows) {
+        e = overflow_reset(t);
         prof_begin(c, TK_KID_COUNT, &ev);
         bool done = false;
-        if (!e && t->fresh && t->t.lbits >= SR_MIN_LBITS) e = count_by_ranges(t, keys, offs, cols, &done);
-        if (!e && !done) e = count_by_atomics(t, keys, offs, cols);
+        if (!e && t->fresh && t->t.lbits >= SR_MIN_LBITS) e = count_by_ranges(t, bk, &done);
+        if (!e && !done) e = count_by_atomics(t, bk);
         prof_end(c, TK_KID_COUNT, ev, windows);
         if (!e) e = check_launch(c, "count insert");
         if (!e) t->fresh = false;
@@ -1081,9 +1189,7 @@ int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
         t->fresh = false;
         e = check_launch(c, "table fill");
     }
-    if (keys) dfree(c, keys);
-    if (offs) dfree(c, offs);
-    dfree(c, hist);
+    for (BucketKeys &b : bk) table_bucket_free(t, &b);
     if (e && t->fresh && t->t.slots) {
         // a failed first pass must not leave unwritten slots behind
         k_fill_empty<<<stream_grid(c, t->capacity, 256), 256, 0, c->stream>>>(t->t.slots, t->capacity, 0);
@@ -1094,6 +1200,34 @@ int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
     t->total += windows;
     t->distinct_valid = false;
     return drain_overflow(t);
+}
+
+// Resets the window counter before a group of pass-1 calls.
+int table_count_begin(tk_table *t) {
+    return cuda_check(t->ctx, cudaMemsetAsync(t->d_counters + 1, 0, 8, t->ctx->stream), "window counter");
+}
+
+// Counts every window of one or more packed read arrays into the table: pass
+// 1 per set, then one partitioned pass 2 over all of them (the table is
+// touched once for all of them); sets beyond MAX_KEY_SEGS are counted in
+// further groups.
+int table_count_many(tk_table *t, const tk_reads *const *sets, int nsets) {
+    for (int g0 = 0; g0 < nsets; g0 += MAX_KEY_SEGS) {
+        const int g1 = std::min(nsets, g0 + MAX_KEY_SEGS);
+        uint64_t total_len = 0;
+        for (int s = g0; s < g1; s++) total_len += sets[s]->seq_len;
+        if (total_len == 0) continue;
+        TK_TRY(table_count_begin(t));
+        std::vector<BucketKeys> bk(g1 - g0);
+        int e = TK_OK;
+        for (int s = g0; s < g1 && !e; s++) e = table_bucket_pass(t, sets[s], &bk[s - g0]);
+        if (e) {
+            for (BucketKeys &b : bk) table_bucket_free(t, &b);
+            return e;
+        }
+        TK_TRY(table_count_buckets(t, bk));
+    }
+    return TK_OK;
 }
 
 int table_count_seq(tk_table *t, const tk_reads *r) { return table_count_many(t, &r, 1); }

@@ -179,13 +179,15 @@ class ReadSet:
             keep.append(k)
         hs = (C.c_void_p * n)()
         ctx.check(ctx.lib.tk_reads_parse_many(ctx.h, ptrs, lens, n, N.TK_HOST, hs), "tk_reads_parse_many")
-        out = []
-        for i in range(n):
-            rs = cls.__new__(cls)
-            rs.ctx, rs.lib, rs._keep, rs._host_text = ctx, ctx.lib, None, texts[i]
-            rs._adopt(C.c_void_p(hs[i]))
-            out.append(rs)
-        return out
+        return [cls._adopted(ctx, C.c_void_p(hs[i]), texts[i]) for i in range(n)]
+
+    @classmethod
+    def _adopted(cls, ctx: Context, h, text) -> "ReadSet":
+        """A read set around a handle the library returned for host text `text`."""
+        rs = cls.__new__(cls)
+        rs.ctx, rs.lib, rs._keep, rs._host_text = ctx, ctx.lib, None, text
+        rs._adopt(h)
+        return rs
 
     def free(self) -> None:
         if getattr(self, "h", None) and _live():
@@ -286,6 +288,20 @@ class KmerTable:
         """Counts several read sets in one pass over the table."""
         arr = (C.c_void_p * len(sets))(*[s.h.value for s in sets])
         self.ctx.check(self.lib.tk_table_add_reads_multi(self.h, arr, len(sets)), "tk_table_add_reads_multi")
+
+    def count_texts(self, texts: list) -> list:
+        """Host texts -> read sets, counted into the table as they land
+        (tk_table_count_texts: each text's first counting pass runs while the
+        later texts upload).  Returns the read sets, in order."""
+        n = len(texts)
+        ptrs, lens, keep = (C.c_void_p * n)(), (C.c_uint64 * n)(), []
+        for i, t in enumerate(texts):
+            ptr, ln, k = _host_ptr(t)
+            ptrs[i], lens[i] = ptr, ln
+            keep.append(k)
+        hs = (C.c_void_p * n)()
+        self.ctx.check(self.lib.tk_table_count_texts(self.h, ptrs, lens, n, N.TK_HOST, hs), "tk_table_count_texts")
+        return [ReadSet._adopted(self.ctx, C.c_void_p(hs[i]), texts[i]) for i in range(n)]
 
     def count_text(self, text: Buffer) -> None:
         ptr, n, keep = _host_ptr(text)

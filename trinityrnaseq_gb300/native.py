@@ -67,6 +67,7 @@ SIGNATURES = {
     "tk_table_create": (C.c_int, [vp, C.c_int, C.c_int, u64, P(vp)]),
     "tk_table_add_reads": (C.c_int, [vp, vp]),
     "tk_table_add_reads_multi": (C.c_int, [vp, P(vp), u32]),
+    "tk_table_count_texts": (C.c_int, [vp, P(vp), P(u64), u32, C.c_int, P(vp)]),
     "tk_table_count_text": (C.c_int, [vp, vp, u64, C.c_int]),
     "tk_table_info": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
     "tk_table_histo": (C.c_int, [vp, u64, u64, vp]),
