@@ -54,6 +54,13 @@ def test_jellyfish_count_histo_dump(native_built, oracle, golden, tmp_path):
     with open(tmp_path / "all.fa", "wb") as fh:
         run([jf, "dump", "-L", 1, "db2.jf"], cwd=tmp_path, stdout=fh)
     assert (tmp_path / "all.fa").read_bytes() == oracle.dump(keys, counts, 25, 1)
+    # several input files (and an empty one) are counted as their concatenation
+    parts = [golden / "left.fa", golden / "right.fa", tmp_path / "empty.fa", golden / "bulk.fa"]
+    (tmp_path / "empty.fa").write_bytes(b"")
+    run([jf, "count", "-m", 25, "-s", "1G", "-C", "-o", "db3.jf", *parts], cwd=tmp_path)
+    with open(tmp_path / "multi.fa", "wb") as fh:
+        run([jf, "dump", "-L", 1, "db3.jf"], cwd=tmp_path, stdout=fh)
+    assert (tmp_path / "multi.fa").read_bytes() == oracle.dump(keys, counts, 25, 1)
 
 
 def test_fastaToKmerCoverageStats(native_built, oracle, golden, tmp_path):

@@ -96,6 +96,7 @@ struct Side {
     std::string tag;                    // left / right / single
     std::vector<std::string> files;
     std::vector<char> fastq;
+    std::vector<char> fasta;            // the side's reads as FASTA (seqtk-trinity's output), until counted
     tk_reads *fq = nullptr, *fa = nullptr;
     std::vector<uint32_t> med;
     std::vector<float> mean, sd;
@@ -214,24 +215,40 @@ int main(int argc, char **argv) {
         if (n && fmt != (fa_in ? TK_FMT_FASTA : TK_FMT_FASTQ))
             die("%s input is not %s", d.tag.c_str(), fa_in ? "FASTA" : "FASTQ");
         d.n = n;
-        if (fa_in) {
-            // FASTA is counted as it is (insilico:692-705 concatenates it)
-            check(tk_table_add_reads(t, d.fq), ctx, "k-mer count");
-            continue;
-        }
+        if (fa_in) continue;   // FASTA is counted as it is (insilico:692-705 concatenates it)
         // seqtk-trinity seq -A -R {1|2} [-r]: "-r" for the side whose library letter is R
         const char letter = s < ss.size() ? ss[s] : 0;
         const int flags = TK_FA_IF_MISSING | (letter == 'R' ? TK_FA_REVCOMP : 0);
         const int append = d.tag == "right" ? 2 : 1;
         uint64_t flen = 0;
         check(tk_reads_to_fasta(d.fq, append, flags, TK_HOST, nullptr, 0, &flen), ctx, "fastq to fasta");
-        std::vector<char> fa(flen ? flen : 1);
-        check(tk_reads_to_fasta(d.fq, append, flags, TK_HOST, fa.data(), fa.size(), &flen), ctx, "fastq to fasta");
-        check(tk_reads_parse(ctx, fa.data(), flen, TK_HOST, &d.fa), ctx, "parse converted reads");
-        check(tk_table_add_reads(t, d.fa), ctx, "k-mer count");
+        d.fasta.resize(flen ? flen : 1);
+        check(tk_reads_to_fasta(d.fq, append, flags, TK_HOST, d.fasta.data(), d.fasta.size(), &flen), ctx,
+              "fastq to fasta");
+        d.fasta.resize(flen);
     }
-    if (fa_in)
+    // both sides counted in one pass over the table (jellyfish counts
+    // `cat left.fa right.fa`, insilico:617-626)
+    if (fa_in) {
+        std::vector<const tk_reads *> sets;
+        for (Side &d : sides) sets.push_back(d.fq);
+        check(tk_table_add_reads_multi(t, sets.data(), (uint32_t)sets.size()), ctx, "k-mer count");
         for (Side &d : sides) d.fa = d.fq;
+    } else {
+        std::vector<const char *> texts;
+        std::vector<uint64_t> lens;
+        for (Side &d : sides) {
+            texts.push_back(d.fasta.data());
+            lens.push_back(d.fasta.size());
+        }
+        std::vector<tk_reads *> fa(sides.size(), nullptr);
+        check(tk_table_count_texts(t, texts.data(), lens.data(), (uint32_t)texts.size(), TK_HOST, fa.data()), ctx,
+              "k-mer count");
+        for (size_t s = 0; s < sides.size(); s++) {
+            sides[s].fa = fa[s];
+            std::vector<char>().swap(sides[s].fasta);
+        }
+    }
     for (Side &d : sides) {
         d.med.resize(d.n ? d.n : 1);
         d.mean.resize(d.n ? d.n : 1);

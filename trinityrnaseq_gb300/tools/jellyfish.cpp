@@ -121,10 +121,29 @@ static int cmd_count(int argc, char **argv) {
     if (reprobes > 0) check(tk_ctx_set_reprobes(ctx, reprobes), ctx, "set reprobes");
     tk_table *t = nullptr;
     check(tk_table_create(ctx, k, canonical ? 1 : 0, 0, &t), ctx, "table create");
-    for (const std::string &f : files) {
-        std::vector<char> text = read_file(f);
-        check(tk_table_count_text(t, text.data(), text.size(), TK_HOST), ctx, ("count " + f).c_str());
+    // every file, cut into record-aligned pieces of about 1 GB, counted in one
+    // pass over the table: each piece is parsed and bucketed while the later
+    // ones upload (tk_table_count_texts)
+    std::vector<std::vector<char>> texts;
+    for (const std::string &f : files) texts.push_back(read_file(f));
+    std::vector<const char *> ptrs;
+    std::vector<uint64_t> lens;
+    for (const std::vector<char> &x : texts) {
+        const uint32_t n = (uint32_t)std::min<uint64_t>(16, std::max<uint64_t>(1, x.size() >> 30));
+        std::vector<uint64_t> cuts(n + 1);
+        check(tk_split_records(x.data(), x.size(), n, cuts.data()), ctx, "split records");
+        for (uint32_t i = 0; i < n; i++) {
+            ptrs.push_back(x.data() + cuts[i]);
+            lens.push_back(cuts[i + 1] - cuts[i]);
+        }
     }
+    std::vector<tk_reads *> sets(ptrs.size(), nullptr);
+    std::string what = "count";
+    for (const std::string &f : files) what += " " + f;
+    check(tk_table_count_texts(t, ptrs.data(), lens.data(), (uint32_t)ptrs.size(), TK_HOST, sets.data()), ctx,
+          what.c_str());
+    for (tk_reads *r : sets) tk_reads_free(r);
+    texts.clear();
     Db db;
     db.k = (uint32_t)k;
     db.canonical = canonical ? 1 : 0;
