@@ -667,7 +667,8 @@ def norm_bench(ctx, left, right, args):
             if outs is None:
                 lens.append(nm.extract_into(r))
             else:
-                lens.append(nm.extract_into(r, outs[i].data_ptr(), outs[i].numel()))
+                # the left side's records go down while the right side's are extracted
+                lens.append(nm.extract_into(r, outs[i].data_ptr(), outs[i].numel(), overlap=True))
         c = nm.counts
         nm.free()
         return c, lens
@@ -697,9 +698,10 @@ def norm_bench(ctx, left, right, args):
     ctx.set_profiling(False)
 
     def whole():
-        fqs = [kmer.ReadSet(ctx, h.numpy()) for h in h_fq]
+        fqs = kmer.ReadSet.parse_many(ctx, [h.numpy() for h in h_fq])   # the right side uploads during the left's parse
         fas = prep_count_stats(fqs)
         tail(fas, fqs, h_out)
+        ctx.synchronize()
         for r in fas + fqs:
             r.free()
 
