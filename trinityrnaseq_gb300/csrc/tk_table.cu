@@ -91,8 +91,9 @@ __device__ __forceinline__ void thread_windows(const uint64_t *__restrict__ code
 }
 
 // Pass 1a: k-mers per (hash bucket, column) and the HLL sketch of the batch.
-// hist is bucket-major with `cols` columns per bucket; read set s uses the
-// columns [col0, col0 + gridDim.x), one per block: hist[bucket * cols + col0 + block].
+// hist is bucket-major with `cols` columns per bucket; the read set uses the
+// columns [col0, col0 + gridDim.x), one per block: hist[bucket * cols + col0 + block]
+// (each read set has a histogram and key buffer of its own, col0 = 0).
 // Each count is rounded up to a multiple of 4 keys, so every (bucket, column)
 // region of the key buffer starts on a 32-byte sector; pass 1b pads the
 // rounding with EMPTY_KEY, which the insert skips.  Pass 1b's block of
