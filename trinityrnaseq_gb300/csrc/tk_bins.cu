@@ -26,6 +26,7 @@
 #include "tk_internal.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 
@@ -309,10 +310,10 @@ namespace tk {
 int parse_reads(tk_ctx *c, tk_reads *r);
 
 // block sizes the count kernel is tuned over, per device (0 = not tuned yet)
-static int g_tuned_block[64];
+static std::atomic<int> g_tuned_block[64];   // several contexts (server slots) may share a device
 // slice load factor (per mille) chosen per device on the first batch of at
 // least BIN_TUNE_MIN windows (0 = not tuned yet: the caller's default)
-static int g_tuned_load[64];
+static std::atomic<int> g_tuned_load[64];
 constexpr uint64_t BIN_TUNE_MIN = 50ull << 20;
 
 template <bool CANON>
@@ -423,12 +424,13 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
     if (!e) e = alloc((void **)&d_lbits, n_bins, "bin slice sizes");
     if (!e) e = alloc((void **)&d_ovf, n_bins * 4, "bin overflow flags");
     std::vector<uint32_t> ovf(n_bins);
-    if (!e && !g_tuned_load[c->device & 63] && n && kmers >= BIN_TUNE_MIN) {
+    if (!e && !g_tuned_load[c->device & 63].load() && n && kmers >= BIN_TUNE_MIN) {
         // autotune the slice load factor once per device on a batch of this
         // size: fill + count timed for each candidate (fuller slices are
         // smaller to fill and sweep but probe longer); the dumps do not
         // depend on it, every bin's records being sorted by key
-        const int tb = g_tuned_block[c->device & 63] ? g_tuned_block[c->device & 63] : 256;
+        const int tb0 = g_tuned_block[c->device & 63].load();
+        const int tb = tb0 ? tb0 : 256;
         double best = 1e30;
         int best_pm = (int)(load * 1000 + 0.5);
         for (int pm : {450, 600, 750}) {
@@ -456,14 +458,16 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
             if (e) break;
             if (ms < best) { best = ms; best_pm = pm; }
         }
-        if (!e) g_tuned_load[c->device & 63] = best_pm;
+        if (!e) g_tuned_load[c->device & 63].store(best_pm);
     }
-    const int load_pm = g_tuned_load[c->device & 63] ? g_tuned_load[c->device & 63] : (int)(load * 1000 + 0.5);
+    const int tl = g_tuned_load[c->device & 63].load();
+    const int load_pm = tl ? tl : (int)(load * 1000 + 0.5);
     if (!e) size_slices(load_pm / 1000.0);
     // 4. fill + persistent count, captured in a CUDA graph; a slice that
     //    overflowed is doubled and the graph rebuilt and relaunched
     int relaunch = 0;
-    int block = g_tuned_block[c->device & 63] ? g_tuned_block[c->device & 63] : 256;
+    const int tblk = g_tuned_block[c->device & 63].load();
+    int block = tblk ? tblk : 256;
     for (int round = 0; !e && round < 6; round++) {
         if (slots) { dfree(c, slots); slots = nullptr; }
         if ((e = dmalloc(c, (void **)&slots, total * sizeof(Slot), "bin tables"))) break;
@@ -471,7 +475,7 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
         cudaMemcpyAsync(d_lbits, lbits.data(), n_bins, cudaMemcpyHostToDevice, c->stream);
         cudaMemsetAsync(d_ovf, 0, n_bins * 4, c->stream);
         BinGeom g{d_seq0, d_base, d_lbits, n_bins};
-        if (round == 0 && !g_tuned_block[c->device & 63] && n) {
+        if (round == 0 && !tblk && n) {
             // autotune the block shape once per device on this batch (timed launches, same result each time)
             double best = 1e30;
             for (int cand : {128, 256, 512}) {
@@ -490,7 +494,7 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
                 cudaEventDestroy(b2);
                 if (ms < best) { best = ms; block = cand; }
             }
-            g_tuned_block[c->device & 63] = block;
+            g_tuned_block[c->device & 63].store(block);
             cudaMemsetAsync(d_ovf, 0, n_bins * 4, c->stream);
             if ((e = check_launch(c, "bin autotune"))) break;
         }
