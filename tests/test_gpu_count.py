@@ -284,3 +284,18 @@ def test_multi_set_partitioned_table_and_deferred_fallback(native_built, oracle)
         run = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, timeout=600)
         assert run.returncode == 0, run.stderr[-2000:]
         assert run.stdout == want, cap
+
+
+def test_count_texts_error_leaves_the_context_usable(ctx, oracle):
+    """A malformed text among the pieces fails the call (no read set is
+    returned, the key buffers of the texts before it are freed); the context
+    and a new table still count exactly afterwards."""
+    good = synth.transcriptome_reads(seed=64, n_reads=20000).tobytes()
+    bad = b"@r1\nACGT\n+\nIIII\n@r2\nACGT\n"
+    t = KmerTable(ctx, 25, True)
+    with pytest.raises(native.TrinkmerError):
+        t.count_texts([np.frombuffer(good, dtype=np.uint8), np.frombuffer(bad, dtype=np.uint8)])
+    t2 = KmerTable(ctx, 25, True)
+    sets = t2.count_texts([np.frombuffer(good, dtype=np.uint8)])
+    assert sets[0].n_reads == 20000
+    assert_pairs(t2.dump(1), oracle.count(good, 25, True))
