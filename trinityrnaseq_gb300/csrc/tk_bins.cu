@@ -319,9 +319,12 @@ constexpr uint64_t BIN_TUNE_MIN = 50ull << 20;
 template <bool CANON>
 static void launch_count(tk_ctx *c, int block, const uint8_t *seq, uint64_t n, int k, BinGeom g, Slot *slots,
                          uint32_t *ovf) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin_count<CANON>, block, 0);
-    unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)c->sm_count;   // persistent: one wave
+    // one block per chunk of block x 32 positions: the blocks start in index
+    // order as earlier ones finish, so the bins being counted at any moment
+    // are those of a short stretch of the text and their slices stay in L2
+    // (a persistent grid's warps drift apart over the text)
+    const uint64_t span = (uint64_t)block * BC_SPAN;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + span - 1) / span, 0x7FFFFFFFull));
     k_bin_count<CANON><<<grid, block, 0, c->stream>>>(seq, n, k, g, slots, c->max_probes, ovf);
     c->launches++;
 }
