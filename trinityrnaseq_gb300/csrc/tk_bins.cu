@@ -12,7 +12,8 @@
 //  3. host autotuning: every bin gets its own table slice, a power of two at
 //     most `load` full for its estimated distinct k-mers; the count kernel's
 //     block size is picked by timing candidates on the first batch;
-//  4. one persistent counting launch over all bins, captured in a CUDA graph
+//  4. one counting launch over all bins (a block per chunk of the text, so
+//     the bins in flight are those of a short stretch), captured in a CUDA graph
 //     together with the slice fill (re-launched when a slice overflows, with
 //     that slice doubled); the context keeps the executable graph and each
 //     later batch updates it in place rather than instantiating it again;
@@ -127,7 +128,8 @@ __global__ void k_bin_fill(Slot *slots, uint64_t n) {
     }
 }
 
-// The persistent counting launch: all bins, each k-mer into its bin's slice.
+// The counting launch: all bins, each k-mer into its bin's slice (a block per
+// chunk of BC_SPAN positions per thread; the loop also serves smaller grids).
 template <bool CANON>
 __global__ void k_bin_count(const uint8_t *__restrict__ seq, uint64_t n, int k, BinGeom g, Slot *__restrict__ slots,
                             int max_probes, uint32_t *__restrict__ overflow) {
@@ -466,7 +468,7 @@ static int bins_run(tk_ctx *c, const char *text, uint64_t len, int where, const 
     const int tl = g_tuned_load[c->device & 63].load();
     const int load_pm = tl ? tl : (int)(load * 1000 + 0.5);
     if (!e) size_slices(load_pm / 1000.0);
-    // 4. fill + persistent count, captured in a CUDA graph; a slice that
+    // 4. fill + count, captured in a CUDA graph; a slice that
     //    overflowed is doubled and the graph rebuilt and relaunched
     int relaunch = 0;
     const int tblk = g_tuned_block[c->device & 63].load();
