@@ -11,16 +11,17 @@
 //     per bin (bins found per thread by binary search over bin starts);
 //  3. host autotuning: every bin gets its own table slice, a power of two at
 //     most `load` full for its estimated distinct k-mers; the count kernel's
-//     block size is picked by timing candidates on the first batch;
+//     block size and the load factor are picked once per device by timing
+//     candidates;
 //  4. one counting launch over all bins (a block per chunk of the text, so
 //     the bins in flight are those of a short stretch), captured in a CUDA graph
 //     together with the slice fill (re-launched when a slice overflows, with
 //     that slice doubled); the context keeps the executable graph and each
 //     later batch updates it in place rather than instantiating it again;
-//  5. one compaction of every slice into (bin << 2k | key, count), one radix
-//     sort (past 2^(64 - 2k) bins: a sort by k-mer, then a stable sort of the
-//     record order by bin), one K4 formatting pass; bin b's dump is a
-//     contiguous byte range.
+//  5. one compaction of every slice into ((local bin << 2k) | key, count), in
+//     groups of 2^(64 - 2k) bins so that the pair fits 64 bits, one radix sort
+//     per group, one K4 formatting pass; bin b's dump is a contiguous byte
+//     range.
 //
 // Each bin's dump equals a separate plain `jellyfish count` + `dump -L m` of
 // that bin (sorted by key).
